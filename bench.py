@@ -1,0 +1,419 @@
+#!/usr/bin/env python3
+"""Benchmark of the LBVH rebuild + trace hot path on GB300.
+
+Default workload (the per-frame rebuild configuration): a geodesic icosphere
+of 2,099,520 fp32 triangles displaced by seeded value-noise fBm, 16 frames
+each perturbing every vertex by N(0, 1e-3); every step is one frame: full
+LBVH rebuild (depth 20) + 1920x1080 primary rays + shadow ray + one mirror
+ray per pixel.  Metric: frame Mtri/s = triangles rebuilt and traced per
+second (N / frame time); build Mtri/s and trace Mrays/s are reported beside.
+
+  python bench.py [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload frame|torus|pt] [--gpus N]
+
+Multi-GPU: the path does not shard (one global sort per frame), so N > 1
+runs N independent replicas (one per rank, torchrun) and value is the sum
+of the replicas' frames over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "raytracer-gpupro4_gb300"))
+
+METRIC = "LBVH build Mtri/s; trace Mrays/s; batched/adjoint vs plain, same GB300"
+BUILD_BYTES_PER_TRI = 256  # bounds 36 + Morton 44 + sort 68 + emit/refit 108
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=16)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["frame", "torus", "pt"], default="frame")
+    ap.add_argument("--freq", type=int, default=324, help="icosphere frequency (324 -> 2,099,520 triangles)")
+    ap.add_argument("--depth", type=int, default=20)
+    ap.add_argument("--frames", type=int, default=16)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+
+    def init(self, backend):
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+        self.pg.all_reduce(t)
+        return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9 and f[1].replace(".", "").isdigit():
+                    rows.append(f)
+        except OSError:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except OSError:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """Per-launch DRAM traffic of a kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "ncu_traffic.json"
+    if not p.exists():
+        return None
+    try:
+        return json.loads(p.read_text()).get(kernel)
+    except (ValueError, OSError):
+        return None
+
+
+# ---------------------------------------------------------------------------
+def frame_workload(args):
+    from rtgpu import scenes
+    if args.workload == "torus":
+        tris = scenes.torus()
+        frames = [tris]
+        cam = scenes.torus_camera()
+        name = "torus 65,536 tris, 512x512 primary+shadow+mirror, depth %d" % args.depth
+        light = scenes.TORUS_LIGHT
+    else:
+        s = scenes.icosphere(args.freq)
+        frames = [s.frame(k) for k in range(args.frames)]
+        cam = scenes.sphere_camera()
+        name = ("icosphere %d tris (fBm 0.15, 6 oct), %d frames perturbed N(0,1e-3), full rebuild depth %d, "
+                "1920x1080 primary+shadow+mirror" % (s.n_tris, args.frames, args.depth))
+        light = scenes.TORUS_LIGHT
+    return frames, cam, light, name
+
+
+def run_ours(args, dist: Dist):
+    import torch
+    from rtgpu import _lib as L
+    from rtgpu import build as B
+    from rtgpu.api import LBVH, Context, RayTracer
+
+    B.build_cuda()
+    torch.cuda.set_device(dist.local)
+    dist.init("nccl")
+    dev = torch.device("cuda", dist.local)
+    if args.workload == "pt":
+        return run_pt(args, dist)
+    frames, cam, light, name = frame_workload(args)
+    n = len(frames[0])
+    npx = cam.width * cam.height
+    host = torch.from_numpy(np.stack(frames)).pin_memory()
+    dfr = host.to(dev)
+    ctx = Context(dist.local)
+    lb = LBVH(ctx, n, args.depth)
+    rt = RayTracer(ctx)
+    hits = torch.empty((npx, 4), dtype=torch.int32, device=dev)
+    mirror = torch.empty((npx, 4), dtype=torch.int32, device=dev)
+    vis = torch.empty(npx, dtype=torch.uint8, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+
+    # algorithmic trace bytes of frame 0 from the per-ray test counters
+    lb.Build(dfr[0])
+    _, pst = rt.primary(lb, cam, stats=True, out=hits)
+    _, _, sst, mst = rt.shadow_mirror(lb, cam, light, hits, stats=True, vis=vis, mirror=mirror)
+    ctx.check()
+    pst, sst, mst = (x.to(torch.int64).sum(0).tolist() for x in (pst, sst, mst))
+    visn = vis.cpu().numpy()
+    n_prim = npx
+    n_shadow = int((visn >= 2).sum())
+    n_mirror = int((visn >= 1).sum())
+    bytes_primary = 32 * pst[0] + 40 * pst[1] + 32 * n_prim
+    bytes_secondary = 32 * (sst[0] + mst[0]) + 40 * (sst[1] + mst[1]) + 32 * (n_shadow + n_mirror)
+    rays_per_frame = n_prim + n_shadow + n_mirror
+
+    stream = torch.cuda.current_stream(dev)
+
+    def step(k, evs=None):
+        f = dfr[k % len(frames)]
+        if evs:
+            evs[0].record(stream)
+        lb.Build(f)
+        if evs:
+            evs[1].record(stream)
+        rt.primary(lb, cam, out=hits)
+        if evs:
+            evs[2].record(stream)
+        rt.shadow_mirror(lb, cam, light, hits, vis=vis, mirror=mirror)
+        if evs:
+            evs[3].record(stream)
+
+    for k in range(args.warmup):
+        flush.zero_()
+        step(k)
+    ctx.check()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks(dist.local) as clk:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()  # > L2 (129 MB) written between steps, outside the per-step events
+            step(args.warmup + k, evs[k])
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    dist.barrier()
+    ctx.check()
+    per = np.array([[a.elapsed_time(b) for a, b in zip(e[:-1], e[1:])] for e in evs])  # ms: build, primary, secondary
+    step_ms = per.sum(1)
+    t_total = dist.max(float(step_ms.sum()) / 1e3)
+    frames_done = dist.sum(float(args.steps))
+    value = frames_done * n / t_total / 1e6
+    build_ms, prim_ms, sec_ms = per.mean(0)
+
+    # e2e: the public C ABI call with host buffers, copies inside the timed region
+    e2e = None
+    if not args.no_e2e:
+        hp = np.zeros(npx, L.HIT_DTYPE)
+        hv = np.zeros(npx, np.uint8)
+        hm = np.zeros(npx, L.HIT_DTYPE)
+        hp_t = torch.from_numpy(hp.view(np.int32).reshape(-1)).pin_memory()
+        hv_t = torch.from_numpy(hv).pin_memory()
+        hm_t = torch.from_numpy(hm.view(np.int32).reshape(-1)).pin_memory()
+        hp2 = hp_t.numpy().view(L.HIT_DTYPE)
+        hm2 = hm_t.numpy().view(L.HIT_DTYPE)
+        hv2 = hv_t.numpy()
+        lb2 = LBVH(ctx, n, args.depth)
+        hosts = [host[k].numpy() for k in range(len(frames))]
+        for k in range(args.warmup):
+            rt.render_frame_host(lb2, hosts[k % len(frames)], cam, light, hp2, hv2, hm2)
+        dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            rt.render_frame_host(lb2, hosts[(args.warmup + k) % len(frames)], cam, light, hp2, hv2, hm2)
+        torch.cuda.synchronize()
+        te = dist.max(time.perf_counter() - t0)
+        e2e = {"value": round(frames_done * n / te / 1e6, 3), "unit": "Mtri/s",
+               "h2d_bytes_per_step": int(n * 36), "d2h_bytes_per_step": int(npx * (16 + 1 + 16)),
+               "ms_per_step": round(te / args.steps * 1e3, 3), "call": "rt_render_frame_host (pinned host soup in, hits out)"}
+        lb2.close()
+
+    peak, peak_kind = measured_peaks()
+    groups = {"k_trace_primary": (prim_ms, bytes_primary), "k_trace_secondary": (sec_ms, bytes_secondary),
+              "build (10 kernels)": (build_ms, BUILD_BYTES_PER_TRI * n)}
+    dom = max(groups, key=lambda g: groups[g][0])
+    ms, byts = groups[dom]
+    achieved = byts / (ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                "traffic": ncu_traffic(dom), "algorithmic_bytes_per_launch": int(byts),
+                "avg_launch_ms": round(float(ms), 4)}
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mtri/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(float(step_ms.mean()), 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": name, "triangles": n, "pixels": npx, "depth": args.depth,
+                   "l2": "flushed between steps (256 MiB write outside the per-step events)",
+                   "parallelism": "replicas" if dist.world > 1 else "single GPU"},
+        "components": {"build_ms": round(float(build_ms), 4), "build_mtri_s": round(n / build_ms / 1e3, 2),
+                       "primary_ms": round(float(prim_ms), 4), "secondary_ms": round(float(sec_ms), 4),
+                       "trace_mrays_s": round(rays_per_frame / ((prim_ms + sec_ms) / 1e3) / 1e6, 1),
+                       "rays_per_frame": {"primary": n_prim, "shadow": n_shadow, "mirror": n_mirror},
+                       "wall_s": round(wall, 3)},
+        "roofline": roofline,
+        "e2e": e2e,
+        "gpu_launches": 12 * args.steps,
+    }
+    out["clocks"] = clk.summary()
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_frame_baseline(frames[0], cam, light, args.depth, n)
+    lb.close()
+    ctx.close()
+    return out
+
+
+# ---------------------------------------------------------------------------
+def cpu_frame_baseline(tris, cam, light, depth, n, nthreads=None):
+    """One frame on the host: the oracle port (restated LBVH::Build, 1 thread as
+    the reference runs it) + primary/shadow/mirror traversal on all cores."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    O.build_oracle()
+    nth = nthreads or O.nthreads_default()
+    t0 = time.perf_counter()
+    nodes, ids, keys, _ = O.lbvh_build(tris, depth)
+    t1 = time.perf_counter()
+    hits = O.trace(nodes, depth, ids, tris, O.primary_rays(cam), nthreads=nth)
+    O.shadow_mirror(nodes, depth, ids, tris, cam, light, hits, nthreads=nth)
+    t2 = time.perf_counter()
+    return {"value": round(n / (t2 - t0) / 1e6, 4), "unit": "Mtri/s", "cores": nth, "kind": "port",
+            "sample": f"1 frame: build {t1 - t0:.2f}s on 1 thread, primary+shadow+mirror {t2 - t1:.2f}s on {nth} threads",
+            "cpu": _cpu_name()}
+
+
+def _cpu_name():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "hardware", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def run_reference(args, dist: Dist):
+    """Reference arm: the reference's CPU algorithm on the host cores (its LBVH
+    build single-threaded as written, traversal over all cores), one frame per
+    step, on the same workload and metric."""
+    if dist.rank != 0:
+        return None
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    O.build_oracle()
+    if args.workload == "pt":
+        return {"impl": "reference", "unavailable": "no reference CPU path tracer exists for this workload"}
+    frames, cam, light, name = frame_workload(args)
+    n = len(frames[0])
+    nth = O.nthreads_default()
+    use_ref = O.ref_available()
+    kind = "reference" if use_ref else "port"
+
+    def frame(k):
+        tris = frames[k % len(frames)]
+        if use_ref:  # reference LBVH::Build and LBVH::IntersectP compiled from its sources
+            ref = O.RefStructure(tris, "lbvh", args.depth)
+            nodes, ids = ref.nodes(), ref.ids()
+            prim = np.zeros(cam.width * cam.height, O.HIT_DTYPE)
+            hid, t, u, v = ref.intersect(O.primary_rays(cam), nthreads=nth)
+            prim["id"], prim["t"], prim["u"], prim["v"] = hid, t, u, v
+            O.shadow_mirror(nodes, args.depth, ids, tris, cam, light, prim, nthreads=nth)
+            ref.close()
+        else:
+            nodes, ids, _, _ = O.lbvh_build(tris, args.depth)
+            prim = O.trace(nodes, args.depth, ids, tris, O.primary_rays(cam), nthreads=nth)
+            O.shadow_mirror(nodes, args.depth, ids, tris, cam, light, prim, nthreads=nth)
+
+    for k in range(args.warmup):
+        frame(k)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        frame(args.warmup + k)
+    dt = time.perf_counter() - t0
+    value = args.steps * n / dt / 1e6
+    return {"metric": METRIC, "value": round(value, 4), "unit": "Mtri/s", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": {"workload": name, "triangles": n, "pixels": cam.width * cam.height, "depth": args.depth},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(value, 4), "unit": "Mtri/s", "cores": nth, "kind": kind,
+                             "sample": "every step one full frame: LBVH build on 1 thread, primary/shadow/mirror "
+                                       f"on {nth} threads", "cpu": _cpu_name()},
+            "e2e": {"value": round(value, 4), "unit": "Mtri/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def run_pt(args, dist: Dist):
+    raise SystemExit("the path-tracing workload is run by bench_pt() once rt_pathtrace is benchmarked")
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    if args.impl == "reference":
+        out = run_reference(args, dist)
+    else:
+        out = run_ours(args, dist)
+    if out is not None and dist.rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

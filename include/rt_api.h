@@ -1,0 +1,190 @@
+/*
+ * rt_api.h -- C ABI of the GB300 (sm_103a) LBVH ray-tracing core.
+ *
+ * The entry points replace the per-frame GPU path of the reference demo
+ * (elfrank/raytracer-gpupro4): the acceleration-structure interface
+ * (AccelerationStructures/AccelerationStructure.h:40-67 and
+ * AccelerationStructures/LBVH/LBVH.h:70-118), the GPU build stage
+ * (RayTracerCS/StructureConstruction.h:67-91) and the per-frame render
+ * stages (RayTracerCS/RayTracerCS.h:64-144, RayTracerCS.cpp:241-311).
+ * Direct3D devices and contexts become an opaque rt_ctx bound to one CUDA
+ * device and stream; every call is asynchronous on that stream unless it
+ * says otherwise, returns an rt_status and never throws.
+ *
+ * Plain C types only: pointers marked "device" are CUDA device addresses,
+ * "host" pointers are ordinary host memory (pinned memory makes the copies
+ * asynchronous).  A stream is passed as void* (a cudaStream_t).
+ */
+#ifndef RT_API_H
+#define RT_API_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RT_API_VERSION 1
+
+/* Errors.  The reference returned void / HRESULT and called exit()
+ * (Common/Scenes/Model.cpp:220-222, DeviceCore/D3DComputeShader.cpp:84-92). */
+typedef enum rt_status {
+    RT_OK = 0,
+    RT_ERR_INVALID = 1,   /* bad argument (null pointer, n == 0, depth out of range, ...) */
+    RT_ERR_CAPACITY = 2,  /* more triangles / pixels than the object was created for */
+    RT_ERR_CUDA = 3,      /* a CUDA runtime call failed; see rt_last_error() */
+    RT_ERR_TIMEOUT = 4,   /* a bounded device-side wait gave up (see rt_ctx_check) */
+    RT_ERR_NONFINITE = 5  /* the triangle soup holds NaN or infinite coordinates */
+} rt_status;
+
+/* LBVHNode (LBVH.h:25-28) / Node (Shaders/Structures.hlsl:18-26), 32 bytes.
+ * prim_count = (count << 3) | leaf * 4 | axis;  heap layout: root at 1,
+ * children of i at 2i and 2i+1, slot 0 unused, 1 << depth slots. */
+typedef struct rt_node {
+    float min[3];
+    float max[3];
+    int32_t prim_count;
+    int32_t prim_pos;
+} rt_node;
+
+/* Value written to prim_count and prim_pos of heap slots that no path
+ * reaches when RT_BUILD_CLEAR_UNREACHED is set (LBVH.hlsl:151-154). */
+#define RT_NODE_SENTINEL (-2147483647)
+
+/* Closest hit: {iTriangleId, fU, fV, fT} of Intersection
+ * (Shaders/Structures.hlsl:44-50), 16 bytes.  id = -1: no hit. */
+typedef struct rt_hit {
+    int32_t id;
+    float u, v, t;
+} rt_hit;
+
+/* A ray for rt_trace_rays (Ray, Shaders/Structures.hlsl:28-35, without the
+ * shading factor), 32 bytes.  exclude_id: triangle the ray must ignore
+ * (the triangle it leaves from), -1 for none. */
+typedef struct rt_ray {
+    float o[3];
+    int32_t exclude_id;
+    float d[3];
+    float tmax;
+} rt_ray;
+
+/* Pinhole camera (CSPrimaryRays.hlsl:36-56 with an explicit basis instead
+ * of the inverse world matrix): pixel (i, j) looks along
+ * normalize(right*x*tan + up*y*tan + fwd), x = (2i+1-W)/H, y = -(2j+1-H)/H. */
+typedef struct rt_camera {
+    float eye[3];
+    float right[3];
+    float up[3];
+    float fwd[3];
+    float tan_half_fovy;
+    uint32_t width, height;
+} rt_camera;
+
+typedef struct rt_ctx rt_ctx;
+typedef struct rt_lbvh rt_lbvh;
+
+/* ---- context ------------------------------------------------------- */
+/* Replaces the D3D device + immediate context (RayTracerCS.cpp:67-83). */
+rt_status rt_ctx_create(int device, void* stream, rt_ctx** out);
+rt_status rt_ctx_destroy(rt_ctx* ctx);
+rt_status rt_ctx_set_stream(rt_ctx* ctx, void* stream);
+rt_status rt_ctx_sync(rt_ctx* ctx);
+/* Synchronises, then reports a device-side error flag raised since the
+ * last check (RT_ERR_TIMEOUT, RT_ERR_NONFINITE) and clears it. */
+rt_status rt_ctx_check(rt_ctx* ctx);
+const char* rt_last_error(const rt_ctx* ctx);
+const char* rt_status_string(rt_status s);
+int rt_api_version(void);
+
+/* ---- LBVH ---------------------------------------------------------- */
+/* Creates an LBVH with room for max_tris triangles and 1 << depth heap
+ * slots (LBVH(Primitive**, N, n = 1 << depth), LBVH.h:104; lbvh_depth of
+ * conf.ini:61).  All device memory is allocated here; rebuilds reuse it. */
+rt_status rt_lbvh_create(rt_ctx* ctx, uint32_t max_tris, uint32_t depth, rt_lbvh** out);
+rt_status rt_lbvh_destroy(rt_lbvh* lbvh);
+
+#define RT_BUILD_CLEAR_UNREACHED 1u  /* write RT_NODE_SENTINEL to unreached slots */
+
+/* Full rebuild from a device triangle soup (n x 9 floats: A, B, C):
+ * scene bounds, 30-bit Morton codes, stable LSD radix sort, node emission,
+ * bottom-up refit.  Replaces LBVH::Build (LBVH.cpp:488-632) and
+ * StructureConstruction::GPUBuildStructure (StructureConstruction.cpp:86-131). */
+rt_status rt_lbvh_build(rt_ctx* ctx, rt_lbvh* lbvh, const float* d_tris, uint32_t n, uint32_t flags);
+/* Same from a host soup; the host-to-device copy is part of the call. */
+rt_status rt_lbvh_build_host(rt_ctx* ctx, rt_lbvh* lbvh, const float* h_tris, uint32_t n, uint32_t flags);
+/* Uses a tree built elsewhere (e.g. the reference's CPU LBVH::Build):
+ * host nodes (1 << depth), ordered ids (n) and the soup are uploaded
+ * (RayTracerCS::SelectAccelerationStructure, RayTracerCS.cpp:590-624). */
+rt_status rt_lbvh_import_host(rt_ctx* ctx, rt_lbvh* lbvh, const rt_node* h_nodes, const uint32_t* h_ids,
+                              const float* h_tris, uint32_t n);
+
+/* Device views (GetPtrToElements / GetOrderedElementsIds, LBVH.h:109-113). */
+typedef struct rt_lbvh_view {
+    const rt_node* nodes;      /* device, num_nodes entries */
+    const uint32_t* ids;       /* device, n: triangle id at sorted position */
+    const uint32_t* keys;      /* device, n: sorted Morton codes (valid after rt_lbvh_build) */
+    const float* sorted_tris;  /* device, n x 12 floats: A.xyz,id  B.xyz,0  C.xyz,0 in sorted order */
+    uint32_t n;
+    uint32_t depth;
+    uint32_t num_nodes;        /* 1 << depth (GetNumberOfElements) */
+    uint32_t node_size;        /* 32 (GetSizeOfElement) */
+} rt_lbvh_view;
+rt_status rt_lbvh_view_get(const rt_lbvh* lbvh, rt_lbvh_view* out);
+/* WorldBound() = root box (LBVH.h:115).  Synchronous. */
+rt_status rt_lbvh_world_bound(rt_ctx* ctx, const rt_lbvh* lbvh, float out_min_max[6]);
+/* Synchronous copies to host; any pointer may be NULL. */
+rt_status rt_lbvh_download(rt_ctx* ctx, const rt_lbvh* lbvh, rt_node* h_nodes, uint32_t* h_ids, uint32_t* h_keys);
+
+/* ---- tracing ------------------------------------------------------- */
+/* Optional per-ray statistics: 2 x uint32 {box tests, triangle tests},
+ * the iVisitedNodes counter of LBVH.hlsl:389,404 split in two. */
+
+/* Primary rays + closest hit (CSGeneratePrimaryRays + CSComputeIntersections
+ * -> LBVH_IntersectP, CSPrimaryRays.hlsl:22-69, LBVH.hlsl:363-440).
+ * d_hits: width*height, row-major. */
+rt_status rt_trace_primary(rt_ctx* ctx, const rt_lbvh* lbvh, const rt_camera* cam, rt_hit* d_hits,
+                           uint32_t* d_stats);
+/* Shadow + mirror rays from primary hits (CSComputeColorRT.hlsl:57-177,
+ * 203-210, flat normals).  d_vis per pixel: 0 primary miss, 1 light on the
+ * far side of the surface, 2 occluded, 3 lit.  d_mirror: closest hit of the
+ * mirror ray (id -2 where the primary ray missed).  Either output may be
+ * NULL to skip that ray type. */
+rt_status rt_trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* lbvh, const rt_camera* cam, const float light[3],
+                                 const rt_hit* d_primary, uint8_t* d_vis, rt_hit* d_mirror,
+                                 uint32_t* d_shadow_stats, uint32_t* d_mirror_stats);
+/* Arbitrary rays, closest hit (any_hit = 0) or first hit (any_hit = 1). */
+rt_status rt_trace_rays(rt_ctx* ctx, const rt_lbvh* lbvh, const rt_ray* d_rays, uint32_t n, int any_hit,
+                        rt_hit* d_hits, uint32_t* d_stats);
+
+/* One frame of the dynamic path (RayTracerCS::Render with dynamic=1,
+ * RayTracerCS.cpp:258-295): rebuild from a host soup, primary, shadow and
+ * mirror rays, results copied back to host buffers (any may be NULL). */
+rt_status rt_render_frame_host(rt_ctx* ctx, rt_lbvh* lbvh, const float* h_tris, uint32_t n,
+                               const rt_camera* cam, const float light[3], rt_hit* h_primary,
+                               uint8_t* h_vis, rt_hit* h_mirror);
+
+/* ---- path tracing (CSComputeColorGI.hlsl, ConstantBuffers.h:85-110) --- */
+typedef struct rt_pt_params {
+    uint32_t spp;
+    uint32_t bounces;   /* segments traced per path = bounces + 1 (RayTracerCS.cpp:289) */
+    uint64_t seed;
+    float sky[3];       /* radiance of a miss; the reference adds white (1,1,1) */
+    uint32_t reserved;
+} rt_pt_params;
+/* d_albedo, d_emission: n x 3 floats indexed by triangle id.
+ * d_image: width*height float4 (rgb, 1), progressive mean over spp. */
+rt_status rt_pathtrace(rt_ctx* ctx, const rt_lbvh* lbvh, const float* d_albedo, const float* d_emission,
+                       const rt_camera* cam, const rt_pt_params* p, float* d_image);
+/* Adjoint of rt_pathtrace by path replay: given dL/dImage (width*height
+ * float4), accumulates dL/dalbedo (n x 3) and dL/dLe (3 floats: the shared
+ * radiance of every emitting triangle) into the output buffers (not
+ * cleared by the call). */
+rt_status rt_pathtrace_adjoint(rt_ctx* ctx, const rt_lbvh* lbvh, const float* d_albedo, const float* d_emission,
+                               const rt_camera* cam, const rt_pt_params* p, const float* d_dimage,
+                               float* d_dalbedo, float* d_demission);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RT_API_H */

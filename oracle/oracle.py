@@ -1,0 +1,302 @@
+"""Python binding of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Wraps
+  * oracle/_build/liboracle.so: the C restatement in rt_oracle.c, and
+  * oracle/_ref/libref.so: the reference's own CPU LBVH / BVH code
+    (AccelerationStructures/LBVH/LBVH.cpp, BVH/bvh.cpp), built by
+    ref/build_ref.sh where the reference checkout is present.
+Only tests/, the smoke check and bench.py's CPU-baseline leg import this
+module; the product path never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_LIB = HERE / "_build" / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libref.so"
+
+NODE_DTYPE = np.dtype([("min", "<f4", (3,)), ("max", "<f4", (3,)), ("prim_count", "<i4"), ("prim_pos", "<i4")])
+HIT_DTYPE = np.dtype([("id", "<i4"), ("u", "<f4"), ("v", "<f4"), ("t", "<f4")])
+SENTINEL = -2147483647
+
+
+class OrCamera(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("right", C.c_float * 3), ("up", C.c_float * 3), ("fwd", C.c_float * 3),
+                ("tan_half_fovy", C.c_float), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class OrPtParams(C.Structure):
+    _fields_ = [("spp", C.c_uint32), ("bounces", C.c_uint32), ("seed", C.c_uint64), ("sky", C.c_float * 3)]
+
+
+def build_oracle() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return ORACLE_LIB
+
+
+def build_reference() -> Path | None:
+    """Compiles the reference CPU code when its sources are present."""
+    ref = Path(os.environ.get("RT_REFERENCE_DIR", "/root/reference"))
+    if not (ref / "AccelerationStructures" / "LBVH" / "LBVH.cpp").exists():
+        return None
+    srcs = [HERE / "ref" / "ref_shim.cpp", HERE / "ref" / "build_ref.sh"]
+    if REF_LIB.exists() and all(s.stat().st_mtime <= REF_LIB.stat().st_mtime for s in srcs):
+        return REF_LIB
+    subprocess.run(["bash", str(HERE / "ref" / "build_ref.sh")], check=True, capture_output=True)
+    return REF_LIB
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def to_or_camera(cam) -> OrCamera:
+    o = OrCamera()
+    for f in ("eye", "right", "up", "fwd"):
+        src, dst = getattr(cam, f), getattr(o, f)
+        for c in range(3):
+            dst[c] = src[c]
+    o.tan_half_fovy = cam.tan_half_fovy
+    o.width = cam.width
+    o.height = cam.height
+    return o
+
+
+_olib = None
+_rlib = None
+
+
+def olib() -> C.CDLL:
+    global _olib
+    if _olib is None:
+        if not ORACLE_LIB.exists():
+            build_oracle()
+        L = C.CDLL(str(ORACLE_LIB))
+        vp, u32, i32 = C.c_void_p, C.c_uint32, C.c_int
+        L.or_scene_bounds.argtypes = [vp, u32, vp]
+        L.or_morton.argtypes = [vp, u32, vp, vp]
+        L.or_sort_pairs.argtypes = [vp, vp, u32]
+        L.or_lbvh_emit.argtypes = [vp, vp, vp, u32, u32, vp, vp]
+        L.or_lbvh_build.argtypes = [vp, u32, u32, vp, vp, vp, vp]
+        L.or_trace.argtypes = [vp, u32, vp, vp, vp, u32, vp, vp, i32, i32]
+        L.or_primary_rays.argtypes = [C.POINTER(OrCamera), vp]
+        L.or_shadow_mirror.argtypes = [vp, u32, vp, vp, C.POINTER(OrCamera), vp, vp, vp, vp, vp, vp, i32]
+        L.or_pathtrace.argtypes = [vp, u32, vp, vp, vp, vp, C.POINTER(OrCamera), C.POINTER(OrPtParams), vp, i32]
+        L.or_pathtrace_adjoint.argtypes = [vp, u32, vp, vp, vp, vp, C.POINTER(OrCamera), C.POINTER(OrPtParams),
+                                           vp, vp, vp, i32]
+        L.or_pcg32_first.argtypes = [C.c_uint64, C.c_uint64, u32, vp]
+        L.or_pcg32_first.restype = u32
+        _olib = L
+    return _olib
+
+
+def nthreads_default() -> int:
+    return max(1, os.cpu_count() or 1)
+
+
+# --- build -----------------------------------------------------------------
+def scene_bounds(tris: np.ndarray) -> np.ndarray:
+    out = np.zeros(6, np.float32)
+    olib().or_scene_bounds(_ptr(tris), len(tris), _ptr(out))
+    return out
+
+
+def morton(tris: np.ndarray, bounds: np.ndarray | None = None) -> np.ndarray:
+    if bounds is None:
+        bounds = scene_bounds(tris)
+    keys = np.zeros(len(tris), np.uint32)
+    olib().or_morton(_ptr(tris), len(tris), _ptr(np.ascontiguousarray(bounds, np.float32)), _ptr(keys))
+    return keys
+
+
+def sort_pairs(keys: np.ndarray, ids: np.ndarray | None = None):
+    keys = np.array(keys, np.uint32, copy=True)
+    ids = np.arange(len(keys), dtype=np.uint32) if ids is None else np.array(ids, np.uint32, copy=True)
+    olib().or_sort_pairs(_ptr(keys), _ptr(ids), len(keys))
+    return keys, ids
+
+
+def lbvh_build(tris: np.ndarray, depth: int):
+    """Returns (nodes, ids, keys, reached) of the restated LBVH::Build."""
+    tris = np.ascontiguousarray(tris, np.float32)
+    n = len(tris)
+    nodes = np.zeros(1 << depth, NODE_DTYPE)
+    ids = np.zeros(n, np.uint32)
+    keys = np.zeros(n, np.uint32)
+    reached = np.zeros(1 << depth, np.uint8)
+    olib().or_lbvh_build(_ptr(tris), n, depth, _ptr(nodes), _ptr(ids), _ptr(keys), _ptr(reached))
+    return nodes, ids, keys, reached.astype(bool)
+
+
+# --- tracing ---------------------------------------------------------------
+def rays_array(o, d, tmax, exclude) -> np.ndarray:
+    n = len(d)
+    r = np.zeros((n, 8), np.float32)
+    r[:, 0:3] = o
+    r[:, 3:6] = d
+    r[:, 6] = tmax
+    r[:, 7] = exclude
+    return r
+
+
+def trace(nodes, depth, ids, tris, rays, any_hit=False, nthreads=None, stats=False):
+    rays = np.ascontiguousarray(rays, np.float32)
+    n = len(rays)
+    hits = np.zeros(n, HIT_DTYPE)
+    st = np.zeros((n, 2), np.uint32) if stats else None
+    olib().or_trace(_ptr(nodes), depth, _ptr(ids), _ptr(np.ascontiguousarray(tris, np.float32)), _ptr(rays), n,
+                    _ptr(hits), _ptr(st) if stats else None, int(any_hit), nthreads or nthreads_default())
+    return (hits, st) if stats else hits
+
+
+def primary_rays(cam) -> np.ndarray:
+    oc = to_or_camera(cam)
+    r = np.zeros((cam.width * cam.height, 8), np.float32)
+    olib().or_primary_rays(C.byref(oc), _ptr(r))
+    return r
+
+
+def shadow_mirror(nodes, depth, ids, tris, cam, light, prim, nthreads=None, stats=False):
+    oc = to_or_camera(cam)
+    npx = cam.width * cam.height
+    vis = np.zeros(npx, np.uint8)
+    mirror = np.zeros(npx, HIT_DTYPE)
+    ss = np.zeros((npx, 2), np.uint32) if stats else None
+    ms = np.zeros((npx, 2), np.uint32) if stats else None
+    olib().or_shadow_mirror(_ptr(nodes), depth, _ptr(ids), _ptr(np.ascontiguousarray(tris, np.float32)), C.byref(oc),
+                            _ptr(np.asarray(light, np.float32)), _ptr(np.ascontiguousarray(prim)), _ptr(vis),
+                            _ptr(mirror), _ptr(ss) if stats else None, _ptr(ms) if stats else None,
+                            nthreads or nthreads_default())
+    return (vis, mirror, ss, ms) if stats else (vis, mirror)
+
+
+def pathtrace(nodes, depth, ids, tris, albedo, emission, cam, spp, bounces, seed, sky=(1.0, 1.0, 1.0), nthreads=None):
+    oc = to_or_camera(cam)
+    p = OrPtParams(spp, bounces, seed, (C.c_float * 3)(*sky))
+    img = np.zeros((cam.height * cam.width, 4), np.float32)
+    olib().or_pathtrace(_ptr(nodes), depth, _ptr(ids), _ptr(np.ascontiguousarray(tris, np.float32)),
+                        _ptr(np.ascontiguousarray(albedo, np.float32)), _ptr(np.ascontiguousarray(emission, np.float32)),
+                        C.byref(oc), C.byref(p), _ptr(img), nthreads or nthreads_default())
+    return img
+
+
+def pathtrace_adjoint(nodes, depth, ids, tris, albedo, emission, cam, spp, bounces, seed, d_image,
+                      sky=(1.0, 1.0, 1.0), nthreads=None):
+    oc = to_or_camera(cam)
+    p = OrPtParams(spp, bounces, seed, (C.c_float * 3)(*sky))
+    da = np.zeros((len(tris), 3), np.float64)
+    de = np.zeros(3, np.float64)
+    olib().or_pathtrace_adjoint(_ptr(nodes), depth, _ptr(ids), _ptr(np.ascontiguousarray(tris, np.float32)),
+                                _ptr(np.ascontiguousarray(albedo, np.float32)),
+                                _ptr(np.ascontiguousarray(emission, np.float32)), C.byref(oc), C.byref(p),
+                                _ptr(np.ascontiguousarray(d_image, np.float32)), _ptr(da), _ptr(de),
+                                nthreads or nthreads_default())
+    return da, de
+
+
+def pcg32_first(initstate: int, initseq: int, count: int) -> np.ndarray:
+    out = np.zeros(count, np.uint32)
+    olib().or_pcg32_first(initstate, initseq, count, _ptr(out))
+    return out
+
+
+# --- the reference's own CPU code ------------------------------------------
+def ref_available() -> bool:
+    return REF_LIB.exists()
+
+
+def rlib() -> C.CDLL:
+    global _rlib
+    if _rlib is None:
+        L = C.CDLL(str(REF_LIB))
+        vp, i32 = C.c_void_p, C.c_int
+        L.ref_lbvh_create.argtypes = [vp, i32, i32, i32, C.POINTER(C.c_double)]
+        L.ref_lbvh_create.restype = vp
+        L.ref_bvh_create.argtypes = [vp, i32, i32, i32, C.POINTER(C.c_double)]
+        L.ref_bvh_create.restype = vp
+        L.ref_destroy.argtypes = [vp]
+        L.ref_num_elements.argtypes = [vp]
+        L.ref_num_elements.restype = C.c_uint
+        L.ref_element_size.argtypes = [vp]
+        L.ref_element_size.restype = C.c_uint
+        L.ref_copy_elements.argtypes = [vp, vp]
+        L.ref_copy_ids.argtypes = [vp, vp]
+        L.ref_world_bound.argtypes = [vp, vp]
+        L.ref_intersect.argtypes = [vp, vp, C.c_long, vp, vp, vp, vp, i32]
+        _rlib = L
+    return _rlib
+
+
+class RefStructure:
+    """The reference's LBVH (kind='lbvh') or SAH BVH (kind='bvh') over a soup."""
+
+    def __init__(self, tris: np.ndarray, kind: str = "lbvh", depth: int = 20, max_prims: int = 1):
+        self.tris = np.ascontiguousarray(tris, np.float32)
+        self.n = len(tris)
+        secs = C.c_double(0.0)
+        L = rlib()
+        if kind == "lbvh":
+            self.h = L.ref_lbvh_create(_ptr(self.tris), self.n, depth, 1, C.byref(secs))
+        else:
+            self.h = L.ref_bvh_create(_ptr(self.tris), self.n, max_prims, 1, C.byref(secs))
+        self.build_seconds = secs.value
+        self.kind = kind
+
+    def close(self):
+        if self.h:
+            rlib().ref_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def nodes(self) -> np.ndarray:
+        L = rlib()
+        n = L.ref_num_elements(self.h)
+        assert L.ref_element_size(self.h) == 32 or self.kind != "lbvh"
+        raw = np.zeros(n * L.ref_element_size(self.h), np.uint8)
+        L.ref_copy_elements(self.h, _ptr(raw))
+        return raw.view(NODE_DTYPE) if self.kind == "lbvh" else raw
+
+    def ids(self) -> np.ndarray:
+        out = np.zeros(self.n, np.uint32)
+        rlib().ref_copy_ids(self.h, _ptr(out))
+        return out
+
+    def world_bound(self) -> np.ndarray:
+        out = np.zeros(6, np.float32)
+        rlib().ref_world_bound(self.h, _ptr(out))
+        return out
+
+    def intersect(self, rays: np.ndarray, nthreads=None):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = len(rays)
+        hid = np.zeros(n, np.int32)
+        t = np.zeros(n, np.float32)
+        u = np.zeros(n, np.float32)
+        v = np.zeros(n, np.float32)
+        rlib().ref_intersect(self.h, _ptr(rays), n, _ptr(hid), _ptr(t), _ptr(u), _ptr(v), nthreads or nthreads_default())
+        return hid, t, u, v
+
+
+def reachable_mask(nodes: np.ndarray) -> np.ndarray:
+    """Heap slots reachable from the root of an LBVH node array (children of
+    internal nodes only; unreached slots of the reference are uninitialised)."""
+    m = np.zeros(len(nodes), bool)
+    if len(nodes) < 2:
+        return m
+    m[1] = True
+    leaf = (nodes["prim_count"] & 4) != 0
+    lo = 2
+    while lo < len(nodes):
+        hi = min(2 * lo, len(nodes))
+        par = np.arange(lo, hi) >> 1
+        m[lo:hi] = m[par] & ~leaf[par]
+        lo = hi
+    return m

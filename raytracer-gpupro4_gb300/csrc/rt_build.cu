@@ -1,0 +1,852 @@
+// rt_build.cu -- per-frame LBVH build on sm_103a.
+//
+// Replaces LBVH::Build (AccelerationStructures/LBVH/LBVH.cpp:488-632) and the
+// GPU stage StructureConstruction::GPUBuildStructure
+// (RayTracerCS/StructureConstruction.cpp:86-131: LBVH_PreBuild, bitonic sort,
+// one LBVH_Build dispatch per level, one LBVH_BuildAABB dispatch per level).
+//
+// Launch sequence (all on the context stream, no host synchronisation):
+//   k_bounds        scene AABB (last-block reduction) + scratch reset
+//   k_morton_hist   per-triangle centroid and 30-bit Morton code
+//                   (LBVH.cpp:512, 520-553) + the four 8-bit digit histograms
+//   k_onesweep x4   stable LSD radix sort of (code, id): warp-ballot digit
+//                   ranks, decoupled look-back over tiles, shared-memory
+//                   staged scatter.  Result = qsort(cmpMorton) order
+//                   (LBVH.cpp:21-38).
+//   k_emit_tiles    per-tile aggregates of the boundary "record masks"
+//   k_emit_prefix   tile prefixes (one warp)
+//   k_emit_leaves   heap index of every element's leaf, leaf ranges, and the
+//                   triangle pre-gather in sorted order
+//   k_emit_refit    leaf boxes, then an atomic bottom-up walk that writes
+//                   every internal node (parent = h/2, sibling = h^1)
+//
+// Tree = the reference's: LBVH::build_recursive (LBVH.cpp:190-314) splits a
+// sorted range at its highest differing Morton bit, keeps equal-code runs as
+// one leaf, stores node i's children at 2i and 2i+1 and turns every node at
+// heap index >= 2^(depth-1) into a leaf.  For boundary i between sorted
+// elements i and i+1 let delta_i be its highest differing bit (-1 for equal
+// codes).  The split bits on the root path of element k are exactly the
+// "records" of delta seen from k (boundaries whose delta exceeds every delta
+// between them and k), on both sides; a record mask (bit d set for a record
+// with delta d) is an associative scan, so every element's heap index
+// follows from two scans and its own code: depth = popcount(mask), index =
+// 1 followed by the code's bits at the mask positions, high to low.
+#include <algorithm>
+
+#include "rt_internal.cuh"
+
+namespace {
+
+constexpr uint32_t kFull = 0xffffffffu;
+
+__device__ __forceinline__ int hb(uint32_t x) { return 31 - __clz(x); }
+
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// ---------------------------------------------------------------------------
+// Record-mask operators.  A segment's forward mask holds the deltas that are
+// records when the segment is scanned from its right end; combining left
+// segment A with right segment B keeps B and the records of A above max(B)
+// (= highest bit of B).  The backward mask is the mirror image.
+__device__ __forceinline__ uint32_t keep_above(uint32_t m, int b) {
+    return (b < 0) ? m : (m & ~((2u << b) - 1u));
+}
+__device__ __forceinline__ uint32_t rec_fwd(uint32_t a, uint32_t b) {  // a left of b
+    return b ? (b | keep_above(a, hb(b))) : a;
+}
+__device__ __forceinline__ uint32_t rec_bwd(uint32_t a, uint32_t b) {  // a left of b
+    return a ? (a | keep_above(b, hb(a))) : b;
+}
+
+__device__ __forceinline__ int delta_of(uint32_t a, uint32_t b) { return (a == b) ? -1 : hb(a ^ b); }
+
+// ---------------------------------------------------------------------------
+// Morton quantisation (LBVH.cpp:538-540) and bit interleave (LBVH.cpp:541-552:
+// z bit j -> 3j, y bit j -> 3j+1, x bit j -> 3j+2, ten bits per axis).
+__device__ __forceinline__ uint32_t quantize(float c, float lo3, float f) {
+    float v = fmul(fsub(c, lo3), f);
+    if (!(v == v)) return 0u;                                   // NaN (flat axis)
+    if (v >= 2147483648.0f || v <= -2147483649.0f) return 0u;   // outside int range
+    return (uint32_t)__float2int_rz(v);
+}
+__device__ __forceinline__ uint32_t spread10(uint32_t x) {
+    x &= 0x3ffu;
+    x = (x | (x << 16)) & 0x030000ffu;
+    x = (x | (x << 8)) & 0x0300f00fu;
+    x = (x | (x << 4)) & 0x030c30c3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+// ---------------------------------------------------------------------------
+// k_bounds: min/max over all vertices (LBVH.cpp:495-516), last block folds the
+// per-block partials and derives the Morton parameters.  Also resets the
+// build's scratch (histograms, tile tickets, look-back words, leaf count) and
+// optionally writes the sentinel into every heap slot.
+__global__ void __launch_bounds__(256) k_bounds(const float* __restrict__ tris, uint32_t n, SceneInfo* scene,
+                                                float* partials, uint32_t* counters, uint32_t* hist,
+                                                uint32_t* lookback, uint32_t lookback_words, rt_node* nodes,
+                                                uint32_t num_nodes, int clear_nodes) {
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t gstride = gridDim.x * blockDim.x;
+
+    for (uint32_t i = gtid; i < 4 * 256; i += gstride) hist[i] = 0u;
+    for (uint32_t i = gtid; i < lookback_words; i += gstride) lookback[i] = 0u;
+    if (gtid >= 1 && gtid < 8) counters[gtid] = 0u;
+    if (clear_nodes) {
+        for (uint32_t i = gtid; i < num_nodes; i += gstride) {
+            rt_node s;
+            s.min[0] = s.min[1] = s.min[2] = 0.0f;
+            s.max[0] = s.max[1] = s.max[2] = 0.0f;
+            s.prim_count = RT_NODE_SENTINEL;
+            s.prim_pos = RT_NODE_SENTINEL;
+            nodes[i] = s;
+        }
+    }
+
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    uint32_t bad = 0;
+    const uint32_t nv = 3u * n;
+    for (uint32_t v = gtid; v < nv; v += gstride) {
+        const float x = __ldg(tris + 3 * (size_t)v + 0), y = __ldg(tris + 3 * (size_t)v + 1),
+                    z = __ldg(tris + 3 * (size_t)v + 2);
+        bad |= !(isfinite(x) && isfinite(y) && isfinite(z));
+        mn[0] = fminf(mn[0], x); mn[1] = fminf(mn[1], y); mn[2] = fminf(mn[2], z);
+        mx[0] = fmaxf(mx[0], x); mx[1] = fmaxf(mx[1], y); mx[2] = fmaxf(mx[2], z);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        for (int c = 0; c < 3; ++c) {
+            mn[c] = fminf(mn[c], __shfl_xor_sync(kFull, mn[c], off));
+            mx[c] = fmaxf(mx[c], __shfl_xor_sync(kFull, mx[c], off));
+        }
+        bad |= __shfl_xor_sync(kFull, bad, off);
+    }
+    __shared__ float s_red[8][7];
+    __shared__ bool s_last;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        for (int c = 0; c < 3; ++c) { s_red[w][c] = mn[c]; s_red[w][3 + c] = mx[c]; }
+        s_red[w][6] = bad ? 1.0f : 0.0f;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float r[7];
+        for (int q = 0; q < 7; ++q) r[q] = s_red[0][q];
+        for (int ww = 1; ww < 8; ++ww) {
+            for (int c = 0; c < 3; ++c) { r[c] = fminf(r[c], s_red[ww][c]); r[3 + c] = fmaxf(r[3 + c], s_red[ww][3 + c]); }
+            r[6] = fmaxf(r[6], s_red[ww][6]);
+        }
+        for (int q = 0; q < 7; ++q) partials[8 * blockIdx.x + q] = r[q];
+        __threadfence();
+        const uint32_t ticket = atomicAdd(&counters[0], 1u);
+        s_last = (ticket == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    if (threadIdx.x == 0) {
+        float r[7];
+        for (int q = 0; q < 7; ++q) r[q] = __ldcg(partials + q);
+        for (uint32_t b = 1; b < gridDim.x; ++b) {
+            for (int c = 0; c < 3; ++c) {
+                r[c] = fminf(r[c], __ldcg(partials + 8 * b + c));
+                r[3 + c] = fmaxf(r[3 + c], __ldcg(partials + 8 * b + 3 + c));
+            }
+            r[6] = fmaxf(r[6], __ldcg(partials + 8 * b + 6));
+        }
+        SceneInfo s;
+        for (int c = 0; c < 3; ++c) {
+            s.bmin[c] = r[c];
+            s.bmax[c] = r[3 + c];
+            const float mx3 = fmul(3.0f, r[3 + c]);   // VertMax = 3.0f*VertMax (LBVH.cpp:521)
+            s.lo3[c] = fmul(3.0f, r[c]);             // VertMin = 3.0f*VertMin (:522)
+            s.f[c] = fdiv(1024.0f, fsub(mx3, s.lo3[c]));  // (:523-526)
+        }
+        s.nonfinite = r[6] != 0.0f;
+        s.pad[0] = s.pad[1] = s.pad[2] = 0;
+        *scene = s;
+        counters[0] = 0u;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_morton_hist: codes + ids, and the per-pass digit histograms for the
+// radix sort (block-local, warp-aggregated, then one global add per bin).
+constexpr int kMortonThreads = 512;
+
+__global__ void __launch_bounds__(kMortonThreads) k_morton_hist(const float* __restrict__ tris, uint32_t n,
+                                                                const SceneInfo* __restrict__ scene,
+                                                                uint32_t* __restrict__ keys,
+                                                                uint32_t* __restrict__ ids, uint32_t* hist,
+                                                                uint32_t* err) {
+    __shared__ float s_tri[kMortonThreads * 9];
+    __shared__ uint32_t s_hist[4][256];
+    for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0u;
+    const SceneInfo sc = *scene;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && sc.nonfinite) atomicOr(err, RT_DEVERR_NONFINITE);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    for (uint32_t base = blockIdx.x * kMortonThreads; base < n; base += gridDim.x * kMortonThreads) {
+        const uint32_t cnt = min((uint32_t)kMortonThreads, n - base);
+        const float* src = tris + 9 * (size_t)base;
+        for (uint32_t q = threadIdx.x; q < 9 * cnt; q += kMortonThreads) s_tri[q] = __ldg(src + q);
+        __syncthreads();
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = threadIdx.x < cnt;
+        uint32_t code = 0;
+        if (valid) {
+            const float* t = s_tri + 9 * threadIdx.x;
+            uint32_t q[3];
+            for (int c = 0; c < 3; ++c) {
+                const float cen = fadd(fadd(t[c], t[3 + c]), t[6 + c]);  // (V0 + V1) + V2 (LBVH.cpp:512)
+                q[c] = quantize(cen, sc.lo3[c], sc.f[c]);
+            }
+            code = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+            keys[i] = code;
+            ids[i] = i;
+        }
+        const uint32_t vm = __ballot_sync(kFull, valid);
+        if (valid) {
+#pragma unroll
+            for (int p = 0; p < kSortPasses; ++p) {
+                const uint32_t d = (code >> (8 * p)) & 0xffu;
+                const uint32_t peers = __match_any_sync(vm, d);
+                if (lane == __ffs(peers) - 1) atomicAdd(&s_hist[p][d], (uint32_t)__popc(peers));
+            }
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) {
+        const uint32_t v = (&s_hist[0][0])[i];
+        if (v) atomicAdd(&hist[i], v);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Block-wide exclusive sum over 256 threads (one value each).
+__device__ __forceinline__ uint32_t block_excl_sum_256(uint32_t v, uint32_t* s_tmp /*8*/) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) s_tmp[w] = x;
+    __syncthreads();
+    uint32_t wp = 0;
+    for (int q = 0; q < w; ++q) wp += s_tmp[q];
+    __syncthreads();
+    return wp + x - v;
+}
+
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagInc = 2u << 30;
+constexpr uint32_t kFlagMask = 3u << 30;
+constexpr uint32_t kValMask = (1u << 30) - 1u;
+
+// k_onesweep: one LSD pass over 8 bits.  Each CTA takes the next tile ticket
+// (so every tile it waits on belongs to a CTA that is already running),
+// ranks its keys stably per digit with warp ballots, publishes its digit
+// counts, looks back over earlier tiles for the global digit offsets, and
+// scatters through shared memory so that each digit's run is written
+// contiguously.
+__global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __restrict__ keys_in,
+                                                           const uint32_t* __restrict__ ids_in,
+                                                           uint32_t* __restrict__ keys_out,
+                                                           uint32_t* __restrict__ ids_out, uint32_t n, int pass,
+                                                           const uint32_t* __restrict__ hist, uint32_t* lookback,
+                                                           uint32_t* tile_counter, uint32_t* err) {
+    __shared__ uint32_t s_keys[kSortTile];
+    __shared__ uint32_t s_ids[kSortTile];
+    __shared__ uint32_t s_warp[kSortThreads / 32][256];
+    __shared__ uint32_t s_lstart[256];
+    __shared__ uint32_t s_gofs[256];
+    __shared__ uint32_t s_tmp[8];
+    __shared__ uint32_t s_tile;
+
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    if (t == 0) s_tile = atomicAdd(tile_counter, 1u);
+    for (int i = lane; i < 256; i += 32) s_warp[w][i] = 0u;
+    const uint32_t gbase = block_excl_sum_256(hist[pass * 256 + t], s_tmp);  // includes __syncthreads
+    const uint32_t tile = s_tile;
+    const uint32_t base = tile * (uint32_t)kSortTile;
+    const int shift = 8 * pass;
+
+    uint32_t key[kSortItems], idv[kSortItems], rank[kSortItems];
+#pragma unroll
+    for (int i = 0; i < kSortItems; ++i) {
+        const uint32_t idx = base + w * (32 * kSortItems) + i * 32 + lane;
+        const bool valid = idx < n;
+        key[i] = valid ? keys_in[idx] : 0xffffffffu;
+        idv[i] = valid ? ids_in[idx] : 0u;
+    }
+    const uint32_t lt = lanemask_lt();
+#pragma unroll
+    for (int i = 0; i < kSortItems; ++i) {
+        const uint32_t idx = base + w * (32 * kSortItems) + i * 32 + lane;
+        const bool valid = idx < n;
+        const uint32_t d = (key[i] >> shift) & 0xffu;
+        uint32_t peers = __ballot_sync(kFull, valid);
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            const bool bit = (d >> b) & 1u;
+            const uint32_t m = __ballot_sync(kFull, bit);
+            peers &= bit ? m : ~m;
+        }
+        const uint32_t cnt = s_warp[w][d];
+        __syncwarp();
+        if (valid && lane == __ffs(peers) - 1) s_warp[w][d] = cnt + __popc(peers);
+        rank[i] = cnt + __popc(peers & lt);
+        __syncwarp();
+    }
+    __syncthreads();
+
+    // digit t: per-warp exclusive prefixes and the tile count
+    uint32_t run = 0;
+#pragma unroll
+    for (int ww = 0; ww < kSortThreads / 32; ++ww) {
+        const uint32_t c = s_warp[ww][t];
+        s_warp[ww][t] = run;
+        run += c;
+    }
+    const uint32_t count = run;
+
+    // decoupled look-back (bounded)
+    uint32_t* my = lookback + (size_t)tile * 256 + t;
+    st_relaxed(my, (tile == 0 ? kFlagInc : kFlagAgg) | count);
+    uint32_t excl = 0;
+    if (tile > 0) {
+        int p = (int)tile - 1;
+        uint32_t spins = 0;
+        while (p >= 0) {
+            const uint32_t v = ld_relaxed(lookback + (size_t)p * 256 + t);
+            const uint32_t f = v & kFlagMask;
+            if (f == 0u) {
+                if (++spins > kSpinLimit) {
+                    atomicOr(err, RT_DEVERR_TIMEOUT);
+                    break;
+                }
+                continue;
+            }
+            excl += v & kValMask;
+            if (f == kFlagInc) break;
+            --p;
+        }
+        st_relaxed(my, kFlagInc | (excl + count));
+    }
+
+    const uint32_t lstart = block_excl_sum_256(count, s_tmp);
+    s_lstart[t] = lstart;
+    s_gofs[t] = gbase + excl - lstart;
+    __syncthreads();
+
+#pragma unroll
+    for (int i = 0; i < kSortItems; ++i) {
+        const uint32_t idx = base + w * (32 * kSortItems) + i * 32 + lane;
+        if (idx < n) {
+            const uint32_t d = (key[i] >> shift) & 0xffu;
+            const uint32_t pos = s_lstart[d] + s_warp[w][d] + rank[i];
+            if (pos < (uint32_t)kSortTile) {
+                s_keys[pos] = key[i];
+                s_ids[pos] = idv[i];
+            } else {
+                atomicOr(err, RT_DEVERR_BOUNDS);
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t tile_n = (n - base < (uint32_t)kSortTile) ? (n - base) : (uint32_t)kSortTile;
+    for (uint32_t j = t; j < tile_n; j += kSortThreads) {
+        const uint32_t k = s_keys[j];
+        const uint32_t gp = s_gofs[(k >> shift) & 0xffu] + j;
+        if (gp < n) {
+            keys_out[gp] = k;
+            ids_out[gp] = s_ids[j];
+        } else {
+            atomicOr(err, RT_DEVERR_BOUNDS);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Ordered (non-commutative) reductions / scans of record masks.
+template <bool FWD>
+__device__ __forceinline__ uint32_t rec_op(uint32_t a, uint32_t b) {
+    return FWD ? rec_fwd(a, b) : rec_bwd(a, b);
+}
+
+// Warp reduction in lane order; lane 0 receives op(v_0, v_1, ..., v_31).
+template <bool FWD>
+__device__ __forceinline__ uint32_t warp_reduce_ordered(uint32_t v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t o = __shfl_down_sync(kFull, v, off);
+        if (lane + off < 32) v = rec_op<FWD>(v, o);
+    }
+    return v;
+}
+
+// Block-wide exclusive prefix (fwd, from the left) and exclusive suffix
+// (bwd, from the right) of one value pair per thread, 256 threads.
+__device__ __forceinline__ void block_scan_records(uint32_t vf, uint32_t vb, uint32_t* pre_f, uint32_t* suf_b,
+                                                   uint32_t* s_f /*8*/, uint32_t* s_b /*8*/) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t xf = vf;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, xf, off);
+        if (lane >= off) xf = rec_fwd(y, xf);
+    }
+    uint32_t xb = vb;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_down_sync(kFull, xb, off);
+        if (lane + off < 32) xb = rec_bwd(xb, y);
+    }
+    if (lane == 31) s_f[w] = xf;  // inclusive fwd total of the warp
+    if (lane == 0) s_b[w] = xb;   // inclusive bwd total of the warp
+    __syncthreads();
+    uint32_t wf = 0, wb = 0;
+    for (int q = 0; q < w; ++q) wf = rec_fwd(wf, s_f[q]);
+    for (int q = (kEmitThreads / 32) - 1; q > w; --q) wb = rec_bwd(s_b[q], wb);
+    __syncthreads();
+    uint32_t ef = __shfl_up_sync(kFull, xf, 1);
+    if (lane == 0) ef = 0;
+    uint32_t eb = __shfl_down_sync(kFull, xb, 1);
+    if (lane == 31) eb = 0;
+    *pre_f = rec_fwd(wf, ef);
+    *suf_b = rec_bwd(eb, wb);
+}
+
+// Loads the codes a thread needs and its boundary record bits.
+struct EmitChunk {
+    uint32_t c[kEmitItems + 1];  // codes of elements s .. s+8 (0 beyond n)
+    uint32_t r[kEmitItems];      // record bit of boundaries s .. s+7
+    int dl[kEmitItems + 1];      // delta of boundaries s-1 .. s+7 (dl[q] = delta_{s+q-1})
+};
+
+__device__ __forceinline__ void load_chunk(const uint32_t* __restrict__ keys, uint32_t n, uint32_t s, EmitChunk& e) {
+    uint32_t prev = (s >= 1 && s - 1 < n) ? __ldg(keys + s - 1) : 0u;
+#pragma unroll
+    for (int q = 0; q <= kEmitItems; ++q) e.c[q] = (s + q < n) ? __ldg(keys + s + q) : 0u;
+    e.dl[0] = (s >= 1 && s < n) ? delta_of(prev, e.c[0]) : -1;
+#pragma unroll
+    for (int q = 0; q < kEmitItems; ++q) {
+        const uint32_t i = s + q;  // boundary i between i and i+1
+        const int d = (i + 1 < n) ? delta_of(e.c[q], e.c[q + 1]) : -1;
+        e.dl[q + 1] = d;
+        e.r[q] = (d >= 0) ? (1u << d) : 0u;
+    }
+}
+
+// k_emit_tiles: per-tile fwd/bwd aggregates of the boundary record masks.
+__global__ void __launch_bounds__(kEmitThreads) k_emit_tiles(const uint32_t* __restrict__ keys, uint32_t n,
+                                                             uint32_t* scan) {
+    __shared__ uint32_t s_f[8], s_b[8];
+    const uint32_t s = blockIdx.x * kEmitTile + threadIdx.x * kEmitItems;
+    EmitChunk e;
+    load_chunk(keys, n, s, e);
+    uint32_t af = 0, ab = 0;
+#pragma unroll
+    for (int q = 0; q < kEmitItems; ++q) af = rec_fwd(af, e.r[q]);
+#pragma unroll
+    for (int q = kEmitItems - 1; q >= 0; --q) ab = rec_bwd(e.r[q], ab);
+    af = warp_reduce_ordered<true>(af);
+    ab = warp_reduce_ordered<false>(ab);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) { s_f[w] = af; s_b[w] = ab; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t tf = 0, tb = 0;
+        for (int q = 0; q < kEmitThreads / 32; ++q) tf = rec_fwd(tf, s_f[q]);
+        for (int q = kEmitThreads / 32 - 1; q >= 0; --q) tb = rec_bwd(s_b[q], tb);
+        scan[4 * blockIdx.x + 0] = tf;
+        scan[4 * blockIdx.x + 1] = tb;
+    }
+}
+
+// k_emit_prefix: exclusive fwd prefix / bwd suffix over the tiles (one warp).
+__global__ void k_emit_prefix(uint32_t* scan, uint32_t tiles) {
+    const int lane = threadIdx.x;
+    const uint32_t per = (tiles + 31) / 32;
+    const uint32_t lo = min(tiles, lane * per), hi = min(tiles, lo + per);
+    uint32_t af = 0, ab = 0;
+    for (uint32_t t = lo; t < hi; ++t) af = rec_fwd(af, scan[4 * t + 0]);
+    for (uint32_t t = hi; t > lo; --t) ab = rec_bwd(scan[4 * (t - 1) + 1], ab);
+    uint32_t xf = af, xb = ab;
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, xf, off);
+        if (lane >= off) xf = rec_fwd(y, xf);
+        const uint32_t z = __shfl_down_sync(kFull, xb, off);
+        if (lane + off < 32) xb = rec_bwd(xb, z);
+    }
+    uint32_t ef = __shfl_up_sync(kFull, xf, 1);
+    if (lane == 0) ef = 0;
+    uint32_t eb = __shfl_down_sync(kFull, xb, 1);
+    if (lane == 31) eb = 0;
+    uint32_t run = ef;
+    for (uint32_t t = lo; t < hi; ++t) {
+        const uint32_t a = scan[4 * t + 0];
+        scan[4 * t + 2] = run;
+        run = rec_fwd(run, a);
+    }
+    run = eb;
+    for (uint32_t t = hi; t > lo; --t) {
+        const uint32_t a = scan[4 * (t - 1) + 1];
+        scan[4 * (t - 1) + 3] = run;
+        run = rec_bwd(a, run);
+    }
+}
+
+// k_emit_leaves: for every sorted element k, the heap index of the leaf that
+// holds it (capped at depth-1), whether it opens / closes that leaf's range,
+// and the triangle pre-gather in sorted order.
+__global__ void __launch_bounds__(kEmitThreads) k_emit_leaves(const uint32_t* __restrict__ keys,
+                                                              const uint32_t* __restrict__ ids,
+                                                              const float* __restrict__ tris, uint32_t n,
+                                                              uint32_t depth, const uint32_t* __restrict__ scan,
+                                                              rt_node* nodes, float4* __restrict__ sorted_tris,
+                                                              uint32_t* leaf_list, uint32_t* leaf_count) {
+    __shared__ uint32_t s_f[8], s_b[8];
+    const uint32_t s = blockIdx.x * kEmitTile + threadIdx.x * kEmitItems;
+    EmitChunk e;
+    load_chunk(keys, n, s, e);
+    uint32_t af = 0, ab = 0;
+#pragma unroll
+    for (int q = 0; q < kEmitItems; ++q) af = rec_fwd(af, e.r[q]);
+#pragma unroll
+    for (int q = kEmitItems - 1; q >= 0; --q) ab = rec_bwd(e.r[q], ab);
+    uint32_t pre, suf;
+    block_scan_records(af, ab, &pre, &suf, s_f, s_b);
+    const uint32_t tile_pre = scan[4 * blockIdx.x + 2];
+    const uint32_t tile_suf = scan[4 * blockIdx.x + 3];
+    uint32_t L[kEmitItems + 1], R[kEmitItems + 1];
+    L[0] = rec_fwd(tile_pre, pre);   // records of boundaries 0 .. s-1
+    R[kEmitItems] = rec_bwd(suf, tile_suf);  // records of boundaries s+8 .. n-2
+#pragma unroll
+    for (int q = 0; q < kEmitItems; ++q) L[q + 1] = rec_fwd(L[q], e.r[q]);
+#pragma unroll
+    for (int q = kEmitItems - 1; q >= 0; --q) R[q] = rec_bwd(e.r[q], R[q + 1]);
+
+    const int leaf_depth = (int)depth - 1;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int q = 0; q < kEmitItems; ++q) {
+        const uint32_t k = s + q;
+        const bool valid = k < n;
+        bool head = false;
+        uint32_t h = 0;
+        if (valid) {
+            const uint32_t anc = L[q] | R[q];
+            const uint32_t code = e.c[q];
+            int dep = __popc(anc);
+            uint32_t m = anc;
+            while (dep > leaf_depth) { m &= m - 1u; --dep; }
+            h = 1u;
+            while (m) {
+                const int b = hb(m);
+                h = (h << 1) | ((code >> b) & 1u);
+                m ^= 1u << b;
+            }
+            const int dprev = e.dl[q], dcur = e.dl[q + 1];
+            head = (k == 0) || (dprev >= 0 && __popc(keep_above(anc, dprev)) < leaf_depth);
+            const bool tail = (k == n - 1) || (dcur >= 0 && __popc(keep_above(anc, dcur)) < leaf_depth);
+            if (head) nodes[h].prim_pos = (int32_t)k;
+            if (tail) nodes[h].prim_count = (int32_t)k;  // range end; k_emit_refit finalises the field
+            // pre-gather in sorted order: A.xyz,id | B.xyz,0 | C.xyz,0
+            const uint32_t id = __ldg(ids + k);
+            const float* tp = tris + 9 * (size_t)id;
+            float v[9];
+#pragma unroll
+            for (int c = 0; c < 9; ++c) v[c] = __ldg(tp + c);
+            sorted_tris[3 * (size_t)k + 0] = make_float4(v[0], v[1], v[2], __int_as_float((int)id));
+            sorted_tris[3 * (size_t)k + 1] = make_float4(v[3], v[4], v[5], 0.0f);
+            sorted_tris[3 * (size_t)k + 2] = make_float4(v[6], v[7], v[8], 0.0f);
+        }
+        // warp-aggregated append of the leaves opened here
+        const uint32_t hm = __ballot_sync(kFull, head);
+        uint32_t basei = 0;
+        if (lane == 0 && hm) basei = atomicAdd(leaf_count, (uint32_t)__popc(hm));
+        basei = __shfl_sync(kFull, basei, 0);
+        if (head) leaf_list[basei + __popc(hm & lanemask_lt())] = h;
+    }
+}
+
+// k_emit_refit: leaf fields and boxes (LBVH.cpp:194-208 / LBVH.hlsl:240-258),
+// then the bottom-up walk: the second of two siblings to arrive at a parent
+// writes it (LBVH.cpp:310-313 / LBVH.hlsl:260-269).  Arrival words carry the
+// build epoch, so they never need clearing.
+__global__ void __launch_bounds__(256) k_emit_refit(const uint32_t* __restrict__ keys, const float4* sorted_tris,
+                                                    uint32_t n, uint32_t depth, rt_node* nodes,
+                                                    const uint32_t* __restrict__ leaf_list,
+                                                    const uint32_t* leaf_count, uint32_t* arrive,
+                                                    uint32_t epoch, uint32_t* err) {
+    const uint32_t nleaves = min(*leaf_count, n);
+    for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < nleaves; li += gridDim.x * blockDim.x) {
+        uint32_t h = leaf_list[li];
+        const int32_t pos = __ldcg(&nodes[h].prim_pos);
+        const int32_t end = __ldcg(&nodes[h].prim_count);
+        const int32_t count = end - pos + 1;
+        if (pos < 0 || end < pos || (uint32_t)end >= n || h >= (1u << depth)) {
+            atomicOr(err, RT_DEVERR_BOUNDS);
+            continue;
+        }
+        float mn[3], mx[3];
+        for (int32_t j = pos; j <= end; ++j) {
+            const float4 a = __ldg(sorted_tris + 3 * (size_t)j), b = __ldg(sorted_tris + 3 * (size_t)j + 1),
+                         c = __ldg(sorted_tris + 3 * (size_t)j + 2);
+            const float lo[3] = {fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z))};
+            const float hi[3] = {fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z))};
+            if (j == pos) {
+                for (int q = 0; q < 3; ++q) { mn[q] = lo[q]; mx[q] = hi[q]; }
+            } else {
+                for (int q = 0; q < 3; ++q) { mn[q] = fminf(mn[q], lo[q]); mx[q] = fmaxf(mx[q], hi[q]); }
+            }
+        }
+        // leaf axis = the reference's round-robin counter at the call that made
+        // the leaf: entry with bit (d_parent - 1) -> (31 - d_parent) % 3; a run
+        // of equal codes recursed down to bit 0 -> 1; the root enters at bit 30.
+        const int dh = 31 - __clz(h);
+        int axis;
+        if (dh == 0) {
+            axis = (count <= 1 || depth <= 1) ? 0 : 1;
+        } else if (count == 1 || dh == (int)depth - 1) {
+            const uint32_t a = (h & 1u) ? __ldg(keys + pos - 1) : __ldg(keys + end);
+            const uint32_t b = (h & 1u) ? __ldg(keys + pos) : __ldg(keys + end + 1);
+            axis = (31 - hb(a ^ b)) % 3;
+        } else {
+            axis = 1;
+        }
+        rt_node nd;
+        for (int q = 0; q < 3; ++q) { nd.min[q] = mn[q]; nd.max[q] = mx[q]; }
+        nd.prim_count = (count << 3) | 4 | axis;
+        nd.prim_pos = pos;
+        nodes[h] = nd;
+        while (h > 1) {
+            __threadfence();
+            const uint32_t old = atomicExch(&arrive[h >> 1], epoch);
+            if (old != epoch) break;  // first of the two children: the sibling finishes the parent
+            __threadfence();
+            const uint32_t sib = h ^ 1u;
+            const float4 s0 = __ldcg(reinterpret_cast<const float4*>(&nodes[sib]));
+            const float4 s1 = __ldcg(reinterpret_cast<const float4*>(&nodes[sib]) + 1);
+            const float smn[3] = {s0.x, s0.y, s0.z}, smx[3] = {s0.w, s1.x, s1.y};
+            const int32_t scount = __float_as_int(s1.z) >> 3, spos = __float_as_int(s1.w);
+            const int32_t lpos = (h & 1u) ? spos : nd.prim_pos;
+            const int32_t rpos = (h & 1u) ? nd.prim_pos : spos;
+            const int32_t pcount = (nd.prim_count >> 3) + scount;
+            if (rpos < 1 || (uint32_t)rpos >= n) {
+                atomicOr(err, RT_DEVERR_BOUNDS);
+                break;
+            }
+            const int d = hb(__ldg(keys + rpos - 1) ^ __ldg(keys + rpos));
+            for (int q = 0; q < 3; ++q) { nd.min[q] = fminf(nd.min[q], smn[q]); nd.max[q] = fmaxf(nd.max[q], smx[q]); }
+            nd.prim_count = (pcount << 3) | ((30 - d) % 3);
+            nd.prim_pos = lpos;
+            h >>= 1;
+            nodes[h] = nd;
+        }
+    }
+}
+
+// Pre-gather for imported trees (ids + soup uploaded from the host).
+__global__ void k_gather_tris(const uint32_t* __restrict__ ids, const float* __restrict__ tris, uint32_t n,
+                              float4* __restrict__ sorted_tris) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const uint32_t id = ids[k];
+        const float* tp = tris + 9 * (size_t)id;
+        sorted_tris[3 * (size_t)k + 0] = make_float4(tp[0], tp[1], tp[2], __int_as_float((int)id));
+        sorted_tris[3 * (size_t)k + 1] = make_float4(tp[3], tp[4], tp[5], 0.0f);
+        sorted_tris[3 * (size_t)k + 2] = make_float4(tp[6], tp[7], tp[8], 0.0f);
+    }
+}
+
+uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+extern "C" rt_status rt_lbvh_create(rt_ctx* ctx, uint32_t max_tris, uint32_t depth, rt_lbvh** out) {
+    if (!ctx || !out) return RT_ERR_INVALID;
+    *out = nullptr;
+    if (max_tris == 0 || max_tris > kMaxTris)
+        return rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_create: max_tris must be in [1, %u]", kMaxTris);
+    if (depth < 1 || depth > (uint32_t)kMaxDepth)
+        return rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_create: depth must be in [1, %d]", kMaxDepth);
+    RT_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+    rt_lbvh* l = new rt_lbvh();
+    l->cap = max_tris;
+    l->depth = depth;
+    l->num_nodes = 1u << depth;
+    l->sort_tiles_cap = ceil_div(max_tris, kSortTile);
+    l->emit_tiles_cap = ceil_div(max_tris, kEmitTile);
+    l->bounds_blocks = std::max(1u, std::min(ceil_div(3ull * max_tris, 256), (uint32_t)ctx->num_sms * 4));
+    const size_t cap = max_tris;
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](void** p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+    };
+    alloc((void**)&l->nodes, sizeof(rt_node) * l->num_nodes);
+    alloc((void**)&l->keys, 4 * cap);
+    alloc((void**)&l->ids, 4 * cap);
+    alloc((void**)&l->keys_alt, 4 * cap);
+    alloc((void**)&l->ids_alt, 4 * cap);
+    alloc((void**)&l->sorted_tris, sizeof(float4) * 3 * cap);
+    alloc((void**)&l->tris, sizeof(float) * 9 * cap);
+    alloc((void**)&l->scene, sizeof(SceneInfo));
+    alloc((void**)&l->partials, sizeof(float) * 8 * l->bounds_blocks);
+    alloc((void**)&l->counters, sizeof(uint32_t) * 8);
+    alloc((void**)&l->hist, sizeof(uint32_t) * 4 * 256);
+    alloc((void**)&l->lookback, sizeof(uint32_t) * kSortPasses * 256 * (size_t)l->sort_tiles_cap);
+    alloc((void**)&l->scan, sizeof(uint32_t) * 4 * (size_t)l->emit_tiles_cap);
+    alloc((void**)&l->leaf_list, 4 * cap);
+    alloc((void**)&l->arrive, sizeof(uint32_t) * std::max(1u, l->num_nodes >> 1));
+    if (e == cudaSuccess) e = cudaMemset(l->counters, 0, sizeof(uint32_t) * 8);
+    if (e == cudaSuccess) e = cudaMemset(l->arrive, 0, sizeof(uint32_t) * std::max(1u, l->num_nodes >> 1));
+    if (e == cudaSuccess) e = cudaMemset(l->nodes, 0, sizeof(rt_node) * l->num_nodes);
+    if (e != cudaSuccess) {
+        rt_lbvh_destroy(l);
+        return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_create: allocation failed: %s", cudaGetErrorString(e));
+    }
+    *out = l;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_lbvh_destroy(rt_lbvh* l) {
+    if (!l) return RT_OK;
+    void* ptrs[] = {l->nodes,    l->keys,     l->ids,      l->keys_alt,  l->ids_alt, l->sorted_tris,
+                    l->tris,     l->scene,    l->partials, l->counters,  l->hist,    l->lookback,
+                    l->scan,     l->leaf_list, l->arrive,  l->f_primary, l->f_mirror, l->f_vis};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete l;
+    return RT_OK;
+}
+
+static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint32_t n, uint32_t flags) {
+    cudaStream_t st = ctx->stream;
+    l->n = n;
+    l->src_tris = d_tris;
+    if (++l->epoch == 0) {  // wrapped: arrival words must be cleared once
+        RT_CHECK_CUDA(ctx, cudaMemsetAsync(l->arrive, 0, sizeof(uint32_t) * std::max(1u, l->num_nodes >> 1), st));
+        l->epoch = 1;
+    }
+    const uint32_t sort_tiles = ceil_div(n, kSortTile);
+    const uint32_t emit_tiles = ceil_div(n, kEmitTile);
+    const uint32_t lb_words = kSortPasses * 256 * sort_tiles;
+    const uint32_t bblocks = std::max(1u, std::min(ceil_div(3ull * n, 256), l->bounds_blocks));
+    k_bounds<<<bblocks, 256, 0, st>>>(d_tris, n, l->scene, l->partials, l->counters, l->hist, l->lookback,
+                                      lb_words, l->nodes, l->num_nodes, (flags & RT_BUILD_CLEAR_UNREACHED) ? 1 : 0);
+    RT_CHECK_LAUNCH(ctx, "k_bounds");
+    const uint32_t mblocks = std::max(1u, std::min(ceil_div(n, kMortonThreads), (uint32_t)ctx->num_sms * 2));
+    k_morton_hist<<<mblocks, kMortonThreads, 0, st>>>(d_tris, n, l->scene, l->keys, l->ids, l->hist, ctx->d_err);
+    RT_CHECK_LAUNCH(ctx, "k_morton_hist");
+    uint32_t *kin = l->keys, *iin = l->ids, *kout = l->keys_alt, *iout = l->ids_alt;
+    for (int p = 0; p < kSortPasses; ++p) {
+        k_onesweep<<<sort_tiles, kSortThreads, 0, st>>>(kin, iin, kout, iout, n, p, l->hist,
+                                                        l->lookback + (size_t)p * 256 * sort_tiles,
+                                                        l->counters + 1 + p, ctx->d_err);
+        RT_CHECK_LAUNCH(ctx, "k_onesweep");
+        std::swap(kin, kout);
+        std::swap(iin, iout);
+    }
+    // four passes: sorted pairs are back in keys / ids
+    k_emit_tiles<<<emit_tiles, kEmitThreads, 0, st>>>(l->keys, n, l->scan);
+    RT_CHECK_LAUNCH(ctx, "k_emit_tiles");
+    k_emit_prefix<<<1, 32, 0, st>>>(l->scan, emit_tiles);
+    RT_CHECK_LAUNCH(ctx, "k_emit_prefix");
+    k_emit_leaves<<<emit_tiles, kEmitThreads, 0, st>>>(l->keys, l->ids, d_tris, n, l->depth, l->scan, l->nodes,
+                                                       l->sorted_tris, l->leaf_list, l->counters + 5);
+    RT_CHECK_LAUNCH(ctx, "k_emit_leaves");
+    const uint32_t rblocks = std::max(1u, std::min(ceil_div(n, 256), (uint32_t)ctx->num_sms * 8));
+    k_emit_refit<<<rblocks, 256, 0, st>>>(l->keys, l->sorted_tris, n, l->depth, l->nodes, l->leaf_list,
+                                          l->counters + 5, l->arrive, l->epoch, ctx->d_err);
+    RT_CHECK_LAUNCH(ctx, "k_emit_refit");
+    l->built_keys = true;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_lbvh_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint32_t n, uint32_t flags) {
+    if (!ctx || !l || !d_tris) return ctx ? rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_build: null argument") : RT_ERR_INVALID;
+    if (n == 0) return rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_build: n must be > 0");
+    if (n > l->cap) return rt_fail(ctx, RT_ERR_CAPACITY, "rt_lbvh_build: n=%u exceeds capacity %u", n, l->cap);
+    return launch_build(ctx, l, d_tris, n, flags);
+}
+
+extern "C" rt_status rt_lbvh_build_host(rt_ctx* ctx, rt_lbvh* l, const float* h_tris, uint32_t n, uint32_t flags) {
+    if (!ctx || !l || !h_tris) return ctx ? rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_build_host: null argument") : RT_ERR_INVALID;
+    if (n == 0) return rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_build_host: n must be > 0");
+    if (n > l->cap) return rt_fail(ctx, RT_ERR_CAPACITY, "rt_lbvh_build_host: n=%u exceeds capacity %u", n, l->cap);
+    RT_CHECK_CUDA(ctx, cudaMemcpyAsync(l->tris, h_tris, sizeof(float) * 9 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+    return launch_build(ctx, l, l->tris, n, flags);
+}
+
+extern "C" rt_status rt_lbvh_import_host(rt_ctx* ctx, rt_lbvh* l, const rt_node* h_nodes, const uint32_t* h_ids,
+                                         const float* h_tris, uint32_t n) {
+    if (!ctx || !l || !h_nodes || !h_ids || !h_tris)
+        return ctx ? rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_import_host: null argument") : RT_ERR_INVALID;
+    if (n == 0) return rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_import_host: n must be > 0");
+    if (n > l->cap) return rt_fail(ctx, RT_ERR_CAPACITY, "rt_lbvh_import_host: n=%u exceeds capacity %u", n, l->cap);
+    cudaStream_t st = ctx->stream;
+    RT_CHECK_CUDA(ctx, cudaMemcpyAsync(l->nodes, h_nodes, sizeof(rt_node) * l->num_nodes, cudaMemcpyHostToDevice, st));
+    RT_CHECK_CUDA(ctx, cudaMemcpyAsync(l->ids, h_ids, 4 * (size_t)n, cudaMemcpyHostToDevice, st));
+    RT_CHECK_CUDA(ctx, cudaMemcpyAsync(l->tris, h_tris, sizeof(float) * 9 * (size_t)n, cudaMemcpyHostToDevice, st));
+    const uint32_t blocks = std::max(1u, std::min(ceil_div(n, 256), (uint32_t)ctx->num_sms * 8));
+    k_gather_tris<<<blocks, 256, 0, st>>>(l->ids, l->tris, n, l->sorted_tris);
+    RT_CHECK_LAUNCH(ctx, "k_gather_tris");
+    l->n = n;
+    l->src_tris = l->tris;
+    l->built_keys = false;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_lbvh_view_get(const rt_lbvh* l, rt_lbvh_view* v) {
+    if (!l || !v) return RT_ERR_INVALID;
+    v->nodes = l->nodes;
+    v->ids = l->ids;
+    v->keys = l->built_keys ? l->keys : nullptr;
+    v->sorted_tris = reinterpret_cast<const float*>(l->sorted_tris);
+    v->n = l->n;
+    v->depth = l->depth;
+    v->num_nodes = l->num_nodes;
+    v->node_size = (uint32_t)sizeof(rt_node);
+    return RT_OK;
+}
+
+extern "C" rt_status rt_lbvh_world_bound(rt_ctx* ctx, const rt_lbvh* l, float out[6]) {
+    if (!ctx || !l || !out) return ctx ? rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_world_bound: null argument") : RT_ERR_INVALID;
+    rt_node root;
+    RT_CHECK_CUDA(ctx, cudaMemcpyAsync(&root, l->nodes + 1, sizeof(rt_node), cudaMemcpyDeviceToHost, ctx->stream));
+    RT_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int c = 0; c < 3; ++c) { out[c] = root.min[c]; out[3 + c] = root.max[c]; }
+    return RT_OK;
+}
+
+extern "C" rt_status rt_lbvh_download(rt_ctx* ctx, const rt_lbvh* l, rt_node* h_nodes, uint32_t* h_ids,
+                                      uint32_t* h_keys) {
+    if (!ctx || !l) return ctx ? rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_download: null argument") : RT_ERR_INVALID;
+    cudaStream_t st = ctx->stream;
+    if (h_nodes) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_nodes, l->nodes, sizeof(rt_node) * l->num_nodes, cudaMemcpyDeviceToHost, st));
+    if (h_ids) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_ids, l->ids, 4 * (size_t)l->n, cudaMemcpyDeviceToHost, st));
+    if (h_keys) {
+        if (!l->built_keys) return rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_download: keys exist only after rt_lbvh_build");
+        RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_keys, l->keys, 4 * (size_t)l->n, cudaMemcpyDeviceToHost, st));
+    }
+    RT_CHECK_CUDA(ctx, cudaStreamSynchronize(st));
+    return RT_OK;
+}

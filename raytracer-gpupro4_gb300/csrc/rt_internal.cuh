@@ -1,0 +1,140 @@
+// rt_internal.cuh -- shared definitions of the sm_103a LBVH core.
+//
+// Arithmetic on the parity-critical paths (Morton quantisation, ray
+// generation, ray/box and ray/triangle tests, shading rays) goes through
+// the __f*_rn intrinsics below: IEEE binary32, round to nearest, never
+// contracted into a fused multiply-add, so each result equals the
+// reference's CPU evaluation (LBVH.cpp, AccelerationStructure.h:70-97,
+// Geometry.h Cross/Dot) bit for bit.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "../../include/rt_api.h"
+
+// ---------------------------------------------------------------------------
+// exact fp32 helpers
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
+
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 sub3(f3 a, f3 b) { return mk3(fsub(a.x, b.x), fsub(a.y, b.y), fsub(a.z, b.z)); }
+// Dot (Geometry.h): (x*x' + y*y') + z*z'
+__device__ __forceinline__ float dot3(f3 a, f3 b) {
+    return fadd(fadd(fmul(a.x, b.x), fmul(a.y, b.y)), fmul(a.z, b.z));
+}
+// Cross (Geometry.h)
+__device__ __forceinline__ f3 cross3(f3 a, f3 b) {
+    return mk3(fsub(fmul(a.y, b.z), fmul(a.z, b.y)), fsub(fmul(a.z, b.x), fmul(a.x, b.z)),
+               fsub(fmul(a.x, b.y), fmul(a.y, b.x)));
+}
+// Normalize (Geometry.h): divide each component by the length
+__device__ __forceinline__ f3 normalize3(f3 v) {
+    float l = fsqrt(dot3(v, v));
+    return mk3(fdiv(v.x, l), fdiv(v.y, l), fdiv(v.z, l));
+}
+
+// std::min / std::max as the reference's CPU code evaluates them:
+// min(a,b) = (b < a) ? b : a, max(a,b) = (a < b) ? b : a (NaN-sensitive).
+__device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }
+
+// ---------------------------------------------------------------------------
+// Device error word (bit set by kernels, read by rt_ctx_check).
+enum : uint32_t {
+    RT_DEVERR_TIMEOUT = 1u,
+    RT_DEVERR_NONFINITE = 2u,
+    RT_DEVERR_BOUNDS = 4u,  // a bounds guard rejected an index (corrupt tree or scratch)
+};
+
+// Scene bounds and Morton parameters produced on the device by the bounds
+// kernel (cbScene of ConstantBuffers.h:112-142 computed instead of uploaded).
+struct SceneInfo {
+    float bmin[3], bmax[3];  // VertMin / VertMax (LBVH.cpp:513-514)
+    float lo3[3];            // 3 * VertMin (LBVH.cpp:522)
+    float f[3];              // 1024 / (3*VertMax - 3*VertMin) (LBVH.cpp:523-526)
+    uint32_t nonfinite;
+    uint32_t pad[3];
+};
+
+// Tiling constants
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 keys per onesweep tile
+constexpr int kSortPasses = 4;                        // 8-bit digits over 30-bit codes
+constexpr int kEmitThreads = 256;
+constexpr int kEmitItems = 8;
+constexpr int kEmitTile = kEmitThreads * kEmitItems;  // 2048 elements per emission tile
+constexpr int kMaxDepth = 26;
+constexpr uint32_t kMaxTris = (1u << 29);
+
+// ---------------------------------------------------------------------------
+struct rt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    uint32_t* d_err = nullptr;  // device error word
+    int num_sms = 0;
+};
+
+struct rt_lbvh {
+    uint32_t cap = 0, depth = 0, num_nodes = 0, n = 0;
+    bool built_keys = false;
+    rt_node* nodes = nullptr;
+    uint32_t* keys = nullptr;
+    uint32_t* ids = nullptr;
+    uint32_t* keys_alt = nullptr;
+    uint32_t* ids_alt = nullptr;
+    float4* sorted_tris = nullptr;  // 3 x float4 per triangle
+    float* tris = nullptr;          // device copy of the soup (host builds / imports)
+    const float* src_tris = nullptr; // soup of the last build / import, indexed by triangle id (borrowed)
+    // build scratch
+    SceneInfo* scene = nullptr;
+    float* partials = nullptr;       // bounds partial reductions, 8 floats per block
+    uint32_t* counters = nullptr;    // [0] bounds ticket, [1..4] sort tile tickets, [5] leaf count
+    uint32_t* hist = nullptr;        // 4 x 256 digit histograms
+    uint32_t* lookback = nullptr;    // 4 passes x sort tiles x 256 status words
+    uint32_t* scan = nullptr;        // emission tiles x 4 (fwd agg, bwd agg, fwd prefix, bwd suffix)
+    uint32_t* leaf_list = nullptr;   // cap
+    uint32_t* arrive = nullptr;      // 1 << (depth-1) refit arrival words (epoch-tagged)
+    uint32_t epoch = 0;
+    uint32_t sort_tiles_cap = 0, emit_tiles_cap = 0, bounds_blocks = 0;
+    // frame buffers for rt_render_frame_host (grown on demand)
+    rt_hit* f_primary = nullptr;
+    rt_hit* f_mirror = nullptr;
+    uint8_t* f_vis = nullptr;
+    size_t f_pixels = 0;
+};
+
+// ---------------------------------------------------------------------------
+// error plumbing (host)
+rt_status rt_fail(rt_ctx* ctx, rt_status s, const char* fmt, ...);
+
+#define RT_CHECK_CUDA(ctx, call)                                                               \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return rt_fail((ctx), RT_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+#define RT_CHECK_LAUNCH(ctx, what)                                                              \
+    do {                                                                                        \
+        cudaError_t e_ = cudaGetLastError();                                                    \
+        if (e_ != cudaSuccess)                                                                  \
+            return rt_fail((ctx), RT_ERR_CUDA, "launch of %s failed: %s", what, cudaGetErrorString(e_)); \
+    } while (0)
+
+// Bounded spin used by every device-side wait (look-back): after this many
+// polls the waiter records RT_DEVERR_TIMEOUT and stops waiting.
+constexpr uint32_t kSpinLimit = 1u << 22;

@@ -1,0 +1,231 @@
+// rt_trace.cu -- primary, shadow and mirror rays over the LBVH on sm_103a.
+//
+// Replaces the per-bounce dispatches of RayTracerCS::Render
+// (RayTracerCS/RayTracerCS.cpp:284-295): CSGeneratePrimaryRays
+// (Shaders/CS/CSPrimaryRays.hlsl:22-69) and CSComputeIntersections
+// (CSIntersections.hlsl:18-39) are fused into k_trace_primary (rays are made
+// in registers, no 48-byte ray buffer round trip); the shadow ray and the
+// mirror bounce of CSComputeColor (CSComputeColorRT.hlsl:57-177, 203-210,
+// flat normals, no textures) are k_trace_secondary.
+#include <algorithm>
+
+#include "rt_traverse.cuh"
+
+using namespace rt;
+
+namespace {
+
+constexpr int kTraceThreads = 128;
+
+__device__ __forceinline__ void store_hit(rt_hit* out, const Hit& h) {
+    *reinterpret_cast<int4*>(out) = make_int4(h.id, __float_as_int(h.u), __float_as_int(h.v), __float_as_int(h.t));
+}
+
+template <bool STATS>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_camera cam,
+                                                                 rt_hit* __restrict__ hits,
+                                                                 uint32_t* __restrict__ stats) {
+    const uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t i, j;
+    if (!tile_pixel(tile, threadIdx.x & 31, cam.width, cam.height, &i, &j)) return;
+    const f3 d = primary_dir(cam, i, j);
+    const RayState r = make_ray(mk3(cam.eye[0], cam.eye[1], cam.eye[2]), d, 1e16f, -1);
+    uint32_t nb = 0, nt = 0;
+    const Hit h = trace_ray<STATS>(r, tr, false, &nb, &nt);
+    const size_t p = (size_t)j * cam.width + i;
+    store_hit(hits + p, h);
+    if (STATS) {
+        stats[2 * p] = nb;
+        stats[2 * p + 1] = nt;
+    }
+}
+
+// Shadow (any hit) and mirror (closest hit) rays of one pixel.
+template <bool STATS>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_secondary(
+    TreeRef tr, const float* __restrict__ soup, rt_camera cam, float lx, float ly, float lz, const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis,
+    rt_hit* __restrict__ mirror, uint32_t* __restrict__ sstats, uint32_t* __restrict__ mstats) {
+    const uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t i, j;
+    if (!tile_pixel(tile, threadIdx.x & 31, cam.width, cam.height, &i, &j)) return;
+    const size_t p = (size_t)j * cam.width + i;
+    const int4 ph = __ldg(reinterpret_cast<const int4*>(prim + p));
+    const int id = ph.x;
+    uint32_t snb = 0, snt = 0, mnb = 0, mnt = 0;
+    if (id < 0) {
+        if (vis) vis[p] = 0;
+        if (mirror) {
+            Hit m;
+            m.id = -2; m.u = -1.0f; m.v = -1.0f; m.t = 0.0f;
+            store_hit(mirror + p, m);
+        }
+    } else {
+        const float t = __int_as_float(ph.w);
+        const f3 d = primary_dir(cam, i, j);
+        const f3 o = mk3(cam.eye[0], cam.eye[1], cam.eye[2]);
+        const float* tp = soup + 9 * (size_t)id;
+        const f3 A = mk3(__ldg(tp), __ldg(tp + 1), __ldg(tp + 2));
+        const f3 B = mk3(__ldg(tp + 3), __ldg(tp + 4), __ldg(tp + 5));
+        const f3 C = mk3(__ldg(tp + 6), __ldg(tp + 7), __ldg(tp + 8));
+        const f3 N = normalize3(cross3(sub3(B, A), sub3(C, A)));   // CSComputeColorRT.hlsl:61-63,75
+        f3 Nf = N;
+        if (dot3(Nf, d) > 0.0f) Nf = mk3(-N.x, -N.y, -N.z);        // :126-131
+        const f3 P = mk3(fadd(o.x, fmul(t, d.x)), fadd(o.y, fmul(t, d.y)), fadd(o.z, fmul(t, d.z)));  // :134-135
+        f3 L = mk3(fsub(P.x, lx), fsub(P.y, ly), fsub(P.z, lz));   // :136
+        const float dist = fsqrt(dot3(L, L));                      // :137
+        L = mk3(fdiv(L.x, dist), fdiv(L.y, dist), fdiv(L.z, dist)); // :138
+        if (vis) {
+            const float ls = dot3(N, L), rs = dot3(N, d);          // :145-146
+            uint8_t code = 1;
+            if (fmul(ls, rs) > 0.0f) {                             // :147
+                const RayState sr = make_ray(P, mk3(-L.x, -L.y, -L.z), dist, id);  // :149-153
+                const Hit sh = trace_ray<STATS>(sr, tr, true, &snb, &snt);
+                code = (sh.id >= 0) ? 2 : 3;
+            }
+            vis[p] = code;
+        }
+        if (mirror) {
+            const float k = fmul(2.0f, dot3(d, Nf));               // reflect(d, N) = d - 2*dot(d,N)*N
+            const f3 R = normalize3(mk3(fsub(d.x, fmul(k, Nf.x)), fsub(d.y, fmul(k, Nf.y)), fsub(d.z, fmul(k, Nf.z))));
+            const RayState mr = make_ray(P, R, 1e16f, id);
+            const Hit mh = trace_ray<STATS>(mr, tr, false, &mnb, &mnt);
+            store_hit(mirror + p, mh);
+        }
+    }
+    if (STATS) {
+        if (sstats) { sstats[2 * p] = snb; sstats[2 * p + 1] = snt; }
+        if (mstats) { mstats[2 * p] = mnb; mstats[2 * p + 1] = mnt; }
+    }
+}
+
+template <bool STATS>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_rays(TreeRef tr, const rt_ray* __restrict__ rays, uint32_t n,
+                                                              int any_hit, rt_hit* __restrict__ hits,
+                                                              uint32_t* __restrict__ stats) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float4 a = __ldg(reinterpret_cast<const float4*>(rays + k));
+    const float4 b = __ldg(reinterpret_cast<const float4*>(rays + k) + 1);
+    const RayState r = make_ray(mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), b.w, __float_as_int(a.w));
+    uint32_t nb = 0, nt = 0;
+    const Hit h = trace_ray<STATS>(r, tr, any_hit != 0, &nb, &nt);
+    store_hit(hits + k, h);
+    if (STATS) {
+        stats[2 * k] = nb;
+        stats[2 * k + 1] = nt;
+    }
+}
+
+}  // namespace
+
+TreeRef tree_ref(const rt_ctx* ctx, const rt_lbvh* l) {
+    TreeRef t;
+    t.nodes = l->nodes;
+    t.tris = l->sorted_tris;
+    t.num_nodes = l->num_nodes;
+    t.n = l->n;
+    t.err = ctx->d_err;
+    return t;
+}
+
+namespace {
+
+uint32_t pixel_blocks(const rt_camera* cam) {
+    const uint64_t tiles = (uint64_t)((cam->width + 7) / 8) * ((cam->height + 3) / 4);
+    return (uint32_t)((tiles * 32 + kTraceThreads - 1) / kTraceThreads);
+}
+
+rt_status check_trace_args(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, const char* who) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (!l || !cam) return rt_fail(ctx, RT_ERR_INVALID, "%s: null argument", who);
+    if (l->n == 0) return rt_fail(ctx, RT_ERR_INVALID, "%s: the LBVH has not been built", who);
+    if (cam->width == 0 || cam->height == 0 || (uint64_t)cam->width * cam->height > (1ull << 31))
+        return rt_fail(ctx, RT_ERR_INVALID, "%s: bad image size %ux%u", who, cam->width, cam->height);
+    return RT_OK;
+}
+
+}  // namespace
+
+extern "C" rt_status rt_trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, rt_hit* d_hits,
+                                      uint32_t* d_stats) {
+    rt_status s = check_trace_args(ctx, l, cam, "rt_trace_primary");
+    if (s != RT_OK) return s;
+    if (!d_hits) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_primary: null output");
+    const uint32_t blocks = pixel_blocks(cam);
+    if (d_stats)
+        k_trace_primary<true><<<blocks, kTraceThreads, 0, ctx->stream>>>(tree_ref(ctx, l), *cam, d_hits, d_stats);
+    else
+        k_trace_primary<false><<<blocks, kTraceThreads, 0, ctx->stream>>>(tree_ref(ctx, l), *cam, d_hits, nullptr);
+    RT_CHECK_LAUNCH(ctx, "k_trace_primary");
+    return RT_OK;
+}
+
+extern "C" rt_status rt_trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, const float light[3],
+                                            const rt_hit* d_primary, uint8_t* d_vis, rt_hit* d_mirror,
+                                            uint32_t* d_shadow_stats, uint32_t* d_mirror_stats) {
+    rt_status s = check_trace_args(ctx, l, cam, "rt_trace_shadow_mirror");
+    if (s != RT_OK) return s;
+    if (!light || !d_primary) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_shadow_mirror: null argument");
+    if (!l->src_tris) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_shadow_mirror: no triangle soup bound");
+    const uint32_t blocks = pixel_blocks(cam);
+    if (d_shadow_stats || d_mirror_stats)
+        k_trace_secondary<true><<<blocks, kTraceThreads, 0, ctx->stream>>>(
+            tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_vis, d_mirror,
+            d_shadow_stats, d_mirror_stats);
+    else
+        k_trace_secondary<false><<<blocks, kTraceThreads, 0, ctx->stream>>>(
+            tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_vis, d_mirror,
+            nullptr, nullptr);
+    RT_CHECK_LAUNCH(ctx, "k_trace_secondary");
+    return RT_OK;
+}
+
+extern "C" rt_status rt_trace_rays(rt_ctx* ctx, const rt_lbvh* l, const rt_ray* d_rays, uint32_t n, int any_hit,
+                                   rt_hit* d_hits, uint32_t* d_stats) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (!l || !d_rays || !d_hits) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_rays: null argument");
+    if (l->n == 0) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_rays: the LBVH has not been built");
+    if (n == 0) return RT_OK;
+    const uint32_t blocks = (n + kTraceThreads - 1) / kTraceThreads;
+    if (d_stats)
+        k_trace_rays<true><<<blocks, kTraceThreads, 0, ctx->stream>>>(tree_ref(ctx, l), d_rays, n, any_hit,
+                                                                      d_hits, d_stats);
+    else
+        k_trace_rays<false><<<blocks, kTraceThreads, 0, ctx->stream>>>(tree_ref(ctx, l), d_rays, n, any_hit,
+                                                                       d_hits, nullptr);
+    RT_CHECK_LAUNCH(ctx, "k_trace_rays");
+    return RT_OK;
+}
+
+extern "C" rt_status rt_render_frame_host(rt_ctx* ctx, rt_lbvh* l, const float* h_tris, uint32_t n,
+                                          const rt_camera* cam, const float light[3], rt_hit* h_primary,
+                                          uint8_t* h_vis, rt_hit* h_mirror) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (!l || !h_tris || !cam || !light) return rt_fail(ctx, RT_ERR_INVALID, "rt_render_frame_host: null argument");
+    const size_t px = (size_t)cam->width * cam->height;
+    if (px == 0 || px > (1ull << 31)) return rt_fail(ctx, RT_ERR_INVALID, "rt_render_frame_host: bad image size");
+    if (px > l->f_pixels) {  // frame buffers grow on the first call at a new size
+        RT_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (l->f_primary) cudaFree(l->f_primary);
+        if (l->f_mirror) cudaFree(l->f_mirror);
+        if (l->f_vis) cudaFree(l->f_vis);
+        l->f_primary = nullptr; l->f_mirror = nullptr; l->f_vis = nullptr; l->f_pixels = 0;
+        RT_CHECK_CUDA(ctx, cudaMalloc((void**)&l->f_primary, sizeof(rt_hit) * px));
+        RT_CHECK_CUDA(ctx, cudaMalloc((void**)&l->f_mirror, sizeof(rt_hit) * px));
+        RT_CHECK_CUDA(ctx, cudaMalloc((void**)&l->f_vis, px));
+        l->f_pixels = px;
+    }
+    rt_status s = rt_lbvh_build_host(ctx, l, h_tris, n, 0);
+    if (s != RT_OK) return s;
+    s = rt_trace_primary(ctx, l, cam, l->f_primary, nullptr);
+    if (s != RT_OK) return s;
+    s = rt_trace_shadow_mirror(ctx, l, cam, light, l->f_primary, h_vis ? l->f_vis : nullptr,
+                               h_mirror ? l->f_mirror : nullptr, nullptr, nullptr);
+    if (s != RT_OK) return s;
+    cudaStream_t st = ctx->stream;
+    if (h_primary) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_primary, l->f_primary, sizeof(rt_hit) * px, cudaMemcpyDeviceToHost, st));
+    if (h_vis) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_vis, l->f_vis, px, cudaMemcpyDeviceToHost, st));
+    if (h_mirror) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_mirror, l->f_mirror, sizeof(rt_hit) * px, cudaMemcpyDeviceToHost, st));
+    RT_CHECK_CUDA(ctx, cudaStreamSynchronize(st));
+    return RT_OK;
+}

@@ -1,0 +1,258 @@
+// rt_traverse.cuh -- closest-hit / any-hit traversal of the heap-layout LBVH.
+//
+// Restates LBVH_IntersectP (RayTracerCS/Shaders/AccelerationStructures/
+// LBVH.hlsl:363-440) and LBVH::IntersectP (LBVH.cpp:919-1039) as a
+// stack-based walk with the same visit order: at an internal node both
+// children (heap slots 2i, 2i+1: one 64-byte line) are box-tested, the near
+// child (chosen by the sign of the ray direction on the node's axis field,
+// LBVH.hlsl:432) is entered first and a hit far child is pushed with its
+// entry distance; a popped node is entered only if that distance still does
+// not exceed the closest hit.  This enters exactly the nodes the reference's
+// trail walk enters and performs the same number of box and triangle tests.
+//
+// Box test = RayBoxInterval (LBVH.cpp:634-659), triangle test =
+// RayTriangleTest (AccelerationStructure.h:70-97), both in the reference's
+// operation order without contraction.  Ties at equal t keep the smaller
+// triangle id.  The excluded triangle is skipped (LBVH.hlsl:415).
+#pragma once
+#include "rt_internal.cuh"
+
+namespace rt {
+
+constexpr int kStackSize = 32;  // > kMaxDepth
+
+// Bounds of the arrays a traversal may touch; an index outside them (only
+// possible with a corrupt tree) sets RT_DEVERR_BOUNDS and stops that ray.
+struct TreeRef {
+    const rt_node* __restrict__ nodes;
+    const float4* __restrict__ tris;
+    uint32_t num_nodes;
+    uint32_t n;
+    uint32_t* err;
+};
+
+struct RayState {
+    f3 o, d, inv;
+    int sgn[3];
+    int exclude;
+    float tmax;
+    bool exact;  // some 1/d is infinite: use the reference's NaN-sensitive min/max
+};
+
+__device__ __forceinline__ RayState make_ray(f3 o, f3 d, float tmax, int exclude) {
+    RayState r;
+    r.o = o;
+    r.d = d;
+    r.inv = mk3(fdiv(1.0f, d.x), fdiv(1.0f, d.y), fdiv(1.0f, d.z));
+    r.sgn[0] = d.x < 0.0f;  // signo[] of LBVH.cpp:983-985
+    r.sgn[1] = d.y < 0.0f;
+    r.sgn[2] = d.z < 0.0f;
+    r.exclude = exclude;
+    r.tmax = tmax;
+    r.exact = isinf(r.inv.x) || isinf(r.inv.y) || isinf(r.inv.z);
+    return r;
+}
+
+template <bool EXACT>
+__device__ __forceinline__ float vmin(float a, float b) { return EXACT ? smin(a, b) : fminf(a, b); }
+template <bool EXACT>
+__device__ __forceinline__ float vmax(float a, float b) { return EXACT ? smax(a, b) : fmaxf(a, b); }
+
+// Returns true when the reference would enter the node: not (T1 < 0 or
+// T0 > best_t) after the empty-interval reset.  With every 1/d finite no
+// product is NaN and fminf/fmaxf equal std::min/std::max.
+template <bool EXACT>
+__device__ __forceinline__ bool box_enter(const RayState& r, float mnx, float mny, float mnz, float mxx, float mxy,
+                                          float mxz, float best_t, float* t0out) {
+    const float dMx = fmul(fsub(mxx, r.o.x), r.inv.x), dMy = fmul(fsub(mxy, r.o.y), r.inv.y),
+                dMz = fmul(fsub(mxz, r.o.z), r.inv.z);
+    const float dmx = fmul(fsub(mnx, r.o.x), r.inv.x), dmy = fmul(fsub(mny, r.o.y), r.inv.y),
+                dmz = fmul(fsub(mnz, r.o.z), r.inv.z);
+    float t0 = vmin<EXACT>(dmx, dMx);
+    float t1 = vmax<EXACT>(dmx, dMx);
+    t0 = vmax<EXACT>(t0, vmin<EXACT>(dmy, dMy));
+    t1 = vmin<EXACT>(t1, vmax<EXACT>(dmy, dMy));
+    t0 = vmax<EXACT>(t0, vmin<EXACT>(dmz, dMz));
+    t1 = vmin<EXACT>(t1, vmax<EXACT>(dmz, dMz));
+    if (t0 > t1) { t0 = -1.0f; t1 = -1.0f; }
+    *t0out = t0;
+    return !(t1 < 0.0f) && !(t0 > best_t);
+}
+
+struct Hit {
+    int id;
+    float u, v, t;
+};
+
+// Moller-Trumbore, AccelerationStructure.h:70-97.
+__device__ __forceinline__ bool tri_test(const RayState& r, float4 a, float4 b, float4 c, float* u, float* v,
+                                         float* t) {
+    const f3 A = mk3(a.x, a.y, a.z);
+    const f3 E1 = sub3(mk3(b.x, b.y, b.z), A);
+    const f3 E2 = sub3(mk3(c.x, c.y, c.z), A);
+    const f3 P = cross3(r.d, E2);
+    float det = dot3(E1, P);
+    det = __frcp_rn(det);  // 1.0f / det, correctly rounded
+    const f3 T = sub3(r.o, A);
+    const float uu = fmul(dot3(T, P), det);
+    const f3 Q = cross3(T, E1);
+    const float vv = fmul(dot3(r.d, Q), det);
+    const float tt = fmul(dot3(E2, Q), det);
+    *u = uu;
+    *v = vv;
+    *t = tt;
+    return (uu >= 0.0f) && (uu <= 1.0f) && (vv >= 0.0f) && (fadd(uu, vv) <= 1.0f) && (tt >= 0.0f);
+}
+
+struct NodeBox {
+    float4 a, b;  // a = min.xyz,max.x  b = max.yz,prim_count,prim_pos
+};
+
+__device__ __forceinline__ NodeBox load_node(const rt_node* __restrict__ nodes, uint32_t i) {
+    const float4* p = reinterpret_cast<const float4*>(nodes + i);
+    NodeBox nb;
+    nb.a = __ldg(p);
+    nb.b = __ldg(p + 1);
+    return nb;
+}
+
+template <bool EXACT, bool STATS>
+__device__ __forceinline__ Hit traverse(const RayState& r, const TreeRef& tr_, bool any_hit, uint32_t* nbox_out,
+                                        uint32_t* ntri_out) {
+    const rt_node* __restrict__ nodes = tr_.nodes;
+    const float4* __restrict__ tris = tr_.tris;
+    Hit best;
+    best.id = -1;
+    best.u = -1.0f;
+    best.v = -1.0f;
+    best.t = r.tmax;
+    uint32_t nbox = 0, ntri = 0;
+    uint32_t stack_node[kStackSize];
+    float stack_t0[kStackSize];
+    int sp = 0;
+
+    NodeBox cur = load_node(nodes, 1);
+    float t0;
+    if (STATS) ++nbox;
+    bool have = box_enter<EXACT>(r, cur.a.x, cur.a.y, cur.a.z, cur.a.w, cur.b.x, cur.b.y, best.t, &t0);
+    uint32_t node = 1;
+    while (true) {
+        if (have) {
+            const int pc = __float_as_int(cur.b.z);
+            if (pc & 4) {
+                int cnt = pc >> 3;
+                const int pos = __float_as_int(cur.b.w);
+                if (pos < 0 || cnt < 0 || (uint32_t)pos + (uint32_t)cnt > tr_.n) {
+                    atomicOr(tr_.err, RT_DEVERR_BOUNDS);
+                    cnt = 0;
+                }
+                for (int i = 0; i < cnt; ++i) {
+                    const float4* tp = tris + 3 * (size_t)(pos + i);
+                    const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                    if (STATS) ++ntri;
+                    const int id = __float_as_int(a.w);
+                    if (id == r.exclude) continue;
+                    float u, v, t;
+                    if (tri_test(r, a, b, c, &u, &v, &t)) {
+                        if (t < best.t || (t == best.t && best.id >= 0 && id < best.id)) {
+                            best.t = t;
+                            best.u = u;
+                            best.v = v;
+                            best.id = id;
+                        }
+                    }
+                }
+                if (any_hit && best.id >= 0) break;
+                have = false;
+            } else {
+                const uint32_t c0 = node << 1;
+                if (c0 + 1 >= tr_.num_nodes) {
+                    atomicOr(tr_.err, RT_DEVERR_BOUNDS);
+                    break;
+                }
+                const float4* p = reinterpret_cast<const float4*>(nodes + c0);
+                const float4 l0 = __ldg(p), l1 = __ldg(p + 1), r0 = __ldg(p + 2), r1 = __ldg(p + 3);
+                float tl, tr;
+                const bool hl = box_enter<EXACT>(r, l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, best.t, &tl);
+                const bool hr = box_enter<EXACT>(r, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, best.t, &tr);
+                if (STATS) nbox += 2;
+                const int near_right = r.sgn[pc & 3];
+                const bool hn = near_right ? hr : hl, hf = near_right ? hl : hr;
+                const float tf = near_right ? tl : tr;
+                const uint32_t nn = c0 | (uint32_t)near_right, nf = nn ^ 1u;
+                if (hn) {
+                    if (hf) {
+                        stack_node[sp] = nf;
+                        stack_t0[sp] = tf;
+                        ++sp;
+                    }
+                    node = nn;
+                    cur.a = near_right ? r0 : l0;
+                    cur.b = near_right ? r1 : l1;
+                    continue;
+                } else if (hf) {
+                    node = nf;
+                    cur.a = near_right ? l0 : r0;
+                    cur.b = near_right ? l1 : r1;
+                    continue;
+                }
+                have = false;
+            }
+        }
+        // pop: re-check the stored entry distance against the current best
+        bool found = false;
+        while (sp > 0) {
+            --sp;
+            if (!(stack_t0[sp] > best.t)) {
+                node = stack_node[sp];
+                found = true;
+                break;
+            }
+        }
+        if (!found) break;
+        cur = load_node(nodes, node);
+        have = true;
+    }
+    if (STATS) {
+        *nbox_out = nbox;
+        *ntri_out = ntri;
+    }
+    return best;
+}
+
+// Warp-uniform dispatch between the fast and the NaN-exact box test.
+template <bool STATS>
+__device__ __forceinline__ Hit trace_ray(const RayState& r, const TreeRef& tr, bool any_hit, uint32_t* nbox,
+                                         uint32_t* ntri) {
+    if (__any_sync(__activemask(), r.exact)) return traverse<true, STATS>(r, tr, any_hit, nbox, ntri);
+    return traverse<false, STATS>(r, tr, any_hit, nbox, ntri);
+}
+
+// Primary ray of pixel (i, j): CSPrimaryRays.hlsl:36-56 with the basis camera.
+__device__ __forceinline__ f3 camera_dir(const rt_camera& cam, float x, float y) {
+    const float dx = fmul(x, cam.tan_half_fovy), dy = fmul(y, cam.tan_half_fovy);
+    f3 d;
+    d.x = fadd(fadd(fmul(cam.right[0], dx), fmul(cam.up[0], dy)), cam.fwd[0]);
+    d.y = fadd(fadd(fmul(cam.right[1], dx), fmul(cam.up[1], dy)), cam.fwd[1]);
+    d.z = fadd(fadd(fmul(cam.right[2], dx), fmul(cam.up[2], dy)), cam.fwd[2]);
+    return normalize3(d);
+}
+
+__device__ __forceinline__ f3 primary_dir(const rt_camera& cam, uint32_t i, uint32_t j) {
+    const float inv = fdiv(1.0f, (float)cam.height);
+    const float x = fmul((float)(2 * (int)i + 1 - (int)cam.width), inv);
+    const float y = -fmul((float)(2 * (int)j + 1 - (int)cam.height), inv);
+    return camera_dir(cam, x, y);
+}
+
+// Pixel of lane `lane` of warp tile `tile`: 8 x 4 pixel tiles for coherence.
+__device__ __forceinline__ bool tile_pixel(uint32_t tile, uint32_t lane, uint32_t w, uint32_t h, uint32_t* i,
+                                           uint32_t* j) {
+    const uint32_t tiles_x = (w + 7) / 8;
+    const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
+    *i = tx * 8 + (lane & 7);
+    *j = ty * 4 + (lane >> 3);
+    return *i < w && *j < h;
+}
+
+}  // namespace rt

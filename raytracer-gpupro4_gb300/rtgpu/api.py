@@ -1,0 +1,246 @@
+"""Python mirror of the reference's stage API over the C ABI.
+
+  * ``LBVH``  -- the AccelerationStructure interface of the reference's LBVH
+    (AccelerationStructures/AccelerationStructure.h:40-67, LBVH/LBVH.h:70-118):
+    Build(), GetPtrToElements(), GetSizeOfElement(), GetNumberOfElements(),
+    GetOrderedElementsIds(), WorldBound(), GetName().
+  * ``StructureConstruction`` -- GPUBuildStructure(depth) of
+    RayTracerCS/StructureConstruction.h:78-82.
+  * ``RayTracer`` -- the per-frame stages of RayTracerCS::Render
+    (RayTracerCS.cpp:241-311): primary rays, intersections, shadow and
+    mirror rays, path-traced GI.
+
+Every call goes through librtgb300.so (no CPU fallback).  PyTorch provides
+device memory and the CUDA stream only.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+
+def _dev_ptr(t: torch.Tensor) -> C.c_void_p:
+    assert t.is_cuda and t.is_contiguous()
+    return C.c_void_p(t.data_ptr())
+
+
+def _host_ptr(a: np.ndarray) -> C.c_void_p:
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """rt_ctx bound to a CUDA device and torch's current stream on it."""
+
+    def __init__(self, device: int = 0, stream: torch.cuda.Stream | None = None):
+        self.device = device
+        self.torch_device = torch.device("cuda", device)
+        self.stream = stream if stream is not None else torch.cuda.current_stream(self.torch_device)
+        h = C.c_void_p()
+        L.check(L.lib().rt_ctx_create(device, C.c_void_p(self.stream.cuda_stream), C.byref(h)), None, "rt_ctx_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            L.lib().rt_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self):
+        """Synchronise and raise if a device-side error flag was set."""
+        L.check(L.lib().rt_ctx_check(self.h), self.h, "rt_ctx_check")
+
+    def sync(self):
+        L.check(L.lib().rt_ctx_sync(self.h), self.h, "rt_ctx_sync")
+
+
+class LBVH:
+    """Device LBVH (heap layout, 1 << depth slots of 32 bytes)."""
+
+    def __init__(self, ctx: Context, max_tris: int, depth: int = 20):
+        self.ctx = ctx
+        self.depth = depth
+        h = C.c_void_p()
+        L.check(L.lib().rt_lbvh_create(ctx.h, max_tris, depth, C.byref(h)), ctx.h, "rt_lbvh_create")
+        self.h = h
+        self._tris = None
+        self.n = 0
+
+    def close(self):
+        if self.h:
+            L.lib().rt_lbvh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # LBVH::Build (LBVH.cpp:488-632)
+    def Build(self, tris, flags: int = 0) -> "LBVH":
+        if isinstance(tris, torch.Tensor):
+            t = tris.contiguous()
+            assert t.dtype == torch.float32 and t.shape[-1] == 9
+            self._tris = t  # the LBVH borrows the soup (as LBVH borrows Primitive**)
+            L.check(L.lib().rt_lbvh_build(self.ctx.h, self.h, _dev_ptr(t), t.shape[0], flags), self.ctx.h,
+                    "rt_lbvh_build")
+            self.n = t.shape[0]
+        else:
+            a = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+            L.check(L.lib().rt_lbvh_build_host(self.ctx.h, self.h, _host_ptr(a), len(a), flags), self.ctx.h,
+                    "rt_lbvh_build_host")
+            self._tris = None
+            self.n = len(a)
+            self.ctx.sync()
+        return self
+
+    def Import(self, nodes: np.ndarray, ids: np.ndarray, tris: np.ndarray) -> "LBVH":
+        """Uses a tree built elsewhere (RayTracerCS::SelectAccelerationStructure)."""
+        nodes = np.ascontiguousarray(nodes).view(L.NODE_DTYPE)
+        ids = np.ascontiguousarray(ids, np.uint32)
+        tris = np.ascontiguousarray(tris, np.float32)
+        assert len(nodes) == (1 << self.depth)
+        L.check(L.lib().rt_lbvh_import_host(self.ctx.h, self.h, _host_ptr(nodes), _host_ptr(ids), _host_ptr(tris),
+                                            len(tris)), self.ctx.h, "rt_lbvh_import_host")
+        self.n = len(tris)
+        self.ctx.sync()
+        return self
+
+    def view(self) -> L.LbvhView:
+        v = L.LbvhView()
+        L.check(L.lib().rt_lbvh_view_get(self.h, C.byref(v)), self.ctx.h, "rt_lbvh_view_get")
+        return v
+
+    def GetName(self) -> str:
+        return "LBVH"
+
+    def GetNumberOfElements(self) -> int:
+        return 1 << self.depth
+
+    def GetSizeOfElement(self) -> int:
+        return 32
+
+    def download(self, nodes=True, ids=True, keys=False):
+        hn = np.zeros(1 << self.depth, L.NODE_DTYPE) if nodes else None
+        hi = np.zeros(self.n, np.uint32) if ids else None
+        hk = np.zeros(self.n, np.uint32) if keys else None
+        L.check(L.lib().rt_lbvh_download(self.ctx.h, self.h, _host_ptr(hn) if nodes else None,
+                                         _host_ptr(hi) if ids else None, _host_ptr(hk) if keys else None),
+                self.ctx.h, "rt_lbvh_download")
+        return hn, hi, hk
+
+    def GetPtrToElements(self) -> np.ndarray:
+        return self.download(True, False, False)[0]
+
+    def GetOrderedElementsIds(self) -> np.ndarray:
+        return self.download(False, True, False)[1]
+
+    def keys(self) -> np.ndarray:
+        return self.download(False, False, True)[2]
+
+    def WorldBound(self) -> np.ndarray:
+        out = (C.c_float * 6)()
+        L.check(L.lib().rt_lbvh_world_bound(self.ctx.h, self.h, out), self.ctx.h, "rt_lbvh_world_bound")
+        return np.array(out[:], np.float32)
+
+
+class StructureConstruction:
+    """GPUBuildStructure(depth) over a device soup (StructureConstruction.cpp:86-131)."""
+
+    def __init__(self, ctx: Context, max_tris: int, depth: int):
+        self.lbvh = LBVH(ctx, max_tris, depth)
+
+    def GPUBuildStructure(self, tris) -> LBVH:
+        return self.lbvh.Build(tris)
+
+
+def hits_to_numpy(t: torch.Tensor) -> np.ndarray:
+    return t.cpu().numpy().view(L.HIT_DTYPE).reshape(-1)
+
+
+class RayTracer:
+    """Per-frame stages over an LBVH (RayTracerCS::Render)."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+
+    def _alloc_hits(self, n: int) -> torch.Tensor:
+        return torch.empty((n, 4), dtype=torch.int32, device=self.ctx.torch_device)
+
+    def primary(self, lbvh: LBVH, cam: L.Camera, stats: bool = False, out: torch.Tensor | None = None):
+        npx = cam.width * cam.height
+        hits = out if out is not None else self._alloc_hits(npx)
+        st = torch.empty((npx, 2), dtype=torch.int32, device=self.ctx.torch_device) if stats else None
+        L.check(L.lib().rt_trace_primary(self.ctx.h, lbvh.h, C.byref(cam), _dev_ptr(hits),
+                                         _dev_ptr(st) if stats else None), self.ctx.h, "rt_trace_primary")
+        return (hits, st) if stats else hits
+
+    def shadow_mirror(self, lbvh: LBVH, cam: L.Camera, light, primary: torch.Tensor, stats: bool = False,
+                      vis: torch.Tensor | None = None, mirror: torch.Tensor | None = None):
+        npx = cam.width * cam.height
+        vis = vis if vis is not None else torch.empty(npx, dtype=torch.uint8, device=self.ctx.torch_device)
+        mirror = mirror if mirror is not None else self._alloc_hits(npx)
+        ss = torch.empty((npx, 2), dtype=torch.int32, device=self.ctx.torch_device) if stats else None
+        ms = torch.empty((npx, 2), dtype=torch.int32, device=self.ctx.torch_device) if stats else None
+        lf = (C.c_float * 3)(*light)
+        L.check(L.lib().rt_trace_shadow_mirror(self.ctx.h, lbvh.h, C.byref(cam), lf, _dev_ptr(primary),
+                                               _dev_ptr(vis), _dev_ptr(mirror), _dev_ptr(ss) if stats else None,
+                                               _dev_ptr(ms) if stats else None), self.ctx.h,
+                "rt_trace_shadow_mirror")
+        return (vis, mirror, ss, ms) if stats else (vis, mirror)
+
+    def rays(self, lbvh: LBVH, rays: torch.Tensor, any_hit: bool = False, stats: bool = False):
+        """rays: (n, 8) float32 device tensor laid out as rt_ray {o, exclude(int bits), d, tmax}."""
+        n = rays.shape[0]
+        hits = self._alloc_hits(n)
+        st = torch.empty((n, 2), dtype=torch.int32, device=self.ctx.torch_device) if stats else None
+        L.check(L.lib().rt_trace_rays(self.ctx.h, lbvh.h, _dev_ptr(rays), n, int(any_hit), _dev_ptr(hits),
+                                      _dev_ptr(st) if stats else None), self.ctx.h, "rt_trace_rays")
+        return (hits, st) if stats else hits
+
+    def render_frame_host(self, lbvh: LBVH, tris: np.ndarray, cam: L.Camera, light, primary: np.ndarray,
+                          vis: np.ndarray, mirror: np.ndarray):
+        lf = (C.c_float * 3)(*light)
+        L.check(L.lib().rt_render_frame_host(self.ctx.h, lbvh.h, _host_ptr(tris), len(tris), C.byref(cam), lf,
+                                             _host_ptr(primary), _host_ptr(vis), _host_ptr(mirror)),
+                self.ctx.h, "rt_render_frame_host")
+
+    def pathtrace(self, lbvh: LBVH, albedo: torch.Tensor, emission: torch.Tensor, cam: L.Camera, spp: int,
+                  bounces: int, seed: int, sky=(1.0, 1.0, 1.0), out: torch.Tensor | None = None) -> torch.Tensor:
+        img = out if out is not None else torch.empty((cam.height * cam.width, 4), dtype=torch.float32,
+                                                      device=self.ctx.torch_device)
+        p = L.PtParams(spp, bounces, seed, (C.c_float * 3)(*sky), 0)
+        L.check(L.lib().rt_pathtrace(self.ctx.h, lbvh.h, _dev_ptr(albedo), _dev_ptr(emission), C.byref(cam),
+                                     C.byref(p), _dev_ptr(img)), self.ctx.h, "rt_pathtrace")
+        return img
+
+    def pathtrace_adjoint(self, lbvh: LBVH, albedo: torch.Tensor, emission: torch.Tensor, cam: L.Camera, spp: int,
+                          bounces: int, seed: int, d_image: torch.Tensor, sky=(1.0, 1.0, 1.0)):
+        d_alb = torch.zeros_like(albedo)
+        d_le = torch.zeros(3, dtype=torch.float32, device=self.ctx.torch_device)
+        p = L.PtParams(spp, bounces, seed, (C.c_float * 3)(*sky), 0)
+        L.check(L.lib().rt_pathtrace_adjoint(self.ctx.h, lbvh.h, _dev_ptr(albedo), _dev_ptr(emission), C.byref(cam),
+                                             C.byref(p), _dev_ptr(d_image.contiguous()), _dev_ptr(d_alb),
+                                             _dev_ptr(d_le)), self.ctx.h, "rt_pathtrace_adjoint")
+        return d_alb, d_le
+
+
+def rays_tensor(o, d, tmax, exclude, device) -> torch.Tensor:
+    """Packs rays into the rt_ray layout as an (n, 8) float32 tensor."""
+    n = len(d)
+    r = np.zeros((n, 8), np.float32)
+    r[:, 0:3] = o
+    r[:, 3] = np.asarray(exclude, np.int32).view(np.float32) if np.ndim(exclude) else np.int32(exclude).view(np.float32)
+    r[:, 4:7] = d
+    r[:, 7] = tmax
+    return torch.from_numpy(r).to(device)

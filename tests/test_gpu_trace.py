@@ -1,0 +1,145 @@
+"""GPU traversal parity against the oracle's restatement of LBVH_IntersectP
+(LBVH.hlsl:363-440) and the shading rays of CSComputeColorRT.hlsl:
+closest-hit ids bit-exact, t / u / v bit-exact (tolerance stated by the
+contract: 1e-6 relative), per-ray box/triangle test counts equal."""
+import numpy as np
+import pytest
+
+from conftest import camera_from_array, golden_cases, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def build_both(ctx, oracle_mod, tris, depth):
+    import torch
+    from rtgpu.api import LBVH
+    lb = LBVH(ctx, len(tris), depth)
+    dt = torch.from_numpy(np.ascontiguousarray(tris)).cuda()
+    lb.Build(dt)
+    nodes, ids, keys, _ = oracle_mod.lbvh_build(tris, depth)
+    return lb, dt, nodes, ids
+
+
+def assert_hits_equal(gpu, ref, what):
+    assert np.array_equal(gpu["id"], ref["id"]), f"{what}: {np.sum(gpu['id'] != ref['id'])} id mismatches"
+    hit = ref["id"] >= 0
+    t_rel = np.abs(gpu["t"][hit] - ref["t"][hit]) / np.maximum(np.abs(ref["t"][hit]), 1e-30)
+    assert t_rel.max(initial=0.0) <= 1e-6, what
+    # the kernels evaluate the reference's operation order without contraction: exact
+    assert np.array_equal(gpu["t"], ref["t"]) and np.array_equal(gpu["u"], ref["u"]) and np.array_equal(gpu["v"], ref["v"])
+
+
+@pytest.fixture(scope="module")
+def torus_scene(gpu_ctx, oracle_mod):
+    from rtgpu import scenes
+    tris = scenes.torus()
+    lb, dt, nodes, ids = build_both(gpu_ctx, oracle_mod, tris, 20)
+    return tris, lb, dt, nodes, ids
+
+
+def test_primary_torus_512(gpu_ctx, oracle_mod, torus_scene):
+    from rtgpu import scenes
+    from rtgpu.api import RayTracer, hits_to_numpy
+    tris, lb, dt, nodes, ids = torus_scene
+    cam = scenes.torus_camera()
+    hits, st = RayTracer(gpu_ctx).primary(lb, cam, stats=True)
+    gpu_ctx.check()
+    oh, ost = oracle_mod.trace(nodes, 20, ids, tris, oracle_mod.primary_rays(cam), stats=True)
+    assert_hits_equal(hits_to_numpy(hits), oh, "primary")
+    assert np.array_equal(st.cpu().numpy().astype(np.uint32), ost)
+    assert (oh["id"] >= 0).mean() > 0.2
+
+
+def test_shadow_mirror_torus_512(gpu_ctx, oracle_mod, torus_scene):
+    from rtgpu import scenes
+    from rtgpu.api import RayTracer, hits_to_numpy
+    tris, lb, dt, nodes, ids = torus_scene
+    cam = scenes.torus_camera()
+    rt = RayTracer(gpu_ctx)
+    hits = rt.primary(lb, cam)
+    vis, mirror, ss, ms = rt.shadow_mirror(lb, cam, scenes.TORUS_LIGHT, hits, stats=True)
+    gpu_ctx.check()
+    oh = oracle_mod.trace(nodes, 20, ids, tris, oracle_mod.primary_rays(cam))
+    ovis, omir, oss, oms = oracle_mod.shadow_mirror(nodes, 20, ids, tris, cam, scenes.TORUS_LIGHT, oh, stats=True)
+    assert np.array_equal(vis.cpu().numpy(), ovis)
+    assert set(np.unique(ovis)) >= {0, 2, 3}
+    assert_hits_equal(hits_to_numpy(mirror), omir, "mirror")
+    assert np.array_equal(ss.cpu().numpy().astype(np.uint32), oss)
+    assert np.array_equal(ms.cpu().numpy().astype(np.uint32), oms)
+
+
+@pytest.mark.parametrize("any_hit", [False, True])
+def test_generic_rays_with_exclusion(gpu_ctx, oracle_mod, any_hit):
+    """Random rays inside a triangle soup, half leaving from a triangle they
+    must exclude, some with axis-aligned directions (infinite 1/d: the
+    reference's NaN-sensitive std::min/std::max path)."""
+    import torch
+    from rtgpu import scenes
+    from rtgpu.api import RayTracer, hits_to_numpy, rays_tensor
+    tris = scenes.random_soup(50000, seed=51)
+    lb, dt, nodes, ids = build_both(gpu_ctx, oracle_mod, tris, 18)
+    rng = np.random.default_rng(52)
+    n = 40000
+    src = rng.integers(0, len(tris), n)
+    o = tris[src].reshape(n, 3, 3).mean(axis=1).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d[: n // 8, rng.integers(0, 3)] = 0.0           # exact zero components
+    d[n // 8: n // 4, :2] = 0.0
+    d[n // 8: n // 4, 2] = 1.0
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    excl = np.where(np.arange(n) % 2 == 0, src, -1).astype(np.int32)
+    tmax = np.where(np.arange(n) % 3 == 0, 0.05, 1e16).astype(np.float32)
+    hits, st = RayTracer(gpu_ctx).rays(lb, rays_tensor(o, d, tmax, excl, "cuda"), any_hit=any_hit, stats=True)
+    gpu_ctx.check()
+    orays = oracle_mod.rays_array(o, d, tmax, excl)
+    oh, ost = oracle_mod.trace(nodes, 18, ids, tris, orays, any_hit=any_hit, stats=True)
+    g = hits_to_numpy(hits)
+    if any_hit:
+        assert np.array_equal(g["id"] >= 0, oh["id"] >= 0)
+        assert np.array_equal(g["id"], oh["id"])
+    else:
+        assert_hits_equal(g, oh, "rays")
+    assert np.array_equal(st.cpu().numpy().astype(np.uint32), ost)
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_trace_on_reference_tree(gpu_ctx, case):
+    """The reference's own CPU-built tree (golden fixture) imported through
+    rt_lbvh_import_host and traced on the GPU: hits equal the reference's
+    LBVH::IntersectP up to its tie order (t bit-exact)."""
+    import torch
+    from rtgpu._lib import NODE_DTYPE, RT_NODE_SENTINEL
+    from rtgpu.api import LBVH, RayTracer, hits_to_numpy, rays_tensor
+    g = load_golden(case)
+    depth = int(g["depth"])
+    nodes = np.zeros(1 << depth, NODE_DTYPE)
+    nodes["prim_count"] = RT_NODE_SENTINEL
+    nodes["prim_pos"] = RT_NODE_SENTINEL
+    nodes[g["node_index"]] = g["nodes"].astype(NODE_DTYPE)
+    lb = LBVH(gpu_ctx, len(g["tris"]), depth).Import(nodes, g["ids"], g["tris"])
+    r = g["rays"]
+    hits = hits_to_numpy(RayTracer(gpu_ctx).rays(lb, rays_tensor(r[:, 0:3], r[:, 3:6], r[:, 6], r[:, 7].astype(np.int32), "cuda")))
+    gpu_ctx.check()
+    assert np.array_equal(hits["t"], g["hit_t"])
+    diff = hits["id"] != g["hit_id"]
+    assert np.all(hits["id"][diff] < g["hit_id"][diff])  # tie rule: smallest id among equal t
+    assert diff.mean() < 0.01
+
+
+def test_render_frame_host_equals_device_path(gpu_ctx, torus_scene):
+    from rtgpu import scenes
+    from rtgpu._lib import HIT_DTYPE
+    from rtgpu.api import LBVH, RayTracer, hits_to_numpy
+    tris, lb, dt, nodes, ids = torus_scene
+    cam = scenes.torus_camera(320, 200)
+    rt = RayTracer(gpu_ctx)
+    hits = rt.primary(lb, cam)
+    vis, mirror = rt.shadow_mirror(lb, cam, scenes.TORUS_LIGHT, hits)
+    lb2 = LBVH(gpu_ctx, len(tris), 20)
+    hp = np.zeros(cam.width * cam.height, HIT_DTYPE)
+    hv = np.zeros(cam.width * cam.height, np.uint8)
+    hm = np.zeros(cam.width * cam.height, HIT_DTYPE)
+    rt.render_frame_host(lb2, tris, cam, scenes.TORUS_LIGHT, hp, hv, hm)
+    assert np.array_equal(hp, hits_to_numpy(hits))
+    assert np.array_equal(hv, vis.cpu().numpy())
+    assert np.array_equal(hm, hits_to_numpy(mirror))
