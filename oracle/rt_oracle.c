@@ -240,14 +240,27 @@ static inline int tri_test(const float* A, const float* B, const float* C, const
     return (uu >= 0.0f) && (uu <= 1.0f) && (vv >= 0.0f) && ((uu + vv) <= 1.0f) && (tt >= 0.0f);
 }
 
-/* Closest hit over the implicit heap: LBVH_IntersectP (LBVH.hlsl:363-440),
- * the stackless "trail" walk of LBVH::IntersectP (LBVH.cpp:973-1038).
- * Differences from the CPU code, following the GPU shader:
+/* Closest hit over the implicit heap: LBVH_IntersectP (LBVH.hlsl:363-440) /
+ * LBVH::IntersectP (LBVH.cpp:919-1039), with the same box test, the same
+ * triangle test, the same pruning (a node is entered unless T1 < 0 or
+ * T0 > closest t, LBVH.cpp:992 / LBVH.hlsl:390) and depth-first order.
+ * Differences, none of which changes a result:
  *   - the excluded triangle is skipped without overwriting it (LBVH.hlsl:415;
  *     LBVH.cpp:1015 overwrites TriangleID, which only matters for rays that
  *     carry an exclusion);
  *   - ties at equal t keep the smaller triangle id, so the result does not
- *     depend on the order triangles are tested in. */
+ *     depend on the order triangles are tested in;
+ *   - the near child is chosen by the ray direction on the node's split
+ *     axis.  The reference indexes signo[] with the stored axis field
+ *     (LBVH.cpp:1033, LBVH.hlsl:432), which build_recursive sets to
+ *     (30 - bit) % 3: one axis after the one the bit splits (bits 3k+2,
+ *     3k+1, 3k split x, y, z).  The split axis is (field + 2) % 3.  Visiting
+ *     order only changes how many nodes are tested, not the closest hit
+ *     under the tie rule; the golden tests against LBVH::IntersectP pin it.
+ * Walk: both children of an entered internal node (heap slots 2i, 2i+1) are
+ * box-tested together, the near one is entered, a hit far one is pushed with
+ * its entry distance and re-checked against the closest t when popped.
+ * Box tests are counted as 1 (root) + 2 per entered internal node. */
 static void trace_one(const or_node* nodes, const uint32_t* ids, const float* tris, const float* r,
                       or_hit* out, uint32_t* stats, int any_hit) {
     const float o[3] = {r[0], r[1], r[2]};
@@ -257,40 +270,63 @@ static void trace_one(const or_node* nodes, const uint32_t* ids, const float* tr
     int sgn[3] = {d[0] < 0.0f, d[1] < 0.0f, d[2] < 0.0f};
     float best_t = r[6], best_u = -1.0f, best_v = -1.0f;
     int best_id = -1;
-    uint32_t nbox = 0, ntri = 0;
-    uint32_t node = 1, trail = 1;
-    do {
-        const or_node* nd = &nodes[node];
-        float T0, T1;
-        box_interval(nd, o, inv, &T0, &T1);
-        ++nbox;
-        int p = __builtin_ctz(trail + 1);
-        if ((T0 > best_t) || (T1 < 0.0f)) {
-            trail = (trail >> p) + 1;
-            node = (node >> p) ^ 1u;
-        } else if (nd->prim_count & 4) {
-            int cnt = nd->prim_count >> 3;
-            int pos = nd->prim_pos;
-            for (int i = 0; i < cnt; ++i) {
-                ++ntri;
-                int id = (int)ids[pos + i];
-                if (id == exclude) continue;
-                const float* t = tris + 9 * (size_t)id;
-                float u, v, tt;
-                if (tri_test(t, t + 3, t + 6, o, d, &u, &v, &tt)) {
-                    if (tt < best_t || (tt == best_t && best_id >= 0 && id < best_id)) {
-                        best_t = tt; best_u = u; best_v = v; best_id = id;
+    uint32_t nbox = 1, ntri = 0;
+    uint32_t stack_node[64];
+    float stack_t0[64];
+    int sp = 0;
+    float T0, T1;
+    box_interval(&nodes[1], o, inv, &T0, &T1);
+    int have = !(T1 < 0.0f) && !(T0 > best_t);
+    uint32_t node = 1;
+    for (;;) {
+        if (have) {
+            const or_node* nd = &nodes[node];
+            if (nd->prim_count & 4) {
+                int cnt = nd->prim_count >> 3;
+                int pos = nd->prim_pos;
+                for (int i = 0; i < cnt; ++i) {
+                    ++ntri;
+                    int id = (int)ids[pos + i];
+                    if (id == exclude) continue;
+                    const float* t = tris + 9 * (size_t)id;
+                    float u, v, tt;
+                    if (tri_test(t, t + 3, t + 6, o, d, &u, &v, &tt)) {
+                        if (tt < best_t || (tt == best_t && best_id >= 0 && id < best_id)) {
+                            best_t = tt; best_u = u; best_v = v; best_id = id;
+                        }
                     }
                 }
+                if (any_hit && best_id >= 0) break;
+            } else {
+                const uint32_t c0 = node << 1;
+                float tl, tr, t1l, t1r;
+                box_interval(&nodes[c0], o, inv, &tl, &t1l);
+                box_interval(&nodes[c0 + 1], o, inv, &tr, &t1r);
+                nbox += 2;
+                const int hl = !(t1l < 0.0f) && !(tl > best_t);
+                const int hr = !(t1r < 0.0f) && !(tr > best_t);
+                const int near_right = sgn[((nd->prim_count & 3) + 2) % 3];
+                const int hn = near_right ? hr : hl, hf = near_right ? hl : hr;
+                const float tf = near_right ? tl : tr;
+                const uint32_t nn = c0 | (uint32_t)near_right, nf = nn ^ 1u;
+                if (hn) {
+                    if (hf) { stack_node[sp] = nf; stack_t0[sp] = tf; ++sp; }
+                    node = nn;
+                    continue;
+                } else if (hf) {
+                    node = nf;
+                    continue;
+                }
             }
-            if (any_hit && best_id >= 0) break;
-            trail = (trail >> p) + 1;
-            node = (node >> p) ^ 1u;
-        } else {
-            trail <<= 1;
-            node = (node << 1) | (uint32_t)sgn[nd->prim_count & 3];
         }
-    } while (trail > 1);
+        int found = 0;
+        while (sp > 0) {
+            --sp;
+            if (!(stack_t0[sp] > best_t)) { node = stack_node[sp]; found = 1; break; }
+        }
+        if (!found) break;
+        have = 1;
+    }
     out->id = best_id;
     out->u = best_u;
     out->v = best_v;

@@ -2,18 +2,22 @@
 //
 // Restates LBVH_IntersectP (RayTracerCS/Shaders/AccelerationStructures/
 // LBVH.hlsl:363-440) and LBVH::IntersectP (LBVH.cpp:919-1039) as a
-// stack-based walk with the same visit order: at an internal node both
-// children (heap slots 2i, 2i+1: one 64-byte line) are box-tested, the near
-// child (chosen by the sign of the ray direction on the node's axis field,
-// LBVH.hlsl:432) is entered first and a hit far child is pushed with its
-// entry distance; a popped node is entered only if that distance still does
-// not exceed the closest hit.  This enters exactly the nodes the reference's
-// trail walk enters and performs the same number of box and triangle tests.
+// stack-based depth-first walk: at an internal node both children (heap
+// slots 2i, 2i+1: one 64-byte line) are box-tested, the near child is
+// entered first and a hit far child is pushed with its entry distance; a
+// popped node is entered only if that distance still does not exceed the
+// closest hit (the reference's pruning, LBVH.cpp:992).  The near child is
+// chosen by the ray direction on the node's split axis; the reference
+// indexes signo[] with the stored axis field (LBVH.cpp:1033), which
+// build_recursive sets one axis past the split axis, so it orders children
+// arbitrarily.  Order changes only the number of tests, not the closest hit:
+// ties at equal t keep the smaller triangle id.  The CPU oracle walks the
+// same order and counts the same tests.
 //
 // Box test = RayBoxInterval (LBVH.cpp:634-659), triangle test =
 // RayTriangleTest (AccelerationStructure.h:70-97), both in the reference's
-// operation order without contraction.  Ties at equal t keep the smaller
-// triangle id.  The excluded triangle is skipped (LBVH.hlsl:415).
+// operation order without contraction.  The excluded triangle is skipped
+// (LBVH.hlsl:415).
 #pragma once
 #include "rt_internal.cuh"
 
@@ -33,7 +37,7 @@ struct TreeRef {
 
 struct RayState {
     f3 o, d, inv;
-    int sgn[3];
+    uint32_t sgn;  // bit c set when d[c] < 0 (signo[] of LBVH.cpp:983-985)
     int exclude;
     float tmax;
     bool exact;  // some 1/d is infinite: use the reference's NaN-sensitive min/max
@@ -44,9 +48,7 @@ __device__ __forceinline__ RayState make_ray(f3 o, f3 d, float tmax, int exclude
     r.o = o;
     r.d = d;
     r.inv = mk3(fdiv(1.0f, d.x), fdiv(1.0f, d.y), fdiv(1.0f, d.z));
-    r.sgn[0] = d.x < 0.0f;  // signo[] of LBVH.cpp:983-985
-    r.sgn[1] = d.y < 0.0f;
-    r.sgn[2] = d.z < 0.0f;
+    r.sgn = (uint32_t)(d.x < 0.0f) | ((uint32_t)(d.y < 0.0f) << 1) | ((uint32_t)(d.z < 0.0f) << 2);
     r.exclude = exclude;
     r.tmax = tmax;
     r.exact = isinf(r.inv.x) || isinf(r.inv.y) || isinf(r.inv.z);
@@ -176,7 +178,10 @@ __device__ __forceinline__ Hit traverse(const RayState& r, const TreeRef& tr_, b
                 const bool hl = box_enter<EXACT>(r, l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, best.t, &tl);
                 const bool hr = box_enter<EXACT>(r, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, best.t, &tr);
                 if (STATS) nbox += 2;
-                const int near_right = r.sgn[pc & 3];
+                // near child by the split axis: the stored field is (30 - bit) % 3,
+                // the axis the bit splits is (field + 2) % 3
+                const int field = pc & 3;
+                const int near_right = (r.sgn >> (field == 0 ? 2 : field - 1)) & 1;
                 const bool hn = near_right ? hr : hl, hf = near_right ? hl : hr;
                 const float tf = near_right ? tl : tr;
                 const uint32_t nn = c0 | (uint32_t)near_right, nf = nn ^ 1u;

@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 from conftest import camera_from_array, golden_cases, load_golden
+import tri_np
 
 pytestmark = pytest.mark.gpu
 
@@ -120,10 +121,7 @@ def test_trace_on_reference_tree(gpu_ctx, case):
     r = g["rays"]
     hits = hits_to_numpy(RayTracer(gpu_ctx).rays(lb, rays_tensor(r[:, 0:3], r[:, 3:6], r[:, 6], r[:, 7].astype(np.int32), "cuda")))
     gpu_ctx.check()
-    assert np.array_equal(hits["t"], g["hit_t"])
-    diff = hits["id"] != g["hit_id"]
-    assert np.all(hits["id"][diff] < g["hit_id"][diff])  # tie rule: smallest id among equal t
-    assert diff.mean() < 0.01
+    tri_np.assert_matches_reference(hits["id"], hits["t"], g["hit_id"], g["hit_t"], r, g["tris"])
 
 
 def test_render_frame_host_equals_device_path(gpu_ctx, torus_scene):
