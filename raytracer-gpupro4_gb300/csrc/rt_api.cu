@@ -44,19 +44,21 @@ extern "C" rt_status rt_ctx_create(int device, void* stream, rt_ctx** out) {
     c->device = device;
     c->stream = static_cast<cudaStream_t>(stream);
     if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
-        cudaMalloc((void**)&c->d_err, sizeof(uint32_t)) != cudaSuccess ||
-        cudaMemset(c->d_err, 0, sizeof(uint32_t)) != cudaSuccess) {
-        if (c->d_err) cudaFree(c->d_err);
+        cudaMalloc((void**)&c->d_words, 64 * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMemset(c->d_words, 0, 64 * sizeof(uint32_t)) != cudaSuccess) {
+        if (c->d_words) cudaFree(c->d_words);
         delete c;
         return RT_ERR_CUDA;
     }
+    c->d_err = c->d_words;
+    c->d_work = c->d_words + 16;
     *out = c;
     return RT_OK;
 }
 
 extern "C" rt_status rt_ctx_destroy(rt_ctx* ctx) {
     if (!ctx) return RT_OK;
-    if (ctx->d_err) cudaFree(ctx->d_err);
+    if (ctx->d_words) cudaFree(ctx->d_words);
     delete ctx;
     return RT_OK;
 }

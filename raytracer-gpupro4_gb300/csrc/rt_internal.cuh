@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <string>
@@ -84,7 +85,9 @@ struct rt_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     std::string last_error;
-    uint32_t* d_err = nullptr;  // device error word
+    uint32_t* d_err = nullptr;   // device error word (d_words[0])
+    uint32_t* d_work = nullptr;  // work counters of the persistent kernels (d_words[16..])
+    uint32_t* d_words = nullptr; // 64 device words
     int num_sms = 0;
 };
 
@@ -138,3 +141,24 @@ rt_status rt_fail(rt_ctx* ctx, rt_status s, const char* fmt, ...);
 // Bounded spin used by every device-side wait (look-back): after this many
 // polls the waiter records RT_DEVERR_TIMEOUT and stops waiting.
 constexpr uint32_t kSpinLimit = 1u << 22;
+
+// Grid of a persistent kernel: as many blocks as fit on every SM at once,
+// capped by the number of 32-item tiles.
+template <typename K>
+inline uint32_t persistent_blocks(const rt_ctx* ctx, K kernel, int threads, uint32_t tiles) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const uint64_t full = (uint64_t)per_sm * (uint64_t)ctx->num_sms;
+    const uint64_t need = ((uint64_t)tiles * 32 + threads - 1) / threads;
+    return (uint32_t)std::max<uint64_t>(1, std::min(full, need));
+}
+
+// Work-counter slots (ctx->d_work) of the persistent kernels.
+enum : int { kWorkPrimary = 0, kWorkSecondary = 1, kWorkRays = 2, kWorkPath = 3, kWorkAdjoint = 4 };
+
+inline rt_status reset_work(rt_ctx* ctx, int slot) {
+    RT_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_work + slot, 0, sizeof(uint32_t), ctx->stream));
+    return RT_OK;
+}
+

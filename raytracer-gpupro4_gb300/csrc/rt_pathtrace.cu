@@ -125,13 +125,26 @@ __device__ __forceinline__ int trace_path(const TreeRef& tr, const float* __rest
     return ns;
 }
 
+__device__ __forceinline__ void path_pixel(const TreeRef& tr, const float* __restrict__ soup,
+                                           const float* __restrict__ albedo, const float* __restrict__ emission,
+                                           const PathParams& P, float4* __restrict__ image, uint32_t i, uint32_t j);
+
 __global__ void __launch_bounds__(kPtThreads) k_pathtrace(TreeRef tr, const float* __restrict__ soup,
                                                           const float* __restrict__ albedo,
                                                           const float* __restrict__ emission, PathParams P,
-                                                          float4* __restrict__ image) {
-    const uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t i, j;
-    if (!tile_pixel(tile, threadIdx.x & 31, P.cam.width, P.cam.height, &i, &j)) return;
+                                                          float4* __restrict__ image, uint32_t* work,
+                                                          uint32_t num_tiles) {
+    for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
+        uint32_t i, j;
+        if (tile_pixel(tile, threadIdx.x & 31, P.cam.width, P.cam.height, &i, &j))
+            path_pixel(tr, soup, albedo, emission, P, image, i, j);
+        __syncwarp();
+    }
+}
+
+__device__ __forceinline__ void path_pixel(const TreeRef& tr, const float* __restrict__ soup,
+                                           const float* __restrict__ albedo, const float* __restrict__ emission,
+                                           const PathParams& P, float4* __restrict__ image, uint32_t i, uint32_t j) {
     float acc[3] = {0.0f, 0.0f, 0.0f};
     for (uint32_t n = 0; n < P.spp; ++n) {
         const float fant = fdiv((float)n, (float)(n + 1));
@@ -158,11 +171,12 @@ __global__ void __launch_bounds__(kPtThreads) k_pathtrace(TreeRef tr, const floa
 __global__ void __launch_bounds__(kPtThreads) k_pathtrace_adjoint(
     TreeRef tr, const float* __restrict__ soup,
     const float* __restrict__ albedo, const float* __restrict__ emission, PathParams P,
-    const float4* __restrict__ dimage, float* __restrict__ dalbedo, float* __restrict__ demission) {
-    const uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t i, j;
+    const float4* __restrict__ dimage, float* __restrict__ dalbedo, float* __restrict__ demission, uint32_t* work,
+    uint32_t num_tiles) {
     float dle[3] = {0.0f, 0.0f, 0.0f};
-    if (tile_pixel(tile, threadIdx.x & 31, P.cam.width, P.cam.height, &i, &j)) {
+    for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
+        uint32_t i, j;
+        if (!tile_pixel(tile, threadIdx.x & 31, P.cam.width, P.cam.height, &i, &j)) continue;
         const float4 g4 = __ldg(dimage + (size_t)j * P.cam.width + i);
         const float gimg[3] = {g4.x, g4.y, g4.z};
         for (uint32_t n = 0; n < P.spp; ++n) {
@@ -219,9 +233,8 @@ rt_status pt_args(rt_ctx* ctx, const rt_lbvh* l, const float* a, const float* e,
     return RT_OK;
 }
 
-uint32_t px_blocks(const rt_camera* cam) {
-    const uint64_t tiles = (uint64_t)((cam->width + 7) / 8) * ((cam->height + 3) / 4);
-    return (uint32_t)((tiles * 32 + kPtThreads - 1) / kPtThreads);
+uint32_t px_tiles(const rt_camera* cam) {
+    return (uint32_t)(((cam->width + 7) / 8) * ((cam->height + 3) / 4));
 }
 
 }  // namespace
@@ -234,8 +247,11 @@ extern "C" rt_status rt_pathtrace(rt_ctx* ctx, const rt_lbvh* l, const float* d_
     rt_status s = pt_args(ctx, l, d_albedo, d_emission, cam, p, &P, "rt_pathtrace");
     if (s != RT_OK) return s;
     if (!d_image) return rt_fail(ctx, RT_ERR_INVALID, "rt_pathtrace: null image");
-    k_pathtrace<<<px_blocks(cam), kPtThreads, 0, ctx->stream>>>(tree_ref(ctx, l), l->src_tris, d_albedo,
-                                                               d_emission, P, reinterpret_cast<float4*>(d_image));
+    if ((s = reset_work(ctx, kWorkPath)) != RT_OK) return s;
+    const uint32_t tiles = px_tiles(cam);
+    k_pathtrace<<<persistent_blocks(ctx, k_pathtrace, kPtThreads, tiles), kPtThreads, 0, ctx->stream>>>(
+        tree_ref(ctx, l), l->src_tris, d_albedo, d_emission, P, reinterpret_cast<float4*>(d_image),
+        ctx->d_work + kWorkPath, tiles);
     RT_CHECK_LAUNCH(ctx, "k_pathtrace");
     return RT_OK;
 }
@@ -247,9 +263,12 @@ extern "C" rt_status rt_pathtrace_adjoint(rt_ctx* ctx, const rt_lbvh* l, const f
     rt_status s = pt_args(ctx, l, d_albedo, d_emission, cam, p, &P, "rt_pathtrace_adjoint");
     if (s != RT_OK) return s;
     if (!d_dimage || !d_dalbedo || !d_demission) return rt_fail(ctx, RT_ERR_INVALID, "rt_pathtrace_adjoint: null buffer");
-    k_pathtrace_adjoint<<<px_blocks(cam), kPtThreads, 0, ctx->stream>>>(
-        tree_ref(ctx, l), l->src_tris, d_albedo, d_emission, P, reinterpret_cast<const float4*>(d_dimage),
-        d_dalbedo, d_demission);
+    if ((s = reset_work(ctx, kWorkAdjoint)) != RT_OK) return s;
+    const uint32_t tiles = px_tiles(cam);
+    k_pathtrace_adjoint<<<persistent_blocks(ctx, k_pathtrace_adjoint, kPtThreads, tiles), kPtThreads, 0,
+                          ctx->stream>>>(tree_ref(ctx, l), l->src_tris, d_albedo, d_emission, P,
+                                         reinterpret_cast<const float4*>(d_dimage), d_dalbedo, d_demission,
+                                         ctx->d_work + kWorkAdjoint, tiles);
     RT_CHECK_LAUNCH(ctx, "k_pathtrace_adjoint");
     return RT_OK;
 }

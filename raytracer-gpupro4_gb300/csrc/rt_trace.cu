@@ -7,6 +7,11 @@
 // in registers, no 48-byte ray buffer round trip); the shadow ray and the
 // mirror bounce of CSComputeColor (CSComputeColorRT.hlsl:57-177, 203-210,
 // flat normals, no textures) are k_trace_secondary.
+//
+// All three kernels are persistent: a grid sized to fill every SM once, each
+// warp pulling 32-ray tiles (8 x 4 pixels) from a work counter until the
+// image is done.  Ray cost varies by three orders of magnitude across the
+// image, so a static grid leaves SMs idle behind the last heavy tiles.
 #include <algorithm>
 
 #include "rt_traverse.cuh"
@@ -24,30 +29,33 @@ __device__ __forceinline__ void store_hit(rt_hit* out, const Hit& h) {
 template <bool STATS>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_camera cam,
                                                                  rt_hit* __restrict__ hits,
-                                                                 uint32_t* __restrict__ stats) {
-    const uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t i, j;
-    if (!tile_pixel(tile, threadIdx.x & 31, cam.width, cam.height, &i, &j)) return;
-    const f3 d = primary_dir(cam, i, j);
-    const RayState r = make_ray(mk3(cam.eye[0], cam.eye[1], cam.eye[2]), d, 1e16f, -1);
-    uint32_t nb = 0, nt = 0;
-    const Hit h = trace_ray<STATS>(r, tr, false, &nb, &nt);
-    const size_t p = (size_t)j * cam.width + i;
-    store_hit(hits + p, h);
-    if (STATS) {
-        stats[2 * p] = nb;
-        stats[2 * p + 1] = nt;
+                                                                 uint32_t* __restrict__ stats, uint32_t* work,
+                                                                 uint32_t num_tiles) {
+    for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
+        uint32_t i, j;
+        if (tile_pixel(tile, threadIdx.x & 31, cam.width, cam.height, &i, &j)) {
+            const f3 d = primary_dir(cam, i, j);
+            const RayState r = make_ray(mk3(cam.eye[0], cam.eye[1], cam.eye[2]), d, 1e16f, -1);
+            uint32_t nb = 0, nt = 0;
+            const Hit h = trace_ray<STATS>(r, tr, false, &nb, &nt);
+            const size_t p = (size_t)j * cam.width + i;
+            store_hit(hits + p, h);
+            if (STATS) {
+                stats[2 * p] = nb;
+                stats[2 * p + 1] = nt;
+            }
+        }
+        __syncwarp();
     }
 }
 
 // Shadow (any hit) and mirror (closest hit) rays of one pixel.
 template <bool STATS>
-__global__ void __launch_bounds__(kTraceThreads) k_trace_secondary(
-    TreeRef tr, const float* __restrict__ soup, rt_camera cam, float lx, float ly, float lz, const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis,
-    rt_hit* __restrict__ mirror, uint32_t* __restrict__ sstats, uint32_t* __restrict__ mstats) {
-    const uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t i, j;
-    if (!tile_pixel(tile, threadIdx.x & 31, cam.width, cam.height, &i, &j)) return;
+__device__ __forceinline__ void secondary_pixel(const TreeRef& tr, const float* __restrict__ soup,
+                                                const rt_camera& cam, float lx, float ly, float lz,
+                                                const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis,
+                                                rt_hit* __restrict__ mirror, uint32_t* __restrict__ sstats,
+                                                uint32_t* __restrict__ mstats, uint32_t i, uint32_t j) {
     const size_t p = (size_t)j * cam.width + i;
     const int4 ph = __ldg(reinterpret_cast<const int4*>(prim + p));
     const int id = ph.x;
@@ -99,21 +107,52 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_secondary(
 }
 
 template <bool STATS>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_secondary(
+    TreeRef tr, const float* __restrict__ soup, rt_camera cam, float lx, float ly, float lz,
+    const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis, rt_hit* __restrict__ mirror,
+    uint32_t* __restrict__ sstats, uint32_t* __restrict__ mstats, uint32_t* work, uint32_t num_tiles) {
+    for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
+        uint32_t i, j;
+        if (tile_pixel(tile, threadIdx.x & 31, cam.width, cam.height, &i, &j))
+            secondary_pixel<STATS>(tr, soup, cam, lx, ly, lz, prim, vis, mirror, sstats, mstats, i, j);
+        __syncwarp();
+    }
+}
+
+template <bool STATS>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_rays(TreeRef tr, const rt_ray* __restrict__ rays, uint32_t n,
                                                               int any_hit, rt_hit* __restrict__ hits,
-                                                              uint32_t* __restrict__ stats) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const float4 a = __ldg(reinterpret_cast<const float4*>(rays + k));
-    const float4 b = __ldg(reinterpret_cast<const float4*>(rays + k) + 1);
-    const RayState r = make_ray(mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), b.w, __float_as_int(a.w));
-    uint32_t nb = 0, nt = 0;
-    const Hit h = trace_ray<STATS>(r, tr, any_hit != 0, &nb, &nt);
-    store_hit(hits + k, h);
-    if (STATS) {
-        stats[2 * k] = nb;
-        stats[2 * k + 1] = nt;
+                                                              uint32_t* __restrict__ stats, uint32_t* work) {
+    const uint32_t num_tiles = (n + 31) / 32;
+    for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
+        const uint32_t k = tile * 32 + (threadIdx.x & 31);
+        if (k < n) {
+            const float4 a = __ldg(reinterpret_cast<const float4*>(rays + k));
+            const float4 b = __ldg(reinterpret_cast<const float4*>(rays + k) + 1);
+            const RayState r = make_ray(mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), b.w, __float_as_int(a.w));
+            uint32_t nb = 0, nt = 0;
+            const Hit h = trace_ray<STATS>(r, tr, any_hit != 0, &nb, &nt);
+            store_hit(hits + k, h);
+            if (STATS) {
+                stats[2 * k] = nb;
+                stats[2 * k + 1] = nt;
+            }
+        }
+        __syncwarp();
     }
+}
+
+uint32_t pixel_tiles(const rt_camera* cam) {
+    return (uint32_t)(((cam->width + 7) / 8) * ((cam->height + 3) / 4));
+}
+
+rt_status check_trace_args(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, const char* who) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (!l || !cam) return rt_fail(ctx, RT_ERR_INVALID, "%s: null argument", who);
+    if (l->n == 0) return rt_fail(ctx, RT_ERR_INVALID, "%s: the LBVH has not been built", who);
+    if (cam->width == 0 || cam->height == 0 || (uint64_t)cam->width * cam->height > (1ull << 31))
+        return rt_fail(ctx, RT_ERR_INVALID, "%s: bad image size %ux%u", who, cam->width, cam->height);
+    return RT_OK;
 }
 
 }  // namespace
@@ -128,34 +167,23 @@ TreeRef tree_ref(const rt_ctx* ctx, const rt_lbvh* l) {
     return t;
 }
 
-namespace {
-
-uint32_t pixel_blocks(const rt_camera* cam) {
-    const uint64_t tiles = (uint64_t)((cam->width + 7) / 8) * ((cam->height + 3) / 4);
-    return (uint32_t)((tiles * 32 + kTraceThreads - 1) / kTraceThreads);
-}
-
-rt_status check_trace_args(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, const char* who) {
-    if (!ctx) return RT_ERR_INVALID;
-    if (!l || !cam) return rt_fail(ctx, RT_ERR_INVALID, "%s: null argument", who);
-    if (l->n == 0) return rt_fail(ctx, RT_ERR_INVALID, "%s: the LBVH has not been built", who);
-    if (cam->width == 0 || cam->height == 0 || (uint64_t)cam->width * cam->height > (1ull << 31))
-        return rt_fail(ctx, RT_ERR_INVALID, "%s: bad image size %ux%u", who, cam->width, cam->height);
-    return RT_OK;
-}
-
-}  // namespace
-
 extern "C" rt_status rt_trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, rt_hit* d_hits,
                                       uint32_t* d_stats) {
     rt_status s = check_trace_args(ctx, l, cam, "rt_trace_primary");
     if (s != RT_OK) return s;
     if (!d_hits) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_primary: null output");
-    const uint32_t blocks = pixel_blocks(cam);
-    if (d_stats)
-        k_trace_primary<true><<<blocks, kTraceThreads, 0, ctx->stream>>>(tree_ref(ctx, l), *cam, d_hits, d_stats);
-    else
-        k_trace_primary<false><<<blocks, kTraceThreads, 0, ctx->stream>>>(tree_ref(ctx, l), *cam, d_hits, nullptr);
+    if ((s = reset_work(ctx, kWorkPrimary)) != RT_OK) return s;
+    const uint32_t tiles = pixel_tiles(cam);
+    uint32_t* work = ctx->d_work + kWorkPrimary;
+    if (d_stats) {
+        auto k = k_trace_primary<true>;
+        k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
+            tree_ref(ctx, l), *cam, d_hits, d_stats, work, tiles);
+    } else {
+        auto k = k_trace_primary<false>;
+        k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
+            tree_ref(ctx, l), *cam, d_hits, nullptr, work, tiles);
+    }
     RT_CHECK_LAUNCH(ctx, "k_trace_primary");
     return RT_OK;
 }
@@ -167,15 +195,20 @@ extern "C" rt_status rt_trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const
     if (s != RT_OK) return s;
     if (!light || !d_primary) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_shadow_mirror: null argument");
     if (!l->src_tris) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_shadow_mirror: no triangle soup bound");
-    const uint32_t blocks = pixel_blocks(cam);
-    if (d_shadow_stats || d_mirror_stats)
-        k_trace_secondary<true><<<blocks, kTraceThreads, 0, ctx->stream>>>(
+    if ((s = reset_work(ctx, kWorkSecondary)) != RT_OK) return s;
+    const uint32_t tiles = pixel_tiles(cam);
+    uint32_t* work = ctx->d_work + kWorkSecondary;
+    if (d_shadow_stats || d_mirror_stats) {
+        auto k = k_trace_secondary<true>;
+        k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
             tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_vis, d_mirror,
-            d_shadow_stats, d_mirror_stats);
-    else
-        k_trace_secondary<false><<<blocks, kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_vis, d_mirror,
-            nullptr, nullptr);
+            d_shadow_stats, d_mirror_stats, work, tiles);
+    } else {
+        auto k = k_trace_secondary<false>;
+        k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
+            tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_vis, d_mirror, nullptr,
+            nullptr, work, tiles);
+    }
     RT_CHECK_LAUNCH(ctx, "k_trace_secondary");
     return RT_OK;
 }
@@ -186,13 +219,19 @@ extern "C" rt_status rt_trace_rays(rt_ctx* ctx, const rt_lbvh* l, const rt_ray* 
     if (!l || !d_rays || !d_hits) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_rays: null argument");
     if (l->n == 0) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_rays: the LBVH has not been built");
     if (n == 0) return RT_OK;
-    const uint32_t blocks = (n + kTraceThreads - 1) / kTraceThreads;
-    if (d_stats)
-        k_trace_rays<true><<<blocks, kTraceThreads, 0, ctx->stream>>>(tree_ref(ctx, l), d_rays, n, any_hit,
-                                                                      d_hits, d_stats);
-    else
-        k_trace_rays<false><<<blocks, kTraceThreads, 0, ctx->stream>>>(tree_ref(ctx, l), d_rays, n, any_hit,
-                                                                       d_hits, nullptr);
+    rt_status s = reset_work(ctx, kWorkRays);
+    if (s != RT_OK) return s;
+    const uint32_t tiles = (n + 31) / 32;
+    uint32_t* work = ctx->d_work + kWorkRays;
+    if (d_stats) {
+        auto k = k_trace_rays<true>;
+        k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
+            tree_ref(ctx, l), d_rays, n, any_hit, d_hits, d_stats, work);
+    } else {
+        auto k = k_trace_rays<false>;
+        k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
+            tree_ref(ctx, l), d_rays, n, any_hit, d_hits, nullptr, work);
+    }
     RT_CHECK_LAUNCH(ctx, "k_trace_rays");
     return RT_OK;
 }

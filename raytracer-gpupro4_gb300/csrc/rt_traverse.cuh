@@ -133,90 +133,94 @@ __device__ __forceinline__ Hit traverse(const RayState& r, const TreeRef& tr_, b
     float stack_t0[kStackSize];
     int sp = 0;
 
+    // pop: the next stacked node whose entry distance still does not exceed
+    // the closest hit (the far child is re-checked, LBVH.cpp:992)
+    auto pop = [&](uint32_t& nd) -> bool {
+        while (sp > 0) {
+            --sp;
+            if (!(stack_t0[sp] > best.t)) {
+                nd = stack_node[sp];
+                return true;
+            }
+        }
+        return false;
+    };
+
     NodeBox cur = load_node(nodes, 1);
     float t0;
     if (STATS) ++nbox;
     bool have = box_enter<EXACT>(r, cur.a.x, cur.a.y, cur.a.z, cur.a.w, cur.b.x, cur.b.y, best.t, &t0);
     uint32_t node = 1;
-    while (true) {
-        if (have) {
+    // while-while: lanes descend through internal nodes until each holds a
+    // leaf (or has nothing left), then the warp tests leaf triangles together.
+    while (have) {
+        while (!(__float_as_int(cur.b.z) & 4)) {
             const int pc = __float_as_int(cur.b.z);
-            if (pc & 4) {
-                int cnt = pc >> 3;
-                const int pos = __float_as_int(cur.b.w);
-                if (pos < 0 || cnt < 0 || (uint32_t)pos + (uint32_t)cnt > tr_.n) {
-                    atomicOr(tr_.err, RT_DEVERR_BOUNDS);
-                    cnt = 0;
-                }
-                for (int i = 0; i < cnt; ++i) {
-                    const float4* tp = tris + 3 * (size_t)(pos + i);
-                    const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-                    if (STATS) ++ntri;
-                    const int id = __float_as_int(a.w);
-                    if (id == r.exclude) continue;
-                    float u, v, t;
-                    if (tri_test(r, a, b, c, &u, &v, &t)) {
-                        if (t < best.t || (t == best.t && best.id >= 0 && id < best.id)) {
-                            best.t = t;
-                            best.u = u;
-                            best.v = v;
-                            best.id = id;
-                        }
-                    }
-                }
-                if (any_hit && best.id >= 0) break;
+            const uint32_t c0 = node << 1;
+            if (c0 + 1 >= tr_.num_nodes) {
+                atomicOr(tr_.err, RT_DEVERR_BOUNDS);
                 have = false;
-            } else {
-                const uint32_t c0 = node << 1;
-                if (c0 + 1 >= tr_.num_nodes) {
-                    atomicOr(tr_.err, RT_DEVERR_BOUNDS);
-                    break;
-                }
-                const float4* p = reinterpret_cast<const float4*>(nodes + c0);
-                const float4 l0 = __ldg(p), l1 = __ldg(p + 1), r0 = __ldg(p + 2), r1 = __ldg(p + 3);
-                float tl, tr;
-                const bool hl = box_enter<EXACT>(r, l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, best.t, &tl);
-                const bool hr = box_enter<EXACT>(r, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, best.t, &tr);
-                if (STATS) nbox += 2;
-                // near child by the split axis: the stored field is (30 - bit) % 3,
-                // the axis the bit splits is (field + 2) % 3
-                const int field = pc & 3;
-                const int near_right = (r.sgn >> (field == 0 ? 2 : field - 1)) & 1;
-                const bool hn = near_right ? hr : hl, hf = near_right ? hl : hr;
-                const float tf = near_right ? tl : tr;
-                const uint32_t nn = c0 | (uint32_t)near_right, nf = nn ^ 1u;
-                if (hn) {
-                    if (hf) {
-                        stack_node[sp] = nf;
-                        stack_t0[sp] = tf;
-                        ++sp;
-                    }
-                    node = nn;
-                    cur.a = near_right ? r0 : l0;
-                    cur.b = near_right ? r1 : l1;
-                    continue;
-                } else if (hf) {
-                    node = nf;
-                    cur.a = near_right ? l0 : r0;
-                    cur.b = near_right ? l1 : r1;
-                    continue;
-                }
-                have = false;
-            }
-        }
-        // pop: re-check the stored entry distance against the current best
-        bool found = false;
-        while (sp > 0) {
-            --sp;
-            if (!(stack_t0[sp] > best.t)) {
-                node = stack_node[sp];
-                found = true;
                 break;
             }
+            const float4* p = reinterpret_cast<const float4*>(nodes + c0);
+            const float4 l0 = __ldg(p), l1 = __ldg(p + 1), r0 = __ldg(p + 2), r1 = __ldg(p + 3);
+            float tl, tr;
+            const bool hl = box_enter<EXACT>(r, l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, best.t, &tl);
+            const bool hr = box_enter<EXACT>(r, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, best.t, &tr);
+            if (STATS) nbox += 2;
+            // near child by the split axis: the stored field is (30 - bit) % 3,
+            // the axis the bit splits is (field + 2) % 3
+            const int field = pc & 3;
+            const int near_right = (r.sgn >> (field == 0 ? 2 : field - 1)) & 1;
+            const bool hn = near_right ? hr : hl, hf = near_right ? hl : hr;
+            const float tf = near_right ? tl : tr;
+            const uint32_t nn = c0 | (uint32_t)near_right, nf = nn ^ 1u;
+            if (hn) {
+                if (hf) {
+                    stack_node[sp] = nf;
+                    stack_t0[sp] = tf;
+                    ++sp;
+                }
+                node = nn;
+                cur.a = near_right ? r0 : l0;
+                cur.b = near_right ? r1 : l1;
+            } else if (hf) {
+                node = nf;
+                cur.a = near_right ? l0 : r0;
+                cur.b = near_right ? l1 : r1;
+            } else {
+                have = pop(node);
+                if (!have) break;
+                cur = load_node(nodes, node);
+            }
         }
-        if (!found) break;
-        cur = load_node(nodes, node);
-        have = true;
+        if (!have) break;
+        // leaf: triangles [pos, pos + cnt) of the sorted, pre-gathered array
+        int cnt = __float_as_int(cur.b.z) >> 3;
+        const int pos = __float_as_int(cur.b.w);
+        if (pos < 0 || cnt < 0 || (uint32_t)pos + (uint32_t)cnt > tr_.n) {
+            atomicOr(tr_.err, RT_DEVERR_BOUNDS);
+            cnt = 0;
+        }
+        for (int i = 0; i < cnt; ++i) {
+            const float4* tp = tris + 3 * (size_t)(pos + i);
+            const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            if (STATS) ++ntri;
+            const int id = __float_as_int(a.w);
+            if (id == r.exclude) continue;
+            float u, v, t;
+            if (tri_test(r, a, b, c, &u, &v, &t)) {
+                if (t < best.t || (t == best.t && best.id >= 0 && id < best.id)) {
+                    best.t = t;
+                    best.u = u;
+                    best.v = v;
+                    best.id = id;
+                }
+            }
+        }
+        if (any_hit && best.id >= 0) break;
+        have = pop(node);
+        if (have) cur = load_node(nodes, node);
     }
     if (STATS) {
         *nbox_out = nbox;
@@ -248,6 +252,14 @@ __device__ __forceinline__ f3 primary_dir(const rt_camera& cam, uint32_t i, uint
     const float x = fmul((float)(2 * (int)i + 1 - (int)cam.width), inv);
     const float y = -fmul((float)(2 * (int)j + 1 - (int)cam.height), inv);
     return camera_dir(cam, x, y);
+}
+
+// Persistent warps: each warp takes the next 32-item tile from a work counter
+// (reset before the launch), so heavy tiles never queue behind an idle SM.
+__device__ __forceinline__ uint32_t next_tile(uint32_t* work) {
+    uint32_t t = 0;
+    if ((threadIdx.x & 31) == 0) t = atomicAdd(work, 1u);
+    return __shfl_sync(0xffffffffu, t, 0);
 }
 
 // Pixel of lane `lane` of warp tile `tile`: 8 x 4 pixel tiles for coherence.

@@ -1,0 +1,111 @@
+// rt_frame_demo -- drives the C++ stage classes the way the reference's main
+// loop drives RayTracerCS (App.cpp:64-86): build the scene's LBVH through the
+// AccelerationStructure interface, then render frames with the dynamic
+// per-frame rebuild.  Used by the GPU tests to check the C++ layer against
+// the Python binding of the same C ABI.
+//
+//   rt_frame_demo <soup.f32> <n> <camera.f32> <width> <height> <lx> <ly> <lz> <depth> <frames> <out_prefix>
+//
+// soup.f32: n x 9 float32; camera.f32: eye, right, up, fwd (3 floats each),
+// tan(fovy/2).  Writes <out_prefix>.primary / .vis / .mirror (raw rt_hit /
+// uint8 arrays of the last frame) and prints one JSON summary line.
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "rt_stages.h"
+
+static std::vector<float> read_floats(const char* path, size_t count) {
+    std::vector<float> v(count);
+    FILE* f = std::fopen(path, "rb");
+    if (!f || std::fread(v.data(), sizeof(float), count, f) != count) {
+        std::fprintf(stderr, "cannot read %zu floats from %s\n", count, path);
+        std::exit(2);
+    }
+    std::fclose(f);
+    return v;
+}
+
+template <typename T>
+static void write_raw(const std::string& path, const std::vector<T>& v) {
+    FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f || std::fwrite(v.data(), sizeof(T), v.size(), f) != v.size()) {
+        std::fprintf(stderr, "cannot write %s\n", path.c_str());
+        std::exit(2);
+    }
+    std::fclose(f);
+}
+
+int main(int argc, char** argv) {
+    if (argc != 12) {
+        std::fprintf(stderr, "usage: %s soup n camera width height lx ly lz depth frames out_prefix\n", argv[0]);
+        return 2;
+    }
+    const unsigned n = (unsigned)std::strtoul(argv[2], nullptr, 10);
+    std::vector<float> soup = read_floats(argv[1], (size_t)n * 9);
+    std::vector<float> c = read_floats(argv[3], 13);
+    rt_camera cam;
+    for (int k = 0; k < 3; ++k) {
+        cam.eye[k] = c[k];
+        cam.right[k] = c[3 + k];
+        cam.up[k] = c[6 + k];
+        cam.fwd[k] = c[9 + k];
+    }
+    cam.tan_half_fovy = c[12];
+    cam.width = (uint32_t)std::atoi(argv[4]);
+    cam.height = (uint32_t)std::atoi(argv[5]);
+    const float light[3] = {std::strtof(argv[6], nullptr), std::strtof(argv[7], nullptr), std::strtof(argv[8], nullptr)};
+    const unsigned depth = (unsigned)std::atoi(argv[9]);
+    const int frames = std::atoi(argv[10]);
+    const std::string out = argv[11];
+    try {
+        rtgb::Context ctx(0);
+        // static path: Model::RebuildStructure -> LBVH::Build, then the
+        // structure is handed to the renderer (RayTracerCS.cpp:590-624)
+        rtgb::LBVHGpu lbvh(ctx, soup.data(), n, 1 << depth);
+        auto t0 = std::chrono::steady_clock::now();
+        lbvh.Build();
+        ctx.Sync();
+        float secs = std::chrono::duration<float>(std::chrono::steady_clock::now() - t0).count();
+        rtgb::AccelerationStructure* as = &lbvh;
+        const rtgb::LBVHNode* nodes = static_cast<const rtgb::LBVHNode*>(as->GetPtrToElements());
+        rtgb::BBox wb = as->WorldBound();
+        const bool bound_ok = wb.pMin.x == nodes[1].minCoord.x && wb.pMax.z == nodes[1].maxCoord.z;
+        // one ray through the single-ray interface, towards the first triangle's centroid
+        rtgb::Ray ray;
+        ray.o = rtgb::Vector3{cam.eye[0], cam.eye[1], cam.eye[2]};
+        const float cx = (soup[0] + soup[3] + soup[6]) / 3.f, cy = (soup[1] + soup[4] + soup[7]) / 3.f,
+                    cz = (soup[2] + soup[5] + soup[8]) / 3.f;
+        ray.d = rtgb::Vector3{cx - ray.o.x, cy - ray.o.y, cz - ray.o.z};
+        rtgb::TIntersection hit = as->IntersectP(ray);
+
+        // dynamic path: RayTracerCS::Render with the per-frame GPU rebuild
+        rtgb::Scene scene;
+        scene.soup = soup.data();
+        scene.numPrimitives = n;
+        rtgb::RayTracerCS rt(ctx, scene, cam, light, depth, true);
+        auto t1 = std::chrono::steady_clock::now();
+        for (int f = 0; f < frames; ++f) rt.Render();
+        ctx.Check();
+        float fsecs = std::chrono::duration<float>(std::chrono::steady_clock::now() - t1).count();
+        std::vector<rt_hit> prim = rt.DownloadPrimary();
+        std::vector<uint8_t> vis = rt.DownloadVisibility();
+        std::vector<rt_hit> mir = rt.DownloadMirror();
+        write_raw(out + ".primary", prim);
+        write_raw(out + ".vis", vis);
+        write_raw(out + ".mirror", mir);
+        size_t hits = 0, lit = 0;
+        for (auto& h : prim) hits += h.id >= 0;
+        for (auto v : vis) lit += v == 3;
+        std::printf("{\"name\": \"%s\", \"n\": %u, \"depth\": %u, \"elements\": %u, \"element_size\": %zu, "
+                    "\"build_s\": %.6f, \"world_bound_ok\": %s, \"single_ray_id\": %d, \"single_ray_t\": %.9g, "
+                    "\"frames\": %d, \"frames_s\": %.6f, \"primary_hits\": %zu, \"lit\": %zu, \"samples\": %u}\n",
+                    as->GetName(), n, depth, as->GetNumberOfElements(), as->GetSizeOfElement(), secs,
+                    bound_ok ? "true" : "false", hit.IDTr, hit.t, frames, fsecs, hits, lit, rt.GetNumSamples());
+    } catch (const rtgb::Error& e) {
+        std::fprintf(stderr, "error: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}

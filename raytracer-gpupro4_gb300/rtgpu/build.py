@@ -97,18 +97,20 @@ def build_host(force: bool = False) -> Path | None:
     lib_srcs = [s for s in srcs if s.name != "rt_frame_demo.cpp"]
     hdrs = sorted(HOST.glob("*.h"))
     cxx = os.environ.get("CXX", "g++")
-    inc = ["-I", str(INCLUDE), "-I", str(HOST), "-I", str(_cuda_home() / "include")]
+    cuda = _cuda_home()
+    inc = ["-I", str(INCLUDE), "-I", str(HOST), "-I", str(cuda / "include")]
+    cudart = ["-L", str(cuda / "lib64"), "-lcudart", f"-Wl,-rpath,{cuda / 'lib64'}"]
     HOST_BUILD.mkdir(parents=True, exist_ok=True)
     if force or _newer(lib_srcs + hdrs + [INCLUDE / "rt_api.h", LIB], HOST_LIB):
         tmp = HOST_LIB.with_suffix(".so.tmp")
         _run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", *inc, *map(str, lib_srcs), "-o", str(tmp),
-              "-L", str(BUILD), "-lrtgb300", f"-Wl,-rpath,{BUILD}"])
+              "-L", str(BUILD), "-lrtgb300", f"-Wl,-rpath,{BUILD}", *cudart])
         os.replace(tmp, HOST_LIB)
     demo_src = HOST / "rt_frame_demo.cpp"
     if demo_src.exists() and (force or _newer([demo_src, HOST_LIB] + hdrs, DEMO)):
         _run([cxx, "-O2", "-std=c++17", *inc, str(demo_src), "-o", str(DEMO),
               "-L", str(HOST_BUILD), "-lrthost", "-L", str(BUILD), "-lrtgb300",
-              f"-Wl,-rpath,{HOST_BUILD}", f"-Wl,-rpath,{BUILD}"])
+              f"-Wl,-rpath,{HOST_BUILD}", f"-Wl,-rpath,{BUILD}", *cudart])
     return HOST_LIB
 
 
