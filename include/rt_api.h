@@ -119,6 +119,29 @@ rt_status rt_lbvh_build_host(rt_ctx* ctx, rt_lbvh* lbvh, const float* h_tris, ui
 rt_status rt_lbvh_import_host(rt_ctx* ctx, rt_lbvh* lbvh, const rt_node* h_nodes, const uint32_t* h_ids,
                               const float* h_tris, uint32_t n);
 
+/* Allocation-free rebuild.  No counterpart in the reference: it exists for
+ * callers that may not allocate device memory when they rebuild -- a host
+ * capturing its frame into a CUDA graph, an engine whose allocator owns all
+ * device memory, a real-time loop that cannot absorb an allocation's
+ * implicit synchronisation.  The caller passes the device soup (n x 9
+ * floats) and every output: d_nodes (1 << depth rt_node), d_ids and d_keys
+ * (n each), d_sorted_tris (n x 12 floats, the layout of rt_lbvh_view).  The
+ * results equal rt_lbvh_build's.  All scratch lives in one fixed device
+ * array of 5,577,088 bytes that every GPU loading this library holds until the
+ * process exits; n above RT_NOALLOC_MAX_TRIS or depth above
+ * RT_NOALLOC_MAX_DEPTH returns RT_ERR_CAPACITY.  The first call on a device
+ * looks up that array's device address (cudaGetSymbolAddress), so make it
+ * before any stream capture.  Every call reuses the same array and clears
+ * what must start at zero; calls that overlap on the GPU race on it and
+ * must be serialised by the caller.  ctx may be NULL; if given, it receives
+ * the error message (rt_last_error).  Asynchronous on `stream`; calls no
+ * allocating routine. */
+#define RT_NOALLOC_MAX_TRIS 262144u
+#define RT_NOALLOC_MAX_DEPTH 20u
+rt_status rt_lbvh_build_noalloc(rt_ctx* ctx, void* stream, const float* d_tris, uint32_t n, uint32_t depth,
+                                uint32_t flags, rt_node* d_nodes, uint32_t* d_ids, uint32_t* d_keys,
+                                float* d_sorted_tris);
+
 /* Device views (GetPtrToElements / GetOrderedElementsIds, LBVH.h:109-113). */
 typedef struct rt_lbvh_view {
     const rt_node* nodes;      /* device, num_nodes entries */

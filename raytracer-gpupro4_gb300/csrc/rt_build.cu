@@ -850,3 +850,133 @@ extern "C" rt_status rt_lbvh_download(rt_ctx* ctx, const rt_lbvh* l, rt_node* h_
     RT_CHECK_CUDA(ctx, cudaStreamSynchronize(st));
     return RT_OK;
 }
+
+// ===========================================================================
+// Allocation-free LBVH build.
+//
+// Some callers cannot call cudaMalloc at the moment they need a rebuild: a
+// host that is capturing its frame into a CUDA graph (an allocation inside
+// stream capture is an error), an engine whose device memory is owned by
+// its own allocator and must not be touched behind its back, or a real-time
+// loop that cannot afford the implicit synchronisation of an allocation.
+// rt_lbvh_build_noalloc serves them: the caller passes the soup and every
+// output buffer, and all of the build's scratch (sort ping-pong buffers,
+// digit histograms, look-back words, tile scans, leaf list, refit arrival
+// words) lives in the fixed array below, which the CUDA module reserves on
+// every GPU that loads this library and keeps until the process exits.
+//
+// Limits: at most RT_NOALLOC_MAX_TRIS triangles (the 512 x 512 = 262,144
+// primitives the reference's own GPU rebuild handles, BitonicSort.cpp:20-27)
+// and depth at most RT_NOALLOC_MAX_DEPTH (the reference default, conf.ini).
+// The array is shared by every call: a call clears what has to start at
+// zero, so consecutive calls are independent, but calls that overlap on the
+// GPU (two streams, two threads) race on it and must be serialised by the
+// caller.
+namespace {
+
+constexpr uint32_t kNoAllocTiles = (RT_NOALLOC_MAX_TRIS + kSortTile - 1) / kSortTile;
+constexpr uint32_t kNoAllocEmitTiles = (RT_NOALLOC_MAX_TRIS + kEmitTile - 1) / kEmitTile;
+constexpr uint32_t kNoAllocBoundsBlocks = 2048;
+// word offsets inside the scratch array
+constexpr size_t kNaScene = 0;                                                      // SceneInfo (16 words)
+constexpr size_t kNaCounters = kNaScene + 16;                                       // 8 words
+constexpr size_t kNaHist = kNaCounters + 16;                                        // 4 x 256
+constexpr size_t kNaPartials = kNaHist + 4 * 256;                                   // 8 floats per bounds block
+constexpr size_t kNaLookback = kNaPartials + 8 * kNoAllocBoundsBlocks;              // 4 x 256 per sort tile
+constexpr size_t kNaScan = kNaLookback + (size_t)kSortPasses * 256 * kNoAllocTiles;  // 4 per emission tile
+constexpr size_t kNaLeaves = kNaScan + 4 * (size_t)kNoAllocEmitTiles;               // one per triangle
+constexpr size_t kNaKeysAlt = kNaLeaves + RT_NOALLOC_MAX_TRIS;
+constexpr size_t kNaIdsAlt = kNaKeysAlt + RT_NOALLOC_MAX_TRIS;
+constexpr size_t kNaArrive = kNaIdsAlt + RT_NOALLOC_MAX_TRIS;                       // 1 << (depth - 1)
+constexpr size_t kNaErr = kNaArrive + ((size_t)1 << (RT_NOALLOC_MAX_DEPTH - 1));
+constexpr size_t kNaWords = kNaErr + 64;
+
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNaWords];
+
+// Device address of g_noalloc_scratch and the SM count, per device; filled
+// on the first call on that device.
+struct NoAllocDevice {
+    uint32_t* scratch = nullptr;
+    int num_sms = 0;
+};
+constexpr int kNoAllocMaxDevices = 64;
+NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
+
+}  // namespace
+
+extern "C" rt_status rt_lbvh_build_noalloc(rt_ctx* ctx, void* stream, const float* d_tris, uint32_t n, uint32_t depth,
+                                           uint32_t flags, rt_node* d_nodes, uint32_t* d_ids, uint32_t* d_keys,
+                                           float* d_sorted_tris) {
+    if (!d_tris || !d_nodes || !d_ids || !d_keys || !d_sorted_tris)
+        return rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_build_noalloc: null buffer");
+    if (n == 0 || depth == 0) return rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_build_noalloc: n and depth must be > 0");
+    if (n > RT_NOALLOC_MAX_TRIS || depth > RT_NOALLOC_MAX_DEPTH)
+        return rt_fail(ctx, RT_ERR_CAPACITY,
+                       "rt_lbvh_build_noalloc: n=%u depth=%u exceeds the fixed scratch (at most %u triangles, depth %u)",
+                       n, depth, RT_NOALLOC_MAX_TRIS, RT_NOALLOC_MAX_DEPTH);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
+        return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_build_noalloc: no usable current device");
+    NoAllocDevice& D = g_noalloc_dev[dev];
+    if (!D.scratch) {  // set-up, once per device, with that device current
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_build_noalloc: cudaGetSymbolAddress failed: %s",
+                           cudaGetErrorString(e));
+        e = cudaDeviceGetAttribute(&D.num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess)
+            return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_build_noalloc: cudaDeviceGetAttribute failed: %s",
+                           cudaGetErrorString(e));
+        D.scratch = static_cast<uint32_t*>(p);
+    }
+    uint32_t* S = D.scratch;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    SceneInfo* scene = reinterpret_cast<SceneInfo*>(S + kNaScene);
+    uint32_t* counters = S + kNaCounters;
+    uint32_t* hist = S + kNaHist;
+    float* partials = reinterpret_cast<float*>(S + kNaPartials);
+    uint32_t* lookback = S + kNaLookback;
+    uint32_t* scan = S + kNaScan;
+    uint32_t* leaves = S + kNaLeaves;
+    uint32_t* keys_alt = S + kNaKeysAlt;
+    uint32_t* ids_alt = S + kNaIdsAlt;
+    uint32_t* arrive = S + kNaArrive;
+    uint32_t* err = S + kNaErr;
+    const uint32_t num_nodes = 1u << depth;
+    // what must start at zero: the bounds ticket and the refit arrival words
+    // (the other counters, histograms and look-back words are reset by k_bounds)
+    e = cudaMemsetAsync(counters, 0, 8 * sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(arrive, 0, sizeof(uint32_t) * std::max(1u, num_nodes >> 1), st);
+    if (e != cudaSuccess)
+        return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_build_noalloc: cudaMemsetAsync failed: %s", cudaGetErrorString(e));
+    const uint32_t epoch = 1;
+    const uint32_t sort_tiles = ceil_div(n, kSortTile);
+    const uint32_t emit_tiles = ceil_div(n, kEmitTile);
+    const uint32_t lb_words = kSortPasses * 256 * sort_tiles;
+    const uint32_t bblocks =
+        std::max(1u, std::min({ceil_div(3ull * n, 256), (uint32_t)D.num_sms * 4, kNoAllocBoundsBlocks}));
+    k_bounds<<<bblocks, 256, 0, st>>>(d_tris, n, scene, partials, counters, hist, lookback, lb_words, d_nodes,
+                                      num_nodes, (flags & RT_BUILD_CLEAR_UNREACHED) ? 1 : 0);
+    const uint32_t mblocks = std::max(1u, std::min(ceil_div(n, kMortonThreads), (uint32_t)D.num_sms * 2));
+    k_morton_hist<<<mblocks, kMortonThreads, 0, st>>>(d_tris, n, scene, d_keys, d_ids, hist, err);
+    uint32_t *kin = d_keys, *iin = d_ids, *kout = keys_alt, *iout = ids_alt;
+    for (int p = 0; p < kSortPasses; ++p) {
+        k_onesweep<<<sort_tiles, kSortThreads, 0, st>>>(kin, iin, kout, iout, n, p, hist,
+                                                        lookback + (size_t)p * 256 * sort_tiles, counters + 1 + p, err);
+        std::swap(kin, kout);
+        std::swap(iin, iout);
+    }
+    k_emit_tiles<<<emit_tiles, kEmitThreads, 0, st>>>(d_keys, n, scan);
+    k_emit_prefix<<<1, 32, 0, st>>>(scan, emit_tiles);
+    k_emit_leaves<<<emit_tiles, kEmitThreads, 0, st>>>(d_keys, d_ids, d_tris, n, depth, scan, d_nodes,
+                                                       reinterpret_cast<float4*>(d_sorted_tris), leaves, counters + 5);
+    const uint32_t rblocks = std::max(1u, std::min(ceil_div(n, 256), (uint32_t)D.num_sms * 8));
+    k_emit_refit<<<rblocks, 256, 0, st>>>(d_keys, reinterpret_cast<const float4*>(d_sorted_tris), n, depth, d_nodes,
+                                          leaves, counters + 5, arrive, epoch, err);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_build_noalloc: launch failed: %s", cudaGetErrorString(e));
+    return RT_OK;
+}

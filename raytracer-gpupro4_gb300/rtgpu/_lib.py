@@ -14,6 +14,8 @@ from .build import LIB
 
 RT_OK, RT_ERR_INVALID, RT_ERR_CAPACITY, RT_ERR_CUDA, RT_ERR_TIMEOUT, RT_ERR_NONFINITE = range(6)
 RT_BUILD_CLEAR_UNREACHED = 1
+RT_NOALLOC_MAX_TRIS = 262144
+RT_NOALLOC_MAX_DEPTH = 20
 RT_NODE_SENTINEL = -2147483647
 
 # Layouts mirrored from include/rt_api.h (LBVHNode / Intersection / Ray of the reference).
@@ -27,6 +29,7 @@ EXPORTED = [
     "rt_ctx_check", "rt_last_error", "rt_lbvh_create", "rt_lbvh_destroy", "rt_lbvh_build", "rt_lbvh_build_host",
     "rt_lbvh_import_host", "rt_lbvh_view_get", "rt_lbvh_world_bound", "rt_lbvh_download", "rt_trace_primary",
     "rt_trace_shadow_mirror", "rt_trace_rays", "rt_render_frame_host", "rt_pathtrace", "rt_pathtrace_adjoint",
+    "rt_lbvh_build_noalloc",
 ]
 
 
@@ -79,6 +82,7 @@ def lib() -> C.CDLL:
         "rt_render_frame_host": (i32, [vp, vp, vp, u32, C.POINTER(Camera), fp, vp, vp, vp]),
         "rt_pathtrace": (i32, [vp, vp, vp, vp, C.POINTER(Camera), C.POINTER(PtParams), vp]),
         "rt_pathtrace_adjoint": (i32, [vp, vp, vp, vp, C.POINTER(Camera), C.POINTER(PtParams), vp, vp, vp]),
+        "rt_lbvh_build_noalloc": (i32, [vp, vp, vp, u32, u32, u32, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
