@@ -118,14 +118,29 @@ __global__ void __launch_bounds__(256) k_bounds(const float* __restrict__ tris, 
 
     float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     uint32_t bad = 0;
-    const uint32_t nv = 3u * n;
-    for (uint32_t v = gtid; v < nv; v += gstride) {
-        const float x = __ldg(tris + 3 * (size_t)v + 0), y = __ldg(tris + 3 * (size_t)v + 1),
-                    z = __ldg(tris + 3 * (size_t)v + 2);
+    auto acc = [&](float x, float y, float z) {
         bad |= !(isfinite(x) && isfinite(y) && isfinite(z));
         mn[0] = fminf(mn[0], x); mn[1] = fminf(mn[1], y); mn[2] = fminf(mn[2], z);
         mx[0] = fmaxf(mx[0], x); mx[1] = fmaxf(mx[1], y); mx[2] = fmaxf(mx[2], z);
+    };
+    const size_t nv = 3 * (size_t)n;
+    size_t v0 = 0;
+    if ((reinterpret_cast<uintptr_t>(tris) & 15u) == 0) {
+        // 16-byte loads: 3 float4 = 4 vertices (x0 y0 z0 x1 | y1 z1 x2 y2 | z2 x3 y3 z3)
+        const float4* t4 = reinterpret_cast<const float4*>(tris);
+        const size_t ng = nv / 4;
+#pragma unroll 2
+        for (size_t g = gtid; g < ng; g += gstride) {
+            const float4 a = __ldg(t4 + 3 * g), b = __ldg(t4 + 3 * g + 1), c = __ldg(t4 + 3 * g + 2);
+            acc(a.x, a.y, a.z);
+            acc(a.w, b.x, b.y);
+            acc(b.z, b.w, c.x);
+            acc(c.y, c.z, c.w);
+        }
+        v0 = ng * 4;
     }
+    for (size_t v = v0 + gtid; v < nv; v += gstride)
+        acc(__ldg(tris + 3 * v), __ldg(tris + 3 * v + 1), __ldg(tris + 3 * v + 2));
     for (int off = 16; off > 0; off >>= 1) {
         for (int c = 0; c < 3; ++c) {
             mn[c] = fminf(mn[c], __shfl_xor_sync(kFull, mn[c], off));
@@ -156,15 +171,37 @@ __global__ void __launch_bounds__(256) k_bounds(const float* __restrict__ tris, 
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    if (threadIdx.x == 0) {
+    // the last block folds the per-block partials: strided over its threads,
+    // then a warp / block reduction (order-free: min and max are exact)
+    {
         float r[7];
-        for (int q = 0; q < 7; ++q) r[q] = __ldcg(partials + q);
-        for (uint32_t b = 1; b < gridDim.x; ++b) {
+        for (int c = 0; c < 3; ++c) { r[c] = INFINITY; r[3 + c] = -INFINITY; }
+        r[6] = 0.0f;
+        for (uint32_t b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
             for (int c = 0; c < 3; ++c) {
                 r[c] = fminf(r[c], __ldcg(partials + 8 * b + c));
                 r[3 + c] = fmaxf(r[3 + c], __ldcg(partials + 8 * b + 3 + c));
             }
             r[6] = fmaxf(r[6], __ldcg(partials + 8 * b + 6));
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            for (int c = 0; c < 3; ++c) {
+                r[c] = fminf(r[c], __shfl_xor_sync(kFull, r[c], off));
+                r[3 + c] = fmaxf(r[3 + c], __shfl_xor_sync(kFull, r[3 + c], off));
+            }
+            r[6] = fmaxf(r[6], __shfl_xor_sync(kFull, r[6], off));
+        }
+        __syncthreads();
+        if (lane == 0)
+            for (int q = 0; q < 7; ++q) s_red[w][q] = r[q];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        float r[7];
+        for (int q = 0; q < 7; ++q) r[q] = s_red[0][q];
+        for (int ww = 1; ww < 8; ++ww) {
+            for (int c = 0; c < 3; ++c) { r[c] = fminf(r[c], s_red[ww][c]); r[3 + c] = fmaxf(r[3 + c], s_red[ww][3 + c]); }
+            r[6] = fmaxf(r[6], s_red[ww][6]);
         }
         SceneInfo s;
         for (int c = 0; c < 3; ++c) {
@@ -567,7 +604,21 @@ __global__ void __launch_bounds__(kEmitThreads) k_emit_leaves(const uint32_t* __
             const bool tail = (k == n - 1) || (dcur >= 0 && __popc(keep_above(anc, dcur)) < leaf_depth);
             if (head) nodes[h].prim_pos = (int32_t)k;
             if (tail) nodes[h].prim_count = (int32_t)k;  // range end; k_emit_refit finalises the field
-            // pre-gather in sorted order: A.xyz,id | B.xyz,0 | C.xyz,0
+        }
+        // warp-aggregated append of the leaves opened here
+        const uint32_t hm = __ballot_sync(kFull, head);
+        uint32_t basei = 0;
+        if (lane == 0 && hm) basei = atomicAdd(leaf_count, (uint32_t)__popc(hm));
+        basei = __shfl_sync(kFull, basei, 0);
+        if (head) leaf_list[basei + __popc(hm & lanemask_lt())] = h;
+    }
+    // pre-gather in sorted order (A.xyz,id | B.xyz,0 | C.xyz,0), lane-contiguous
+    // so that the 48-byte records of a warp are written as one contiguous run
+    const uint32_t tbase = blockIdx.x * kEmitTile;
+#pragma unroll 2
+    for (int q = 0; q < kEmitItems; ++q) {
+        const uint32_t k = tbase + q * kEmitThreads + threadIdx.x;
+        if (k < n) {
             const uint32_t id = __ldg(ids + k);
             const float* tp = tris + 9 * (size_t)id;
             float v[9];
@@ -577,12 +628,6 @@ __global__ void __launch_bounds__(kEmitThreads) k_emit_leaves(const uint32_t* __
             sorted_tris[3 * (size_t)k + 1] = make_float4(v[3], v[4], v[5], 0.0f);
             sorted_tris[3 * (size_t)k + 2] = make_float4(v[6], v[7], v[8], 0.0f);
         }
-        // warp-aggregated append of the leaves opened here
-        const uint32_t hm = __ballot_sync(kFull, head);
-        uint32_t basei = 0;
-        if (lane == 0 && hm) basei = atomicAdd(leaf_count, (uint32_t)__popc(hm));
-        basei = __shfl_sync(kFull, basei, 0);
-        if (head) leaf_list[basei + __popc(hm & lanemask_lt())] = h;
     }
 }
 
@@ -606,6 +651,7 @@ __global__ void __launch_bounds__(256) k_emit_refit(const uint32_t* __restrict__
             continue;
         }
         float mn[3], mx[3];
+#pragma unroll 4
         for (int32_t j = pos; j <= end; ++j) {
             const float4 a = __ldg(sorted_tris + 3 * (size_t)j), b = __ldg(sorted_tris + 3 * (size_t)j + 1),
                          c = __ldg(sorted_tris + 3 * (size_t)j + 2);
@@ -637,10 +683,13 @@ __global__ void __launch_bounds__(256) k_emit_refit(const uint32_t* __restrict__
         nd.prim_pos = pos;
         nodes[h] = nd;
         while (h > 1) {
-            __threadfence();
-            const uint32_t old = atomicExch(&arrive[h >> 1], epoch);
+            // release our node, acquire the sibling's: one acq_rel exchange per level
+            uint32_t old;
+            asm volatile("atom.acq_rel.gpu.global.exch.b32 %0, [%1], %2;"
+                         : "=r"(old)
+                         : "l"(arrive + (h >> 1)), "r"(epoch)
+                         : "memory");
             if (old != epoch) break;  // first of the two children: the sibling finishes the parent
-            __threadfence();
             const uint32_t sib = h ^ 1u;
             const float4 s0 = __ldcg(reinterpret_cast<const float4*>(&nodes[sib]));
             const float4 s1 = __ldcg(reinterpret_cast<const float4*>(&nodes[sib]) + 1);

@@ -92,9 +92,13 @@ struct PathParams {
     float sky[3];
 };
 
-// Traces one path; returns the number of hit segments and their triangle ids.
-__device__ __forceinline__ int trace_path(const TreeRef& tr, const float* __restrict__ soup, const PathParams& P, uint32_t i, uint32_t j,
-                                          uint32_t sample, int* seg, bool* missed) {
+// Traces one path; returns the number of hit segments and their triangle
+// ids.  Called by all lanes of the warp together (valid == false for lanes
+// past the image edge): every segment is one warp-wide traversal in which
+// lanes whose path already ended only help.
+__device__ __forceinline__ int trace_path(const TreeRef& tr, const float* __restrict__ soup, const PathParams& P,
+                                          bool valid, uint32_t i, uint32_t j, uint32_t sample, int* seg,
+                                          bool* missed) {
     Pcg32 g;
     pt_seed(g, P.seed, (uint64_t)j * P.cam.width + i, sample);
     const float inv = fdiv(1.0f, (float)P.cam.height);
@@ -107,27 +111,35 @@ __device__ __forceinline__ int trace_path(const TreeRef& tr, const float* __rest
     int exclude = -1;
     int ns = 0;
     *missed = false;
+    bool alive = valid;
     for (uint32_t s = 0; s <= P.bounces && s < (uint32_t)kMaxSeg; ++s) {
         const RayState r = make_ray(o, d, 1e16f, exclude);
         uint32_t nb, nt;
-        const Hit h = trace_ray<false>(r, tr, false, &nb, &nt);
-        if (h.id < 0) {
-            *missed = true;
-            break;
+        const Hit h = trace_ray<false>(r, alive, tr, false, &nb, &nt);
+        if (alive) {
+            if (h.id < 0) {
+                *missed = true;
+                alive = false;
+            } else {
+                seg[ns++] = h.id;
+                if (s == P.bounces) {
+                    alive = false;
+                } else {
+                    const f3 N = facing_normal(soup, h.id, d);
+                    o = mk3(fadd(o.x, fmul(h.t, d.x)), fadd(o.y, fmul(h.t, d.y)), fadd(o.z, fmul(h.t, d.z)));
+                    d = cosine_dir(g, N);
+                    exclude = h.id;
+                }
+            }
         }
-        seg[ns++] = h.id;
-        if (s == P.bounces) break;
-        const f3 N = facing_normal(soup, h.id, d);
-        o = mk3(fadd(o.x, fmul(h.t, d.x)), fadd(o.y, fmul(h.t, d.y)), fadd(o.z, fmul(h.t, d.z)));
-        d = cosine_dir(g, N);
-        exclude = h.id;
     }
     return ns;
 }
 
 __device__ __forceinline__ void path_pixel(const TreeRef& tr, const float* __restrict__ soup,
                                            const float* __restrict__ albedo, const float* __restrict__ emission,
-                                           const PathParams& P, float4* __restrict__ image, uint32_t i, uint32_t j);
+                                           const PathParams& P, float4* __restrict__ image, bool valid, uint32_t i,
+                                           uint32_t j);
 
 __global__ void __launch_bounds__(kPtThreads) k_pathtrace(TreeRef tr, const float* __restrict__ soup,
                                                           const float* __restrict__ albedo,
@@ -136,15 +148,16 @@ __global__ void __launch_bounds__(kPtThreads) k_pathtrace(TreeRef tr, const floa
                                                           uint32_t num_tiles) {
     for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
         uint32_t i, j;
-        if (tile_pixel(tile, threadIdx.x & 31, P.cam.width, P.cam.height, &i, &j))
-            path_pixel(tr, soup, albedo, emission, P, image, i, j);
-        __syncwarp();
+        const bool valid = tile_pixel(tile, threadIdx.x & 31, P.cam.width, P.cam.height, &i, &j);
+        if (!valid) i = j = 0;
+        path_pixel(tr, soup, albedo, emission, P, image, valid, i, j);
     }
 }
 
 __device__ __forceinline__ void path_pixel(const TreeRef& tr, const float* __restrict__ soup,
                                            const float* __restrict__ albedo, const float* __restrict__ emission,
-                                           const PathParams& P, float4* __restrict__ image, uint32_t i, uint32_t j) {
+                                           const PathParams& P, float4* __restrict__ image, bool valid, uint32_t i,
+                                           uint32_t j) {
     float acc[3] = {0.0f, 0.0f, 0.0f};
     for (uint32_t n = 0; n < P.spp; ++n) {
         const float fant = fdiv((float)n, (float)(n + 1));
@@ -152,7 +165,7 @@ __device__ __forceinline__ void path_pixel(const TreeRef& tr, const float* __res
         for (int c = 0; c < 3; ++c) acc[c] = fmul(acc[c], fant);
         int seg[kMaxSeg];
         bool missed;
-        const int ns = trace_path(tr, soup, P, i, j, n, seg, &missed);
+        const int ns = trace_path(tr, soup, P, valid, i, j, n, seg, &missed);
         float beta[3] = {1.0f, 1.0f, 1.0f};
         for (int s = 0; s < ns; ++s) {
             const float* le = emission + 3 * (size_t)seg[s];
@@ -165,7 +178,7 @@ __device__ __forceinline__ void path_pixel(const TreeRef& tr, const float* __res
         if (missed)
             for (int c = 0; c < 3; ++c) acc[c] = fadd(acc[c], fmul(fmul(fact, beta[c]), P.sky[c]));
     }
-    image[(size_t)j * P.cam.width + i] = make_float4(acc[0], acc[1], acc[2], 1.0f);
+    if (valid) image[(size_t)j * P.cam.width + i] = make_float4(acc[0], acc[1], acc[2], 1.0f);
 }
 
 __global__ void __launch_bounds__(kPtThreads) k_pathtrace_adjoint(
@@ -176,8 +189,9 @@ __global__ void __launch_bounds__(kPtThreads) k_pathtrace_adjoint(
     float dle[3] = {0.0f, 0.0f, 0.0f};
     for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
         uint32_t i, j;
-        if (!tile_pixel(tile, threadIdx.x & 31, P.cam.width, P.cam.height, &i, &j)) continue;
-        const float4 g4 = __ldg(dimage + (size_t)j * P.cam.width + i);
+        const bool valid = tile_pixel(tile, threadIdx.x & 31, P.cam.width, P.cam.height, &i, &j);
+        if (!valid) i = j = 0;
+        const float4 g4 = valid ? __ldg(dimage + (size_t)j * P.cam.width + i) : make_float4(0.f, 0.f, 0.f, 0.f);
         const float gimg[3] = {g4.x, g4.y, g4.z};
         for (uint32_t n = 0; n < P.spp; ++n) {
             // weight of sample n in the progressive mean
@@ -185,7 +199,7 @@ __global__ void __launch_bounds__(kPtThreads) k_pathtrace_adjoint(
             for (uint32_t m = n + 1; m < P.spp; ++m) w *= (float)m / (float)(m + 1);
             int seg[kMaxSeg];
             bool missed;
-            const int ns = trace_path(tr, soup, P, i, j, n, seg, &missed);
+            const int ns = trace_path(tr, soup, P, valid, i, j, n, seg, &missed);
             float beta[kMaxSeg][3];
             beta[0][0] = beta[0][1] = beta[0][2] = 1.0f;
             for (int s = 0; s + 1 < ns; ++s)

@@ -33,11 +33,13 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_
                                                                  uint32_t num_tiles) {
     for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
         uint32_t i, j;
-        if (tile_pixel(tile, threadIdx.x & 31, cam.width, cam.height, &i, &j)) {
-            const f3 d = primary_dir(cam, i, j);
-            const RayState r = make_ray(mk3(cam.eye[0], cam.eye[1], cam.eye[2]), d, 1e16f, -1);
-            uint32_t nb = 0, nt = 0;
-            const Hit h = trace_ray<STATS>(r, tr, false, &nb, &nt);
+        const bool valid = tile_pixel(tile, threadIdx.x & 31, cam.width, cam.height, &i, &j);
+        if (!valid) i = j = 0;  // lanes past the image edge only help the warp
+        const f3 d = primary_dir(cam, i, j);
+        const RayState r = make_ray(mk3(cam.eye[0], cam.eye[1], cam.eye[2]), d, 1e16f, -1);
+        uint32_t nb = 0, nt = 0;
+        const Hit h = trace_ray<STATS>(r, valid, tr, false, &nb, &nt);
+        if (valid) {
             const size_t p = (size_t)j * cam.width + i;
             store_hit(hits + p, h);
             if (STATS) {
@@ -45,62 +47,65 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_
                 stats[2 * p + 1] = nt;
             }
         }
-        __syncwarp();
     }
 }
 
-// Shadow (any hit) and mirror (closest hit) rays of one pixel.
+// Shadow (any hit) and mirror (closest hit) rays of one pixel.  Called by
+// all lanes of the warp together (valid == false for lanes past the image
+// edge); rays of pixels whose primary ray missed, or whose light is behind
+// the surface, are traced with active == false.
 template <bool STATS>
 __device__ __forceinline__ void secondary_pixel(const TreeRef& tr, const float* __restrict__ soup,
                                                 const rt_camera& cam, float lx, float ly, float lz,
                                                 const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis,
                                                 rt_hit* __restrict__ mirror, uint32_t* __restrict__ sstats,
-                                                uint32_t* __restrict__ mstats, uint32_t i, uint32_t j) {
+                                                uint32_t* __restrict__ mstats, bool valid, uint32_t i, uint32_t j) {
     const size_t p = (size_t)j * cam.width + i;
-    const int4 ph = __ldg(reinterpret_cast<const int4*>(prim + p));
+    int4 ph = make_int4(-1, 0, 0, 0);
+    if (valid) ph = __ldg(reinterpret_cast<const int4*>(prim + p));
     const int id = ph.x;
+    const bool has = valid && id >= 0;
     uint32_t snb = 0, snt = 0, mnb = 0, mnt = 0;
-    if (id < 0) {
-        if (vis) vis[p] = 0;
-        if (mirror) {
-            Hit m;
-            m.id = -2; m.u = -1.0f; m.v = -1.0f; m.t = 0.0f;
-            store_hit(mirror + p, m);
-        }
-    } else {
+    f3 N = mk3(0.f, 0.f, 1.f), Nf = N, P = mk3(0.f, 0.f, 0.f), L = mk3(0.f, 0.f, 1.f), d = mk3(0.f, 0.f, 1.f);
+    float dist = 1.0f;
+    bool cast = false;
+    if (has) {
         const float t = __int_as_float(ph.w);
-        const f3 d = primary_dir(cam, i, j);
+        d = primary_dir(cam, i, j);
         const f3 o = mk3(cam.eye[0], cam.eye[1], cam.eye[2]);
         const float* tp = soup + 9 * (size_t)id;
         const f3 A = mk3(__ldg(tp), __ldg(tp + 1), __ldg(tp + 2));
         const f3 B = mk3(__ldg(tp + 3), __ldg(tp + 4), __ldg(tp + 5));
         const f3 C = mk3(__ldg(tp + 6), __ldg(tp + 7), __ldg(tp + 8));
-        const f3 N = normalize3(cross3(sub3(B, A), sub3(C, A)));   // CSComputeColorRT.hlsl:61-63,75
-        f3 Nf = N;
+        N = normalize3(cross3(sub3(B, A), sub3(C, A)));            // CSComputeColorRT.hlsl:61-63,75
+        Nf = N;
         if (dot3(Nf, d) > 0.0f) Nf = mk3(-N.x, -N.y, -N.z);        // :126-131
-        const f3 P = mk3(fadd(o.x, fmul(t, d.x)), fadd(o.y, fmul(t, d.y)), fadd(o.z, fmul(t, d.z)));  // :134-135
-        f3 L = mk3(fsub(P.x, lx), fsub(P.y, ly), fsub(P.z, lz));   // :136
-        const float dist = fsqrt(dot3(L, L));                      // :137
+        P = mk3(fadd(o.x, fmul(t, d.x)), fadd(o.y, fmul(t, d.y)), fadd(o.z, fmul(t, d.z)));  // :134-135
+        L = mk3(fsub(P.x, lx), fsub(P.y, ly), fsub(P.z, lz));      // :136
+        dist = fsqrt(dot3(L, L));                                  // :137
         L = mk3(fdiv(L.x, dist), fdiv(L.y, dist), fdiv(L.z, dist)); // :138
-        if (vis) {
-            const float ls = dot3(N, L), rs = dot3(N, d);          // :145-146
-            uint8_t code = 1;
-            if (fmul(ls, rs) > 0.0f) {                             // :147
-                const RayState sr = make_ray(P, mk3(-L.x, -L.y, -L.z), dist, id);  // :149-153
-                const Hit sh = trace_ray<STATS>(sr, tr, true, &snb, &snt);
-                code = (sh.id >= 0) ? 2 : 3;
-            }
-            vis[p] = code;
-        }
-        if (mirror) {
-            const float k = fmul(2.0f, dot3(d, Nf));               // reflect(d, N) = d - 2*dot(d,N)*N
-            const f3 R = normalize3(mk3(fsub(d.x, fmul(k, Nf.x)), fsub(d.y, fmul(k, Nf.y)), fsub(d.z, fmul(k, Nf.z))));
-            const RayState mr = make_ray(P, R, 1e16f, id);
-            const Hit mh = trace_ray<STATS>(mr, tr, false, &mnb, &mnt);
-            store_hit(mirror + p, mh);
-        }
+        const float ls = dot3(N, L), rs = dot3(N, d);              // :145-146
+        cast = fmul(ls, rs) > 0.0f;                                // :147
     }
-    if (STATS) {
+    if (vis) {  // uniform across the warp
+        const RayState sr = make_ray(P, mk3(-L.x, -L.y, -L.z), dist, id);  // :149-153
+        const Hit sh = trace_ray<STATS>(sr, cast, tr, true, &snb, &snt);
+        if (valid) vis[p] = !has ? 0 : (!cast ? 1 : (sh.id >= 0 ? 2 : 3));
+    }
+    if (mirror) {
+        f3 R = mk3(0.f, 0.f, 1.f);
+        if (has) {
+            const float k = fmul(2.0f, dot3(d, Nf));               // reflect(d, N) = d - 2*dot(d,N)*N
+            R = normalize3(mk3(fsub(d.x, fmul(k, Nf.x)), fsub(d.y, fmul(k, Nf.y)), fsub(d.z, fmul(k, Nf.z))));
+        }
+        const RayState mr = make_ray(P, R, 1e16f, id);
+        Hit mh = trace_ray<STATS>(mr, has, tr, false, &mnb, &mnt);
+        if (!has) {
+            mh.id = -2; mh.u = -1.0f; mh.v = -1.0f; mh.t = 0.0f;
+        }
+        if (valid) store_hit(mirror + p, mh);
+    }
+    if (STATS && valid) {
         if (sstats) { sstats[2 * p] = snb; sstats[2 * p + 1] = snt; }
         if (mstats) { mstats[2 * p] = mnb; mstats[2 * p + 1] = mnt; }
     }
@@ -113,9 +118,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_secondary(
     uint32_t* __restrict__ sstats, uint32_t* __restrict__ mstats, uint32_t* work, uint32_t num_tiles) {
     for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
         uint32_t i, j;
-        if (tile_pixel(tile, threadIdx.x & 31, cam.width, cam.height, &i, &j))
-            secondary_pixel<STATS>(tr, soup, cam, lx, ly, lz, prim, vis, mirror, sstats, mstats, i, j);
-        __syncwarp();
+        const bool valid = tile_pixel(tile, threadIdx.x & 31, cam.width, cam.height, &i, &j);
+        if (!valid) i = j = 0;
+        secondary_pixel<STATS>(tr, soup, cam, lx, ly, lz, prim, vis, mirror, sstats, mstats, valid, i, j);
     }
 }
 
@@ -126,19 +131,22 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_rays(TreeRef tr, const 
     const uint32_t num_tiles = (n + 31) / 32;
     for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
         const uint32_t k = tile * 32 + (threadIdx.x & 31);
-        if (k < n) {
-            const float4 a = __ldg(reinterpret_cast<const float4*>(rays + k));
-            const float4 b = __ldg(reinterpret_cast<const float4*>(rays + k) + 1);
-            const RayState r = make_ray(mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), b.w, __float_as_int(a.w));
-            uint32_t nb = 0, nt = 0;
-            const Hit h = trace_ray<STATS>(r, tr, any_hit != 0, &nb, &nt);
+        const bool valid = k < n;
+        float4 a = make_float4(0.f, 0.f, 0.f, __int_as_float(-1)), b = make_float4(0.f, 0.f, 1.f, 1.f);
+        if (valid) {
+            a = __ldg(reinterpret_cast<const float4*>(rays + k));
+            b = __ldg(reinterpret_cast<const float4*>(rays + k) + 1);
+        }
+        const RayState r = make_ray(mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), b.w, __float_as_int(a.w));
+        uint32_t nb = 0, nt = 0;
+        const Hit h = trace_ray<STATS>(r, valid, tr, any_hit != 0, &nb, &nt);
+        if (valid) {
             store_hit(hits + k, h);
             if (STATS) {
                 stats[2 * k] = nb;
                 stats[2 * k + 1] = nt;
             }
         }
-        __syncwarp();
     }
 }
 

@@ -118,11 +118,42 @@ __device__ __forceinline__ NodeBox load_node(const rt_node* __restrict__ nodes, 
     return nb;
 }
 
+// Order key of a candidate hit: (t, id) as one unsigned 64-bit number, so
+// the tie rule (smaller t, then smaller id) is an integer minimum.  Accepted
+// hits have t >= 0; the sign bit is dropped so that -0 and +0 compare equal,
+// as they do in the reference's float comparison.
+__device__ __forceinline__ uint64_t hit_key(float t, int id) {
+    return ((uint64_t)(__float_as_uint(t) & 0x7fffffffu) << 32) | (uint32_t)id;
+}
+
+__device__ __forceinline__ uint64_t shfl_u64(uint64_t v, int src) {
+    const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)v, src);
+    const uint32_t hi = __shfl_sync(0xffffffffu, (uint32_t)(v >> 32), src);
+    return ((uint64_t)hi << 32) | lo;
+}
+__device__ __forceinline__ uint64_t shfl_down_u64(uint64_t v, int off) {
+    const uint32_t lo = __shfl_down_sync(0xffffffffu, (uint32_t)v, off);
+    const uint32_t hi = __shfl_down_sync(0xffffffffu, (uint32_t)(v >> 32), off);
+    return ((uint64_t)hi << 32) | lo;
+}
+
+// Warp-cooperative traversal.  All 32 lanes of the warp call it together;
+// lanes with active == false only help.  Each round, every lane descends
+// through internal nodes until it holds a leaf or has nothing left (the
+// descent diverges), then the warp tests the triangles of all held leaves
+// together: the (lane, triangle) pairs are numbered by a prefix sum of the
+// leaf sizes and processed 32 at a time, so consecutive lanes read
+// consecutive triangles and a 200-triangle leaf costs 7 warp steps instead of
+// 200.  A segmented minimum over hit_key returns each lane's closest
+// accepted hit; that is the result of testing the leaf's triangles in any
+// order under the tie rule, so hits and test counts equal the oracle's.
 template <bool EXACT, bool STATS>
-__device__ __forceinline__ Hit traverse(const RayState& r, const TreeRef& tr_, bool any_hit, uint32_t* nbox_out,
-                                        uint32_t* ntri_out) {
+__device__ __forceinline__ Hit traverse(const RayState& r, bool active, const TreeRef& tr_, bool any_hit,
+                                        uint32_t* nbox_out, uint32_t* ntri_out) {
+    constexpr uint32_t kFull = 0xffffffffu;
     const rt_node* __restrict__ nodes = tr_.nodes;
     const float4* __restrict__ tris = tr_.tris;
+    const int lane = threadIdx.x & 31;
     Hit best;
     best.id = -1;
     best.u = -1.0f;
@@ -146,81 +177,154 @@ __device__ __forceinline__ Hit traverse(const RayState& r, const TreeRef& tr_, b
         return false;
     };
 
-    NodeBox cur = load_node(nodes, 1);
-    float t0;
-    if (STATS) ++nbox;
-    bool have = box_enter<EXACT>(r, cur.a.x, cur.a.y, cur.a.z, cur.a.w, cur.b.x, cur.b.y, best.t, &t0);
+    NodeBox cur;
+    cur.a = make_float4(0.f, 0.f, 0.f, 0.f);
+    cur.b = cur.a;
+    bool have = false;
     uint32_t node = 1;
-    // while-while: lanes descend through internal nodes until each holds a
-    // leaf (or has nothing left), then the warp tests leaf triangles together.
-    while (have) {
-        while (!(__float_as_int(cur.b.z) & 4)) {
-            const int pc = __float_as_int(cur.b.z);
-            const uint32_t c0 = node << 1;
-            if (c0 + 1 >= tr_.num_nodes) {
-                atomicOr(tr_.err, RT_DEVERR_BOUNDS);
-                have = false;
-                break;
-            }
-            const float4* p = reinterpret_cast<const float4*>(nodes + c0);
-            const float4 l0 = __ldg(p), l1 = __ldg(p + 1), r0 = __ldg(p + 2), r1 = __ldg(p + 3);
-            float tl, tr;
-            const bool hl = box_enter<EXACT>(r, l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, best.t, &tl);
-            const bool hr = box_enter<EXACT>(r, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, best.t, &tr);
-            if (STATS) nbox += 2;
-            // near child by the split axis: the stored field is (30 - bit) % 3,
-            // the axis the bit splits is (field + 2) % 3
-            const int field = pc & 3;
-            const int near_right = (r.sgn >> (field == 0 ? 2 : field - 1)) & 1;
-            const bool hn = near_right ? hr : hl, hf = near_right ? hl : hr;
-            const float tf = near_right ? tl : tr;
-            const uint32_t nn = c0 | (uint32_t)near_right, nf = nn ^ 1u;
-            if (hn) {
-                if (hf) {
-                    stack_node[sp] = nf;
-                    stack_t0[sp] = tf;
-                    ++sp;
+    if (active) {
+        cur = load_node(nodes, 1);
+        if (STATS) ++nbox;
+        float t0;
+        have = box_enter<EXACT>(r, cur.a.x, cur.a.y, cur.a.z, cur.a.w, cur.b.x, cur.b.y, best.t, &t0);
+    }
+    while (__any_sync(kFull, have)) {
+        // 1) descent to a leaf
+        if (have) {
+            while (!(__float_as_int(cur.b.z) & 4)) {
+                const int pc = __float_as_int(cur.b.z);
+                const uint32_t c0 = node << 1;
+                if (c0 + 1 >= tr_.num_nodes) {
+                    atomicOr(tr_.err, RT_DEVERR_BOUNDS);
+                    have = false;
+                    break;
                 }
-                node = nn;
-                cur.a = near_right ? r0 : l0;
-                cur.b = near_right ? r1 : l1;
-            } else if (hf) {
-                node = nf;
-                cur.a = near_right ? l0 : r0;
-                cur.b = near_right ? l1 : r1;
+                const float4* p = reinterpret_cast<const float4*>(nodes + c0);
+                const float4 l0 = __ldg(p), l1 = __ldg(p + 1), r0 = __ldg(p + 2), r1 = __ldg(p + 3);
+                float tl, tr;
+                const bool hl = box_enter<EXACT>(r, l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, best.t, &tl);
+                const bool hr = box_enter<EXACT>(r, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, best.t, &tr);
+                if (STATS) nbox += 2;
+                // near child by the split axis: the stored field is (30 - bit) % 3,
+                // the axis the bit splits is (field + 2) % 3
+                const int field = pc & 3;
+                const int near_right = (r.sgn >> (field == 0 ? 2 : field - 1)) & 1;
+                const bool hn = near_right ? hr : hl, hf = near_right ? hl : hr;
+                const float tf = near_right ? tl : tr;
+                const uint32_t nn = c0 | (uint32_t)near_right, nf = nn ^ 1u;
+                if (hn) {
+                    if (hf) {
+                        stack_node[sp] = nf;
+                        stack_t0[sp] = tf;
+                        ++sp;
+                    }
+                    node = nn;
+                    cur.a = near_right ? r0 : l0;
+                    cur.b = near_right ? r1 : l1;
+                } else if (hf) {
+                    node = nf;
+                    cur.a = near_right ? l0 : r0;
+                    cur.b = near_right ? l1 : r1;
+                } else {
+                    have = pop(node);
+                    if (!have) break;
+                    cur = load_node(nodes, node);
+                }
+            }
+        }
+        __syncwarp();
+        // 2) the warp tests the held leaves' triangles [pos, pos + cnt)
+        int cnt = 0, pos = 0;
+        if (have) {
+            cnt = __float_as_int(cur.b.z) >> 3;
+            pos = __float_as_int(cur.b.w);
+            if (pos < 0 || cnt < 0 || (uint32_t)pos + (uint32_t)cnt > tr_.n) {
+                atomicOr(tr_.err, RT_DEVERR_BOUNDS);
+                cnt = 0;
+            }
+        }
+        if (STATS) ntri += (uint32_t)cnt;
+        uint32_t incl = (uint32_t)cnt;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, incl, off);
+            if (lane >= off) incl += y;
+        }
+        const uint32_t total = __shfl_sync(kFull, incl, 31);
+        const uint32_t excl = incl - (uint32_t)cnt;
+        uint64_t my_best = hit_key(best.t, best.id >= 0 ? best.id : 0);
+        for (uint32_t base = 0; base < total; base += 32) {
+            const uint32_t p = base + lane;
+            // owner of pair p: the first lane whose inclusive prefix exceeds p
+            int o = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const uint32_t v = __shfl_sync(kFull, incl, o + step - 1);
+                if (v <= p) o += step;
+            }
+            const uint32_t o_excl = __shfl_sync(kFull, excl, o);
+            const int o_pos = __shfl_sync(kFull, pos, o);
+            RayState ro;
+            ro.o = mk3(__shfl_sync(kFull, r.o.x, o), __shfl_sync(kFull, r.o.y, o), __shfl_sync(kFull, r.o.z, o));
+            ro.d = mk3(__shfl_sync(kFull, r.d.x, o), __shfl_sync(kFull, r.d.y, o), __shfl_sync(kFull, r.d.z, o));
+            const int o_exclude = __shfl_sync(kFull, r.exclude, o);
+            const uint64_t o_best = shfl_u64(my_best, o);
+            uint64_t key = ~0ull;
+            float kt = 0.0f, ku = 0.0f, kv = 0.0f;
+            if (p < total) {
+                const float4* tp = tris + 3 * (size_t)(o_pos + (p - o_excl));
+                const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                const int id = __float_as_int(a.w);
+                float u, v, t;
+                if (id != o_exclude && tri_test(ro, a, b, c, &u, &v, &t)) {
+                    const uint64_t k = hit_key(t, id);
+                    if (k < o_best) {
+                        key = k;
+                        kt = t;
+                        ku = u;
+                        kv = v;
+                    }
+                }
+            }
+            // segmented minimum: lanes of one owner are contiguous; afterwards
+            // the first lane of each owner's run holds that run's minimum
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint64_t k2 = shfl_down_u64(key, off);
+                const float t2 = __shfl_down_sync(kFull, kt, off);
+                const float u2 = __shfl_down_sync(kFull, ku, off);
+                const float v2 = __shfl_down_sync(kFull, kv, off);
+                const int o2 = __shfl_down_sync(kFull, o, off);
+                if (lane + off < 32 && o2 == o && k2 < key) {
+                    key = k2;
+                    kt = t2;
+                    ku = u2;
+                    kv = v2;
+                }
+            }
+            const bool mine = cnt > 0 && excl < base + 32 && incl > base;
+            const int head = mine ? (int)(max(excl, base) - base) : lane;
+            const uint64_t hk = shfl_u64(key, head);
+            const float ht = __shfl_sync(kFull, kt, head);
+            const float hu = __shfl_sync(kFull, ku, head);
+            const float hv = __shfl_sync(kFull, kv, head);
+            if (mine && hk < my_best) {
+                my_best = hk;
+                best.t = ht;
+                best.u = hu;
+                best.v = hv;
+                best.id = (int)(uint32_t)hk;
+            }
+        }
+        // 3) next node
+        if (have) {
+            if (any_hit && best.id >= 0) {
+                have = false;
             } else {
                 have = pop(node);
-                if (!have) break;
-                cur = load_node(nodes, node);
+                if (have) cur = load_node(nodes, node);
             }
         }
-        if (!have) break;
-        // leaf: triangles [pos, pos + cnt) of the sorted, pre-gathered array
-        int cnt = __float_as_int(cur.b.z) >> 3;
-        const int pos = __float_as_int(cur.b.w);
-        if (pos < 0 || cnt < 0 || (uint32_t)pos + (uint32_t)cnt > tr_.n) {
-            atomicOr(tr_.err, RT_DEVERR_BOUNDS);
-            cnt = 0;
-        }
-        for (int i = 0; i < cnt; ++i) {
-            const float4* tp = tris + 3 * (size_t)(pos + i);
-            const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-            if (STATS) ++ntri;
-            const int id = __float_as_int(a.w);
-            if (id == r.exclude) continue;
-            float u, v, t;
-            if (tri_test(r, a, b, c, &u, &v, &t)) {
-                if (t < best.t || (t == best.t && best.id >= 0 && id < best.id)) {
-                    best.t = t;
-                    best.u = u;
-                    best.v = v;
-                    best.id = id;
-                }
-            }
-        }
-        if (any_hit && best.id >= 0) break;
-        have = pop(node);
-        if (have) cur = load_node(nodes, node);
     }
     if (STATS) {
         *nbox_out = nbox;
@@ -229,12 +333,14 @@ __device__ __forceinline__ Hit traverse(const RayState& r, const TreeRef& tr_, b
     return best;
 }
 
-// Warp-uniform dispatch between the fast and the NaN-exact box test.
+// Warp-uniform dispatch between the fast and the NaN-exact box test.  Must be
+// called by all 32 lanes of the warp together (inactive lanes pass
+// active == false).
 template <bool STATS>
-__device__ __forceinline__ Hit trace_ray(const RayState& r, const TreeRef& tr, bool any_hit, uint32_t* nbox,
-                                         uint32_t* ntri) {
-    if (__any_sync(__activemask(), r.exact)) return traverse<true, STATS>(r, tr, any_hit, nbox, ntri);
-    return traverse<false, STATS>(r, tr, any_hit, nbox, ntri);
+__device__ __forceinline__ Hit trace_ray(const RayState& r, bool active, const TreeRef& tr, bool any_hit,
+                                         uint32_t* nbox, uint32_t* ntri) {
+    if (__any_sync(0xffffffffu, active && r.exact)) return traverse<true, STATS>(r, active, tr, any_hit, nbox, ntri);
+    return traverse<false, STATS>(r, active, tr, any_hit, nbox, ntri);
 }
 
 // Primary ray of pixel (i, j): CSPrimaryRays.hlsl:36-56 with the basis camera.
