@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=16)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["frame", "torus", "pt"], default="frame")
+    ap.add_argument("--workload", choices=["frame", "torus", "pt", "adjoint"], default="frame")
     ap.add_argument("--freq", type=int, default=324, help="icosphere frequency (324 -> 2,099,520 triangles)")
     ap.add_argument("--depth", type=int, default=20)
     ap.add_argument("--frames", type=int, default=16)
@@ -184,14 +184,14 @@ def run_ours(args, dist: Dist):
     import torch
     from rtgpu import _lib as L
     from rtgpu import build as B
-    from rtgpu.api import LBVH, Context, RayTracer
+    from rtgpu.api import LBVH, Context, Frame, RayTracer
 
     B.build_cuda()
     torch.cuda.set_device(dist.local)
     dist.init("nccl")
     dev = torch.device("cuda", dist.local)
-    if args.workload == "pt":
-        return run_pt(args, dist)
+    if args.workload in ("pt", "adjoint"):
+        return run_pt(args, dist, adjoint=args.workload == "adjoint")
     frames, cam, light, name = frame_workload(args)
     n = len(frames[0])
     npx = cam.width * cam.height
@@ -235,28 +235,49 @@ def run_ours(args, dist: Dist):
         if evs:
             evs[3].record(stream)
 
+    # (1) per-stage split: the frame issued call by call with events between stages
     for k in range(args.warmup):
         flush.zero_()
         step(k)
     ctx.check()
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.zero_()  # > L2 (129 MB) written between steps, outside the per-step events
+        step(args.warmup + k, evs[k])
+    torch.cuda.synchronize()
+    ctx.check()
+    per = np.array([[a.elapsed_time(b) for a, b in zip(e[:-1], e[1:])] for e in evs])  # ms: build, primary, secondary
+    build_ms, prim_ms, sec_ms = per.mean(0)
+    stream_frame_ms = float(per.sum(1).mean())
+
+    # (2) the timed steps: each frame is one CUDA-graph launch (rt_frame_capture
+    # of rebuild + primary + shadow + mirror), one graph per frame buffer
+    graphs = [Frame(ctx, lb, dfr[k], cam, light, hits, vis, mirror) for k in range(len(frames))]
+    for k in range(args.warmup):
+        flush.zero_()
+        graphs[k % len(graphs)].launch()
+    ctx.check()
+    gevs = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(args.steps)]
     dist.barrier()
     torch.cuda.synchronize()
     with Clocks(dist.local) as clk:
         t0 = time.perf_counter()
         for k in range(args.steps):
-            flush.zero_()  # > L2 (129 MB) written between steps, outside the per-step events
-            step(args.warmup + k, evs[k])
+            flush.zero_()
+            gevs[k][0].record(stream)
+            graphs[(args.warmup + k) % len(graphs)].launch()
+            gevs[k][1].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     dist.barrier()
     ctx.check()
-    per = np.array([[a.elapsed_time(b) for a, b in zip(e[:-1], e[1:])] for e in evs])  # ms: build, primary, secondary
-    step_ms = per.sum(1)
+    step_ms = np.array([e[0].elapsed_time(e[1]) for e in gevs])
     t_total = dist.max(float(step_ms.sum()) / 1e3)
     frames_done = dist.sum(float(args.steps))
     value = frames_done * n / t_total / 1e6
-    build_ms, prim_ms, sec_ms = per.mean(0)
+    for g in graphs:
+        g.close()
 
     # e2e: the public C ABI call with host buffers, copies inside the timed region
     e2e = None
@@ -303,7 +324,8 @@ def run_ours(args, dist: Dist):
         "config": {"workload": name, "triangles": n, "pixels": npx, "depth": args.depth,
                    "l2": "flushed between steps (256 MiB write outside the per-step events)",
                    "parallelism": "replicas" if dist.world > 1 else "single GPU"},
-        "components": {"build_ms": round(float(build_ms), 4), "build_mtri_s": round(n / build_ms / 1e3, 2),
+        "components": {"graph_frame_ms": round(float(step_ms.mean()), 4), "stream_frame_ms": round(stream_frame_ms, 4),
+                       "build_ms": round(float(build_ms), 4), "build_mtri_s": round(n / build_ms / 1e3, 2),
                        "primary_ms": round(float(prim_ms), 4), "secondary_ms": round(float(sec_ms), 4),
                        "trace_mrays_s": round(rays_per_frame / ((prim_ms + sec_ms) / 1e3) / 1e6, 1),
                        "rays_per_frame": {"primary": n_prim, "shadow": n_shadow, "mirror": n_mirror},
@@ -359,8 +381,9 @@ def run_reference(args, dist: Dist):
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as O
     O.build_oracle()
-    if args.workload == "pt":
-        return {"impl": "reference", "unavailable": "no reference CPU path tracer exists for this workload"}
+    if args.workload in ("pt", "adjoint"):
+        return {"impl": "reference", "unavailable": "the reference has no CPU path tracer or adjoint; its GI is "
+                "an HLSL shader (unavailable on this box)"}
     frames, cam, light, name = frame_workload(args)
     n = len(frames[0])
     nth = O.nthreads_default()
@@ -400,8 +423,120 @@ def run_reference(args, dist: Dist):
             "e2e": {"value": round(value, 4), "unit": "Mtri/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
-def run_pt(args, dist: Dist):
-    raise SystemExit("the path-tracing workload is run by bench_pt() once rt_pathtrace is benchmarked")
+def run_pt(args, dist: Dist, adjoint: bool = False):
+    """Path-traced GI (closed box + 262,144 random triangles, 1024x1024, 4 spp,
+    4 bounces), or with adjoint=True the differentiable workload (same scene at
+    512x512, 8 spp, 3 bounces: forward render + L2 image loss + adjoint
+    gradients w.r.t. every albedo and the emitter radiance).  A step = LBVH
+    rebuild + render (+ backward)."""
+    import torch
+    from rtgpu import scenes
+    from rtgpu.api import LBVH, Context, RayTracer
+    from rtgpu.autograd import render
+    dev = torch.device("cuda", dist.local)
+    sc = scenes.gi_box(262144, seed=3)
+    if adjoint:
+        W = H = 512
+        spp, bounces = 8, 3
+    else:
+        W = H = 1024
+        spp, bounces = 4, 4
+    cam = scenes.gi_camera(W, H)
+    n = len(sc.tris)
+    ctx = Context(dist.local)
+    lb = LBVH(ctx, n, args.depth)
+    rt = RayTracer(ctx)
+    tris = torch.from_numpy(sc.tris).to(dev)
+    alb = torch.from_numpy(sc.albedo).to(dev)
+    em = torch.from_numpy(sc.emission).to(dev)
+    mask = torch.from_numpy((sc.emission[:, 0] > 0).astype(np.float32)).to(dev)
+    le = torch.tensor([10.0, 10.0, 10.0], device=dev)
+    img = torch.empty((W * H, 4), dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    target = None
+    if adjoint:
+        rng = np.random.Generator(np.random.PCG64(7))
+        talb = np.clip(sc.albedo + rng.uniform(-0.1, 0.1, sc.albedo.shape), 0, 1).astype(np.float32)
+        lb.Build(tris)
+        with torch.no_grad():
+            target = render(torch.from_numpy(talb).to(dev), le, mask, rt, lb, cam, spp, bounces, 12345)
+    stream = torch.cuda.current_stream(dev)
+    fwd_ev, bwd_ev = [], []
+
+    def step(k, evs=None):
+        seed = 1000 + k
+        if evs:
+            evs[0].record(stream)
+        lb.Build(tris)
+        if adjoint:
+            a = alb.clone().requires_grad_(True)
+            lp = le.clone().requires_grad_(True)
+            out = render(a, lp, mask, rt, lb, cam, spp, bounces, seed)
+            if evs:
+                evs[1].record(stream)
+            loss = ((out[:, :3] - target[:, :3]) ** 2).mean()
+            loss.backward()
+        else:
+            rt.pathtrace(lb, alb, em, cam, spp, bounces, seed, out=img)
+            if evs:
+                evs[1].record(stream)
+        if evs:
+            evs[2].record(stream)
+
+    for k in range(args.warmup):
+        flush.zero_()
+        step(k)
+    ctx.check()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks(dist.local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            step(args.warmup + k, evs[k])
+        torch.cuda.synchronize()
+    dist.barrier()
+    ctx.check()
+    per = np.array([[e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])] for e in evs])  # ms: build+forward, backward
+    step_ms = per.sum(1)
+    t_total = dist.max(float(step_ms.sum()) / 1e3)
+    samples = W * H * spp * dist.sum(float(args.steps))
+    value = samples / t_total / 1e6
+    name = (f"GI box {n} tris, {W}x{H}, {spp} spp, {bounces} bounces" +
+            (", forward + L2 loss + adjoint (albedo x3, emitter radiance)" if adjoint else ""))
+    out = {"metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": dist.world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(float(step_ms.mean()), 4),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded procedural scene)",
+           "config": {"workload": name, "triangles": n, "pixels": W * H, "spp": spp, "bounces": bounces,
+                      "depth": args.depth, "l2": "flushed between steps (256 MiB write outside the events)"},
+           "components": {"build_plus_forward_ms": round(float(per[:, 0].mean()), 4),
+                          "segments_per_step_upper_bound": W * H * spp * (bounces + 1)},
+           "clocks": clk.summary(), "gpu_launches": (10 + 1 + (1 if adjoint else 0)) * args.steps}
+    if adjoint:
+        out["components"]["backward_ms"] = round(float(per[:, 1].mean()), 4)
+        out["components"]["backward_over_forward"] = round(float(per[:, 1].mean() / per[:, 0].mean()), 3)
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_pt_baseline(sc, cam, spp, bounces, args.depth)
+    lb.close()
+    ctx.close()
+    return out
+
+
+def cpu_pt_baseline(sc, cam, spp, bounces, depth):
+    """The oracle's path tracer on a 128x128 crop of the image, all host cores."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    from rtgpu import scenes
+    O.build_oracle()
+    nth = O.nthreads_default()
+    nodes, ids, _, _ = O.lbvh_build(sc.tris, depth)
+    crop = scenes.look_at(cam.eye[:], (0.5, 0.5, 1.0), vfov_deg=60.0 * 128 / cam.height, width=128, height=128)
+    t0 = time.perf_counter()
+    O.pathtrace(nodes, depth, ids, sc.tris, sc.albedo, sc.emission, crop, spp, bounces, 1000, nthreads=nth)
+    dt = time.perf_counter() - t0
+    return {"value": round(128 * 128 * spp / dt / 1e6, 4), "unit": "Msamples/s", "cores": nth, "kind": "port",
+            "sample": f"128x128 crop, {spp} spp, {bounces} bounces, {dt:.2f}s on {nth} threads", "cpu": _cpu_name()}
 
 
 def main():

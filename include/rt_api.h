@@ -187,6 +187,22 @@ rt_status rt_render_frame_host(rt_ctx* ctx, rt_lbvh* lbvh, const float* h_tris, 
                                const rt_camera* cam, const float light[3], rt_hit* h_primary,
                                uint8_t* h_vis, rt_hit* h_mirror);
 
+/* ---- one frame as a CUDA graph ------------------------------------- */
+/* The dynamic per-frame path (RayTracerCS::Render with dynamic=1,
+ * RayTracerCS.cpp:258-295: rebuild, primary rays, shadow + mirror rays)
+ * captured once and replayed with one launch.  All pointers, the camera and
+ * the light are fixed at capture; write new vertex data into d_tris (or
+ * capture one rt_frame per soup buffer).  d_vis / d_mirror may be NULL.
+ * Capturing synchronises the context stream; rt_frame_launch is
+ * asynchronous on it.  rt_frame_node_count: nodes in the captured graph. */
+typedef struct rt_frame rt_frame;
+rt_status rt_frame_capture(rt_ctx* ctx, rt_lbvh* lbvh, const float* d_tris, uint32_t n, uint32_t flags,
+                           const rt_camera* cam, const float light[3], rt_hit* d_primary, uint8_t* d_vis,
+                           rt_hit* d_mirror, rt_frame** out);
+rt_status rt_frame_launch(rt_ctx* ctx, rt_frame* frame);
+uint32_t rt_frame_node_count(const rt_frame* frame);
+rt_status rt_frame_destroy(rt_frame* frame);
+
 /* ---- path tracing (CSComputeColorGI.hlsl, ConstantBuffers.h:85-110) --- */
 typedef struct rt_pt_params {
     uint32_t spp;

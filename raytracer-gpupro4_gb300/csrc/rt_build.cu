@@ -104,7 +104,14 @@ __global__ void __launch_bounds__(256) k_bounds(const float* __restrict__ tris, 
 
     for (uint32_t i = gtid; i < 4 * 256; i += gstride) hist[i] = 0u;
     for (uint32_t i = gtid; i < lookback_words; i += gstride) lookback[i] = 0u;
-    if (gtid >= 1 && gtid < 8) counters[gtid] = 0u;
+    // counters: [0] bounds ticket (reset by the last block), [1..4] sort tile
+    // tickets, [5] leaf count, [6] refit epoch (advanced once per build, so a
+    // replayed CUDA graph of the build still tags every arrival afresh)
+    if (gtid >= 1 && gtid < 6) counters[gtid] = 0u;
+    if (gtid == 0) {
+        uint32_t e = counters[6] + 1u;
+        counters[6] = e ? e : 1u;  // 0 is the value of cleared arrival words
+    }
     if (clear_nodes) {
         for (uint32_t i = gtid; i < num_nodes; i += gstride) {
             rt_node s;
@@ -492,7 +499,13 @@ __device__ __forceinline__ void load_chunk(const uint32_t* __restrict__ keys, ui
 
 // k_emit_tiles: per-tile fwd/bwd aggregates of the boundary record masks.
 __global__ void __launch_bounds__(kEmitThreads) k_emit_tiles(const uint32_t* __restrict__ keys, uint32_t n,
-                                                             uint32_t* scan) {
+                                                             uint32_t* scan, uint32_t* arrive, uint32_t arrive_words,
+                                                             const uint32_t* epoch_word) {
+    // epoch 1 means the first build or a wrapped epoch counter: the refit's
+    // arrival words may hold any old epoch and are cleared before k_emit_refit
+    if (*epoch_word == 1u)
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < arrive_words; i += gridDim.x * blockDim.x)
+            arrive[i] = 0u;
     __shared__ uint32_t s_f[8], s_b[8];
     const uint32_t s = blockIdx.x * kEmitTile + threadIdx.x * kEmitItems;
     EmitChunk e;
@@ -634,13 +647,14 @@ __global__ void __launch_bounds__(kEmitThreads) k_emit_leaves(const uint32_t* __
 // k_emit_refit: leaf fields and boxes (LBVH.cpp:194-208 / LBVH.hlsl:240-258),
 // then the bottom-up walk: the second of two siblings to arrive at a parent
 // writes it (LBVH.cpp:310-313 / LBVH.hlsl:260-269).  Arrival words carry the
-// build epoch, so they never need clearing.
+// build epoch (counters[6], advanced by k_bounds), so they never need clearing.
 __global__ void __launch_bounds__(256) k_emit_refit(const uint32_t* __restrict__ keys, const float4* sorted_tris,
                                                     uint32_t n, uint32_t depth, rt_node* nodes,
                                                     const uint32_t* __restrict__ leaf_list,
                                                     const uint32_t* leaf_count, uint32_t* arrive,
-                                                    uint32_t epoch, uint32_t* err) {
+                                                    const uint32_t* epoch_word, uint32_t* err) {
     const uint32_t nleaves = min(*leaf_count, n);
+    const uint32_t epoch = *epoch_word;
     for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < nleaves; li += gridDim.x * blockDim.x) {
         uint32_t h = leaf_list[li];
         const int32_t pos = __ldcg(&nodes[h].prim_pos);
@@ -791,10 +805,6 @@ static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint
     cudaStream_t st = ctx->stream;
     l->n = n;
     l->src_tris = d_tris;
-    if (++l->epoch == 0) {  // wrapped: arrival words must be cleared once
-        RT_CHECK_CUDA(ctx, cudaMemsetAsync(l->arrive, 0, sizeof(uint32_t) * std::max(1u, l->num_nodes >> 1), st));
-        l->epoch = 1;
-    }
     const uint32_t sort_tiles = ceil_div(n, kSortTile);
     const uint32_t emit_tiles = ceil_div(n, kEmitTile);
     const uint32_t lb_words = kSortPasses * 256 * sort_tiles;
@@ -815,7 +825,8 @@ static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint
         std::swap(iin, iout);
     }
     // four passes: sorted pairs are back in keys / ids
-    k_emit_tiles<<<emit_tiles, kEmitThreads, 0, st>>>(l->keys, n, l->scan);
+    k_emit_tiles<<<emit_tiles, kEmitThreads, 0, st>>>(l->keys, n, l->scan, l->arrive, std::max(1u, l->num_nodes >> 1),
+                                                      l->counters + 6);
     RT_CHECK_LAUNCH(ctx, "k_emit_tiles");
     k_emit_prefix<<<1, 32, 0, st>>>(l->scan, emit_tiles);
     RT_CHECK_LAUNCH(ctx, "k_emit_prefix");
@@ -824,7 +835,7 @@ static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint
     RT_CHECK_LAUNCH(ctx, "k_emit_leaves");
     const uint32_t rblocks = std::max(1u, std::min(ceil_div(n, 256), (uint32_t)ctx->num_sms * 8));
     k_emit_refit<<<rblocks, 256, 0, st>>>(l->keys, l->sorted_tris, n, l->depth, l->nodes, l->leaf_list,
-                                          l->counters + 5, l->arrive, l->epoch, ctx->d_err);
+                                          l->counters + 5, l->arrive, l->counters + 6, ctx->d_err);
     RT_CHECK_LAUNCH(ctx, "k_emit_refit");
     l->built_keys = true;
     return RT_OK;
@@ -994,13 +1005,13 @@ extern "C" rt_status rt_lbvh_build_noalloc(rt_ctx* ctx, void* stream, const floa
     uint32_t* arrive = S + kNaArrive;
     uint32_t* err = S + kNaErr;
     const uint32_t num_nodes = 1u << depth;
-    // what must start at zero: the bounds ticket and the refit arrival words
-    // (the other counters, histograms and look-back words are reset by k_bounds)
+    // what must start at zero: the bounds ticket, the refit epoch (k_bounds
+    // advances it to 1) and the refit arrival words; the other counters,
+    // histograms and look-back words are reset by k_bounds
     e = cudaMemsetAsync(counters, 0, 8 * sizeof(uint32_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(arrive, 0, sizeof(uint32_t) * std::max(1u, num_nodes >> 1), st);
     if (e != cudaSuccess)
         return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_build_noalloc: cudaMemsetAsync failed: %s", cudaGetErrorString(e));
-    const uint32_t epoch = 1;
     const uint32_t sort_tiles = ceil_div(n, kSortTile);
     const uint32_t emit_tiles = ceil_div(n, kEmitTile);
     const uint32_t lb_words = kSortPasses * 256 * sort_tiles;
@@ -1017,13 +1028,13 @@ extern "C" rt_status rt_lbvh_build_noalloc(rt_ctx* ctx, void* stream, const floa
         std::swap(kin, kout);
         std::swap(iin, iout);
     }
-    k_emit_tiles<<<emit_tiles, kEmitThreads, 0, st>>>(d_keys, n, scan);
+    k_emit_tiles<<<emit_tiles, kEmitThreads, 0, st>>>(d_keys, n, scan, arrive, std::max(1u, num_nodes >> 1), counters + 6);
     k_emit_prefix<<<1, 32, 0, st>>>(scan, emit_tiles);
     k_emit_leaves<<<emit_tiles, kEmitThreads, 0, st>>>(d_keys, d_ids, d_tris, n, depth, scan, d_nodes,
                                                        reinterpret_cast<float4*>(d_sorted_tris), leaves, counters + 5);
     const uint32_t rblocks = std::max(1u, std::min(ceil_div(n, 256), (uint32_t)D.num_sms * 8));
     k_emit_refit<<<rblocks, 256, 0, st>>>(d_keys, reinterpret_cast<const float4*>(d_sorted_tris), n, depth, d_nodes,
-                                          leaves, counters + 5, arrive, epoch, err);
+                                          leaves, counters + 5, arrive, counters + 6, err);
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_build_noalloc: launch failed: %s", cudaGetErrorString(e));

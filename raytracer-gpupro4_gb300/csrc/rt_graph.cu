@@ -1,0 +1,87 @@
+// rt_graph.cu -- one frame of the dynamic path captured as a CUDA graph.
+//
+// RayTracerCS::Render with dynamic = 1 (RayTracerCS.cpp:258-295) issues the
+// rebuild (2*depth + 46 dispatches in the reference) and the trace stages
+// every frame.  Here the 10 build kernels, the two work-counter resets and
+// the two trace kernels of one frame are captured once and replayed with a
+// single cudaGraphLaunch, so the frame carries no per-kernel launch cost.
+// Every kernel parameter (soup pointer, camera, output buffers) is fixed at
+// capture time; a caller that streams new vertex data writes it into the
+// captured soup buffer, or captures one frame object per buffer.
+#include "rt_internal.cuh"
+
+struct rt_frame {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint32_t nodes = 0;
+};
+
+extern "C" rt_status rt_frame_capture(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint32_t n, uint32_t flags,
+                                      const rt_camera* cam, const float light[3], rt_hit* d_primary, uint8_t* d_vis,
+                                      rt_hit* d_mirror, rt_frame** out) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (!l || !d_tris || !cam || !light || !d_primary || !out)
+        return rt_fail(ctx, RT_ERR_INVALID, "rt_frame_capture: null argument");
+    *out = nullptr;
+    // capture on a private stream (the legacy default stream cannot be captured)
+    cudaStream_t cs = nullptr;
+    RT_CHECK_CUDA(ctx, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    // the context stream's pending work must finish before the private stream
+    // records the frame (the frame reads buffers that work may still write)
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(cs);
+        return rt_fail(ctx, RT_ERR_CUDA, "rt_frame_capture: %s", cudaGetErrorString(e));
+    }
+    cudaStream_t saved = ctx->stream;
+    ctx->stream = cs;
+    rt_status s = RT_OK;
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        s = rt_lbvh_build(ctx, l, d_tris, n, flags);
+        if (s == RT_OK) s = rt_trace_primary(ctx, l, cam, d_primary, nullptr);
+        if (s == RT_OK && (d_vis || d_mirror))
+            s = rt_trace_shadow_mirror(ctx, l, cam, light, d_primary, d_vis, d_mirror, nullptr, nullptr);
+        e = cudaStreamEndCapture(cs, &graph);
+    }
+    ctx->stream = saved;
+    cudaStreamDestroy(cs);
+    if (s != RT_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return s;
+    }
+    if (e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return rt_fail(ctx, RT_ERR_CUDA, "rt_frame_capture: stream capture failed: %s", cudaGetErrorString(e));
+    }
+    rt_frame* f = new rt_frame();
+    f->graph = graph;
+    e = cudaGraphInstantiate(&f->exec, graph, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        delete f;
+        return rt_fail(ctx, RT_ERR_CUDA, "rt_frame_capture: cudaGraphInstantiate failed: %s", cudaGetErrorString(e));
+    }
+    size_t count = 0;
+    if (cudaGraphGetNodes(graph, nullptr, &count) == cudaSuccess) f->nodes = (uint32_t)count;
+    *out = f;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_frame_launch(rt_ctx* ctx, rt_frame* f) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (!f || !f->exec) return rt_fail(ctx, RT_ERR_INVALID, "rt_frame_launch: null frame");
+    RT_CHECK_CUDA(ctx, cudaGraphLaunch(f->exec, ctx->stream));
+    return RT_OK;
+}
+
+extern "C" uint32_t rt_frame_node_count(const rt_frame* f) { return f ? f->nodes : 0u; }
+
+extern "C" rt_status rt_frame_destroy(rt_frame* f) {
+    if (!f) return RT_OK;
+    if (f->exec) cudaGraphExecDestroy(f->exec);
+    if (f->graph) cudaGraphDestroy(f->graph);
+    delete f;
+    return RT_OK;
+}

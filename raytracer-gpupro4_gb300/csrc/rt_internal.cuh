@@ -105,13 +105,12 @@ struct rt_lbvh {
     // build scratch
     SceneInfo* scene = nullptr;
     float* partials = nullptr;       // bounds partial reductions, 8 floats per block
-    uint32_t* counters = nullptr;    // [0] bounds ticket, [1..4] sort tile tickets, [5] leaf count
+    uint32_t* counters = nullptr;    // [0] bounds ticket, [1..4] sort tile tickets, [5] leaf count, [6] refit epoch
     uint32_t* hist = nullptr;        // 4 x 256 digit histograms
     uint32_t* lookback = nullptr;    // 4 passes x sort tiles x 256 status words
     uint32_t* scan = nullptr;        // emission tiles x 4 (fwd agg, bwd agg, fwd prefix, bwd suffix)
     uint32_t* leaf_list = nullptr;   // cap
     uint32_t* arrive = nullptr;      // 1 << (depth-1) refit arrival words (epoch-tagged)
-    uint32_t epoch = 0;
     uint32_t sort_tiles_cap = 0, emit_tiles_cap = 0, bounds_blocks = 0;
     // frame buffers for rt_render_frame_host (grown on demand)
     rt_hit* f_primary = nullptr;

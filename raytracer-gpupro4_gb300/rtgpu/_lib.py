@@ -29,7 +29,7 @@ EXPORTED = [
     "rt_ctx_check", "rt_last_error", "rt_lbvh_create", "rt_lbvh_destroy", "rt_lbvh_build", "rt_lbvh_build_host",
     "rt_lbvh_import_host", "rt_lbvh_view_get", "rt_lbvh_world_bound", "rt_lbvh_download", "rt_trace_primary",
     "rt_trace_shadow_mirror", "rt_trace_rays", "rt_render_frame_host", "rt_pathtrace", "rt_pathtrace_adjoint",
-    "rt_lbvh_build_noalloc",
+    "rt_lbvh_build_noalloc", "rt_frame_capture", "rt_frame_launch", "rt_frame_node_count", "rt_frame_destroy",
 ]
 
 
@@ -83,6 +83,10 @@ def lib() -> C.CDLL:
         "rt_pathtrace": (i32, [vp, vp, vp, vp, C.POINTER(Camera), C.POINTER(PtParams), vp]),
         "rt_pathtrace_adjoint": (i32, [vp, vp, vp, vp, C.POINTER(Camera), C.POINTER(PtParams), vp, vp, vp]),
         "rt_lbvh_build_noalloc": (i32, [vp, vp, vp, u32, u32, u32, vp, vp, vp, vp]),
+        "rt_frame_capture": (i32, [vp, vp, vp, u32, u32, C.POINTER(Camera), fp, vp, vp, vp, C.POINTER(vp)]),
+        "rt_frame_launch": (i32, [vp, vp]),
+        "rt_frame_node_count": (u32, [vp]),
+        "rt_frame_destroy": (i32, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -235,6 +235,43 @@ class RayTracer:
         return d_alb, d_le
 
 
+class Frame:
+    """One frame of the dynamic path (rebuild + primary + shadow + mirror)
+    captured as a CUDA graph (rt_frame_capture); launch() replays it."""
+
+    def __init__(self, ctx: Context, lbvh: LBVH, tris: torch.Tensor, cam: L.Camera, light, primary: torch.Tensor,
+                 vis: torch.Tensor | None, mirror: torch.Tensor | None, flags: int = 0):
+        self.ctx = ctx
+        self._keep = (tris, primary, vis, mirror)
+        h = C.c_void_p()
+        lf = (C.c_float * 3)(*light)
+        L.check(L.lib().rt_frame_capture(ctx.h, lbvh.h, _dev_ptr(tris), tris.shape[0], flags, C.byref(cam), lf,
+                                         _dev_ptr(primary), _dev_ptr(vis) if vis is not None else None,
+                                         _dev_ptr(mirror) if mirror is not None else None, C.byref(h)),
+                ctx.h, "rt_frame_capture")
+        self.h = h
+        lbvh.n = tris.shape[0]
+        lbvh._tris = tris
+
+    def launch(self):
+        L.check(L.lib().rt_frame_launch(self.ctx.h, self.h), self.ctx.h, "rt_frame_launch")
+
+    @property
+    def nodes(self) -> int:
+        return int(L.lib().rt_frame_node_count(self.h))
+
+    def close(self):
+        if self.h:
+            L.lib().rt_frame_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def rays_tensor(o, d, tmax, exclude, device) -> torch.Tensor:
     """Packs rays into the rt_ray layout as an (n, 8) float32 tensor."""
     n = len(d)

@@ -1,0 +1,45 @@
+"""The per-frame rebuild + trace captured as a CUDA graph (rt_frame_capture)
+replays to the same bits as the direct calls, frame after frame (the refit's
+arrival epoch lives in device memory, so replays stay correct)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_graph_frames_equal_direct_calls(gpu_ctx):
+    import torch
+    from rtgpu import scenes
+    from rtgpu.api import LBVH, Frame, RayTracer, hits_to_numpy
+    s = scenes.icosphere(freq=40)
+    frames = [torch.from_numpy(s.frame(k)).cuda() for k in range(3)]
+    cam = scenes.sphere_camera(320, 180)
+    light = scenes.TORUS_LIGHT
+    n = frames[0].shape[0]
+    npx = cam.width * cam.height
+    lb_g = LBVH(gpu_ctx, n, 16)
+    prim = torch.empty((npx, 4), dtype=torch.int32, device="cuda")
+    vis = torch.empty(npx, dtype=torch.uint8, device="cuda")
+    mir = torch.empty((npx, 4), dtype=torch.int32, device="cuda")
+    graphs = [Frame(gpu_ctx, lb_g, f, cam, light, prim, vis, mir) for f in frames]
+    assert graphs[0].nodes >= 14
+    rt = RayTracer(gpu_ctx)
+    lb_d = LBVH(gpu_ctx, n, 16)
+    for rep in range(2):
+        for k, f in enumerate(frames):
+            graphs[k].launch()
+            gpu_ctx.check()
+            gp, gv, gm = hits_to_numpy(prim), vis.cpu().numpy(), hits_to_numpy(mir)
+            g_nodes, g_ids, g_keys = lb_g.download(True, True, True)
+            lb_d.Build(f)
+            dp = rt.primary(lb_d, cam)
+            dv, dm = rt.shadow_mirror(lb_d, cam, light, dp)
+            gpu_ctx.check()
+            d_nodes, d_ids, d_keys = lb_d.download(True, True, True)
+            assert np.array_equal(g_keys, d_keys) and np.array_equal(g_ids, d_ids)
+            assert np.array_equal(g_nodes, d_nodes), f"replay {rep} frame {k}: nodes differ"
+            assert np.array_equal(gp, hits_to_numpy(dp))
+            assert np.array_equal(gv, dv.cpu().numpy())
+            assert np.array_equal(gm, hits_to_numpy(dm))
+    for g in graphs:
+        g.close()
