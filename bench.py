@@ -43,7 +43,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=16)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["frame", "torus", "pt", "adjoint"], default="frame")
+    ap.add_argument("--workload", choices=["frame", "torus", "pt", "adjoint", "batch"], default="frame")
+    ap.add_argument("--scenes", type=int, default=256, help="batch workload: number of scenes")
+    ap.add_argument("--batch-res", type=int, default=256, help="batch workload: square image size per scene")
     ap.add_argument("--freq", type=int, default=324, help="icosphere frequency (324 -> 2,099,520 triangles)")
     ap.add_argument("--depth", type=int, default=20)
     ap.add_argument("--frames", type=int, default=16)
@@ -192,6 +194,8 @@ def run_ours(args, dist: Dist):
     dev = torch.device("cuda", dist.local)
     if args.workload in ("pt", "adjoint"):
         return run_pt(args, dist, adjoint=args.workload == "adjoint")
+    if args.workload == "batch":
+        return run_batch(args, dist)
     frames, cam, light, name = frame_workload(args)
     n = len(frames[0])
     npx = cam.width * cam.height
@@ -343,6 +347,212 @@ def run_ours(args, dist: Dist):
 
 
 # ---------------------------------------------------------------------------
+def batch_workload(args):
+    from rtgpu import scenes
+    sizes = scenes.batch_sizes(args.scenes)
+    soup = scenes.batch_scene(sizes)
+    cams, lights = scenes.batch_views(len(sizes), args.batch_res, args.batch_res)
+    name = ("batch of %d random-soup scenes, N_i = round(exp U[ln 1e3, ln 2e5]) (sum %d tris), depth %d, "
+            "%dx%d primary+shadow per scene" % (len(sizes), int(sizes.sum()), args.depth, args.batch_res,
+                                               args.batch_res))
+    return sizes, soup, cams, lights, name
+
+
+def run_batch(args, dist: Dist):
+    """Batched form: every step rebuilds all scenes of the batch and traces a
+    primary and a shadow ray per pixel of each, as one CUDA-graph launch of
+    the batched build + the persistent (scene, tile) trace kernel, after the
+    autotuner has picked the trace's launch shape.  The same work issued as a
+    plain per-scene loop (rt_lbvh_build + rt_trace_primary +
+    rt_trace_shadow_mirror per scene) is timed beside it."""
+    import torch
+    from rtgpu import autotune
+    from rtgpu.api import LBVH, Batch, BatchFrame, Context, RayTracer
+
+    dev = torch.device("cuda", dist.local)
+    sizes, soup, cams, lights, name = batch_workload(args)
+    S = len(sizes)
+    total = int(sizes.sum())
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    W = H = args.batch_res
+    npx = W * H
+    host = torch.from_numpy(soup).pin_memory()
+    dsoup = host.to(dev)
+    ctx = Context(dist.local)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+
+    b = Batch(ctx, sizes, args.depth)
+    b.set_views(cams, lights)
+    hits, vis = b.alloc_outputs()
+    b.build(dsoup)
+    ctx.check()
+    tune_cache = autotune.TuneCache(Path(tempfile.gettempdir()) / "rtgpu_batch_tuning.json")
+    best = autotune.autotune_batch(b, hits, vis, cache=tune_cache)
+
+    # plain per-scene loop with the per-ray test counters: algorithmic bytes
+    lb = LBVH(ctx, int(sizes.max()), args.depth)
+    rt = RayTracer(ctx)
+    phits = torch.empty((S, npx, 4), dtype=torch.int32, device=dev)
+    pvis = torch.empty((S, npx), dtype=torch.uint8, device=dev)
+    nb = nt = 0
+    n_shadow = 0
+    for s in range(S):
+        lb.Build(dsoup[off[s]:off[s + 1]])
+        _, pst = rt.primary(lb, cams[s], stats=True, out=phits[s])
+        _, _, sst, _ = rt.shadow_mirror(lb, cams[s], lights[s], phits[s], stats=True, vis=pvis[s], with_mirror=False)
+        nb += int(pst[:, 0].sum() + sst[:, 0].sum())
+        nt += int(pst[:, 1].sum() + sst[:, 1].sum())
+        n_shadow += int((pvis[s] >= 2).sum())
+    ctx.check()
+    rays = S * npx + n_shadow
+    trace_bytes = 32 * nb + 40 * nt + 32 * rays
+
+    def plain_step():
+        for s in range(S):
+            lb.Build(dsoup[off[s]:off[s + 1]])
+            rt.primary(lb, cams[s], out=phits[s])
+            rt.shadow_mirror(lb, cams[s], lights[s], phits[s], vis=pvis[s], with_mirror=False)
+
+    def timed(fn, steps):
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(steps)]
+        torch.cuda.synchronize()
+        for k in range(steps):
+            flush.zero_()
+            evs[k][0].record(stream)
+            fn()
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        ctx.check()
+        return np.array([a.elapsed_time(c) for a, c in evs])
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        plain_step()
+    plain_ms = timed(plain_step, max(1, min(args.steps, 4)))
+
+    # batched, stream-issued, with the build / trace split
+    def split_step(evs):
+        evs[0].record(stream)
+        b.build(dsoup)
+        evs[1].record(stream)
+        b.trace(hits, vis)
+        evs[2].record(stream)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        b.build(dsoup)
+        b.trace(hits, vis)
+    sevs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.zero_()
+        split_step(sevs[k])
+    torch.cuda.synchronize()
+    ctx.check()
+    per = np.array([[e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])] for e in sevs])
+    build_ms, trace_ms = per.mean(0)
+    # parity of the batched frame with the plain loop (same trees, same rays)
+    assert torch.equal(hits.view(S, npx, 4), phits) and torch.equal(vis.view(S, npx), pvis), \
+        "batched and per-scene results differ"
+
+    # timed steps: one CUDA-graph launch per batched frame
+    frame = BatchFrame(ctx, b, dsoup, hits, vis)
+    for _ in range(args.warmup):
+        flush.zero_()
+        frame.launch()
+    ctx.check()
+    dist.barrier()
+    with Clocks(dist.local) as clk:
+        step_ms = timed(frame.launch, args.steps)
+    dist.barrier()
+    t_total = dist.max(float(step_ms.sum()) / 1e3)
+    value = dist.sum(float(args.steps)) * total / t_total / 1e6
+
+    # e2e: pinned host soup in, hits + visibility out, inside the timed region
+    e2e = None
+    if not args.no_e2e:
+        hh = torch.empty(hits.shape, dtype=hits.dtype).pin_memory()
+        hv = torch.empty(vis.shape, dtype=vis.dtype).pin_memory()
+
+        def e2e_step():
+            dsoup.copy_(host, non_blocking=True)
+            frame.launch()
+            hh.copy_(hits, non_blocking=True)
+            hv.copy_(vis, non_blocking=True)
+
+        for _ in range(args.warmup):
+            e2e_step()
+        torch.cuda.synchronize()
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        te = dist.max(time.perf_counter() - t0)
+        e2e = {"value": round(dist.sum(float(args.steps)) * total / te / 1e6, 3), "unit": "Mtri/s",
+               "h2d_bytes_per_step": int(host.numel() * 4), "d2h_bytes_per_step": int(hits.numel() * 4 + vis.numel()),
+               "ms_per_step": round(te / args.steps * 1e3, 3),
+               "call": "pinned soup -> rt_batch_frame_capture graph (build + trace) -> pinned hits/vis"}
+    frame.close()
+
+    peak, peak_kind = measured_peaks()
+    groups = {"k_batch_trace": (trace_ms, trace_bytes), "batched build (9 kernels)": (build_ms, BUILD_BYTES_PER_TRI * total)}
+    dom = max(groups, key=lambda g: groups[g][0])
+    ms, byts = groups[dom]
+    achieved = byts / (ms / 1e3) / 1e9
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mtri/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(float(step_ms.mean()), 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded random soups)",
+        "config": {"workload": name, "scenes": S, "triangles": total, "pixels_per_scene": npx, "depth": args.depth,
+                   "l2": "flushed between steps (256 MiB write outside the per-step events); inputs 346 MB > L2",
+                   "parallelism": "replicas" if dist.world > 1 else "single GPU"},
+        "components": {"graph_frame_ms": round(float(step_ms.mean()), 4), "build_ms": round(float(build_ms), 4),
+                       "trace_ms": round(float(trace_ms), 4), "build_mtri_s": round(total / build_ms / 1e3, 1),
+                       "trace_mrays_s": round(rays / (trace_ms / 1e3) / 1e6, 1),
+                       "rays": {"primary": S * npx, "shadow": n_shadow},
+                       "plain_loop_ms": round(float(plain_ms.mean()), 4),
+                       "batched_vs_plain": round(float(plain_ms.mean()) / float(step_ms.mean()), 3),
+                       "tuning": best},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": ncu_traffic(dom),
+                     "algorithmic_bytes_per_launch": int(byts), "avg_launch_ms": round(float(ms), 4)},
+        "e2e": e2e,
+        "gpu_launches": 13 * args.steps,  # 12 build kernels + k_batch_trace per graph
+    }
+    out["clocks"] = clk.summary()
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_batch_baseline(soup, off, cams, lights, args.depth)
+    b.close()
+    lb.close()
+    ctx.close()
+    return out
+
+
+def cpu_batch_baseline(soup, off, cams, lights, depth, budget_s: float = 15.0):
+    """Scenes of the batch on the host (oracle port: build on 1 thread, primary
+    + shadow on all cores) until about budget_s seconds have passed."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    O.build_oracle()
+    nth = O.nthreads_default()
+    done_tris = 0
+    t0 = time.perf_counter()
+    s = 0
+    while s < len(off) - 1 and time.perf_counter() - t0 < budget_s:
+        tris = soup[off[s]:off[s + 1]]
+        nodes, ids, _, _ = O.lbvh_build(tris, depth)
+        prim = O.trace(nodes, depth, ids, tris, O.primary_rays(cams[s]), nthreads=nth)
+        O.shadow_mirror(nodes, depth, ids, tris, cams[s], lights[s], prim, nthreads=nth)
+        done_tris += len(tris)
+        s += 1
+    dt = time.perf_counter() - t0
+    return {"value": round(done_tris / dt / 1e6, 4), "unit": "Mtri/s", "cores": nth, "kind": "port",
+            "sample": f"first {s} scenes ({done_tris} tris) in {dt:.1f}s: build on 1 thread, primary+shadow on {nth}",
+            "cpu": _cpu_name()}
+
+
 def cpu_frame_baseline(tris, cam, light, depth, n, nthreads=None):
     """One frame on the host: the oracle port (restated LBVH::Build, 1 thread as
     the reference runs it) + primary/shadow/mirror traversal on all cores."""
@@ -384,6 +594,8 @@ def run_reference(args, dist: Dist):
     if args.workload in ("pt", "adjoint"):
         return {"impl": "reference", "unavailable": "the reference has no CPU path tracer or adjoint; its GI is "
                 "an HLSL shader (unavailable on this box)"}
+    if args.workload == "batch":
+        return run_reference_batch(args, dist, O)
     frames, cam, light, name = frame_workload(args)
     n = len(frames[0])
     nth = O.nthreads_default()
@@ -420,6 +632,56 @@ def run_reference(args, dist: Dist):
             "cpu_baseline": {"value": round(value, 4), "unit": "Mtri/s", "cores": nth, "kind": kind,
                              "sample": "every step one full frame: LBVH build on 1 thread, primary/shadow/mirror "
                                        f"on {nth} threads", "cpu": _cpu_name()},
+            "e2e": {"value": round(value, 4), "unit": "Mtri/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def run_reference_batch(args, dist: Dist, O):
+    """Reference arm of the batched workload: the reference has no batched
+    form, so each step is the per-scene loop on the host (LBVH::Build on one
+    thread, primary + shadow on all cores) over a rotating sample of 16 scenes."""
+    sizes, soup, cams, lights, name = batch_workload(args)
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    nth = O.nthreads_default()
+    use_ref = O.ref_available()
+    per_step = 16
+
+    def one(s):
+        tris = soup[off[s]:off[s + 1]]
+        if use_ref:
+            ref = O.RefStructure(tris, "lbvh", args.depth)
+            nodes, ids = ref.nodes(), ref.ids()
+            prim = np.zeros(cams[s].width * cams[s].height, O.HIT_DTYPE)
+            hid, t, u, v = ref.intersect(O.primary_rays(cams[s]), nthreads=nth)
+            prim["id"], prim["t"], prim["u"], prim["v"] = hid, t, u, v
+            ref.close()
+        else:
+            nodes, ids, _, _ = O.lbvh_build(tris, args.depth)
+            prim = O.trace(nodes, args.depth, ids, tris, O.primary_rays(cams[s]), nthreads=nth)
+        O.shadow_mirror(nodes, args.depth, ids, tris, cams[s], lights[s], prim, nthreads=nth)
+        return len(tris)
+
+    k = 0
+    for _ in range(args.warmup):
+        for _ in range(per_step):
+            one(k % len(sizes))
+            k += 1
+    t0 = time.perf_counter()
+    tris_done = 0
+    for _ in range(args.steps):
+        for _ in range(per_step):
+            tris_done += one(k % len(sizes))
+            k += 1
+    dt = time.perf_counter() - t0
+    value = tris_done / dt / 1e6
+    kind = "reference" if use_ref else "port"
+    return {"metric": METRIC, "value": round(value, 4), "unit": "Mtri/s", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded random soups)",
+            "config": {"workload": name, "scenes": len(sizes), "triangles": int(sizes.sum()), "depth": args.depth},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(value, 4), "unit": "Mtri/s", "cores": nth, "kind": kind,
+                             "sample": f"every step {per_step} scenes of the batch (rotating): LBVH build on 1 thread, "
+                                       f"primary+shadow on {nth} threads", "cpu": _cpu_name()},
             "e2e": {"value": round(value, 4), "unit": "Mtri/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

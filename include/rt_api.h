@@ -203,6 +203,63 @@ rt_status rt_frame_launch(rt_ctx* ctx, rt_frame* frame);
 uint32_t rt_frame_node_count(const rt_frame* frame);
 rt_status rt_frame_destroy(rt_frame* frame);
 
+/* ---- batched scenes ------------------------------------------------- */
+/* Up to 256 independent scenes rebuilt and traced together: one pass of the
+ * build kernels over the concatenated soups and one persistent trace kernel
+ * over (scene, 8x4 pixel tile) work items, in place of n_scenes rounds of
+ * Model::RebuildStructure (Model.cpp:163-205) + RayTracerCS::Render
+ * (RayTracerCS.cpp:241-311).  Scene s is triangles [off_s, off_s + count_s)
+ * of the soup passed to rt_batch_build, off_s = count_0 + ... + count_{s-1};
+ * its tree equals rt_lbvh_build of those triangles alone (same nodes,
+ * scene-local PrimPos and ids), stored in its own 1 << depth heap.
+ * rt_batch_create allocates everything once for the given scene sizes
+ * (every scene non-empty, depth <= RT_BATCH_MAX_DEPTH); rt_batch_build and
+ * rt_batch_trace allocate nothing, so both can be captured in a graph
+ * (rt_batch_frame_capture). */
+#define RT_BATCH_MAX_SCENES 256u
+#define RT_BATCH_MAX_DEPTH 23u
+typedef struct rt_batch rt_batch;
+rt_status rt_batch_create(rt_ctx* ctx, uint32_t n_scenes, const uint32_t* h_tri_counts, uint32_t depth,
+                          rt_batch** out);
+rt_status rt_batch_destroy(rt_batch* batch);
+uint32_t rt_batch_scene_count(const rt_batch* batch);
+/* d_tris: device, (sum of counts) x 9 floats.  The soup stays borrowed
+ * until the next build (the shadow rays read it). */
+rt_status rt_batch_build(rt_ctx* ctx, rt_batch* batch, const float* d_tris, uint32_t flags);
+/* Scene `scene`'s tree, in the layout of a single-scene view (device
+ * pointers into the batch's arrays). */
+rt_status rt_batch_view_get(const rt_batch* batch, uint32_t scene, rt_lbvh_view* out);
+/* Synchronous copies of scene `scene`'s nodes (1 << depth), scene-local
+ * ids and sorted codes (its triangle count each); any pointer may be NULL. */
+rt_status rt_batch_download(rt_ctx* ctx, const rt_batch* batch, uint32_t scene, rt_node* h_nodes, uint32_t* h_ids,
+                            uint32_t* h_keys);
+/* Per-scene cameras (host, n_scenes, one common width x height) and point
+ * lights (host, n_scenes x 3 floats), copied to the device on the context
+ * stream; the host arrays may be reused when the call returns. */
+rt_status rt_batch_set_views(rt_ctx* ctx, rt_batch* batch, const rt_camera* h_cams, const float* h_lights);
+/* Primary rays (rt_trace_primary) and, when d_vis is not NULL, shadow rays
+ * (rt_trace_shadow_mirror's vis codes) of every pixel of every scene.
+ * d_hits: device, n_scenes x width x height rt_hit (scene-major, each
+ * scene row-major, hit ids scene-local); d_vis: the same shape in bytes. */
+rt_status rt_batch_trace(rt_ctx* ctx, const rt_batch* batch, rt_hit* d_hits, uint8_t* d_vis);
+/* Launch shape of rt_batch_trace.  threads: 64, 128 or 256 per block;
+ * blocks_per_sm: 0 = as many as fit; grab: tiles a warp takes per
+ * work-counter increment (1 to 16); order: 0 = scene-major work items
+ * (the tiles of one scene are consecutive), 1 = interleaved (tile-major). */
+typedef struct rt_batch_tuning {
+    uint32_t threads;
+    uint32_t blocks_per_sm;
+    uint32_t grab;
+    uint32_t order;
+} rt_batch_tuning;
+rt_status rt_batch_set_tuning(rt_ctx* ctx, rt_batch* batch, const rt_batch_tuning* t);
+rt_status rt_batch_get_tuning(const rt_batch* batch, rt_batch_tuning* t);
+/* One batched frame (rt_batch_build + rt_batch_trace with the current
+ * views and tuning) captured as a CUDA graph; launch / destroy it with
+ * rt_frame_launch / rt_frame_destroy. */
+rt_status rt_batch_frame_capture(rt_ctx* ctx, rt_batch* batch, const float* d_tris, uint32_t flags, rt_hit* d_hits,
+                                 uint8_t* d_vis, rt_frame** out);
+
 /* ---- path tracing (CSComputeColorGI.hlsl, ConstantBuffers.h:85-110) --- */
 typedef struct rt_pt_params {
     uint32_t spp;

@@ -307,12 +307,35 @@ constexpr uint32_t kValMask = (1u << 30) - 1u;
 // counts, looks back over earlier tiles for the global digit offsets, and
 // scatters through shared memory so that each digit's run is written
 // contiguously.
+//
+// SCENE = true is the batched build's last pass: the digit is the scene of
+// the element's triangle id (scene_off: S + 1 triangle offsets, S <= 256),
+// which groups the scenes while keeping each scene's Morton order.
+constexpr uint32_t kMaxBatchScenes = 256;
+
+__device__ __forceinline__ uint32_t scene_of(const uint32_t* off, uint32_t S, uint32_t k) {
+    uint32_t lo = 0, hi = S;  // off[lo] <= k < off[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (off[mid] <= k) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+template <bool SCENE>
+__device__ __forceinline__ uint32_t sort_digit(uint32_t key, uint32_t id, int shift, const uint32_t* s_off, uint32_t S) {
+    return SCENE ? scene_of(s_off, S, id) : ((key >> shift) & 0xffu);
+}
+
+template <bool SCENE>
 __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __restrict__ keys_in,
                                                            const uint32_t* __restrict__ ids_in,
                                                            uint32_t* __restrict__ keys_out,
                                                            uint32_t* __restrict__ ids_out, uint32_t n, int pass,
                                                            const uint32_t* __restrict__ hist, uint32_t* lookback,
-                                                           uint32_t* tile_counter, uint32_t* err) {
+                                                           uint32_t* tile_counter, uint32_t* err,
+                                                           const uint32_t* __restrict__ scene_off = nullptr,
+                                                           uint32_t S = 0) {
     __shared__ uint32_t s_keys[kSortTile];
     __shared__ uint32_t s_ids[kSortTile];
     __shared__ uint32_t s_warp[kSortThreads / 32][256];
@@ -320,8 +343,11 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
     __shared__ uint32_t s_gofs[256];
     __shared__ uint32_t s_tmp[8];
     __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_off[SCENE ? kMaxBatchScenes + 1 : 1];
 
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    if (SCENE)
+        for (uint32_t q = t; q <= S; q += kSortThreads) s_off[q] = scene_off[q];
     if (t == 0) s_tile = atomicAdd(tile_counter, 1u);
     for (int i = lane; i < 256; i += 32) s_warp[w][i] = 0u;
     const uint32_t gbase = block_excl_sum_256(hist[pass * 256 + t], s_tmp);  // includes __syncthreads
@@ -342,7 +368,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
     for (int i = 0; i < kSortItems; ++i) {
         const uint32_t idx = base + w * (32 * kSortItems) + i * 32 + lane;
         const bool valid = idx < n;
-        const uint32_t d = (key[i] >> shift) & 0xffu;
+        const uint32_t d = sort_digit<SCENE>(key[i], idv[i], shift, s_off, S);
         uint32_t peers = __ballot_sync(kFull, valid);
 #pragma unroll
         for (int b = 0; b < 8; ++b) {
@@ -401,7 +427,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
     for (int i = 0; i < kSortItems; ++i) {
         const uint32_t idx = base + w * (32 * kSortItems) + i * 32 + lane;
         if (idx < n) {
-            const uint32_t d = (key[i] >> shift) & 0xffu;
+            const uint32_t d = sort_digit<SCENE>(key[i], idv[i], shift, s_off, S);
             const uint32_t pos = s_lstart[d] + s_warp[w][d] + rank[i];
             if (pos < (uint32_t)kSortTile) {
                 s_keys[pos] = key[i];
@@ -415,7 +441,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
     const uint32_t tile_n = (n - base < (uint32_t)kSortTile) ? (n - base) : (uint32_t)kSortTile;
     for (uint32_t j = t; j < tile_n; j += kSortThreads) {
         const uint32_t k = s_keys[j];
-        const uint32_t gp = s_gofs[(k >> shift) & 0xffu] + j;
+        const uint32_t gp = s_gofs[sort_digit<SCENE>(k, s_ids[j], shift, s_off, S)] + j;
         if (gp < n) {
             keys_out[gp] = k;
             ids_out[gp] = s_ids[j];
@@ -570,7 +596,8 @@ __global__ void __launch_bounds__(kEmitThreads) k_emit_leaves(const uint32_t* __
                                                               const float* __restrict__ tris, uint32_t n,
                                                               uint32_t depth, const uint32_t* __restrict__ scan,
                                                               rt_node* nodes, float4* __restrict__ sorted_tris,
-                                                              uint32_t* leaf_list, uint32_t* leaf_count) {
+                                                              uint32_t* leaf_list, uint32_t* leaf_count,
+                                                              uint32_t* err) {
     __shared__ uint32_t s_f[8], s_b[8];
     const uint32_t s = blockIdx.x * kEmitTile + threadIdx.x * kEmitItems;
     EmitChunk e;
@@ -632,7 +659,11 @@ __global__ void __launch_bounds__(kEmitThreads) k_emit_leaves(const uint32_t* __
     for (int q = 0; q < kEmitItems; ++q) {
         const uint32_t k = tbase + q * kEmitThreads + threadIdx.x;
         if (k < n) {
-            const uint32_t id = __ldg(ids + k);
+            uint32_t id = __ldg(ids + k);
+            if (id >= n) {  // only after a failed sort (look-back timeout)
+                atomicOr(err, RT_DEVERR_BOUNDS);
+                id = 0;
+            }
             const float* tp = tris + 9 * (size_t)id;
             float v[9];
 #pragma unroll
@@ -648,6 +679,10 @@ __global__ void __launch_bounds__(kEmitThreads) k_emit_leaves(const uint32_t* __
 // then the bottom-up walk: the second of two siblings to arrive at a parent
 // writes it (LBVH.cpp:310-313 / LBVH.hlsl:260-269).  Arrival words carry the
 // build epoch (counters[6], advanced by k_bounds), so they never need clearing.
+__device__ __forceinline__ void refit_leaf(uint32_t h, const uint32_t* __restrict__ keys, const float4* sorted_tris,
+                                           uint32_t n, uint32_t depth, rt_node* nodes, uint32_t* arrive,
+                                           uint32_t epoch, uint32_t* err);
+
 __global__ void __launch_bounds__(256) k_emit_refit(const uint32_t* __restrict__ keys, const float4* sorted_tris,
                                                     uint32_t n, uint32_t depth, rt_node* nodes,
                                                     const uint32_t* __restrict__ leaf_list,
@@ -655,14 +690,25 @@ __global__ void __launch_bounds__(256) k_emit_refit(const uint32_t* __restrict__
                                                     const uint32_t* epoch_word, uint32_t* err) {
     const uint32_t nleaves = min(*leaf_count, n);
     const uint32_t epoch = *epoch_word;
-    for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < nleaves; li += gridDim.x * blockDim.x) {
-        uint32_t h = leaf_list[li];
+    for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < nleaves; li += gridDim.x * blockDim.x)
+        refit_leaf(leaf_list[li], keys, sorted_tris, n, depth, nodes, arrive, epoch, err);
+}
+
+// One leaf of one tree: its fields and box, then the walk to the root.
+// keys / sorted_tris / nodes / arrive are the tree's own (scene-offset) arrays.
+__device__ __forceinline__ void refit_leaf(uint32_t h, const uint32_t* __restrict__ keys, const float4* sorted_tris,
+                                           uint32_t n, uint32_t depth, rt_node* nodes, uint32_t* arrive,
+                                           uint32_t epoch, uint32_t* err) {
+    {
         const int32_t pos = __ldcg(&nodes[h].prim_pos);
         const int32_t end = __ldcg(&nodes[h].prim_count);
         const int32_t count = end - pos + 1;
-        if (pos < 0 || end < pos || (uint32_t)end >= n || h >= (1u << depth)) {
+        // a child below the root has a sibling range beside it: pos > 0 for a
+        // right child, end + 1 < n for a left one (the axis reads that key)
+        if (pos < 0 || end < pos || (uint32_t)end >= n || h >= (1u << depth) ||
+            (h > 1u && ((h & 1u) ? pos == 0 : (uint32_t)end + 1u >= n))) {
             atomicOr(err, RT_DEVERR_BOUNDS);
-            continue;
+            return;
         }
         float mn[3], mx[3];
 #pragma unroll 4
@@ -817,7 +863,7 @@ static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint
     RT_CHECK_LAUNCH(ctx, "k_morton_hist");
     uint32_t *kin = l->keys, *iin = l->ids, *kout = l->keys_alt, *iout = l->ids_alt;
     for (int p = 0; p < kSortPasses; ++p) {
-        k_onesweep<<<sort_tiles, kSortThreads, 0, st>>>(kin, iin, kout, iout, n, p, l->hist,
+        k_onesweep<false><<<sort_tiles, kSortThreads, 0, st>>>(kin, iin, kout, iout, n, p, l->hist,
                                                         l->lookback + (size_t)p * 256 * sort_tiles,
                                                         l->counters + 1 + p, ctx->d_err);
         RT_CHECK_LAUNCH(ctx, "k_onesweep");
@@ -831,7 +877,7 @@ static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint
     k_emit_prefix<<<1, 32, 0, st>>>(l->scan, emit_tiles);
     RT_CHECK_LAUNCH(ctx, "k_emit_prefix");
     k_emit_leaves<<<emit_tiles, kEmitThreads, 0, st>>>(l->keys, l->ids, d_tris, n, l->depth, l->scan, l->nodes,
-                                                       l->sorted_tris, l->leaf_list, l->counters + 5);
+                                                       l->sorted_tris, l->leaf_list, l->counters + 5, ctx->d_err);
     RT_CHECK_LAUNCH(ctx, "k_emit_leaves");
     const uint32_t rblocks = std::max(1u, std::min(ceil_div(n, 256), (uint32_t)ctx->num_sms * 8));
     k_emit_refit<<<rblocks, 256, 0, st>>>(l->keys, l->sorted_tris, n, l->depth, l->nodes, l->leaf_list,
@@ -1023,7 +1069,7 @@ extern "C" rt_status rt_lbvh_build_noalloc(rt_ctx* ctx, void* stream, const floa
     k_morton_hist<<<mblocks, kMortonThreads, 0, st>>>(d_tris, n, scene, d_keys, d_ids, hist, err);
     uint32_t *kin = d_keys, *iin = d_ids, *kout = keys_alt, *iout = ids_alt;
     for (int p = 0; p < kSortPasses; ++p) {
-        k_onesweep<<<sort_tiles, kSortThreads, 0, st>>>(kin, iin, kout, iout, n, p, hist,
+        k_onesweep<false><<<sort_tiles, kSortThreads, 0, st>>>(kin, iin, kout, iout, n, p, hist,
                                                         lookback + (size_t)p * 256 * sort_tiles, counters + 1 + p, err);
         std::swap(kin, kout);
         std::swap(iin, iout);
@@ -1031,12 +1077,490 @@ extern "C" rt_status rt_lbvh_build_noalloc(rt_ctx* ctx, void* stream, const floa
     k_emit_tiles<<<emit_tiles, kEmitThreads, 0, st>>>(d_keys, n, scan, arrive, std::max(1u, num_nodes >> 1), counters + 6);
     k_emit_prefix<<<1, 32, 0, st>>>(scan, emit_tiles);
     k_emit_leaves<<<emit_tiles, kEmitThreads, 0, st>>>(d_keys, d_ids, d_tris, n, depth, scan, d_nodes,
-                                                       reinterpret_cast<float4*>(d_sorted_tris), leaves, counters + 5);
+                                                       reinterpret_cast<float4*>(d_sorted_tris), leaves, counters + 5, err);
     const uint32_t rblocks = std::max(1u, std::min(ceil_div(n, 256), (uint32_t)D.num_sms * 8));
     k_emit_refit<<<rblocks, 256, 0, st>>>(d_keys, reinterpret_cast<const float4*>(d_sorted_tris), n, depth, d_nodes,
                                           leaves, counters + 5, arrive, counters + 6, err);
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_build_noalloc: launch failed: %s", cudaGetErrorString(e));
+    return RT_OK;
+}
+
+// ===========================================================================
+// Batched build: S independent scenes (S <= 256) built by one pass of the
+// build kernels over their concatenated soups.  Scene s's triangles are
+// [tri_off[s], tri_off[s+1]); its tree is the single-scene tree of those
+// triangles, stored in its own heap of 1 << depth slots at node_off[s], with
+// PrimPos and the ordered ids local to the scene.
+//   kb_init          per-scene bounds reset, scratch reset, epoch
+//   kb_bounds        per-scene bounds over host-made one-scene chunks
+//   kb_morton_hist   codes with each scene's own Morton parameters
+//   k_onesweep x4+1  four code passes, then a stable pass on the scene
+//   kb_emit_tiles / k_emit_prefix / kb_emit_leaves
+//                    the record scans with a separator record (bit 31) at
+//                    every scene boundary, so no scan crosses two scenes
+//   kb_emit_refit    the per-leaf refit walk in each scene's heap
+namespace {
+
+constexpr uint32_t kChunkTris = 4096;
+constexpr int kSepBit = 31;
+
+__device__ __forceinline__ void atomic_min_f(float* a, float v) {
+    v = fadd(v, 0.0f);  // -0 -> +0
+    if (v >= 0.0f) atomicMin(reinterpret_cast<int*>(a), __float_as_int(v));
+    else atomicMax(reinterpret_cast<unsigned*>(a), __float_as_uint(v));
+}
+__device__ __forceinline__ void atomic_max_f(float* a, float v) {
+    v = fadd(v, 0.0f);
+    if (v >= 0.0f) atomicMax(reinterpret_cast<int*>(a), __float_as_int(v));
+    else atomicMin(reinterpret_cast<unsigned*>(a), __float_as_uint(v));
+}
+
+__global__ void kb_init(float* sbounds, uint32_t S, const uint32_t* __restrict__ tri_off, uint32_t* counters,
+                        uint32_t* hist, uint32_t* lookback, uint32_t lb_words, rt_node* nodes, uint32_t num_nodes,
+                        int clear_nodes) {
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    for (uint32_t i = gtid; i < 8 * S; i += gs) {
+        const uint32_t c = i & 7u;
+        sbounds[i] = c < 3 ? INFINITY : (c < 6 ? -INFINITY : 0.0f);
+    }
+    for (uint32_t i = gtid; i < 5 * 256; i += gs) {
+        const uint32_t s = i - 4 * 256;
+        hist[i] = (i >= 4 * 256 && s < S) ? tri_off[s + 1] - tri_off[s] : 0u;  // pass 4: scene sizes
+    }
+    for (uint32_t i = gtid; i < lb_words; i += gs) lookback[i] = 0u;
+    if (gtid < 6) counters[gtid] = 0u;
+    if (gtid == 6) {
+        const uint32_t e = counters[6] + 1u;
+        counters[6] = e ? e : 1u;
+    }
+    if (clear_nodes)
+        for (uint32_t i = gtid; i < num_nodes; i += gs) {
+            rt_node s;
+            s.min[0] = s.min[1] = s.min[2] = 0.0f;
+            s.max[0] = s.max[1] = s.max[2] = 0.0f;
+            s.prim_count = RT_NODE_SENTINEL;
+            s.prim_pos = RT_NODE_SENTINEL;
+            nodes[i] = s;
+        }
+}
+
+__global__ void __launch_bounds__(256) kb_bounds(const float* __restrict__ tris, const uint32_t* __restrict__ chunks,
+                                                 float* sbounds, uint32_t* err) {
+    const uint32_t s = chunks[3 * blockIdx.x], beg = chunks[3 * blockIdx.x + 1], end = chunks[3 * blockIdx.x + 2];
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    uint32_t bad = 0;
+    for (size_t v = 3 * (size_t)beg + threadIdx.x; v < 3 * (size_t)end; v += blockDim.x) {
+        const float x = __ldg(tris + 3 * v), y = __ldg(tris + 3 * v + 1), z = __ldg(tris + 3 * v + 2);
+        bad |= !(isfinite(x) && isfinite(y) && isfinite(z));
+        mn[0] = fminf(mn[0], x); mn[1] = fminf(mn[1], y); mn[2] = fminf(mn[2], z);
+        mx[0] = fmaxf(mx[0], x); mx[1] = fmaxf(mx[1], y); mx[2] = fmaxf(mx[2], z);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        for (int c = 0; c < 3; ++c) {
+            mn[c] = fminf(mn[c], __shfl_xor_sync(kFull, mn[c], off));
+            mx[c] = fmaxf(mx[c], __shfl_xor_sync(kFull, mx[c], off));
+        }
+        bad |= __shfl_xor_sync(kFull, bad, off);
+    }
+    __shared__ float s_red[8][6];
+    __shared__ uint32_t s_bad[8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        for (int c = 0; c < 3; ++c) { s_red[w][c] = mn[c]; s_red[w][3 + c] = mx[c]; }
+        s_bad[w] = bad;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int c = threadIdx.x;
+        float r = s_red[0][c];
+        for (int ww = 1; ww < (int)(blockDim.x / 32); ++ww) r = c < 3 ? fminf(r, s_red[ww][c]) : fmaxf(r, s_red[ww][c]);
+        if (c < 3) atomic_min_f(sbounds + 8 * s + c, r);
+        else atomic_max_f(sbounds + 8 * s + c, r);
+    }
+    if (threadIdx.x == 6) {
+        uint32_t b = 0;
+        for (int ww = 0; ww < (int)(blockDim.x / 32); ++ww) b |= s_bad[ww];
+        if (b) atomicOr(err, RT_DEVERR_NONFINITE);
+    }
+}
+
+__global__ void __launch_bounds__(256) kb_morton_hist(const float* __restrict__ tris, const uint32_t* __restrict__ chunks,
+                                                      const float* __restrict__ sbounds, uint32_t* __restrict__ keys,
+                                                      uint32_t* __restrict__ ids, uint32_t* hist) {
+    __shared__ uint32_t s_hist[4][256];
+    __shared__ float s_par[6];
+    for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0u;
+    const uint32_t s = chunks[3 * blockIdx.x], beg = chunks[3 * blockIdx.x + 1], end = chunks[3 * blockIdx.x + 2];
+    if (threadIdx.x < 3) {  // the scene's Morton parameters, as k_bounds derives them (LBVH.cpp:521-526)
+        const int c = threadIdx.x;
+        const float lo3 = fmul(3.0f, sbounds[8 * s + c]);
+        const float mx3 = fmul(3.0f, sbounds[8 * s + 3 + c]);
+        s_par[c] = lo3;
+        s_par[3 + c] = fdiv(1024.0f, fsub(mx3, lo3));
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    for (uint32_t base = beg; base < end; base += blockDim.x) {
+        const uint32_t k = base + threadIdx.x;
+        const bool valid = k < end;
+        uint32_t code = 0;
+        if (valid) {
+            const float* t = tris + 9 * (size_t)k;
+            uint32_t q[3];
+            for (int c = 0; c < 3; ++c) {
+                const float cen = fadd(fadd(__ldg(t + c), __ldg(t + 3 + c)), __ldg(t + 6 + c));
+                q[c] = quantize(cen, s_par[c], s_par[3 + c]);
+            }
+            code = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+            keys[k] = code;
+            ids[k] = k;
+        }
+        const uint32_t vm = __ballot_sync(kFull, valid);
+        if (valid) {
+#pragma unroll
+            for (int p = 0; p < kSortPasses; ++p) {
+                const uint32_t d = (code >> (8 * p)) & 0xffu;
+                const uint32_t peers = __match_any_sync(vm, d);
+                if (lane == __ffs(peers) - 1) atomicAdd(&s_hist[p][d], (uint32_t)__popc(peers));
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) {
+        const uint32_t v = (&s_hist[0][0])[i];
+        if (v) atomicAdd(&hist[i], v);
+    }
+}
+
+// Boundary deltas of a thread's chunk with a separator record at each
+// scene boundary (off: S + 1 scene offsets in shared memory).
+__device__ __forceinline__ void load_chunk_b(const uint32_t* __restrict__ keys, uint32_t n, uint32_t s,
+                                             const uint32_t* off, uint32_t S, EmitChunk& e) {
+    const uint32_t prev = (s >= 1 && s - 1 < n) ? __ldg(keys + s - 1) : 0u;
+#pragma unroll
+    for (int q = 0; q <= kEmitItems; ++q) e.c[q] = (s + q < n) ? __ldg(keys + s + q) : 0u;
+    uint32_t sc = scene_of(off, S, s < n ? s : n - 1);
+    e.dl[0] = (s >= 1 && s < n) ? (s == off[sc] ? kSepBit : delta_of(prev, e.c[0])) : -1;
+    uint32_t nb = off[sc + 1];
+#pragma unroll
+    for (int q = 0; q < kEmitItems; ++q) {
+        const uint32_t i = s + q;
+        int d = -1;
+        if (i + 1 < n) {
+            if (i + 1 == nb) {
+                d = kSepBit;
+                ++sc;
+                nb = off[sc + 1];
+            } else {
+                d = delta_of(e.c[q], e.c[q + 1]);
+            }
+        }
+        e.dl[q + 1] = d;
+        e.r[q] = (d >= 0) ? (1u << d) : 0u;
+    }
+}
+
+__global__ void __launch_bounds__(kEmitThreads) kb_emit_tiles(const uint32_t* __restrict__ keys, uint32_t n,
+                                                              const uint32_t* __restrict__ tri_off, uint32_t S,
+                                                              uint32_t* scan, uint32_t* arrive, uint32_t arrive_words,
+                                                              const uint32_t* epoch_word) {
+    __shared__ uint32_t s_f[8], s_b[8];
+    __shared__ uint32_t s_off[kMaxBatchScenes + 1];
+    for (uint32_t q = threadIdx.x; q <= S; q += blockDim.x) s_off[q] = tri_off[q];
+    if (*epoch_word == 1u)
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < arrive_words; i += gridDim.x * blockDim.x)
+            arrive[i] = 0u;
+    __syncthreads();
+    const uint32_t s = blockIdx.x * kEmitTile + threadIdx.x * kEmitItems;
+    EmitChunk e;
+    load_chunk_b(keys, n, s, s_off, S, e);
+    uint32_t af = 0, ab = 0;
+#pragma unroll
+    for (int q = 0; q < kEmitItems; ++q) af = rec_fwd(af, e.r[q]);
+#pragma unroll
+    for (int q = kEmitItems - 1; q >= 0; --q) ab = rec_bwd(e.r[q], ab);
+    af = warp_reduce_ordered<true>(af);
+    ab = warp_reduce_ordered<false>(ab);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) { s_f[w] = af; s_b[w] = ab; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t tf = 0, tb = 0;
+        for (int q = 0; q < kEmitThreads / 32; ++q) tf = rec_fwd(tf, s_f[q]);
+        for (int q = kEmitThreads / 32 - 1; q >= 0; --q) tb = rec_bwd(s_b[q], tb);
+        scan[4 * blockIdx.x + 0] = tf;
+        scan[4 * blockIdx.x + 1] = tb;
+    }
+}
+
+__global__ void __launch_bounds__(kEmitThreads) kb_emit_leaves(
+    const uint32_t* __restrict__ keys, const uint32_t* __restrict__ ids, const float* __restrict__ tris, uint32_t n,
+    const uint32_t* __restrict__ tri_off, uint32_t S, uint32_t depth, const uint32_t* __restrict__ scan,
+    rt_node* nodes, float4* __restrict__ sorted_tris, uint32_t* __restrict__ ids_local, uint32_t* leaf_list,
+    uint32_t* leaf_count, uint32_t* err) {
+    __shared__ uint32_t s_f[8], s_b[8];
+    __shared__ uint32_t s_off[kMaxBatchScenes + 1];
+    for (uint32_t q = threadIdx.x; q <= S; q += blockDim.x) s_off[q] = tri_off[q];
+    __syncthreads();
+    const uint32_t s = blockIdx.x * kEmitTile + threadIdx.x * kEmitItems;
+    EmitChunk e;
+    load_chunk_b(keys, n, s, s_off, S, e);
+    uint32_t af = 0, ab = 0;
+#pragma unroll
+    for (int q = 0; q < kEmitItems; ++q) af = rec_fwd(af, e.r[q]);
+#pragma unroll
+    for (int q = kEmitItems - 1; q >= 0; --q) ab = rec_bwd(e.r[q], ab);
+    uint32_t pre, suf;
+    block_scan_records(af, ab, &pre, &suf, s_f, s_b);
+    uint32_t L[kEmitItems + 1], R[kEmitItems + 1];
+    L[0] = rec_fwd(scan[4 * blockIdx.x + 2], pre);
+    R[kEmitItems] = rec_bwd(suf, scan[4 * blockIdx.x + 3]);
+#pragma unroll
+    for (int q = 0; q < kEmitItems; ++q) L[q + 1] = rec_fwd(L[q], e.r[q]);
+#pragma unroll
+    for (int q = kEmitItems - 1; q >= 0; --q) R[q] = rec_bwd(e.r[q], R[q + 1]);
+
+    const int leaf_depth = (int)depth - 1;
+    const int lane = threadIdx.x & 31;
+    uint32_t sc = scene_of(s_off, S, s < n ? s : n - 1);
+#pragma unroll
+    for (int q = 0; q < kEmitItems; ++q) {
+        const uint32_t k = s + q;
+        const bool valid = k < n;
+        bool head = false;
+        uint32_t h = 0;
+        if (valid) {
+            while (k >= s_off[sc + 1]) ++sc;
+            const uint32_t first = s_off[sc], last = s_off[sc + 1] - 1;
+            const uint32_t anc = (L[q] | R[q]) & 0x3fffffffu;  // drop the separator record
+            const uint32_t code = e.c[q];
+            int dep = __popc(anc);
+            uint32_t m = anc;
+            while (dep > leaf_depth) { m &= m - 1u; --dep; }
+            h = 1u;
+            while (m) {
+                const int b = hb(m);
+                h = (h << 1) | ((code >> b) & 1u);
+                m ^= 1u << b;
+            }
+            const int dprev = e.dl[q], dcur = e.dl[q + 1];
+            head = (k == first) || (dprev >= 0 && __popc(keep_above(anc, dprev)) < leaf_depth);
+            const bool tail = (k == last) || (dcur >= 0 && __popc(keep_above(anc, dcur)) < leaf_depth);
+            rt_node* tree = nodes + ((size_t)sc << depth);
+            if (head) tree[h].prim_pos = (int32_t)(k - first);
+            if (tail) tree[h].prim_count = (int32_t)(k - first);
+            h |= sc << 23;  // leaf entry: scene and heap slot
+        }
+        const uint32_t hm = __ballot_sync(kFull, head);
+        uint32_t basei = 0;
+        if (lane == 0 && hm) basei = atomicAdd(leaf_count, (uint32_t)__popc(hm));
+        basei = __shfl_sync(kFull, basei, 0);
+        if (head) leaf_list[basei + __popc(hm & lanemask_lt())] = h;
+    }
+    const uint32_t tbase = blockIdx.x * kEmitTile;
+#pragma unroll 2
+    for (int q = 0; q < kEmitItems; ++q) {
+        const uint32_t k = tbase + q * kEmitThreads + threadIdx.x;
+        if (k < n) {
+            uint32_t id = __ldg(ids + k);
+            const uint32_t sk = scene_of(s_off, S, k);
+            if (id < s_off[sk] || id >= s_off[sk + 1]) {  // only after a failed sort (look-back timeout)
+                atomicOr(err, RT_DEVERR_BOUNDS);
+                id = s_off[sk];
+            }
+            const uint32_t local = id - s_off[sk];
+            const float* tp = tris + 9 * (size_t)id;
+            float v[9];
+#pragma unroll
+            for (int c = 0; c < 9; ++c) v[c] = __ldg(tp + c);
+            sorted_tris[3 * (size_t)k + 0] = make_float4(v[0], v[1], v[2], __int_as_float((int)local));
+            sorted_tris[3 * (size_t)k + 1] = make_float4(v[3], v[4], v[5], 0.0f);
+            sorted_tris[3 * (size_t)k + 2] = make_float4(v[6], v[7], v[8], 0.0f);
+            ids_local[k] = local;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) kb_emit_refit(const uint32_t* __restrict__ keys, const float4* sorted_tris,
+                                                     const uint32_t* __restrict__ tri_off, uint32_t depth,
+                                                     rt_node* nodes, const uint32_t* __restrict__ leaf_list,
+                                                     const uint32_t* leaf_count, uint32_t n, uint32_t* arrive,
+                                                     const uint32_t* epoch_word, uint32_t* err) {
+    const uint32_t nleaves = min(*leaf_count, n);
+    const uint32_t epoch = *epoch_word;
+    for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < nleaves; li += gridDim.x * blockDim.x) {
+        const uint32_t e = leaf_list[li];
+        const uint32_t sc = e >> 23, h = e & ((1u << 23) - 1u);
+        const uint32_t toff = __ldg(tri_off + sc), ns = __ldg(tri_off + sc + 1) - toff;
+        refit_leaf(h, keys + toff, sorted_tris + 3 * (size_t)toff, ns, depth, nodes + ((size_t)sc << depth),
+                   arrive + ((size_t)sc << (depth - 1)), epoch, err);
+    }
+}
+
+}  // namespace
+
+extern "C" rt_status rt_batch_destroy(rt_batch* b) {
+    if (!b) return RT_OK;
+    void* ptrs[] = {b->tri_off, b->node_off, b->chunks, b->nodes, b->keys, b->ids, b->keys_alt, b->ids_alt,
+                    b->ids_local, b->sorted_tris, b->sbounds, b->counters, b->hist, b->lookback, b->scan,
+                    b->leaf_list, b->arrive, b->cams, b->lights};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete b;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_batch_create(rt_ctx* ctx, uint32_t n_scenes, const uint32_t* h_tri_counts, uint32_t depth,
+                                     rt_batch** out) {
+    if (!ctx || !out) return RT_ERR_INVALID;
+    *out = nullptr;
+    if (!h_tri_counts) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_create: null counts");
+    if (n_scenes == 0 || n_scenes > RT_BATCH_MAX_SCENES)
+        return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_create: 1 to %u scenes", RT_BATCH_MAX_SCENES);
+    if (depth < 1 || depth > RT_BATCH_MAX_DEPTH)
+        return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_create: depth must be in [1, %u]", RT_BATCH_MAX_DEPTH);
+    uint64_t total = 0;
+    for (uint32_t s = 0; s < n_scenes; ++s) {
+        if (h_tri_counts[s] == 0) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_create: scene %u is empty", s);
+        total += h_tri_counts[s];
+    }
+    if (total > kMaxTris) return rt_fail(ctx, RT_ERR_CAPACITY, "rt_batch_create: %llu triangles in all", (unsigned long long)total);
+    RT_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+    rt_batch* b = new rt_batch();
+    b->S = n_scenes;
+    b->depth = depth;
+    b->total = (uint32_t)total;
+    b->h_tri_off.resize(n_scenes + 1);
+    std::vector<uint32_t> node_off(n_scenes + 1), chunks;
+    b->h_tri_off[0] = 0;
+    for (uint32_t s = 0; s < n_scenes; ++s) {
+        b->h_tri_off[s + 1] = b->h_tri_off[s] + h_tri_counts[s];
+        for (uint32_t c = b->h_tri_off[s]; c < b->h_tri_off[s + 1]; c += kChunkTris) {
+            chunks.push_back(s);
+            chunks.push_back(c);
+            chunks.push_back(std::min(c + kChunkTris, b->h_tri_off[s + 1]));
+        }
+    }
+    for (uint32_t s = 0; s <= n_scenes; ++s) node_off[s] = s << depth;
+    b->nchunks = (uint32_t)(chunks.size() / 3);
+    const size_t n = total;
+    const size_t num_nodes = (size_t)n_scenes << depth;
+    const uint32_t sort_tiles = ceil_div(n, kSortTile), emit_tiles = ceil_div(n, kEmitTile);
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](void** p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+    };
+    alloc((void**)&b->tri_off, 4 * (n_scenes + 1));
+    alloc((void**)&b->node_off, 4 * (n_scenes + 1));
+    alloc((void**)&b->chunks, 4 * chunks.size());
+    alloc((void**)&b->nodes, sizeof(rt_node) * num_nodes);
+    alloc((void**)&b->keys, 4 * n);
+    alloc((void**)&b->ids, 4 * n);
+    alloc((void**)&b->keys_alt, 4 * n);
+    alloc((void**)&b->ids_alt, 4 * n);
+    alloc((void**)&b->ids_local, 4 * n);
+    alloc((void**)&b->sorted_tris, sizeof(float4) * 3 * n);
+    alloc((void**)&b->sbounds, sizeof(float) * 8 * n_scenes);
+    alloc((void**)&b->counters, sizeof(uint32_t) * 8);
+    alloc((void**)&b->hist, sizeof(uint32_t) * 5 * 256);
+    alloc((void**)&b->lookback, sizeof(uint32_t) * 5 * 256 * (size_t)sort_tiles);
+    alloc((void**)&b->scan, sizeof(uint32_t) * 4 * (size_t)emit_tiles);
+    alloc((void**)&b->leaf_list, 4 * n);
+    alloc((void**)&b->arrive, sizeof(uint32_t) * (num_nodes >> 1));
+    alloc((void**)&b->cams, sizeof(rt_camera) * n_scenes);
+    alloc((void**)&b->lights, sizeof(float) * 3 * n_scenes);
+    if (e == cudaSuccess) e = cudaMemcpy(b->tri_off, b->h_tri_off.data(), 4 * (n_scenes + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->node_off, node_off.data(), 4 * (n_scenes + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->chunks, chunks.data(), 4 * chunks.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(b->counters, 0, sizeof(uint32_t) * 8);
+    if (e == cudaSuccess) e = cudaMemset(b->arrive, 0, sizeof(uint32_t) * (num_nodes >> 1));
+    if (e == cudaSuccess) e = cudaMemset(b->nodes, 0, sizeof(rt_node) * num_nodes);
+    if (e != cudaSuccess) {
+        rt_batch_destroy(b);
+        return rt_fail(ctx, RT_ERR_CUDA, "rt_batch_create: allocation failed: %s", cudaGetErrorString(e));
+    }
+    *out = b;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_batch_build(rt_ctx* ctx, rt_batch* b, const float* d_tris, uint32_t flags) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (!b || !d_tris) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_build: null argument");
+    cudaStream_t st = ctx->stream;
+    const uint32_t n = b->total, S = b->S;
+    const uint32_t sort_tiles = ceil_div(n, kSortTile), emit_tiles = ceil_div(n, kEmitTile);
+    const uint32_t lb_words = 5 * 256 * sort_tiles;
+    const uint32_t num_nodes = S << b->depth;
+    kb_init<<<std::max(1u, std::min(ceil_div(std::max(lb_words, num_nodes), 256), (uint32_t)ctx->num_sms * 8)), 256, 0,
+              st>>>(b->sbounds, S, b->tri_off, b->counters, b->hist, b->lookback, lb_words, b->nodes, num_nodes,
+                    (flags & RT_BUILD_CLEAR_UNREACHED) ? 1 : 0);
+    RT_CHECK_LAUNCH(ctx, "kb_init");
+    kb_bounds<<<b->nchunks, 256, 0, st>>>(d_tris, b->chunks, b->sbounds, ctx->d_err);
+    RT_CHECK_LAUNCH(ctx, "kb_bounds");
+    kb_morton_hist<<<b->nchunks, 256, 0, st>>>(d_tris, b->chunks, b->sbounds, b->keys, b->ids, b->hist);
+    RT_CHECK_LAUNCH(ctx, "kb_morton_hist");
+    uint32_t *kin = b->keys, *iin = b->ids, *kout = b->keys_alt, *iout = b->ids_alt;
+    for (int p = 0; p < 5; ++p) {
+        uint32_t* lbp = b->lookback + (size_t)p * 256 * sort_tiles;
+        if (p < 4)
+            k_onesweep<false><<<sort_tiles, kSortThreads, 0, st>>>(kin, iin, kout, iout, n, p, b->hist, lbp,
+                                                                   b->counters + p, ctx->d_err);
+        else
+            k_onesweep<true><<<sort_tiles, kSortThreads, 0, st>>>(kin, iin, kout, iout, n, p, b->hist, lbp,
+                                                                  b->counters + p, ctx->d_err, b->tri_off, S);
+        RT_CHECK_LAUNCH(ctx, "k_onesweep");
+        std::swap(kin, kout);
+        std::swap(iin, iout);
+    }
+    b->res_keys = kin;  // five passes: the sorted pairs are in the alternate buffers
+    b->res_ids = iin;
+    kb_emit_tiles<<<emit_tiles, kEmitThreads, 0, st>>>(kin, n, b->tri_off, S, b->scan, b->arrive, num_nodes >> 1,
+                                                       b->counters + 6);
+    RT_CHECK_LAUNCH(ctx, "kb_emit_tiles");
+    k_emit_prefix<<<1, 32, 0, st>>>(b->scan, emit_tiles);
+    RT_CHECK_LAUNCH(ctx, "k_emit_prefix");
+    kb_emit_leaves<<<emit_tiles, kEmitThreads, 0, st>>>(kin, iin, d_tris, n, b->tri_off, S, b->depth, b->scan, b->nodes,
+                                                        b->sorted_tris, b->ids_local, b->leaf_list, b->counters + 5,
+                                                        ctx->d_err);
+    RT_CHECK_LAUNCH(ctx, "kb_emit_leaves");
+    const uint32_t rblocks = std::max(1u, std::min(ceil_div(n, 256), (uint32_t)ctx->num_sms * 8));
+    kb_emit_refit<<<rblocks, 256, 0, st>>>(kin, b->sorted_tris, b->tri_off, b->depth, b->nodes, b->leaf_list,
+                                           b->counters + 5, n, b->arrive, b->counters + 6, ctx->d_err);
+    RT_CHECK_LAUNCH(ctx, "kb_emit_refit");
+    b->src_tris = d_tris;
+    b->built = true;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_batch_view_get(const rt_batch* b, uint32_t scene, rt_lbvh_view* v) {
+    if (!b || !v || scene >= b->S || !b->built) return RT_ERR_INVALID;
+    const uint32_t off = b->h_tri_off[scene];
+    v->nodes = b->nodes + ((size_t)scene << b->depth);
+    v->ids = b->ids_local + off;
+    v->keys = b->res_keys + off;
+    v->sorted_tris = reinterpret_cast<const float*>(b->sorted_tris + 3 * (size_t)off);
+    v->n = b->h_tri_off[scene + 1] - off;
+    v->depth = b->depth;
+    v->num_nodes = 1u << b->depth;
+    v->node_size = (uint32_t)sizeof(rt_node);
+    return RT_OK;
+}
+
+extern "C" uint32_t rt_batch_scene_count(const rt_batch* b) { return b ? b->S : 0u; }
+
+extern "C" rt_status rt_batch_download(rt_ctx* ctx, const rt_batch* b, uint32_t scene, rt_node* h_nodes,
+                                       uint32_t* h_ids, uint32_t* h_keys) {
+    if (!ctx) return RT_ERR_INVALID;
+    rt_lbvh_view v;
+    if (rt_batch_view_get(b, scene, &v) != RT_OK)
+        return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_download: no built scene %u", scene);
+    cudaStream_t st = ctx->stream;
+    if (h_nodes)
+        RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_nodes, v.nodes, sizeof(rt_node) * v.num_nodes, cudaMemcpyDeviceToHost, st));
+    if (h_ids) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_ids, v.ids, 4 * (size_t)v.n, cudaMemcpyDeviceToHost, st));
+    if (h_keys) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_keys, v.keys, 4 * (size_t)v.n, cudaMemcpyDeviceToHost, st));
+    RT_CHECK_CUDA(ctx, cudaStreamSynchronize(st));
     return RT_OK;
 }

@@ -16,14 +16,12 @@ struct rt_frame {
     uint32_t nodes = 0;
 };
 
-extern "C" rt_status rt_frame_capture(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint32_t n, uint32_t flags,
-                                      const rt_camera* cam, const float light[3], rt_hit* d_primary, uint8_t* d_vis,
-                                      rt_hit* d_mirror, rt_frame** out) {
-    if (!ctx) return RT_ERR_INVALID;
-    if (!l || !d_tris || !cam || !light || !d_primary || !out)
-        return rt_fail(ctx, RT_ERR_INVALID, "rt_frame_capture: null argument");
+// Records what `record` issues on the context stream into a graph: the
+// context stream is swapped for a private non-blocking stream (the legacy
+// default stream cannot be captured) for the duration of the capture.
+template <typename F>
+static rt_status capture_frame(rt_ctx* ctx, const char* who, F record, rt_frame** out) {
     *out = nullptr;
-    // capture on a private stream (the legacy default stream cannot be captured)
     cudaStream_t cs = nullptr;
     RT_CHECK_CUDA(ctx, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     // the context stream's pending work must finish before the private stream
@@ -31,7 +29,7 @@ extern "C" rt_status rt_frame_capture(rt_ctx* ctx, rt_lbvh* l, const float* d_tr
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
         cudaStreamDestroy(cs);
-        return rt_fail(ctx, RT_ERR_CUDA, "rt_frame_capture: %s", cudaGetErrorString(e));
+        return rt_fail(ctx, RT_ERR_CUDA, "%s: %s", who, cudaGetErrorString(e));
     }
     cudaStream_t saved = ctx->stream;
     ctx->stream = cs;
@@ -39,10 +37,7 @@ extern "C" rt_status rt_frame_capture(rt_ctx* ctx, rt_lbvh* l, const float* d_tr
     cudaGraph_t graph = nullptr;
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        s = rt_lbvh_build(ctx, l, d_tris, n, flags);
-        if (s == RT_OK) s = rt_trace_primary(ctx, l, cam, d_primary, nullptr);
-        if (s == RT_OK && (d_vis || d_mirror))
-            s = rt_trace_shadow_mirror(ctx, l, cam, light, d_primary, d_vis, d_mirror, nullptr, nullptr);
+        s = record();
         e = cudaStreamEndCapture(cs, &graph);
     }
     ctx->stream = saved;
@@ -53,7 +48,7 @@ extern "C" rt_status rt_frame_capture(rt_ctx* ctx, rt_lbvh* l, const float* d_tr
     }
     if (e != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
-        return rt_fail(ctx, RT_ERR_CUDA, "rt_frame_capture: stream capture failed: %s", cudaGetErrorString(e));
+        return rt_fail(ctx, RT_ERR_CUDA, "%s: stream capture failed: %s", who, cudaGetErrorString(e));
     }
     rt_frame* f = new rt_frame();
     f->graph = graph;
@@ -61,12 +56,45 @@ extern "C" rt_status rt_frame_capture(rt_ctx* ctx, rt_lbvh* l, const float* d_tr
     if (e != cudaSuccess) {
         cudaGraphDestroy(graph);
         delete f;
-        return rt_fail(ctx, RT_ERR_CUDA, "rt_frame_capture: cudaGraphInstantiate failed: %s", cudaGetErrorString(e));
+        return rt_fail(ctx, RT_ERR_CUDA, "%s: cudaGraphInstantiate failed: %s", who, cudaGetErrorString(e));
     }
     size_t count = 0;
     if (cudaGraphGetNodes(graph, nullptr, &count) == cudaSuccess) f->nodes = (uint32_t)count;
     *out = f;
     return RT_OK;
+}
+
+extern "C" rt_status rt_frame_capture(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint32_t n, uint32_t flags,
+                                      const rt_camera* cam, const float light[3], rt_hit* d_primary, uint8_t* d_vis,
+                                      rt_hit* d_mirror, rt_frame** out) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (!l || !d_tris || !cam || !light || !d_primary || !out)
+        return rt_fail(ctx, RT_ERR_INVALID, "rt_frame_capture: null argument");
+    return capture_frame(
+        ctx, "rt_frame_capture",
+        [&]() {
+            rt_status s = rt_lbvh_build(ctx, l, d_tris, n, flags);
+            if (s == RT_OK) s = rt_trace_primary(ctx, l, cam, d_primary, nullptr);
+            if (s == RT_OK && (d_vis || d_mirror))
+                s = rt_trace_shadow_mirror(ctx, l, cam, light, d_primary, d_vis, d_mirror, nullptr, nullptr);
+            return s;
+        },
+        out);
+}
+
+extern "C" rt_status rt_batch_frame_capture(rt_ctx* ctx, rt_batch* b, const float* d_tris, uint32_t flags,
+                                            rt_hit* d_hits, uint8_t* d_vis, rt_frame** out) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (!b || !d_tris || !d_hits || !out) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_frame_capture: null argument");
+    if (b->width == 0) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_frame_capture: no views set (rt_batch_set_views)");
+    return capture_frame(
+        ctx, "rt_batch_frame_capture",
+        [&]() {
+            rt_status s = rt_batch_build(ctx, b, d_tris, flags);
+            if (s == RT_OK) s = rt_batch_trace(ctx, b, d_hits, d_vis);
+            return s;
+        },
+        out);
 }
 
 extern "C" rt_status rt_frame_launch(rt_ctx* ctx, rt_frame* f) {

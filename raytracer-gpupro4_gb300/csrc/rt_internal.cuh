@@ -15,6 +15,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <string>
+#include <vector>
 
 #include "../../include/rt_api.h"
 
@@ -119,6 +120,37 @@ struct rt_lbvh {
     size_t f_pixels = 0;
 };
 
+// Many independent scenes built in one pass of the build kernels and traced
+// by one persistent kernel.  Scene s owns triangles [tri_off[s], tri_off[s+1])
+// of the concatenated soup and heap slots [node_off[s], node_off[s+1]).
+struct rt_batch {
+    uint32_t S = 0, depth = 0, total = 0;
+    std::vector<uint32_t> h_tri_off;
+    uint32_t* tri_off = nullptr;   // S + 1
+    uint32_t* node_off = nullptr;  // S + 1
+    uint32_t* chunks = nullptr;    // (scene, begin, end) triples, one scene each
+    uint32_t nchunks = 0;
+    rt_node* nodes = nullptr;      // S << depth
+    uint32_t *keys = nullptr, *ids = nullptr, *keys_alt = nullptr, *ids_alt = nullptr;
+    uint32_t *res_keys = nullptr, *res_ids = nullptr;  // buffers holding the sorted pairs
+    uint32_t* ids_local = nullptr;  // scene-local triangle id at each sorted position
+    float4* sorted_tris = nullptr;  // 3 x float4 per triangle, w of the first = scene-local id
+    float* sbounds = nullptr;       // 8 floats per scene (min xyz, max xyz)
+    uint32_t* counters = nullptr;   // [0..4] sort tickets, [5] leaf count, [6] refit epoch
+    uint32_t* hist = nullptr;       // 5 x 256
+    uint32_t* lookback = nullptr;   // 5 x 256 x sort tiles
+    uint32_t* scan = nullptr;       // 4 per emission tile
+    uint32_t* leaf_list = nullptr;  // total
+    uint32_t* arrive = nullptr;     // S << (depth - 1)
+    const float* src_tris = nullptr;
+    bool built = false;
+    // views of the batched trace (rt_batch_set_views)
+    rt_camera* cams = nullptr;      // S, device
+    float* lights = nullptr;        // 3 S, device
+    uint32_t width = 0, height = 0;
+    rt_batch_tuning tuning = {128u, 0u, 1u, 0u};
+};
+
 // ---------------------------------------------------------------------------
 // error plumbing (host)
 rt_status rt_fail(rt_ctx* ctx, rt_status s, const char* fmt, ...);
@@ -154,7 +186,7 @@ inline uint32_t persistent_blocks(const rt_ctx* ctx, K kernel, int threads, uint
 }
 
 // Work-counter slots (ctx->d_work) of the persistent kernels.
-enum : int { kWorkPrimary = 0, kWorkSecondary = 1, kWorkRays = 2, kWorkPath = 3, kWorkAdjoint = 4 };
+enum : int { kWorkPrimary = 0, kWorkSecondary = 1, kWorkRays = 2, kWorkPath = 3, kWorkAdjoint = 4, kWorkBatch = 5 };
 
 inline rt_status reset_work(rt_ctx* ctx, int slot) {
     RT_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_work + slot, 0, sizeof(uint32_t), ctx->stream));

@@ -50,20 +50,18 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_
     }
 }
 
-// Shadow (any hit) and mirror (closest hit) rays of one pixel.  Called by
-// all lanes of the warp together (valid == false for lanes past the image
-// edge); rays of pixels whose primary ray missed, or whose light is behind
-// the surface, are traced with active == false.
+// Shadow (any hit) and mirror (closest hit) rays of one pixel whose primary
+// hit is ph.  Called by all lanes of the warp together (valid == false for
+// lanes past the image edge); rays of pixels whose primary ray missed, or
+// whose light is behind the surface, are traced with active == false.
 template <bool STATS>
 __device__ __forceinline__ void secondary_pixel(const TreeRef& tr, const float* __restrict__ soup,
-                                                const rt_camera& cam, float lx, float ly, float lz,
-                                                const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis,
-                                                rt_hit* __restrict__ mirror, uint32_t* __restrict__ sstats,
-                                                uint32_t* __restrict__ mstats, bool valid, uint32_t i, uint32_t j) {
+                                                const rt_camera& cam, float lx, float ly, float lz, int4 ph,
+                                                uint8_t* __restrict__ vis, rt_hit* __restrict__ mirror,
+                                                uint32_t* __restrict__ sstats, uint32_t* __restrict__ mstats,
+                                                bool valid, uint32_t i, uint32_t j) {
     const size_t p = (size_t)j * cam.width + i;
-    int4 ph = make_int4(-1, 0, 0, 0);
-    if (valid) ph = __ldg(reinterpret_cast<const int4*>(prim + p));
-    const int id = ph.x;
+    const int id = valid ? ph.x : -1;
     const bool has = valid && id >= 0;
     uint32_t snb = 0, snt = 0, mnb = 0, mnt = 0;
     f3 N = mk3(0.f, 0.f, 1.f), Nf = N, P = mk3(0.f, 0.f, 0.f), L = mk3(0.f, 0.f, 1.f), d = mk3(0.f, 0.f, 1.f);
@@ -120,7 +118,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_secondary(
         uint32_t i, j;
         const bool valid = tile_pixel(tile, threadIdx.x & 31, cam.width, cam.height, &i, &j);
         if (!valid) i = j = 0;
-        secondary_pixel<STATS>(tr, soup, cam, lx, ly, lz, prim, vis, mirror, sstats, mstats, valid, i, j);
+        int4 ph = make_int4(-1, 0, 0, 0);
+        if (valid) ph = __ldg(reinterpret_cast<const int4*>(prim + (size_t)j * cam.width + i));
+        secondary_pixel<STATS>(tr, soup, cam, lx, ly, lz, ph, vis, mirror, sstats, mstats, valid, i, j);
     }
 }
 
@@ -274,5 +274,141 @@ extern "C" rt_status rt_render_frame_host(rt_ctx* ctx, rt_lbvh* l, const float* 
     if (h_vis) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_vis, l->f_vis, px, cudaMemcpyDeviceToHost, st));
     if (h_mirror) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_mirror, l->f_mirror, sizeof(rt_hit) * px, cudaMemcpyDeviceToHost, st));
     RT_CHECK_CUDA(ctx, cudaStreamSynchronize(st));
+    return RT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched trace: primary + shadow rays of every pixel of every scene of an
+// rt_batch.  A work item is one 8 x 4 tile of one scene; warps take `grab`
+// consecutive items per increment of one work counter, so the scenes with
+// the costliest rays never hold the grid back.  The primary hit stays in
+// registers for the shadow ray of the same pixel.
+namespace {
+
+struct BatchTraceArgs {
+    const rt_node* nodes;
+    const float4* sorted_tris;
+    const float* soup;
+    const uint32_t* tri_off;
+    const rt_camera* cams;
+    const float* lights;
+    rt_hit* hits;
+    uint8_t* vis;
+    uint32_t* err;
+    uint32_t S, depth, width, height, tiles_per_scene, grab, order;
+};
+
+__global__ void __launch_bounds__(256) k_batch_trace(BatchTraceArgs a, uint32_t* work) {
+    const uint32_t total = a.S * a.tiles_per_scene;
+    const uint32_t lane = threadIdx.x & 31;
+    const size_t px = (size_t)a.width * a.height;
+    for (;;) {
+        uint32_t g0 = 0;
+        if (lane == 0) g0 = atomicAdd(work, a.grab);
+        g0 = __shfl_sync(0xffffffffu, g0, 0);
+        if (g0 >= total) break;
+        const uint32_t g1 = min(total, g0 + a.grab);
+        for (uint32_t g = g0; g < g1; ++g) {
+            const uint32_t s = a.order ? g % a.S : g / a.tiles_per_scene;
+            const uint32_t tile = a.order ? g / a.S : g % a.tiles_per_scene;
+            const uint32_t toff = __ldg(a.tri_off + s);
+            TreeRef tr;
+            tr.nodes = a.nodes + ((size_t)s << a.depth);
+            tr.tris = a.sorted_tris + 3 * (size_t)toff;
+            tr.num_nodes = 1u << a.depth;
+            tr.n = __ldg(a.tri_off + s + 1) - toff;
+            tr.err = a.err;
+            const rt_camera cam = a.cams[s];
+            uint32_t i, j;
+            const bool valid = tile_pixel(tile, lane, a.width, a.height, &i, &j);
+            if (!valid) i = j = 0;
+            const f3 d = primary_dir(cam, i, j);
+            const RayState r = make_ray(mk3(cam.eye[0], cam.eye[1], cam.eye[2]), d, 1e16f, -1);
+            uint32_t nb = 0, nt = 0;
+            const Hit h = trace_ray<false>(r, valid, tr, false, &nb, &nt);
+            const size_t p = (size_t)j * a.width + i;
+            if (valid) store_hit(a.hits + s * px + p, h);
+            if (a.vis) {  // uniform across the grid
+                const int4 ph = make_int4(h.id, __float_as_int(h.u), __float_as_int(h.v), __float_as_int(h.t));
+                secondary_pixel<false>(tr, a.soup + 9 * (size_t)toff, cam, __ldg(a.lights + 3 * s),
+                                       __ldg(a.lights + 3 * s + 1), __ldg(a.lights + 3 * s + 2), ph,
+                                       a.vis + s * px, nullptr, nullptr, nullptr, valid, i, j);
+            }
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" rt_status rt_batch_set_views(rt_ctx* ctx, rt_batch* b, const rt_camera* h_cams, const float* h_lights) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (!b || !h_cams || !h_lights) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_set_views: null argument");
+    const uint32_t w = h_cams[0].width, h = h_cams[0].height;
+    if (w == 0 || h == 0 || (uint64_t)w * h * b->S > (1ull << 34))
+        return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_set_views: bad image size %ux%u", w, h);
+    for (uint32_t s = 1; s < b->S; ++s)
+        if (h_cams[s].width != w || h_cams[s].height != h)
+            return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_set_views: scene %u is %ux%u, scene 0 is %ux%u", s,
+                           h_cams[s].width, h_cams[s].height, w, h);
+    RT_CHECK_CUDA(ctx, cudaMemcpyAsync(b->cams, h_cams, sizeof(rt_camera) * b->S, cudaMemcpyHostToDevice, ctx->stream));
+    RT_CHECK_CUDA(ctx, cudaMemcpyAsync(b->lights, h_lights, sizeof(float) * 3 * b->S, cudaMemcpyHostToDevice,
+                                       ctx->stream));
+    b->width = w;
+    b->height = h;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_batch_set_tuning(rt_ctx* ctx, rt_batch* b, const rt_batch_tuning* t) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (!b || !t) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_set_tuning: null argument");
+    if (t->threads != 64 && t->threads != 128 && t->threads != 256)
+        return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_set_tuning: threads must be 64, 128 or 256");
+    if (t->grab < 1 || t->grab > 16) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_set_tuning: grab must be in [1, 16]");
+    if (t->order > 1) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_set_tuning: order must be 0 or 1");
+    if (t->blocks_per_sm > 64) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_set_tuning: blocks_per_sm above 64");
+    b->tuning = *t;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_batch_get_tuning(const rt_batch* b, rt_batch_tuning* t) {
+    if (!b || !t) return RT_ERR_INVALID;
+    *t = b->tuning;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_batch_trace(rt_ctx* ctx, const rt_batch* b, rt_hit* d_hits, uint8_t* d_vis) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (!b || !d_hits) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_trace: null argument");
+    if (!b->built) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_trace: the batch has not been built");
+    if (b->width == 0) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_trace: no views set (rt_batch_set_views)");
+    rt_status s = reset_work(ctx, kWorkBatch);
+    if (s != RT_OK) return s;
+    BatchTraceArgs a;
+    a.nodes = b->nodes;
+    a.sorted_tris = b->sorted_tris;
+    a.soup = b->src_tris;
+    a.tri_off = b->tri_off;
+    a.cams = b->cams;
+    a.lights = b->lights;
+    a.hits = d_hits;
+    a.vis = d_vis;
+    a.err = ctx->d_err;
+    a.S = b->S;
+    a.depth = b->depth;
+    a.width = b->width;
+    a.height = b->height;
+    a.tiles_per_scene = ((b->width + 7) / 8) * ((b->height + 3) / 4);
+    a.grab = b->tuning.grab;
+    a.order = b->tuning.order;
+    const int threads = (int)b->tuning.threads;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_trace, threads, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    if (b->tuning.blocks_per_sm) per_sm = std::min(per_sm, (int)b->tuning.blocks_per_sm);
+    const uint64_t items = (uint64_t)a.S * a.tiles_per_scene;
+    const uint64_t need = (items * 32 + threads - 1) / threads;
+    const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)per_sm * ctx->num_sms, need));
+    k_batch_trace<<<blocks, threads, 0, ctx->stream>>>(a, ctx->d_work + kWorkBatch);
+    RT_CHECK_LAUNCH(ctx, "k_batch_trace");
     return RT_OK;
 }

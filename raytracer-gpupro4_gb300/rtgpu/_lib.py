@@ -30,7 +30,11 @@ EXPORTED = [
     "rt_lbvh_import_host", "rt_lbvh_view_get", "rt_lbvh_world_bound", "rt_lbvh_download", "rt_trace_primary",
     "rt_trace_shadow_mirror", "rt_trace_rays", "rt_render_frame_host", "rt_pathtrace", "rt_pathtrace_adjoint",
     "rt_lbvh_build_noalloc", "rt_frame_capture", "rt_frame_launch", "rt_frame_node_count", "rt_frame_destroy",
+    "rt_batch_create", "rt_batch_destroy", "rt_batch_scene_count", "rt_batch_build", "rt_batch_view_get",
+    "rt_batch_download", "rt_batch_set_views", "rt_batch_trace", "rt_batch_set_tuning", "rt_batch_get_tuning", "rt_batch_frame_capture",
 ]
+RT_BATCH_MAX_SCENES = 256
+RT_BATCH_MAX_DEPTH = 23
 
 
 class Camera(C.Structure):
@@ -41,6 +45,10 @@ class Camera(C.Structure):
 class LbvhView(C.Structure):
     _fields_ = [("nodes", C.c_void_p), ("ids", C.c_void_p), ("keys", C.c_void_p), ("sorted_tris", C.c_void_p),
                 ("n", C.c_uint32), ("depth", C.c_uint32), ("num_nodes", C.c_uint32), ("node_size", C.c_uint32)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("threads", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("grab", C.c_uint32), ("order", C.c_uint32)]
 
 
 class PtParams(C.Structure):
@@ -87,6 +95,17 @@ def lib() -> C.CDLL:
         "rt_frame_launch": (i32, [vp, vp]),
         "rt_frame_node_count": (u32, [vp]),
         "rt_frame_destroy": (i32, [vp]),
+        "rt_batch_create": (i32, [vp, u32, vp, u32, C.POINTER(vp)]),
+        "rt_batch_destroy": (i32, [vp]),
+        "rt_batch_scene_count": (u32, [vp]),
+        "rt_batch_build": (i32, [vp, vp, vp, u32]),
+        "rt_batch_view_get": (i32, [vp, u32, C.POINTER(LbvhView)]),
+        "rt_batch_download": (i32, [vp, vp, u32, vp, vp, vp]),
+        "rt_batch_set_views": (i32, [vp, vp, vp, vp]),
+        "rt_batch_trace": (i32, [vp, vp, vp, vp]),
+        "rt_batch_set_tuning": (i32, [vp, vp, C.POINTER(BatchTuning)]),
+        "rt_batch_get_tuning": (i32, [vp, C.POINTER(BatchTuning)]),
+        "rt_batch_frame_capture": (i32, [vp, vp, vp, u32, vp, vp, C.POINTER(vp)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

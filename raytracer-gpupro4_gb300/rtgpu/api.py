@@ -186,16 +186,22 @@ class RayTracer:
         return (hits, st) if stats else hits
 
     def shadow_mirror(self, lbvh: LBVH, cam: L.Camera, light, primary: torch.Tensor, stats: bool = False,
-                      vis: torch.Tensor | None = None, mirror: torch.Tensor | None = None):
+                      vis: torch.Tensor | None = None, mirror: torch.Tensor | None = None,
+                      with_mirror: bool = True):
+        """Shadow rays (vis codes) and, unless with_mirror is False, mirror rays."""
         npx = cam.width * cam.height
         vis = vis if vis is not None else torch.empty(npx, dtype=torch.uint8, device=self.ctx.torch_device)
-        mirror = mirror if mirror is not None else self._alloc_hits(npx)
+        if with_mirror:
+            mirror = mirror if mirror is not None else self._alloc_hits(npx)
+        else:
+            mirror = None
         ss = torch.empty((npx, 2), dtype=torch.int32, device=self.ctx.torch_device) if stats else None
-        ms = torch.empty((npx, 2), dtype=torch.int32, device=self.ctx.torch_device) if stats else None
+        ms = torch.empty((npx, 2), dtype=torch.int32, device=self.ctx.torch_device) if stats and with_mirror else None
         lf = (C.c_float * 3)(*light)
         L.check(L.lib().rt_trace_shadow_mirror(self.ctx.h, lbvh.h, C.byref(cam), lf, _dev_ptr(primary),
-                                               _dev_ptr(vis), _dev_ptr(mirror), _dev_ptr(ss) if stats else None,
-                                               _dev_ptr(ms) if stats else None), self.ctx.h,
+                                               _dev_ptr(vis), _dev_ptr(mirror) if mirror is not None else None,
+                                               _dev_ptr(ss) if stats else None,
+                                               _dev_ptr(ms) if ms is not None else None), self.ctx.h,
                 "rt_trace_shadow_mirror")
         return (vis, mirror, ss, ms) if stats else (vis, mirror)
 
@@ -252,6 +258,128 @@ class Frame:
         self.h = h
         lbvh.n = tris.shape[0]
         lbvh._tris = tris
+
+    def launch(self):
+        L.check(L.lib().rt_frame_launch(self.ctx.h, self.h), self.ctx.h, "rt_frame_launch")
+
+    @property
+    def nodes(self) -> int:
+        return int(L.lib().rt_frame_node_count(self.h))
+
+    def close(self):
+        if self.h:
+            L.lib().rt_frame_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many scenes rebuilt and traced together (rt_batch_*): one pass of the
+    build kernels over the concatenated soups, one persistent trace kernel
+    over (scene, tile) work items.  Scene s's tree equals LBVH.Build of its
+    triangles alone, with scene-local ids."""
+
+    def __init__(self, ctx: Context, tri_counts, depth: int = 20):
+        self.ctx = ctx
+        self.counts = np.ascontiguousarray(tri_counts, np.uint32)
+        self.offsets = np.concatenate([[0], np.cumsum(self.counts, dtype=np.int64)])
+        self.depth = depth
+        self.total = int(self.offsets[-1])
+        h = C.c_void_p()
+        L.check(L.lib().rt_batch_create(ctx.h, len(self.counts), _host_ptr(self.counts), depth, C.byref(h)), ctx.h,
+                "rt_batch_create")
+        self.h = h
+        self._keep = ()
+        self.width = self.height = 0
+
+    @property
+    def n_scenes(self) -> int:
+        return len(self.counts)
+
+    def close(self):
+        if self.h:
+            L.lib().rt_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def build(self, tris: torch.Tensor, flags: int = 0) -> "Batch":
+        t = tris.contiguous()
+        assert t.dtype == torch.float32 and t.shape == (self.total, 9)
+        self._keep = (t,)
+        L.check(L.lib().rt_batch_build(self.ctx.h, self.h, _dev_ptr(t), flags), self.ctx.h, "rt_batch_build")
+        return self
+
+    def view(self, scene: int) -> L.LbvhView:
+        v = L.LbvhView()
+        L.check(L.lib().rt_batch_view_get(self.h, scene, C.byref(v)), self.ctx.h, "rt_batch_view_get")
+        return v
+
+    def download(self, scene: int):
+        """(nodes, ids, keys) of one scene's tree, copied to the host."""
+        n = int(self.counts[scene])
+        nodes = np.zeros(1 << self.depth, L.NODE_DTYPE)
+        ids = np.zeros(n, np.uint32)
+        keys = np.zeros(n, np.uint32)
+        L.check(L.lib().rt_batch_download(self.ctx.h, self.h, scene, _host_ptr(nodes), _host_ptr(ids),
+                                          _host_ptr(keys)), self.ctx.h, "rt_batch_download")
+        return nodes, ids, keys
+
+    def set_views(self, cams, lights) -> "Batch":
+        cams = list(cams)
+        assert len(cams) == self.n_scenes
+        arr = (L.Camera * len(cams))(*cams)
+        lt = np.ascontiguousarray(np.asarray(lights, np.float32).reshape(self.n_scenes, 3))
+        L.check(L.lib().rt_batch_set_views(self.ctx.h, self.h, C.cast(arr, C.c_void_p), _host_ptr(lt)), self.ctx.h,
+                "rt_batch_set_views")
+        self.width, self.height = cams[0].width, cams[0].height
+        return self
+
+    def alloc_outputs(self, shadow: bool = True):
+        px = self.n_scenes * self.width * self.height
+        hits = torch.empty((px, 4), dtype=torch.int32, device=self.ctx.torch_device)
+        vis = torch.empty(px, dtype=torch.uint8, device=self.ctx.torch_device) if shadow else None
+        return hits, vis
+
+    def trace(self, hits: torch.Tensor, vis: torch.Tensor | None = None) -> None:
+        L.check(L.lib().rt_batch_trace(self.ctx.h, self.h, _dev_ptr(hits), _dev_ptr(vis) if vis is not None else None),
+                self.ctx.h, "rt_batch_trace")
+
+    @property
+    def tuning(self) -> dict:
+        t = L.BatchTuning()
+        L.check(L.lib().rt_batch_get_tuning(self.h, C.byref(t)), self.ctx.h, "rt_batch_get_tuning")
+        return {"threads": t.threads, "blocks_per_sm": t.blocks_per_sm, "grab": t.grab, "order": t.order}
+
+    @tuning.setter
+    def tuning(self, cfg: dict) -> None:
+        t = L.BatchTuning(int(cfg["threads"]), int(cfg.get("blocks_per_sm", 0)), int(cfg["grab"]), int(cfg["order"]))
+        L.check(L.lib().rt_batch_set_tuning(self.ctx.h, self.h, C.byref(t)), self.ctx.h, "rt_batch_set_tuning")
+
+
+class BatchFrame:
+    """One batched frame (build + trace) captured as a CUDA graph."""
+
+    def __init__(self, ctx: Context, batch: Batch, tris: torch.Tensor, hits: torch.Tensor,
+                 vis: torch.Tensor | None, flags: int = 0):
+        self.ctx = ctx
+        t = tris.contiguous()
+        self._keep = (t, hits, vis)
+        h = C.c_void_p()
+        L.check(L.lib().rt_batch_frame_capture(ctx.h, batch.h, _dev_ptr(t), flags, _dev_ptr(hits),
+                                               _dev_ptr(vis) if vis is not None else None, C.byref(h)),
+                ctx.h, "rt_batch_frame_capture")
+        self.h = h
+        batch._keep = (t,)
 
     def launch(self):
         L.check(L.lib().rt_frame_launch(self.ctx.h, self.h), self.ctx.h, "rt_frame_launch")

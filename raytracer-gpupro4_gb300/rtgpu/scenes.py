@@ -268,6 +268,23 @@ def batch_sizes(n_scenes: int = 256, lo: int = 1000, hi: int = 200000, seed: int
     return np.round(np.exp(rng.uniform(math.log(lo), math.log(hi), size=n_scenes))).astype(np.int64)
 
 
+def batch_scene(sizes, seed_base: int = 1000) -> np.ndarray:
+    """Concatenated soups of a batch: scene s = random_soup(sizes[s], seed_base + s)."""
+    return np.ascontiguousarray(np.concatenate([random_soup(int(n), seed_base + i) for i, n in enumerate(sizes)]))
+
+
+def batch_views(n_scenes: int, width: int = 256, height: int = 256):
+    """One camera per scene, circling the unit cube of the soups at distance
+    1.7 from its centre, and a light above the cube."""
+    cams, lights = [], []
+    for s in range(n_scenes):
+        a = 2.0 * math.pi * s / max(1, n_scenes)
+        eye = (0.5 + 1.7 * math.sin(a), 0.8, 0.5 - 1.7 * math.cos(a))
+        cams.append(look_at(eye, (0.5, 0.5, 0.5), vfov_deg=60.0, width=width, height=height))
+        lights.append((0.5 + 0.3 * math.cos(a), 2.5, 0.5 + 0.3 * math.sin(a)))
+    return cams, np.asarray(lights, np.float32)
+
+
 # Workload cameras / lights
 TORUS_LIGHT = (1.0, 2.0, 3.0)
 

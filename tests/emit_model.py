@@ -106,3 +106,112 @@ def emit(keys: np.ndarray, depth: int, tile: int = 7):
             out[p] = ((cnt << 3) | ((30 - d) % 3), lpos)
             cur = p
     return out
+
+
+SEP_BIT = 31
+
+
+def emit_batch(keys: np.ndarray, offsets, depth: int, tile: int = 7):
+    """Host model of the batched emission (kb_emit_tiles / kb_emit_leaves /
+    kb_emit_refit): the scenes' sorted codes are concatenated, the boundary
+    between two scenes carries a separator record (bit 31, above every code
+    bit) so that no scan crosses it, and each scene's nodes and positions are
+    local to it.  Returns one {heap index: (prim_count field, prim_pos)} per
+    scene."""
+    keys = [int(k) for k in keys]
+    offsets = [int(o) for o in offsets]
+    n = len(keys)
+    starts = set(offsets[:-1])
+    delta = []
+    for i in range(n - 1):
+        if i + 1 in starts:
+            delta.append(SEP_BIT)
+        else:
+            delta.append(-1 if keys[i] == keys[i + 1] else hb(keys[i] ^ keys[i + 1]))
+    r = [(1 << d) if d >= 0 else 0 for d in delta] + [0]
+    T = (n + tile - 1) // tile
+    aggf, aggb = [0] * T, [0] * T
+    for t in range(T):
+        for i in range(t * tile, min(n, (t + 1) * tile)):
+            aggf[t] = rec_fwd(aggf[t], r[i])
+        for i in reversed(range(t * tile, min(n, (t + 1) * tile))):
+            aggb[t] = rec_bwd(r[i], aggb[t])
+    pre, suf = [0] * T, [0] * T
+    run = 0
+    for t in range(T):
+        pre[t] = run
+        run = rec_fwd(run, aggf[t])
+    run = 0
+    for t in reversed(range(T)):
+        suf[t] = run
+        run = rec_bwd(aggb[t], run)
+    L, R = [0] * (n + 1), [0] * (n + 1)
+    for t in range(T):
+        lo, hi = t * tile, min(n, (t + 1) * tile)
+        run = pre[t]
+        for k in range(lo, hi):
+            L[k] = run
+            run = rec_fwd(run, r[k])
+        run = suf[t]
+        for k in reversed(range(lo, hi)):
+            run = rec_bwd(r[k], run)
+            R[k] = run
+    leaf_depth = depth - 1
+    S = len(offsets) - 1
+    heads = [dict() for _ in range(S)]
+    tails = [dict() for _ in range(S)]
+    sc = 0
+    for k in range(n):
+        while k >= offsets[sc + 1]:
+            sc += 1
+        first, last = offsets[sc], offsets[sc + 1] - 1
+        anc = (L[k] | R[k]) & 0x3FFFFFFF
+        m, dep = anc, bin(anc).count("1")
+        while dep > leaf_depth:
+            m &= m - 1
+            dep -= 1
+        h = 1
+        while m:
+            b = hb(m)
+            h = (h << 1) | ((keys[k] >> b) & 1)
+            m ^= 1 << b
+        dprev = delta[k - 1] if k >= 1 else -1
+        dcur = delta[k] if k < n - 1 else -1
+        head = k == first or (dprev >= 0 and bin(keep_above(anc, dprev)).count("1") < leaf_depth)
+        tail = k == last or (dcur >= 0 and bin(keep_above(anc, dcur)).count("1") < leaf_depth)
+        if head:
+            heads[sc][h] = k - first
+        if tail:
+            tails[sc][h] = k - first
+    outs = []
+    for s in range(S):
+        assert heads[s].keys() == tails[s].keys()
+        ks = keys[offsets[s]:offsets[s + 1]]
+        out, arrived = {}, {}
+        for h in heads[s]:
+            pos, end = heads[s][h], tails[s][h]
+            count = end - pos + 1
+            dh = hb(h)
+            if dh == 0:
+                axis = 0 if (count <= 1 or depth <= 1) else 1
+            elif count == 1 or dh == depth - 1:
+                a, b = (ks[pos - 1], ks[pos]) if (h & 1) else (ks[end], ks[end + 1])
+                axis = (31 - hb(a ^ b)) % 3
+            else:
+                axis = 1
+            out[h] = ((count << 3) | 4 | axis, pos)
+            cur = h
+            while cur > 1:
+                p = cur >> 1
+                if p not in arrived:
+                    arrived[p] = True
+                    break
+                sib = cur ^ 1
+                lpos = out[sib][1] if (cur & 1) else out[cur][1]
+                rpos = out[cur][1] if (cur & 1) else out[sib][1]
+                cnt = (out[cur][0] >> 3) + (out[sib][0] >> 3)
+                d = hb(ks[rpos - 1] ^ ks[rpos])
+                out[p] = ((cnt << 3) | ((30 - d) % 3), lpos)
+                cur = p
+        outs.append(out)
+    return outs
