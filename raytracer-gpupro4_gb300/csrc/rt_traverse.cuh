@@ -24,6 +24,7 @@
 namespace rt {
 
 constexpr int kStackSize = 32;  // > kMaxDepth
+constexpr int kSerialLanes = 16;  // leaf phase: lanes that must share a serial step
 
 // Bounds of the arrays a traversal may touch; an index outside them (only
 // possible with a corrupt tree) sets RT_DEVERR_BOUNDS and stops that ray.
@@ -137,200 +138,295 @@ __device__ __forceinline__ uint64_t shfl_down_u64(uint64_t v, int off) {
     return ((uint64_t)hi << 32) | lo;
 }
 
-// Warp-cooperative traversal.  All 32 lanes of the warp call it together;
-// lanes with active == false only help.  Each round, every lane descends
-// through internal nodes until it holds a leaf or has nothing left (the
-// descent diverges), then the warp tests the triangles of all held leaves
-// together: the (lane, triangle) pairs are numbered by a prefix sum of the
-// leaf sizes and processed 32 at a time, so consecutive lanes read
+// Best accepted hit of one lane's ray (or of the part of a ray a lane works
+// on): key = hit_key(t, id), or hit_key(tmax, 0) while nothing is accepted, so
+// a candidate is accepted exactly when its key is smaller (t < tmax, and the
+// tie rule at equal t).
+struct Best {
+    uint64_t key;
+    float t, u, v;
+    int id;
+};
+
+__device__ __forceinline__ float key_t(uint64_t key) { return __uint_as_float((uint32_t)(key >> 32)); }
+
+// Leaf phase: the warp tests the triangles [pos, pos + cnt) of every lane's
+// held leaf together.  The (lane, triangle) pairs are numbered by a prefix
+// sum of the leaf sizes and processed 32 at a time, so consecutive lanes read
 // consecutive triangles and a 200-triangle leaf costs 7 warp steps instead of
-// 200.  A segmented minimum over hit_key returns each lane's closest
-// accepted hit; that is the result of testing the leaf's triangles in any
-// order under the tie rule, so hits and test counts equal the oracle's.
+// 200.  A segmented minimum over hit_key gives each lane the closest accepted
+// hit of its leaf; that is the result of testing the leaf's triangles in any
+// order under the tie rule.  `bound` is the lane's acceptance key on entry;
+// returns true when b (and the bound) improved.
+template <bool STATS>
+__device__ __forceinline__ bool leaf_phase(const TreeRef& tr_, const RayState& r, bool have, const NodeBox& cur,
+                                           uint64_t& bound, Best& b, uint32_t& ntri) {
+    constexpr uint32_t kFull = 0xffffffffu;
+    const float4* __restrict__ tris = tr_.tris;
+    const int lane = threadIdx.x & 31;
+    int cnt = 0, pos = 0;
+    if (have) {
+        cnt = __float_as_int(cur.b.z) >> 3;
+        pos = __float_as_int(cur.b.w);
+        if (pos < 0 || cnt < 0 || (uint32_t)pos + (uint32_t)cnt > tr_.n) {
+            atomicOr(tr_.err, RT_DEVERR_BOUNDS);
+            cnt = 0;
+        }
+    }
+    if (STATS) ntri += (uint32_t)cnt;
+    bool improved = false;
+    // Serial part: while at least kSerialLanes lanes still have triangles,
+    // each lane tests its own leaf's triangles (no exchange between lanes);
+    // L = the largest count that many lanes reach.  The remainder of every
+    // leaf (the long tails) is pooled below.
+    int L = 0;
+#pragma unroll
+    for (int step = 32; step > 0; step >>= 1)
+        if (__popc(__ballot_sync(kFull, cnt >= L + step)) >= kSerialLanes) L += step;
+    if (L > 0) {
+        const int ns = min(cnt, L);
+        // software pipelined: the next triangle's loads are in flight while
+        // the current one is tested
+        const float4* tp = tris + 3 * (size_t)pos;
+        float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = na, nc = na;
+        if (ns > 0) {
+            na = __ldg(tp);
+            nb = __ldg(tp + 1);
+            nc = __ldg(tp + 2);
+        }
+        for (int j = 0; j < ns; ++j) {
+            const float4 a = na, bb = nb, c = nc;
+            if (j + 1 < ns) {
+                tp += 3;
+                na = __ldg(tp);
+                nb = __ldg(tp + 1);
+                nc = __ldg(tp + 2);
+            }
+            const int id = __float_as_int(a.w);
+            float u, v, t;
+            if (id != r.exclude && tri_test(r, a, bb, c, &u, &v, &t)) {
+                const uint64_t k = hit_key(t, id);
+                if (k < bound) {
+                    bound = k;
+                    b.key = k;
+                    b.t = t;
+                    b.u = u;
+                    b.v = v;
+                    b.id = id;
+                    improved = true;
+                }
+            }
+        }
+        pos += ns;
+        cnt -= ns;
+    }
+    uint32_t incl = (uint32_t)cnt;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, incl, off);
+        if (lane >= off) incl += y;
+    }
+    const uint32_t total = __shfl_sync(kFull, incl, 31);
+    const uint32_t excl = incl - (uint32_t)cnt;
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t p = base + lane;
+        // owner of pair p: the first lane whose inclusive prefix exceeds p
+        int o = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+            const uint32_t v = __shfl_sync(kFull, incl, o + step - 1);
+            if (v <= p) o += step;
+        }
+        const uint32_t o_excl = __shfl_sync(kFull, excl, o);
+        const int o_pos = __shfl_sync(kFull, pos, o);
+        RayState ro;
+        ro.o = mk3(__shfl_sync(kFull, r.o.x, o), __shfl_sync(kFull, r.o.y, o), __shfl_sync(kFull, r.o.z, o));
+        ro.d = mk3(__shfl_sync(kFull, r.d.x, o), __shfl_sync(kFull, r.d.y, o), __shfl_sync(kFull, r.d.z, o));
+        const int o_exclude = __shfl_sync(kFull, r.exclude, o);
+        const uint64_t o_best = shfl_u64(bound, o);
+        uint64_t key = ~0ull;
+        float kt = 0.0f, ku = 0.0f, kv = 0.0f;
+        if (p < total) {
+            const float4* tp = tris + 3 * (size_t)(o_pos + (p - o_excl));
+            const float4 a = __ldg(tp), bb = __ldg(tp + 1), c = __ldg(tp + 2);
+            const int id = __float_as_int(a.w);
+            float u, v, t;
+            if (id != o_exclude && tri_test(ro, a, bb, c, &u, &v, &t)) {
+                const uint64_t k = hit_key(t, id);
+                if (k < o_best) {
+                    key = k;
+                    kt = t;
+                    ku = u;
+                    kv = v;
+                }
+            }
+        }
+        // segmented minimum: lanes of one owner are contiguous; afterwards
+        // the first lane of each owner's run holds that run's minimum
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint64_t k2 = shfl_down_u64(key, off);
+            const float t2 = __shfl_down_sync(kFull, kt, off);
+            const float u2 = __shfl_down_sync(kFull, ku, off);
+            const float v2 = __shfl_down_sync(kFull, kv, off);
+            const int o2 = __shfl_down_sync(kFull, o, off);
+            if (lane + off < 32 && o2 == o && k2 < key) {
+                key = k2;
+                kt = t2;
+                ku = u2;
+                kv = v2;
+            }
+        }
+        const bool mine = cnt > 0 && excl < base + 32 && incl > base;
+        const int head = mine ? (int)(max(excl, base) - base) : lane;
+        const uint64_t hk = shfl_u64(key, head);
+        const float ht = __shfl_sync(kFull, kt, head);
+        const float hu = __shfl_sync(kFull, ku, head);
+        const float hv = __shfl_sync(kFull, kv, head);
+        if (mine && hk < bound) {
+            bound = hk;
+            b.key = hk;
+            b.t = ht;
+            b.u = hu;
+            b.v = hv;
+            b.id = (int)(uint32_t)hk;
+            improved = true;
+        }
+    }
+    return improved;
+}
+
+// Descent of one lane from its held node to the next leaf: both children
+// box-tested, the near one (by the ray direction on the node's split axis)
+// entered, a hit far child pushed with its entry distance; a node with no
+// hit child pops the next stacked node the bound does not prune (the far
+// child is re-checked, LBVH.cpp:992).  The stack is a ring of kStackSize
+// entries holding [base, sp); a depth-first walk never holds more than the
+// tree depth.  Returns false when the lane has nothing left.
+template <bool EXACT, bool STATS>
+__device__ __forceinline__ bool descend(const TreeRef& tr_, const RayState& r, float bt, uint32_t& node, NodeBox& cur,
+                                        uint32_t* stack_node, float* stack_t0, uint32_t& sp, uint32_t base,
+                                        uint32_t& nbox) {
+    const rt_node* __restrict__ nodes = tr_.nodes;
+    while (!(__float_as_int(cur.b.z) & 4)) {
+        const int pc = __float_as_int(cur.b.z);
+        const uint32_t c0 = node << 1;
+        if (c0 + 1 >= tr_.num_nodes) {
+            atomicOr(tr_.err, RT_DEVERR_BOUNDS);
+            return false;
+        }
+        const float4* p = reinterpret_cast<const float4*>(nodes + c0);
+        const float4 l0 = __ldg(p), l1 = __ldg(p + 1), r0 = __ldg(p + 2), r1 = __ldg(p + 3);
+        float tl, tr;
+        const bool hl = box_enter<EXACT>(r, l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, bt, &tl);
+        const bool hr = box_enter<EXACT>(r, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, bt, &tr);
+        if (STATS) nbox += 2;
+        // near child by the split axis: the stored field is (30 - bit) % 3,
+        // the axis the bit splits is (field + 2) % 3
+        const int field = pc & 3;
+        const int near_right = (r.sgn >> (field == 0 ? 2 : field - 1)) & 1;
+        const bool hn = near_right ? hr : hl, hf = near_right ? hl : hr;
+        const float tf = near_right ? tl : tr;
+        const uint32_t nn = c0 | (uint32_t)near_right, nf = nn ^ 1u;
+        if (hn) {
+            if (hf) {
+                if (sp - base >= (uint32_t)kStackSize) {
+                    atomicOr(tr_.err, RT_DEVERR_BOUNDS);
+                    return false;
+                }
+                stack_node[sp & (kStackSize - 1)] = nf;
+                stack_t0[sp & (kStackSize - 1)] = tf;
+                ++sp;
+            }
+            node = nn;
+            cur.a = near_right ? r0 : l0;
+            cur.b = near_right ? r1 : l1;
+        } else if (hf) {
+            node = nf;
+            cur.a = near_right ? l0 : r0;
+            cur.b = near_right ? l1 : r1;
+        } else {
+            bool got = false;
+            while (sp != base) {
+                --sp;
+                if (!(stack_t0[sp & (kStackSize - 1)] > bt)) {
+                    node = stack_node[sp & (kStackSize - 1)];
+                    got = true;
+                    break;
+                }
+            }
+            if (!got) return false;
+            cur = load_node(nodes, node);
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ bool pop_node(const TreeRef& tr_, float bt, uint32_t& node, NodeBox& cur,
+                                         const uint32_t* stack_node, const float* stack_t0, uint32_t& sp,
+                                         uint32_t base) {
+    while (sp != base) {
+        --sp;
+        if (!(stack_t0[sp & (kStackSize - 1)] > bt)) {
+            node = stack_node[sp & (kStackSize - 1)];
+            cur = load_node(tr_.nodes, node);
+            return true;
+        }
+    }
+    return false;
+}
+
+// Warp-cooperative traversal in the oracle's order.  All 32 lanes of the
+// warp call it together; lanes with active == false only help with the leaf
+// phase.  Each round, every lane descends until it holds a leaf or has
+// nothing left, then the warp tests the held leaves' triangles together.
+// Hits and box / triangle test counts equal the oracle's.
 template <bool EXACT, bool STATS>
 __device__ __forceinline__ Hit traverse(const RayState& r, bool active, const TreeRef& tr_, bool any_hit,
                                         uint32_t* nbox_out, uint32_t* ntri_out) {
     constexpr uint32_t kFull = 0xffffffffu;
-    const rt_node* __restrict__ nodes = tr_.nodes;
-    const float4* __restrict__ tris = tr_.tris;
-    const int lane = threadIdx.x & 31;
-    Hit best;
-    best.id = -1;
-    best.u = -1.0f;
-    best.v = -1.0f;
-    best.t = r.tmax;
+    Best b;
+    b.key = hit_key(r.tmax, 0);
+    b.id = -1;
+    b.u = -1.0f;
+    b.v = -1.0f;
+    b.t = r.tmax;
+    uint64_t bound = b.key;
     uint32_t nbox = 0, ntri = 0;
     uint32_t stack_node[kStackSize];
     float stack_t0[kStackSize];
-    int sp = 0;
-
-    // pop: the next stacked node whose entry distance still does not exceed
-    // the closest hit (the far child is re-checked, LBVH.cpp:992)
-    auto pop = [&](uint32_t& nd) -> bool {
-        while (sp > 0) {
-            --sp;
-            if (!(stack_t0[sp] > best.t)) {
-                nd = stack_node[sp];
-                return true;
-            }
-        }
-        return false;
-    };
-
+    uint32_t sp = 0;
     NodeBox cur;
     cur.a = make_float4(0.f, 0.f, 0.f, 0.f);
     cur.b = cur.a;
     bool have = false;
     uint32_t node = 1;
     if (active) {
-        cur = load_node(nodes, 1);
+        cur = load_node(tr_.nodes, 1);
         if (STATS) ++nbox;
         float t0;
-        have = box_enter<EXACT>(r, cur.a.x, cur.a.y, cur.a.z, cur.a.w, cur.b.x, cur.b.y, best.t, &t0);
+        // no t satisfies 0 <= t < tmax when tmax <= 0 or is NaN
+        have = r.tmax > 0.0f && box_enter<EXACT>(r, cur.a.x, cur.a.y, cur.a.z, cur.a.w, cur.b.x, cur.b.y, b.t, &t0);
     }
     while (__any_sync(kFull, have)) {
-        // 1) descent to a leaf
-        if (have) {
-            while (!(__float_as_int(cur.b.z) & 4)) {
-                const int pc = __float_as_int(cur.b.z);
-                const uint32_t c0 = node << 1;
-                if (c0 + 1 >= tr_.num_nodes) {
-                    atomicOr(tr_.err, RT_DEVERR_BOUNDS);
-                    have = false;
-                    break;
-                }
-                const float4* p = reinterpret_cast<const float4*>(nodes + c0);
-                const float4 l0 = __ldg(p), l1 = __ldg(p + 1), r0 = __ldg(p + 2), r1 = __ldg(p + 3);
-                float tl, tr;
-                const bool hl = box_enter<EXACT>(r, l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, best.t, &tl);
-                const bool hr = box_enter<EXACT>(r, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, best.t, &tr);
-                if (STATS) nbox += 2;
-                // near child by the split axis: the stored field is (30 - bit) % 3,
-                // the axis the bit splits is (field + 2) % 3
-                const int field = pc & 3;
-                const int near_right = (r.sgn >> (field == 0 ? 2 : field - 1)) & 1;
-                const bool hn = near_right ? hr : hl, hf = near_right ? hl : hr;
-                const float tf = near_right ? tl : tr;
-                const uint32_t nn = c0 | (uint32_t)near_right, nf = nn ^ 1u;
-                if (hn) {
-                    if (hf) {
-                        stack_node[sp] = nf;
-                        stack_t0[sp] = tf;
-                        ++sp;
-                    }
-                    node = nn;
-                    cur.a = near_right ? r0 : l0;
-                    cur.b = near_right ? r1 : l1;
-                } else if (hf) {
-                    node = nf;
-                    cur.a = near_right ? l0 : r0;
-                    cur.b = near_right ? l1 : r1;
-                } else {
-                    have = pop(node);
-                    if (!have) break;
-                    cur = load_node(nodes, node);
-                }
-            }
-        }
+        if (have) have = descend<EXACT, STATS>(tr_, r, b.t, node, cur, stack_node, stack_t0, sp, 0u, nbox);
         __syncwarp();
-        // 2) the warp tests the held leaves' triangles [pos, pos + cnt)
-        int cnt = 0, pos = 0;
+        leaf_phase<STATS>(tr_, r, have, cur, bound, b, ntri);
         if (have) {
-            cnt = __float_as_int(cur.b.z) >> 3;
-            pos = __float_as_int(cur.b.w);
-            if (pos < 0 || cnt < 0 || (uint32_t)pos + (uint32_t)cnt > tr_.n) {
-                atomicOr(tr_.err, RT_DEVERR_BOUNDS);
-                cnt = 0;
-            }
-        }
-        if (STATS) ntri += (uint32_t)cnt;
-        uint32_t incl = (uint32_t)cnt;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t y = __shfl_up_sync(kFull, incl, off);
-            if (lane >= off) incl += y;
-        }
-        const uint32_t total = __shfl_sync(kFull, incl, 31);
-        const uint32_t excl = incl - (uint32_t)cnt;
-        uint64_t my_best = hit_key(best.t, best.id >= 0 ? best.id : 0);
-        for (uint32_t base = 0; base < total; base += 32) {
-            const uint32_t p = base + lane;
-            // owner of pair p: the first lane whose inclusive prefix exceeds p
-            int o = 0;
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1) {
-                const uint32_t v = __shfl_sync(kFull, incl, o + step - 1);
-                if (v <= p) o += step;
-            }
-            const uint32_t o_excl = __shfl_sync(kFull, excl, o);
-            const int o_pos = __shfl_sync(kFull, pos, o);
-            RayState ro;
-            ro.o = mk3(__shfl_sync(kFull, r.o.x, o), __shfl_sync(kFull, r.o.y, o), __shfl_sync(kFull, r.o.z, o));
-            ro.d = mk3(__shfl_sync(kFull, r.d.x, o), __shfl_sync(kFull, r.d.y, o), __shfl_sync(kFull, r.d.z, o));
-            const int o_exclude = __shfl_sync(kFull, r.exclude, o);
-            const uint64_t o_best = shfl_u64(my_best, o);
-            uint64_t key = ~0ull;
-            float kt = 0.0f, ku = 0.0f, kv = 0.0f;
-            if (p < total) {
-                const float4* tp = tris + 3 * (size_t)(o_pos + (p - o_excl));
-                const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-                const int id = __float_as_int(a.w);
-                float u, v, t;
-                if (id != o_exclude && tri_test(ro, a, b, c, &u, &v, &t)) {
-                    const uint64_t k = hit_key(t, id);
-                    if (k < o_best) {
-                        key = k;
-                        kt = t;
-                        ku = u;
-                        kv = v;
-                    }
-                }
-            }
-            // segmented minimum: lanes of one owner are contiguous; afterwards
-            // the first lane of each owner's run holds that run's minimum
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const uint64_t k2 = shfl_down_u64(key, off);
-                const float t2 = __shfl_down_sync(kFull, kt, off);
-                const float u2 = __shfl_down_sync(kFull, ku, off);
-                const float v2 = __shfl_down_sync(kFull, kv, off);
-                const int o2 = __shfl_down_sync(kFull, o, off);
-                if (lane + off < 32 && o2 == o && k2 < key) {
-                    key = k2;
-                    kt = t2;
-                    ku = u2;
-                    kv = v2;
-                }
-            }
-            const bool mine = cnt > 0 && excl < base + 32 && incl > base;
-            const int head = mine ? (int)(max(excl, base) - base) : lane;
-            const uint64_t hk = shfl_u64(key, head);
-            const float ht = __shfl_sync(kFull, kt, head);
-            const float hu = __shfl_sync(kFull, ku, head);
-            const float hv = __shfl_sync(kFull, kv, head);
-            if (mine && hk < my_best) {
-                my_best = hk;
-                best.t = ht;
-                best.u = hu;
-                best.v = hv;
-                best.id = (int)(uint32_t)hk;
-            }
-        }
-        // 3) next node
-        if (have) {
-            if (any_hit && best.id >= 0) {
-                have = false;
-            } else {
-                have = pop(node);
-                if (have) cur = load_node(nodes, node);
-            }
+            if (any_hit && b.id >= 0) have = false;
+            else have = pop_node(tr_, b.t, node, cur, stack_node, stack_t0, sp, 0u);
         }
     }
     if (STATS) {
         *nbox_out = nbox;
         *ntri_out = ntri;
     }
-    return best;
+    Hit h;
+    h.id = b.id;
+    h.u = b.u;
+    h.v = b.v;
+    h.t = b.t;
+    return h;
 }
 
 // Warp-uniform dispatch between the fast and the NaN-exact box test.  Must be

@@ -141,3 +141,53 @@ def test_render_frame_host_equals_device_path(gpu_ctx, torus_scene):
     assert np.array_equal(hp, hits_to_numpy(hits))
     assert np.array_equal(hv, vis.cpu().numpy())
     assert np.array_equal(hm, hits_to_numpy(mirror))
+
+
+def test_shared_traversal_matches_oracle(gpu_ctx, oracle_mod, torus_scene):
+    """The production traversal (no counters: idle lanes take over stacked
+    subtrees of busy lanes) gives the oracle's hits bit for bit."""
+    from rtgpu import scenes
+    from rtgpu.api import RayTracer, hits_to_numpy
+    tris, lb, dt, nodes, ids = torus_scene
+    rt = RayTracer(gpu_ctx)
+    for cam in (scenes.torus_camera(), scenes.look_at((2.2, 0.3, 0.4), (0.0, 0.0, 0.0), width=640, height=360)):
+        hits = rt.primary(lb, cam)
+        vis, mirror = rt.shadow_mirror(lb, cam, scenes.TORUS_LIGHT, hits)
+        gpu_ctx.check()
+        oh = oracle_mod.trace(nodes, 20, ids, tris, oracle_mod.primary_rays(cam))
+        ovis, omir = oracle_mod.shadow_mirror(nodes, 20, ids, tris, cam, scenes.TORUS_LIGHT, oh)
+        assert_hits_equal(hits_to_numpy(hits), oh, "primary")
+        assert np.array_equal(vis.cpu().numpy(), ovis)
+        assert_hits_equal(hits_to_numpy(mirror), omir, "mirror")
+
+
+@pytest.mark.parametrize("any_hit", [False, True])
+def test_shared_traversal_generic_rays(gpu_ctx, oracle_mod, any_hit):
+    """Random rays in a soup (exclusions, axis-aligned directions, short and
+    non-positive tmax) through the production traversal: closest hits equal
+    the oracle's; any-hit rays report occlusion exactly as the oracle does
+    (which occluder is reported depends on the walk order)."""
+    from rtgpu import scenes
+    from rtgpu.api import RayTracer, hits_to_numpy, rays_tensor
+    tris = scenes.random_soup(50000, seed=61)
+    lb, dt, nodes, ids = build_both(gpu_ctx, oracle_mod, tris, 18)
+    rng = np.random.default_rng(62)
+    n = 40000
+    src = rng.integers(0, len(tris), n)
+    o = tris[src].reshape(n, 3, 3).mean(axis=1).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d[: n // 8, rng.integers(0, 3)] = 0.0
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    excl = np.where(np.arange(n) % 2 == 0, src, -1).astype(np.int32)
+    tmax = np.where(np.arange(n) % 3 == 0, 0.05, 1e16).astype(np.float32)
+    tmax[::97] = 0.0
+    tmax[1::97] = -1.0
+    hits = RayTracer(gpu_ctx).rays(lb, rays_tensor(o, d, tmax, excl, "cuda"), any_hit=any_hit)
+    gpu_ctx.check()
+    oh = oracle_mod.trace(nodes, 18, ids, tris, oracle_mod.rays_array(o, d, tmax, excl), any_hit=any_hit)
+    g = hits_to_numpy(hits)
+    assert not (g["id"][::97] >= 0).any() and not (g["id"][1::97] >= 0).any()
+    if any_hit:
+        assert np.array_equal(g["id"] >= 0, oh["id"] >= 0)
+    else:
+        assert_hits_equal(g, oh, "rays")
