@@ -89,6 +89,11 @@ typedef struct rt_lbvh rt_lbvh;
 rt_status rt_ctx_create(int device, void* stream, rt_ctx** out);
 rt_status rt_ctx_destroy(rt_ctx* ctx);
 rt_status rt_ctx_set_stream(rt_ctx* ctx, void* stream);
+/* Work budget of the camera, shading and generic ray traces: a ray that has
+ * spent more than `budget` box + triangle tests in the per-lane traversal is
+ * handed to a second kernel that traces it with a whole warp (same hit).
+ * 0 turns the hand-over off.  Default 384.  Path tracing never hands over. */
+rt_status rt_ctx_set_trace_budget(rt_ctx* ctx, uint32_t budget);
 rt_status rt_ctx_sync(rt_ctx* ctx);
 /* Synchronises, then reports a device-side error flag raised since the
  * last check (RT_ERR_TIMEOUT, RT_ERR_NONFINITE) and clears it. */

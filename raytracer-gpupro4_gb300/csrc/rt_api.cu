@@ -45,13 +45,16 @@ extern "C" rt_status rt_ctx_create(int device, void* stream, rt_ctx** out) {
     c->stream = static_cast<cudaStream_t>(stream);
     if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
         cudaMalloc((void**)&c->d_words, 64 * sizeof(uint32_t)) != cudaSuccess ||
-        cudaMemset(c->d_words, 0, 64 * sizeof(uint32_t)) != cudaSuccess) {
+        cudaMemset(c->d_words, 0, 64 * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc((void**)&c->d_spill, sizeof(uint32_t) * kSpillCap) != cudaSuccess) {
         if (c->d_words) cudaFree(c->d_words);
+        if (c->d_spill) cudaFree(c->d_spill);
         delete c;
         return RT_ERR_CUDA;
     }
     c->d_err = c->d_words;
     c->d_work = c->d_words + 16;
+    c->d_spill_count = c->d_words + 32;
     *out = c;
     return RT_OK;
 }
@@ -59,6 +62,7 @@ extern "C" rt_status rt_ctx_create(int device, void* stream, rt_ctx** out) {
 extern "C" rt_status rt_ctx_destroy(rt_ctx* ctx) {
     if (!ctx) return RT_OK;
     if (ctx->d_words) cudaFree(ctx->d_words);
+    if (ctx->d_spill) cudaFree(ctx->d_spill);
     delete ctx;
     return RT_OK;
 }
@@ -66,6 +70,12 @@ extern "C" rt_status rt_ctx_destroy(rt_ctx* ctx) {
 extern "C" rt_status rt_ctx_set_stream(rt_ctx* ctx, void* stream) {
     if (!ctx) return RT_ERR_INVALID;
     ctx->stream = static_cast<cudaStream_t>(stream);
+    return RT_OK;
+}
+
+extern "C" rt_status rt_ctx_set_trace_budget(rt_ctx* ctx, uint32_t budget) {
+    if (!ctx) return RT_ERR_INVALID;
+    ctx->trace_budget = budget;
     return RT_OK;
 }
 

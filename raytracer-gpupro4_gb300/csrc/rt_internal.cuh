@@ -82,13 +82,22 @@ constexpr int kMaxDepth = 26;
 constexpr uint32_t kMaxTris = (1u << 29);
 
 // ---------------------------------------------------------------------------
+// Heavy-ray hand-over (see Spill in rt_traverse.cuh): list capacity and the
+// default budget of box + triangle tests a lane spends on one ray before it
+// hands the ray to the warp-per-ray kernel.
+constexpr uint32_t kSpillCap = 1u << 20;
+constexpr uint32_t kDefaultTraceBudget = 384;
+
 struct rt_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     std::string last_error;
     uint32_t* d_err = nullptr;   // device error word (d_words[0])
     uint32_t* d_work = nullptr;  // work counters of the persistent kernels (d_words[16..])
+    uint32_t* d_spill_count = nullptr;  // heavy-ray list length (d_words[32])
     uint32_t* d_words = nullptr; // 64 device words
+    uint32_t* d_spill = nullptr; // heavy-ray list, kSpillCap entries
+    uint32_t trace_budget = kDefaultTraceBudget;  // 0: no hand-over
     int num_sms = 0;
 };
 
@@ -186,7 +195,15 @@ inline uint32_t persistent_blocks(const rt_ctx* ctx, K kernel, int threads, uint
 }
 
 // Work-counter slots (ctx->d_work) of the persistent kernels.
-enum : int { kWorkPrimary = 0, kWorkSecondary = 1, kWorkRays = 2, kWorkPath = 3, kWorkAdjoint = 4, kWorkBatch = 5 };
+enum : int {
+    kWorkPrimary = 0,
+    kWorkSecondary = 1,
+    kWorkRays = 2,
+    kWorkPath = 3,
+    kWorkAdjoint = 4,
+    kWorkBatch = 5,
+    kWorkHeavy = 6
+};
 
 inline rt_status reset_work(rt_ctx* ctx, int slot) {
     RT_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_work + slot, 0, sizeof(uint32_t), ctx->stream));

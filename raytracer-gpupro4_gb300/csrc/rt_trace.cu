@@ -13,6 +13,7 @@
 // image is done.  Ray cost varies by three orders of magnitude across the
 // image, so a static grid leaves SMs idle behind the last heavy tiles.
 #include <algorithm>
+#include <cstring>
 
 #include "rt_traverse.cuh"
 
@@ -26,11 +27,20 @@ __device__ __forceinline__ void store_hit(rt_hit* out, const Hit& h) {
     *reinterpret_cast<int4*>(out) = make_int4(h.id, __float_as_int(h.u), __float_as_int(h.v), __float_as_int(h.t));
 }
 
+// Heavy-ray list entries: kind in the top two bits, pixel or ray index below.
+enum : uint32_t { kHeavyPrimary = 0, kHeavyShadow = 1, kHeavyMirror = 2, kHeavyRay = 3 };
+constexpr uint32_t kHeavyIndexMask = (1u << 30) - 1u;
+
+__device__ __forceinline__ void spill_record(uint32_t* list, int slot, uint32_t kind, size_t index) {
+    list[slot] = (kind << 30) | (uint32_t)index;
+}
+
 template <bool STATS>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_camera cam,
                                                                  rt_hit* __restrict__ hits,
                                                                  uint32_t* __restrict__ stats, uint32_t* work,
-                                                                 uint32_t num_tiles) {
+                                                                 uint32_t num_tiles, Spill spill,
+                                                                 uint32_t* __restrict__ list) {
     for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
         uint32_t i, j;
         const bool valid = tile_pixel(tile, threadIdx.x & 31, cam.width, cam.height, &i, &j);
@@ -38,10 +48,15 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_
         const f3 d = primary_dir(cam, i, j);
         const RayState r = make_ray(mk3(cam.eye[0], cam.eye[1], cam.eye[2]), d, 1e16f, -1);
         uint32_t nb = 0, nt = 0;
-        const Hit h = trace_ray<STATS>(r, valid, tr, false, &nb, &nt);
+        int slot = -1;
+        const Hit h = trace_ray<STATS>(r, valid, tr, false, &nb, &nt, &spill, &slot);
         if (valid) {
             const size_t p = (size_t)j * cam.width + i;
-            store_hit(hits + p, h);
+            if (slot >= 0) {
+                spill_record(list, slot, kHeavyPrimary, p);
+            } else {
+                store_hit(hits + p, h);
+            }
             if (STATS) {
                 stats[2 * p] = nb;
                 stats[2 * p + 1] = nt;
@@ -50,24 +65,25 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_
     }
 }
 
-// Shadow (any hit) and mirror (closest hit) rays of one pixel whose primary
-// hit is ph.  Called by all lanes of the warp together (valid == false for
-// lanes past the image edge); rays of pixels whose primary ray missed, or
-// whose light is behind the surface, are traced with active == false.
-template <bool STATS>
-__device__ __forceinline__ void secondary_pixel(const TreeRef& tr, const float* __restrict__ soup,
-                                                const rt_camera& cam, float lx, float ly, float lz, int4 ph,
-                                                uint8_t* __restrict__ vis, rt_hit* __restrict__ mirror,
-                                                uint32_t* __restrict__ sstats, uint32_t* __restrict__ mstats,
-                                                bool valid, uint32_t i, uint32_t j) {
-    const size_t p = (size_t)j * cam.width + i;
+// The shading rays of one pixel whose primary hit is ph (CSComputeColorRT.hlsl,
+// flat normal, no textures): the shadow ray towards the point light, cast
+// only when the light and the viewer are on the same side of the surface,
+// and the mirror ray.  has = the primary ray hit something.
+struct ShadeRays {
+    RayState shadow, mirror;
+    bool has, cast;
+};
+
+__device__ __forceinline__ ShadeRays shade_rays(const float* __restrict__ soup, const rt_camera& cam, float lx,
+                                                float ly, float lz, int4 ph, bool valid, uint32_t i, uint32_t j,
+                                                bool want_mirror) {
+    ShadeRays s;
     const int id = valid ? ph.x : -1;
-    const bool has = valid && id >= 0;
-    uint32_t snb = 0, snt = 0, mnb = 0, mnt = 0;
+    s.has = valid && id >= 0;
+    s.cast = false;
     f3 N = mk3(0.f, 0.f, 1.f), Nf = N, P = mk3(0.f, 0.f, 0.f), L = mk3(0.f, 0.f, 1.f), d = mk3(0.f, 0.f, 1.f);
     float dist = 1.0f;
-    bool cast = false;
-    if (has) {
+    if (s.has) {
         const float t = __int_as_float(ph.w);
         d = primary_dir(cam, i, j);
         const f3 o = mk3(cam.eye[0], cam.eye[1], cam.eye[2]);
@@ -83,25 +99,54 @@ __device__ __forceinline__ void secondary_pixel(const TreeRef& tr, const float* 
         dist = fsqrt(dot3(L, L));                                  // :137
         L = mk3(fdiv(L.x, dist), fdiv(L.y, dist), fdiv(L.z, dist)); // :138
         const float ls = dot3(N, L), rs = dot3(N, d);              // :145-146
-        cast = fmul(ls, rs) > 0.0f;                                // :147
+        s.cast = fmul(ls, rs) > 0.0f;                              // :147
     }
+    s.shadow = make_ray(P, mk3(-L.x, -L.y, -L.z), dist, id);      // :149-153
+    f3 R = mk3(0.f, 0.f, 1.f);
+    if (want_mirror && s.has) {
+        const float k = fmul(2.0f, dot3(d, Nf));                   // reflect(d, N) = d - 2*dot(d,N)*N
+        R = normalize3(mk3(fsub(d.x, fmul(k, Nf.x)), fsub(d.y, fmul(k, Nf.y)), fsub(d.z, fmul(k, Nf.z))));
+    }
+    s.mirror = make_ray(P, R, 1e16f, id);
+    return s;
+}
+
+__device__ __forceinline__ uint8_t vis_code(bool has, bool cast, bool occluded) {
+    return !has ? 0 : (!cast ? 1 : (occluded ? 2 : 3));
+}
+
+// Shadow (any hit) and mirror (closest hit) rays of one pixel whose primary
+// hit is ph.  Called by all lanes of the warp together (valid == false for
+// lanes past the image edge); rays of pixels whose primary ray missed, or
+// whose light is behind the surface, are traced with active == false.
+template <bool STATS>
+__device__ __forceinline__ void secondary_pixel(const TreeRef& tr, const float* __restrict__ soup,
+                                                const rt_camera& cam, float lx, float ly, float lz, int4 ph,
+                                                uint8_t* __restrict__ vis, rt_hit* __restrict__ mirror,
+                                                uint32_t* __restrict__ sstats, uint32_t* __restrict__ mstats,
+                                                bool valid, uint32_t i, uint32_t j, const Spill* spill,
+                                                uint32_t* __restrict__ list) {
+    const size_t p = (size_t)j * cam.width + i;
+    const ShadeRays s = shade_rays(soup, cam, lx, ly, lz, ph, valid, i, j, mirror != nullptr);
+    uint32_t snb = 0, snt = 0, mnb = 0, mnt = 0;
     if (vis) {  // uniform across the warp
-        const RayState sr = make_ray(P, mk3(-L.x, -L.y, -L.z), dist, id);  // :149-153
-        const Hit sh = trace_ray<STATS>(sr, cast, tr, true, &snb, &snt);
-        if (valid) vis[p] = !has ? 0 : (!cast ? 1 : (sh.id >= 0 ? 2 : 3));
+        int slot = -1;
+        const Hit sh = trace_ray<STATS>(s.shadow, s.cast, tr, true, &snb, &snt, spill, &slot);
+        if (valid) {
+            if (slot >= 0) spill_record(list, slot, kHeavyShadow, p);
+            else vis[p] = vis_code(s.has, s.cast, sh.id >= 0);
+        }
     }
     if (mirror) {
-        f3 R = mk3(0.f, 0.f, 1.f);
-        if (has) {
-            const float k = fmul(2.0f, dot3(d, Nf));               // reflect(d, N) = d - 2*dot(d,N)*N
-            R = normalize3(mk3(fsub(d.x, fmul(k, Nf.x)), fsub(d.y, fmul(k, Nf.y)), fsub(d.z, fmul(k, Nf.z))));
-        }
-        const RayState mr = make_ray(P, R, 1e16f, id);
-        Hit mh = trace_ray<STATS>(mr, has, tr, false, &mnb, &mnt);
-        if (!has) {
+        int slot = -1;
+        Hit mh = trace_ray<STATS>(s.mirror, s.has, tr, false, &mnb, &mnt, spill, &slot);
+        if (!s.has) {
             mh.id = -2; mh.u = -1.0f; mh.v = -1.0f; mh.t = 0.0f;
         }
-        if (valid) store_hit(mirror + p, mh);
+        if (valid) {
+            if (slot >= 0) spill_record(list, slot, kHeavyMirror, p);
+            else store_hit(mirror + p, mh);
+        }
     }
     if (STATS && valid) {
         if (sstats) { sstats[2 * p] = snb; sstats[2 * p + 1] = snt; }
@@ -113,38 +158,101 @@ template <bool STATS>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_secondary(
     TreeRef tr, const float* __restrict__ soup, rt_camera cam, float lx, float ly, float lz,
     const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis, rt_hit* __restrict__ mirror,
-    uint32_t* __restrict__ sstats, uint32_t* __restrict__ mstats, uint32_t* work, uint32_t num_tiles) {
+    uint32_t* __restrict__ sstats, uint32_t* __restrict__ mstats, uint32_t* work, uint32_t num_tiles, Spill spill,
+    uint32_t* __restrict__ list) {
     for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
         uint32_t i, j;
         const bool valid = tile_pixel(tile, threadIdx.x & 31, cam.width, cam.height, &i, &j);
         if (!valid) i = j = 0;
         int4 ph = make_int4(-1, 0, 0, 0);
         if (valid) ph = __ldg(reinterpret_cast<const int4*>(prim + (size_t)j * cam.width + i));
-        secondary_pixel<STATS>(tr, soup, cam, lx, ly, lz, ph, vis, mirror, sstats, mstats, valid, i, j);
+        secondary_pixel<STATS>(tr, soup, cam, lx, ly, lz, ph, vis, mirror, sstats, mstats, valid, i, j, &spill,
+                               list);
     }
+}
+
+__device__ __forceinline__ RayState load_ray(const rt_ray* __restrict__ rays, uint32_t k, bool valid) {
+    float4 a = make_float4(0.f, 0.f, 0.f, __int_as_float(-1)), b = make_float4(0.f, 0.f, 1.f, 1.f);
+    if (valid) {
+        a = __ldg(reinterpret_cast<const float4*>(rays + k));
+        b = __ldg(reinterpret_cast<const float4*>(rays + k) + 1);
+    }
+    return make_ray(mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), b.w, __float_as_int(a.w));
 }
 
 template <bool STATS>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_rays(TreeRef tr, const rt_ray* __restrict__ rays, uint32_t n,
                                                               int any_hit, rt_hit* __restrict__ hits,
-                                                              uint32_t* __restrict__ stats, uint32_t* work) {
+                                                              uint32_t* __restrict__ stats, uint32_t* work,
+                                                              Spill spill, uint32_t* __restrict__ list) {
     const uint32_t num_tiles = (n + 31) / 32;
     for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
         const uint32_t k = tile * 32 + (threadIdx.x & 31);
         const bool valid = k < n;
-        float4 a = make_float4(0.f, 0.f, 0.f, __int_as_float(-1)), b = make_float4(0.f, 0.f, 1.f, 1.f);
-        if (valid) {
-            a = __ldg(reinterpret_cast<const float4*>(rays + k));
-            b = __ldg(reinterpret_cast<const float4*>(rays + k) + 1);
-        }
-        const RayState r = make_ray(mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), b.w, __float_as_int(a.w));
+        const RayState r = load_ray(rays, k, valid);
         uint32_t nb = 0, nt = 0;
-        const Hit h = trace_ray<STATS>(r, valid, tr, any_hit != 0, &nb, &nt);
+        int slot = -1;
+        const Hit h = trace_ray<STATS>(r, valid, tr, any_hit != 0, &nb, &nt, &spill, &slot);
         if (valid) {
-            store_hit(hits + k, h);
+            if (slot >= 0) {
+                spill_record(list, slot, kHeavyRay, k);
+            } else {
+                store_hit(hits + k, h);
+            }
             if (STATS) {
                 stats[2 * k] = nb;
                 stats[2 * k + 1] = nt;
+            }
+        }
+    }
+}
+
+// Second pass over the rays the first pass handed over: one ray per warp
+// (trace_wide), rebuilt from its list entry exactly as the first pass made
+// it, and its result written where the first pass would have written it.
+struct HeavyArgs {
+    TreeRef tr;
+    const float* soup;
+    rt_camera cam;
+    float lx, ly, lz;
+    const rt_hit* prim;   // primary hits (shadow / mirror entries)
+    rt_hit* hits;         // primary or generic-ray output
+    uint8_t* vis;
+    rt_hit* mirror;
+    const rt_ray* rays;
+    int any_hit;          // generic rays
+    const uint32_t* list;
+    const uint32_t* count;
+    uint32_t cap;
+    uint32_t* work;
+};
+
+__global__ void __launch_bounds__(kTraceThreads) k_trace_heavy(HeavyArgs a) {
+    const uint32_t n = min(*a.count, a.cap);
+    const int lane = threadIdx.x & 31;
+    for (uint32_t e = next_tile(a.work); e < n; e = next_tile(a.work)) {
+        const uint32_t entry = __ldg(a.list + e);
+        const uint32_t kind = entry >> 30, idx = entry & kHeavyIndexMask;
+        if (kind == kHeavyPrimary) {
+            const uint32_t i = idx % a.cam.width, j = idx / a.cam.width;
+            const RayState r = make_ray(mk3(a.cam.eye[0], a.cam.eye[1], a.cam.eye[2]), primary_dir(a.cam, i, j),
+                                        1e16f, -1);
+            const Hit h = trace_wide(r, a.tr, false);
+            if (lane == 0) store_hit(a.hits + idx, h);
+        } else if (kind == kHeavyRay) {
+            const RayState r = load_ray(a.rays, idx, true);
+            const Hit h = trace_wide(r, a.tr, a.any_hit != 0);
+            if (lane == 0) store_hit(a.hits + idx, h);
+        } else {
+            const uint32_t i = idx % a.cam.width, j = idx / a.cam.width;
+            const int4 ph = __ldg(reinterpret_cast<const int4*>(a.prim + idx));
+            const ShadeRays s = shade_rays(a.soup, a.cam, a.lx, a.ly, a.lz, ph, true, i, j, kind == kHeavyMirror);
+            if (kind == kHeavyShadow) {
+                const Hit h = trace_wide(s.shadow, a.tr, true);
+                if (lane == 0) a.vis[idx] = vis_code(s.has, s.cast, h.id >= 0);
+            } else {
+                const Hit h = trace_wide(s.mirror, a.tr, false);
+                if (lane == 0) store_hit(a.mirror + idx, h);
             }
         }
     }
@@ -175,25 +283,73 @@ TreeRef tree_ref(const rt_ctx* ctx, const rt_lbvh* l) {
     return t;
 }
 
+namespace {
+
+// Heavy-ray hand-over of one trace call: the list is emptied before the
+// first pass (budget 0 or a counting pass: no hand-over), and the second pass
+// drains it.
+Spill spill_of(rt_ctx* ctx, bool enabled) {
+    Spill sp;
+    sp.count = (enabled && ctx->trace_budget) ? ctx->d_spill_count : nullptr;
+    sp.cap = kSpillCap;
+    sp.budget = ctx->trace_budget;
+    return sp;
+}
+
+rt_status reset_spill(rt_ctx* ctx, const Spill& sp) {
+    if (!sp.count) return RT_OK;
+    RT_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_spill_count, 0, sizeof(uint32_t), ctx->stream));
+    return reset_work(ctx, kWorkHeavy);
+}
+
+rt_status launch_heavy(rt_ctx* ctx, const Spill& sp, HeavyArgs a) {
+    if (!sp.count) return RT_OK;
+    a.list = ctx->d_spill;
+    a.count = ctx->d_spill_count;
+    a.cap = kSpillCap;
+    a.work = ctx->d_work + kWorkHeavy;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_heavy, kTraceThreads, 0) != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    k_trace_heavy<<<(uint32_t)per_sm * ctx->num_sms, kTraceThreads, 0, ctx->stream>>>(a);
+    RT_CHECK_LAUNCH(ctx, "k_trace_heavy");
+    return RT_OK;
+}
+
+HeavyArgs heavy_args(rt_ctx* ctx, const rt_lbvh* l) {
+    HeavyArgs a;
+    memset(&a, 0, sizeof(a));
+    a.tr = tree_ref(ctx, l);
+    return a;
+}
+
+}  // namespace
+
 extern "C" rt_status rt_trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, rt_hit* d_hits,
                                       uint32_t* d_stats) {
     rt_status s = check_trace_args(ctx, l, cam, "rt_trace_primary");
     if (s != RT_OK) return s;
     if (!d_hits) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_primary: null output");
     if ((s = reset_work(ctx, kWorkPrimary)) != RT_OK) return s;
+    const Spill sp = spill_of(ctx, !d_stats && (uint64_t)cam->width * cam->height <= kHeavyIndexMask);
+    if ((s = reset_spill(ctx, sp)) != RT_OK) return s;
     const uint32_t tiles = pixel_tiles(cam);
     uint32_t* work = ctx->d_work + kWorkPrimary;
     if (d_stats) {
         auto k = k_trace_primary<true>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), *cam, d_hits, d_stats, work, tiles);
+            tree_ref(ctx, l), *cam, d_hits, d_stats, work, tiles, sp, ctx->d_spill);
     } else {
         auto k = k_trace_primary<false>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), *cam, d_hits, nullptr, work, tiles);
+            tree_ref(ctx, l), *cam, d_hits, nullptr, work, tiles, sp, ctx->d_spill);
     }
     RT_CHECK_LAUNCH(ctx, "k_trace_primary");
-    return RT_OK;
+    HeavyArgs a = heavy_args(ctx, l);
+    a.cam = *cam;
+    a.hits = d_hits;
+    return launch_heavy(ctx, sp, a);
 }
 
 extern "C" rt_status rt_trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, const float light[3],
@@ -204,21 +360,33 @@ extern "C" rt_status rt_trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const
     if (!light || !d_primary) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_shadow_mirror: null argument");
     if (!l->src_tris) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_shadow_mirror: no triangle soup bound");
     if ((s = reset_work(ctx, kWorkSecondary)) != RT_OK) return s;
+    const bool stats = d_shadow_stats || d_mirror_stats;
+    const Spill sp = spill_of(ctx, !stats && (uint64_t)cam->width * cam->height <= kHeavyIndexMask);
+    if ((s = reset_spill(ctx, sp)) != RT_OK) return s;
     const uint32_t tiles = pixel_tiles(cam);
     uint32_t* work = ctx->d_work + kWorkSecondary;
-    if (d_shadow_stats || d_mirror_stats) {
+    if (stats) {
         auto k = k_trace_secondary<true>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
             tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_vis, d_mirror,
-            d_shadow_stats, d_mirror_stats, work, tiles);
+            d_shadow_stats, d_mirror_stats, work, tiles, sp, ctx->d_spill);
     } else {
         auto k = k_trace_secondary<false>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
             tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_vis, d_mirror, nullptr,
-            nullptr, work, tiles);
+            nullptr, work, tiles, sp, ctx->d_spill);
     }
     RT_CHECK_LAUNCH(ctx, "k_trace_secondary");
-    return RT_OK;
+    HeavyArgs a = heavy_args(ctx, l);
+    a.soup = l->src_tris;
+    a.cam = *cam;
+    a.lx = light[0];
+    a.ly = light[1];
+    a.lz = light[2];
+    a.prim = d_primary;
+    a.vis = d_vis;
+    a.mirror = d_mirror;
+    return launch_heavy(ctx, sp, a);
 }
 
 extern "C" rt_status rt_trace_rays(rt_ctx* ctx, const rt_lbvh* l, const rt_ray* d_rays, uint32_t n, int any_hit,
@@ -229,19 +397,25 @@ extern "C" rt_status rt_trace_rays(rt_ctx* ctx, const rt_lbvh* l, const rt_ray* 
     if (n == 0) return RT_OK;
     rt_status s = reset_work(ctx, kWorkRays);
     if (s != RT_OK) return s;
+    const Spill sp = spill_of(ctx, !d_stats && n <= kHeavyIndexMask);
+    if ((s = reset_spill(ctx, sp)) != RT_OK) return s;
     const uint32_t tiles = (n + 31) / 32;
     uint32_t* work = ctx->d_work + kWorkRays;
     if (d_stats) {
         auto k = k_trace_rays<true>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), d_rays, n, any_hit, d_hits, d_stats, work);
+            tree_ref(ctx, l), d_rays, n, any_hit, d_hits, d_stats, work, sp, ctx->d_spill);
     } else {
         auto k = k_trace_rays<false>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), d_rays, n, any_hit, d_hits, nullptr, work);
+            tree_ref(ctx, l), d_rays, n, any_hit, d_hits, nullptr, work, sp, ctx->d_spill);
     }
     RT_CHECK_LAUNCH(ctx, "k_trace_rays");
-    return RT_OK;
+    HeavyArgs a = heavy_args(ctx, l);
+    a.rays = d_rays;
+    a.any_hit = any_hit;
+    a.hits = d_hits;
+    return launch_heavy(ctx, sp, a);
 }
 
 extern "C" rt_status rt_render_frame_host(rt_ctx* ctx, rt_lbvh* l, const float* h_tris, uint32_t n,
@@ -332,7 +506,7 @@ __global__ void __launch_bounds__(256) k_batch_trace(BatchTraceArgs a, uint32_t*
                 const int4 ph = make_int4(h.id, __float_as_int(h.u), __float_as_int(h.v), __float_as_int(h.t));
                 secondary_pixel<false>(tr, a.soup + 9 * (size_t)toff, cam, __ldg(a.lights + 3 * s),
                                        __ldg(a.lights + 3 * s + 1), __ldg(a.lights + 3 * s + 2), ph,
-                                       a.vis + s * px, nullptr, nullptr, nullptr, valid, i, j);
+                                       a.vis + s * px, nullptr, nullptr, nullptr, valid, i, j, nullptr, nullptr);
             }
         }
     }

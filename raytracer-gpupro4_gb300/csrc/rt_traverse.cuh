@@ -173,7 +173,7 @@ __device__ __forceinline__ bool leaf_phase(const TreeRef& tr_, const RayState& r
             cnt = 0;
         }
     }
-    if (STATS) ntri += (uint32_t)cnt;
+    ntri += (uint32_t)cnt;
     bool improved = false;
     // Serial part: while at least kSerialLanes lanes still have triangles,
     // each lane tests its own leaf's triangles (no exchange between lanes);
@@ -261,28 +261,27 @@ __device__ __forceinline__ bool leaf_phase(const TreeRef& tr_, const RayState& r
                 }
             }
         }
-        // segmented minimum: lanes of one owner are contiguous; afterwards
-        // the first lane of each owner's run holds that run's minimum
+        // segmented minimum of the key (lanes of one owner are contiguous),
+        // carrying the lane that computed it; afterwards the first lane of
+        // each owner's run holds the run's minimum and its source lane
+        int src = lane;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
             const uint64_t k2 = shfl_down_u64(key, off);
-            const float t2 = __shfl_down_sync(kFull, kt, off);
-            const float u2 = __shfl_down_sync(kFull, ku, off);
-            const float v2 = __shfl_down_sync(kFull, kv, off);
+            const int s2 = __shfl_down_sync(kFull, src, off);
             const int o2 = __shfl_down_sync(kFull, o, off);
             if (lane + off < 32 && o2 == o && k2 < key) {
                 key = k2;
-                kt = t2;
-                ku = u2;
-                kv = v2;
+                src = s2;
             }
         }
         const bool mine = cnt > 0 && excl < base + 32 && incl > base;
         const int head = mine ? (int)(max(excl, base) - base) : lane;
         const uint64_t hk = shfl_u64(key, head);
-        const float ht = __shfl_sync(kFull, kt, head);
-        const float hu = __shfl_sync(kFull, ku, head);
-        const float hv = __shfl_sync(kFull, kv, head);
+        const int hs = __shfl_sync(kFull, src, head);
+        const float ht = __shfl_sync(kFull, kt, hs);
+        const float hu = __shfl_sync(kFull, ku, hs);
+        const float hv = __shfl_sync(kFull, kv, hs);
         if (mine && hk < bound) {
             bound = hk;
             b.key = hk;
@@ -320,7 +319,7 @@ __device__ __forceinline__ bool descend(const TreeRef& tr_, const RayState& r, f
         float tl, tr;
         const bool hl = box_enter<EXACT>(r, l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, bt, &tl);
         const bool hr = box_enter<EXACT>(r, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, bt, &tr);
-        if (STATS) nbox += 2;
+        nbox += 2;
         // near child by the split axis: the stored field is (30 - bit) % 3,
         // the axis the bit splits is (field + 2) % 3
         const int field = pc & 3;
@@ -376,14 +375,27 @@ __device__ __forceinline__ bool pop_node(const TreeRef& tr_, float bt, uint32_t&
     return false;
 }
 
-// Warp-cooperative traversal in the oracle's order.  All 32 lanes of the
-// warp call it together; lanes with active == false only help with the leaf
-// phase.  Each round, every lane descends until it holds a leaf or has
-// nothing left, then the warp tests the held leaves' triangles together.
-// Hits and box / triangle test counts equal the oracle's.
+// Hand-over of rays that exceed a work budget.  A lane whose ray has spent
+// more than `budget` box + triangle tests takes a slot of the heavy-ray list
+// (atomicAdd on *count) and stops; the caller records the ray in that slot,
+// and a second kernel traces it with a whole warp (traverse_wide).  When the
+// list is full the lane keeps going.  count == nullptr: no budget.
+struct Spill {
+    uint32_t* count;
+    uint32_t cap;
+    uint32_t budget;
+};
+
+// Warp-cooperative traversal.  All 32 lanes of the warp call it together;
+// lanes with active == false only help with the leaf phase.  Each round,
+// every lane descends until it holds a leaf or has nothing left, then the
+// warp tests the held leaves' triangles together.  Without a budget, hits and
+// box / triangle test counts equal the oracle's.  *slot_out = the heavy-list
+// slot of a ray handed over (its hit is then not valid), else -1.
 template <bool EXACT, bool STATS>
 __device__ __forceinline__ Hit traverse(const RayState& r, bool active, const TreeRef& tr_, bool any_hit,
-                                        uint32_t* nbox_out, uint32_t* ntri_out) {
+                                        uint32_t* nbox_out, uint32_t* ntri_out, const Spill* spill,
+                                        int* slot_out) {
     constexpr uint32_t kFull = 0xffffffffu;
     Best b;
     b.key = hit_key(r.tmax, 0);
@@ -401,9 +413,11 @@ __device__ __forceinline__ Hit traverse(const RayState& r, bool active, const Tr
     cur.b = cur.a;
     bool have = false;
     uint32_t node = 1;
+    int slot = -1;
+    bool budgeted = !STATS && spill != nullptr && spill->count != nullptr;
     if (active) {
         cur = load_node(tr_.nodes, 1);
-        if (STATS) ++nbox;
+        ++nbox;
         float t0;
         // no t satisfies 0 <= t < tmax when tmax <= 0 or is NaN
         have = r.tmax > 0.0f && box_enter<EXACT>(r, cur.a.x, cur.a.y, cur.a.z, cur.a.w, cur.b.x, cur.b.y, b.t, &t0);
@@ -413,14 +427,27 @@ __device__ __forceinline__ Hit traverse(const RayState& r, bool active, const Tr
         __syncwarp();
         leaf_phase<STATS>(tr_, r, have, cur, bound, b, ntri);
         if (have) {
-            if (any_hit && b.id >= 0) have = false;
-            else have = pop_node(tr_, b.t, node, cur, stack_node, stack_t0, sp, 0u);
+            if (any_hit && b.id >= 0) {
+                have = false;
+            } else {
+                have = pop_node(tr_, b.t, node, cur, stack_node, stack_t0, sp, 0u);
+                if (budgeted && have && nbox + ntri > spill->budget) {
+                    const uint32_t s = atomicAdd(spill->count, 1u);
+                    if (s < spill->cap) {
+                        slot = (int)s;
+                        have = false;
+                    } else {
+                        budgeted = false;  // list full: finish here
+                    }
+                }
+            }
         }
     }
     if (STATS) {
         *nbox_out = nbox;
         *ntri_out = ntri;
     }
+    if (slot_out) *slot_out = slot;
     Hit h;
     h.id = b.id;
     h.u = b.u;
@@ -429,14 +456,127 @@ __device__ __forceinline__ Hit traverse(const RayState& r, bool active, const Tr
     return h;
 }
 
+__device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const uint64_t o = shfl_u64(v, (threadIdx.x & 31) ^ off);
+        v = o < v ? o : v;
+    }
+    return v;
+}
+
+// One ray traced by the whole warp (every lane passes the same ray).  Lane 0
+// starts at the root; at the top of each round the lanes with nothing to do
+// take stacked subtrees of the lanes that have some, so after a round or two
+// the ray's subtrees are walked by all 32 lanes at once,
+// each lane with its own stack, and the leaf phase tests their leaves
+// together.  The lanes share one pruning bound: the warp minimum of their
+// hit keys, taken every round.  The closest hit under the tie rule does not
+// depend on which lane tests which subtree, so the hit equals traverse()'s;
+// it is the warp minimum of the lanes' hits.  For any_hit the walk stops at
+// the first accepted hit of any lane.
+template <bool EXACT>
+__device__ __forceinline__ Hit traverse_wide(const RayState& r, const TreeRef& tr_, bool any_hit) {
+    constexpr uint32_t kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;  // warp in block (blocks of at most 256 threads)
+    __shared__ uint32_t s_gn[8][32];
+    __shared__ float s_gt[8][32];
+    const uint64_t init = hit_key(r.tmax, 0);
+    Best b;
+    b.key = init;
+    b.id = -1;
+    b.u = -1.0f;
+    b.v = -1.0f;
+    b.t = r.tmax;
+    uint64_t bound = init;
+    uint32_t nbox = 0, ntri = 0;
+    uint32_t stack_node[kStackSize];
+    float stack_t0[kStackSize];
+    uint32_t sp = 0, base = 0;
+    NodeBox cur;
+    cur.a = make_float4(0.f, 0.f, 0.f, 0.f);
+    cur.b = cur.a;
+    bool have = false;
+    uint32_t node = 1;
+    if (lane == 0) {
+        cur = load_node(tr_.nodes, 1);
+        float t0;
+        have = r.tmax > 0.0f && box_enter<EXACT>(r, cur.a.x, cur.a.y, cur.a.z, cur.a.w, cur.b.x, cur.b.y, r.tmax, &t0);
+    }
+    for (;;) {
+        bound = warp_min_u64(bound);
+        if (any_hit && bound < init) break;
+        // idle lanes take stacked subtrees of busy lanes, oldest (largest)
+        // first: the busy lanes' stack entries are numbered lane by lane and
+        // the r-th idle lane takes entry r, staged through shared memory
+        const uint32_t give = (have && sp != base) ? sp - base : 0u;
+        const uint32_t im = __ballot_sync(kFull, !have);
+        if (im && __any_sync(kFull, give != 0u)) {
+            uint32_t incl = give;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t y = __shfl_up_sync(kFull, incl, off);
+                if (lane >= off) incl += y;
+            }
+            const uint32_t total = __shfl_sync(kFull, incl, 31);
+            const uint32_t excl = incl - give;
+            const uint32_t npair = min((uint32_t)__popc(im), total);
+            if (give && excl < npair) {
+                const uint32_t taken = min(give, npair - excl);
+                for (uint32_t k = 0; k < taken; ++k) {
+                    s_gn[wib][excl + k] = stack_node[(base + k) & (kStackSize - 1)];
+                    s_gt[wib][excl + k] = stack_t0[(base + k) & (kStackSize - 1)];
+                }
+                base += taken;
+            }
+            __syncwarp();
+            const uint32_t irank = __popc(im & ((1u << lane) - 1u));
+            if (!have && irank < npair) {
+                const uint32_t gn = s_gn[wib][irank];
+                const float gt = s_gt[wib][irank];
+                if (!(gt > key_t(bound))) {
+                    node = gn;
+                    cur = load_node(tr_.nodes, gn);
+                    have = true;
+                }
+            }
+            __syncwarp();
+        }
+        if (!__any_sync(kFull, have)) break;
+        if (have) have = descend<EXACT, false>(tr_, r, key_t(bound), node, cur, stack_node, stack_t0, sp, base, nbox);
+        __syncwarp();
+        leaf_phase<false>(tr_, r, have, cur, bound, b, ntri);
+        if (have) have = pop_node(tr_, key_t(bound), node, cur, stack_node, stack_t0, sp, base);
+    }
+    // the warp minimum of the lanes' own hits, with the winner's t, u, v
+    const uint64_t kmin = warp_min_u64(b.key);
+    const uint32_t wm = __ballot_sync(kFull, b.key == kmin);
+    const int w = __ffs(wm) - 1;
+    Hit h;
+    h.id = __shfl_sync(kFull, b.id, w);
+    h.u = __shfl_sync(kFull, b.u, w);
+    h.v = __shfl_sync(kFull, b.v, w);
+    h.t = __shfl_sync(kFull, b.t, w);
+    return h;
+}
+
 // Warp-uniform dispatch between the fast and the NaN-exact box test.  Must be
 // called by all 32 lanes of the warp together (inactive lanes pass
-// active == false).
+// active == false).  spill / slot: see Spill (nullptr: no budget).
 template <bool STATS>
 __device__ __forceinline__ Hit trace_ray(const RayState& r, bool active, const TreeRef& tr, bool any_hit,
-                                         uint32_t* nbox, uint32_t* ntri) {
-    if (__any_sync(0xffffffffu, active && r.exact)) return traverse<true, STATS>(r, active, tr, any_hit, nbox, ntri);
-    return traverse<false, STATS>(r, active, tr, any_hit, nbox, ntri);
+                                         uint32_t* nbox, uint32_t* ntri, const Spill* spill = nullptr,
+                                         int* slot = nullptr) {
+    if (__any_sync(0xffffffffu, active && r.exact))
+        return traverse<true, STATS>(r, active, tr, any_hit, nbox, ntri, spill, slot);
+    return traverse<false, STATS>(r, active, tr, any_hit, nbox, ntri, spill, slot);
+}
+
+// One ray traced by the whole warp; every lane passes the same ray.
+__device__ __forceinline__ Hit trace_wide(const RayState& r, const TreeRef& tr, bool any_hit) {
+    if (r.exact) return traverse_wide<true>(r, tr, any_hit);
+    return traverse_wide<false>(r, tr, any_hit);
 }
 
 // Primary ray of pixel (i, j): CSPrimaryRays.hlsl:36-56 with the basis camera.

@@ -62,6 +62,11 @@ class Context:
     def sync(self):
         L.check(L.lib().rt_ctx_sync(self.h), self.h, "rt_ctx_sync")
 
+    def set_trace_budget(self, budget: int):
+        """Box + triangle tests a ray may spend in the per-lane traversal before
+        it is handed to the warp-per-ray pass (0: never)."""
+        L.check(L.lib().rt_ctx_set_trace_budget(self.h, int(budget)), self.h, "rt_ctx_set_trace_budget")
+
 
 class LBVH:
     """Device LBVH (heap layout, 1 << depth slots of 32 bytes)."""

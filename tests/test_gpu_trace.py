@@ -191,3 +191,56 @@ def test_shared_traversal_generic_rays(gpu_ctx, oracle_mod, any_hit):
         assert np.array_equal(g["id"] >= 0, oh["id"] >= 0)
     else:
         assert_hits_equal(g, oh, "rays")
+
+
+@pytest.mark.parametrize("budget", [1, 24, 0])
+def test_heavy_ray_handover_matches_oracle(gpu_ctx, oracle_mod, torus_scene, budget):
+    """Rays over the work budget are re-traced by the warp-per-ray pass; with
+    a budget of 1 nearly every ray is, with 0 none is: hits, visibility and
+    mirror hits equal the oracle's either way."""
+    from rtgpu import scenes
+    from rtgpu.api import RayTracer, hits_to_numpy
+    tris, lb, dt, nodes, ids = torus_scene
+    rt = RayTracer(gpu_ctx)
+    cam = scenes.look_at((2.2, 0.3, 0.4), (0.0, 0.0, 0.0), width=320, height=200)
+    gpu_ctx.set_trace_budget(budget)
+    try:
+        hits = rt.primary(lb, cam)
+        vis, mirror = rt.shadow_mirror(lb, cam, scenes.TORUS_LIGHT, hits)
+        gpu_ctx.check()
+    finally:
+        gpu_ctx.set_trace_budget(384)
+    oh = oracle_mod.trace(nodes, 20, ids, tris, oracle_mod.primary_rays(cam))
+    ovis, omir = oracle_mod.shadow_mirror(nodes, 20, ids, tris, cam, scenes.TORUS_LIGHT, oh)
+    assert_hits_equal(hits_to_numpy(hits), oh, "primary")
+    assert np.array_equal(vis.cpu().numpy(), ovis)
+    assert_hits_equal(hits_to_numpy(mirror), omir, "mirror")
+
+
+@pytest.mark.parametrize("any_hit", [False, True])
+def test_heavy_ray_handover_generic_rays(gpu_ctx, oracle_mod, any_hit):
+    from rtgpu import scenes
+    from rtgpu.api import RayTracer, hits_to_numpy, rays_tensor
+    tris = scenes.random_soup(30000, seed=71)
+    lb, dt, nodes, ids = build_both(gpu_ctx, oracle_mod, tris, 16)
+    rng = np.random.default_rng(72)
+    n = 20000
+    src = rng.integers(0, len(tris), n)
+    o = tris[src].reshape(n, 3, 3).mean(axis=1).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d[: n // 8, rng.integers(0, 3)] = 0.0
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    excl = np.where(np.arange(n) % 2 == 0, src, -1).astype(np.int32)
+    tmax = np.where(np.arange(n) % 3 == 0, 0.05, 1e16).astype(np.float32)
+    gpu_ctx.set_trace_budget(2)
+    try:
+        hits = RayTracer(gpu_ctx).rays(lb, rays_tensor(o, d, tmax, excl, "cuda"), any_hit=any_hit)
+        gpu_ctx.check()
+    finally:
+        gpu_ctx.set_trace_budget(384)
+    oh = oracle_mod.trace(nodes, 16, ids, tris, oracle_mod.rays_array(o, d, tmax, excl), any_hit=any_hit)
+    g = hits_to_numpy(hits)
+    if any_hit:
+        assert np.array_equal(g["id"] >= 0, oh["id"] >= 0)
+    else:
+        assert_hits_equal(g, oh, "rays")
