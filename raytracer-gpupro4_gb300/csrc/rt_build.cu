@@ -397,23 +397,33 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
     // decoupled look-back (bounded)
     uint32_t* my = lookback + (size_t)tile * 256 + t;
     st_relaxed(my, (tile == 0 ? kFlagInc : kFlagAgg) | count);
+    // Look-back over the predecessors' words for this digit, four at a time
+    // (the four loads are in flight together): add aggregates until an
+    // inclusive prefix; a word not yet published is polled again (bounded).
     uint32_t excl = 0;
     if (tile > 0) {
         int p = (int)tile - 1;
         uint32_t spins = 0;
-        while (p >= 0) {
-            const uint32_t v = ld_relaxed(lookback + (size_t)p * 256 + t);
-            const uint32_t f = v & kFlagMask;
-            if (f == 0u) {
-                if (++spins > kSpinLimit) {
-                    atomicOr(err, RT_DEVERR_TIMEOUT);
-                    break;
-                }
-                continue;
+        bool done = false;
+        while (!done && p >= 0) {
+            uint32_t v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] = (p - q >= 0) ? ld_relaxed(lookback + (size_t)(p - q) * 256 + t) : 0u;
+            int used = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (done || used < q || p - q < 0) continue;
+                const uint32_t f = v[q] & kFlagMask;
+                if (f == 0u) continue;  // not published yet: poll again from here
+                excl += v[q] & kValMask;
+                used = q + 1;
+                if (f == kFlagInc) done = true;
             }
-            excl += v & kValMask;
-            if (f == kFlagInc) break;
-            --p;
+            if (!done && used == 0 && ++spins > kSpinLimit) {
+                atomicOr(err, RT_DEVERR_TIMEOUT);
+                break;
+            }
+            p -= used;
         }
         st_relaxed(my, kFlagInc | (excl + count));
     }
@@ -555,35 +565,46 @@ __global__ void __launch_bounds__(kEmitThreads) k_emit_tiles(const uint32_t* __r
     }
 }
 
-// k_emit_prefix: exclusive fwd prefix / bwd suffix over the tiles (one warp).
-__global__ void k_emit_prefix(uint32_t* scan, uint32_t tiles) {
-    const int lane = threadIdx.x;
-    const uint32_t per = (tiles + 31) / 32;
-    const uint32_t lo = min(tiles, lane * per), hi = min(tiles, lo + per);
+// k_emit_prefix: exclusive fwd prefix / bwd suffix over the tiles (one block
+// of 1024 threads, each over a contiguous run of tiles).
+constexpr int kPrefixThreads = 1024;
+
+__global__ void __launch_bounds__(kPrefixThreads) k_emit_prefix(uint32_t* scan, uint32_t tiles) {
+    __shared__ uint32_t s_f[kPrefixThreads / 32], s_b[kPrefixThreads / 32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const uint32_t per = (tiles + kPrefixThreads - 1) / kPrefixThreads;
+    const uint32_t lo = min(tiles, (uint32_t)t * per), hi = min(tiles, lo + per);
     uint32_t af = 0, ab = 0;
-    for (uint32_t t = lo; t < hi; ++t) af = rec_fwd(af, scan[4 * t + 0]);
-    for (uint32_t t = hi; t > lo; --t) ab = rec_bwd(scan[4 * (t - 1) + 1], ab);
+    for (uint32_t q = lo; q < hi; ++q) af = rec_fwd(af, scan[4 * q + 0]);
+    for (uint32_t q = hi; q > lo; --q) ab = rec_bwd(scan[4 * (q - 1) + 1], ab);
     uint32_t xf = af, xb = ab;
+#pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
         const uint32_t y = __shfl_up_sync(kFull, xf, off);
         if (lane >= off) xf = rec_fwd(y, xf);
         const uint32_t z = __shfl_down_sync(kFull, xb, off);
         if (lane + off < 32) xb = rec_bwd(xb, z);
     }
+    if (lane == 31) s_f[w] = xf;  // inclusive fwd total of the warp
+    if (lane == 0) s_b[w] = xb;   // inclusive bwd total of the warp
+    __syncthreads();
+    uint32_t wf = 0, wb = 0;
+    for (int q = 0; q < w; ++q) wf = rec_fwd(wf, s_f[q]);
+    for (int q = kPrefixThreads / 32 - 1; q > w; --q) wb = rec_bwd(s_b[q], wb);
     uint32_t ef = __shfl_up_sync(kFull, xf, 1);
     if (lane == 0) ef = 0;
     uint32_t eb = __shfl_down_sync(kFull, xb, 1);
     if (lane == 31) eb = 0;
-    uint32_t run = ef;
-    for (uint32_t t = lo; t < hi; ++t) {
-        const uint32_t a = scan[4 * t + 0];
-        scan[4 * t + 2] = run;
+    uint32_t run = rec_fwd(wf, ef);
+    for (uint32_t q = lo; q < hi; ++q) {
+        const uint32_t a = scan[4 * q + 0];
+        scan[4 * q + 2] = run;
         run = rec_fwd(run, a);
     }
-    run = eb;
-    for (uint32_t t = hi; t > lo; --t) {
-        const uint32_t a = scan[4 * (t - 1) + 1];
-        scan[4 * (t - 1) + 3] = run;
+    run = rec_bwd(eb, wb);
+    for (uint32_t q = hi; q > lo; --q) {
+        const uint32_t a = scan[4 * (q - 1) + 1];
+        scan[4 * (q - 1) + 3] = run;
         run = rec_bwd(a, run);
     }
 }
@@ -932,7 +953,7 @@ static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint
     k_bounds<<<bblocks, 256, 0, st>>>(d_tris, n, l->scene, l->partials, l->counters, l->hist, l->lookback,
                                       lb_words, l->nodes, l->num_nodes, (flags & RT_BUILD_CLEAR_UNREACHED) ? 1 : 0);
     RT_CHECK_LAUNCH(ctx, "k_bounds");
-    const uint32_t mblocks = std::max(1u, std::min(ceil_div(n, kMortonThreads), (uint32_t)ctx->num_sms * 2));
+    const uint32_t mblocks = std::max(1u, std::min(ceil_div(n, kMortonThreads), (uint32_t)ctx->num_sms * 4));
     k_morton_hist<<<mblocks, kMortonThreads, 0, st>>>(d_tris, n, l->scene, l->keys, l->ids, l->hist, ctx->d_err);
     RT_CHECK_LAUNCH(ctx, "k_morton_hist");
     uint32_t *kin = l->keys, *iin = l->ids, *kout = l->keys_alt, *iout = l->ids_alt;
@@ -948,7 +969,7 @@ static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint
     k_emit_tiles<<<emit_tiles, kEmitThreads, 0, st>>>(l->keys, n, l->scan, l->arrive, std::max(1u, l->num_nodes >> 1),
                                                       l->counters + 6);
     RT_CHECK_LAUNCH(ctx, "k_emit_tiles");
-    k_emit_prefix<<<1, 32, 0, st>>>(l->scan, emit_tiles);
+    k_emit_prefix<<<1, kPrefixThreads, 0, st>>>(l->scan, emit_tiles);
     RT_CHECK_LAUNCH(ctx, "k_emit_prefix");
     k_emit_leaves<<<emit_tiles, kEmitThreads, 0, st>>>(l->keys, l->ids, d_tris, n, l->depth, l->scan, l->nodes,
                                                        l->sorted_tris, l->leaf_list, l->counters + 5, ctx->d_err);
@@ -1139,7 +1160,7 @@ extern "C" rt_status rt_lbvh_build_noalloc(rt_ctx* ctx, void* stream, const floa
         std::max(1u, std::min({ceil_div(3ull * n, 256), (uint32_t)D.num_sms * 4, kNoAllocBoundsBlocks}));
     k_bounds<<<bblocks, 256, 0, st>>>(d_tris, n, scene, partials, counters, hist, lookback, lb_words, d_nodes,
                                       num_nodes, (flags & RT_BUILD_CLEAR_UNREACHED) ? 1 : 0);
-    const uint32_t mblocks = std::max(1u, std::min(ceil_div(n, kMortonThreads), (uint32_t)D.num_sms * 2));
+    const uint32_t mblocks = std::max(1u, std::min(ceil_div(n, kMortonThreads), (uint32_t)D.num_sms * 4));
     k_morton_hist<<<mblocks, kMortonThreads, 0, st>>>(d_tris, n, scene, d_keys, d_ids, hist, err);
     uint32_t *kin = d_keys, *iin = d_ids, *kout = keys_alt, *iout = ids_alt;
     for (int p = 0; p < kSortPasses; ++p) {
@@ -1149,7 +1170,7 @@ extern "C" rt_status rt_lbvh_build_noalloc(rt_ctx* ctx, void* stream, const floa
         std::swap(iin, iout);
     }
     k_emit_tiles<<<emit_tiles, kEmitThreads, 0, st>>>(d_keys, n, scan, arrive, std::max(1u, num_nodes >> 1), counters + 6);
-    k_emit_prefix<<<1, 32, 0, st>>>(scan, emit_tiles);
+    k_emit_prefix<<<1, kPrefixThreads, 0, st>>>(scan, emit_tiles);
     k_emit_leaves<<<emit_tiles, kEmitThreads, 0, st>>>(d_keys, d_ids, d_tris, n, depth, scan, d_nodes,
                                                        reinterpret_cast<float4*>(d_sorted_tris), leaves, counters + 5, err);
     const uint32_t rblocks = std::max(1u, std::min(ceil_div(n, 256), (uint32_t)D.num_sms * 8));
@@ -1608,7 +1629,7 @@ extern "C" rt_status rt_batch_build(rt_ctx* ctx, rt_batch* b, const float* d_tri
     kb_emit_tiles<<<emit_tiles, kEmitThreads, 0, st>>>(kin, n, b->tri_off, S, b->scan, b->arrive, num_nodes >> 1,
                                                        b->counters + 6);
     RT_CHECK_LAUNCH(ctx, "kb_emit_tiles");
-    k_emit_prefix<<<1, 32, 0, st>>>(b->scan, emit_tiles);
+    k_emit_prefix<<<1, kPrefixThreads, 0, st>>>(b->scan, emit_tiles);
     RT_CHECK_LAUNCH(ctx, "k_emit_prefix");
     kb_emit_leaves<<<emit_tiles, kEmitThreads, 0, st>>>(kin, iin, d_tris, n, b->tri_off, S, b->depth, b->scan, b->nodes,
                                                         b->sorted_tris, b->ids_local, b->leaf_list, b->counters + 5,
