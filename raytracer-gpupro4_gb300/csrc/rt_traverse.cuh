@@ -465,99 +465,234 @@ __device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
     return v;
 }
 
-// One ray traced by the whole warp (every lane passes the same ray).  Lane 0
-// starts at the root; at the top of each round the lanes with nothing to do
-// take stacked subtrees of the lanes that have some, so after a round or two
-// the ray's subtrees are walked by all 32 lanes at once,
-// each lane with its own stack, and the leaf phase tests their leaves
-// together.  The lanes share one pruning bound: the warp minimum of their
-// hit keys, taken every round.  The closest hit under the tie rule does not
-// depend on which lane tests which subtree, so the hit equals traverse()'s;
-// it is the warp minimum of the lanes' hits.  For any_hit the walk stops at
-// the first accepted hit of any lane.
+// One ray traced by the whole warp (every lane passes the same ray): a
+// frontier walk.  The warp keeps a stack of internal nodes the ray enters
+// (node, entry distance) and a queue of leaves in shared memory.  Each step
+// pops up to 32 nodes from the top (the deepest: the walk stays depth-first
+// at the scale of a warp, which bounds the stack by 32 entries per level),
+// tests both children of each, and pushes the entered internal children and
+// queues the entered leaves.  When the queue holds 64 or more triangles, or
+// the stack is empty, the queued leaves still in front of the closest hit are
+// tested 32 (leaf, triangle) pairs at a time and the warp minimum of the
+// (t, id) keys becomes the shared bound.  The closest hit under the tie rule
+// does not depend on the order of the tests, so the hit equals traverse()'s.
+// For any_hit the walk stops at the first accepted hit.
+constexpr int kWideStack = 1024;   // entries per warp (a depth-26 tree needs at most 26 x 32 + 32)
+constexpr int kWideQueue = 128;    // queued leaves per warp
+constexpr int kWideWarps = 4;          // blocks of at most 128 threads
+
+struct WideSmem {
+    uint32_t node[kWideWarps][kWideStack];
+    float t0[kWideWarps][kWideStack];
+    int32_t qpos[kWideWarps][kWideQueue];
+    int32_t qcnt[kWideWarps][kWideQueue];
+    float qt0[kWideWarps][kWideQueue];
+    uint32_t qincl[kWideWarps][kWideQueue];
+};
+
+// One block-wide instance shared by both instantiations of traverse_wide.
+__device__ __forceinline__ WideSmem& wide_smem() {
+    __shared__ WideSmem sm;
+    return sm;
+}
+
 template <bool EXACT>
 __device__ __forceinline__ Hit traverse_wide(const RayState& r, const TreeRef& tr_, bool any_hit) {
     constexpr uint32_t kFull = 0xffffffffu;
+    WideSmem& sm = wide_smem();
     const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;  // warp in block (blocks of at most 256 threads)
-    __shared__ uint32_t s_gn[8][32];
-    __shared__ float s_gt[8][32];
+    const int wib = threadIdx.x >> 5;
+    uint32_t* snode = sm.node[wib];
+    float* st0 = sm.t0[wib];
+    int32_t* qpos = sm.qpos[wib];
+    int32_t* qcnt = sm.qcnt[wib];
+    float* qt0 = sm.qt0[wib];
+    uint32_t* qincl = sm.qincl[wib];
     const uint64_t init = hit_key(r.tmax, 0);
-    Best b;
-    b.key = init;
-    b.id = -1;
-    b.u = -1.0f;
-    b.v = -1.0f;
-    b.t = r.tmax;
-    uint64_t bound = init;
-    uint32_t nbox = 0, ntri = 0;
-    uint32_t stack_node[kStackSize];
-    float stack_t0[kStackSize];
-    uint32_t sp = 0, base = 0;
-    NodeBox cur;
-    cur.a = make_float4(0.f, 0.f, 0.f, 0.f);
-    cur.b = cur.a;
-    bool have = false;
-    uint32_t node = 1;
-    if (lane == 0) {
-        cur = load_node(tr_.nodes, 1);
+    uint64_t best = init;  // uniform across the warp
+    float bu = -1.0f, bv = -1.0f, bt = r.tmax;
+    int size = 0, nq = 0, qtris = 0;  // uniform
+    bool stop = false;
+    // root
+    {
+        const NodeBox root = load_node(tr_.nodes, 1);
         float t0;
-        have = r.tmax > 0.0f && box_enter<EXACT>(r, cur.a.x, cur.a.y, cur.a.z, cur.a.w, cur.b.x, cur.b.y, r.tmax, &t0);
-    }
-    for (;;) {
-        bound = warp_min_u64(bound);
-        if (any_hit && bound < init) break;
-        // idle lanes take stacked subtrees of busy lanes, oldest (largest)
-        // first: the busy lanes' stack entries are numbered lane by lane and
-        // the r-th idle lane takes entry r, staged through shared memory
-        const uint32_t give = (have && sp != base) ? sp - base : 0u;
-        const uint32_t im = __ballot_sync(kFull, !have);
-        if (im && __any_sync(kFull, give != 0u)) {
-            uint32_t incl = give;
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const uint32_t y = __shfl_up_sync(kFull, incl, off);
-                if (lane >= off) incl += y;
-            }
-            const uint32_t total = __shfl_sync(kFull, incl, 31);
-            const uint32_t excl = incl - give;
-            const uint32_t npair = min((uint32_t)__popc(im), total);
-            if (give && excl < npair) {
-                const uint32_t taken = min(give, npair - excl);
-                for (uint32_t k = 0; k < taken; ++k) {
-                    s_gn[wib][excl + k] = stack_node[(base + k) & (kStackSize - 1)];
-                    s_gt[wib][excl + k] = stack_t0[(base + k) & (kStackSize - 1)];
+        const bool enter = r.tmax > 0.0f &&
+                           box_enter<EXACT>(r, root.a.x, root.a.y, root.a.z, root.a.w, root.b.x, root.b.y, r.tmax, &t0);
+        if (enter) {
+            if (__float_as_int(root.b.z) & 4) {
+                if (lane == 0) {
+                    qpos[0] = __float_as_int(root.b.w);
+                    qcnt[0] = __float_as_int(root.b.z) >> 3;
+                    qt0[0] = t0;
                 }
-                base += taken;
-            }
-            __syncwarp();
-            const uint32_t irank = __popc(im & ((1u << lane) - 1u));
-            if (!have && irank < npair) {
-                const uint32_t gn = s_gn[wib][irank];
-                const float gt = s_gt[wib][irank];
-                if (!(gt > key_t(bound))) {
-                    node = gn;
-                    cur = load_node(tr_.nodes, gn);
-                    have = true;
+                nq = 1;
+                qtris = __float_as_int(root.b.z) >> 3;
+            } else {
+                if (lane == 0) {
+                    snode[0] = 1;
+                    st0[0] = t0;
                 }
+                size = 1;
             }
-            __syncwarp();
         }
-        if (!__any_sync(kFull, have)) break;
-        if (have) have = descend<EXACT, false>(tr_, r, key_t(bound), node, cur, stack_node, stack_t0, sp, base, nbox);
-        __syncwarp();
-        leaf_phase<false>(tr_, r, have, cur, bound, b, ntri);
-        if (have) have = pop_node(tr_, key_t(bound), node, cur, stack_node, stack_t0, sp, base);
     }
-    // the warp minimum of the lanes' own hits, with the winner's t, u, v
-    const uint64_t kmin = warp_min_u64(b.key);
-    const uint32_t wm = __ballot_sync(kFull, b.key == kmin);
-    const int w = __ffs(wm) - 1;
+    __syncwarp();
+    while (!stop && (size > 0 || nq > 0)) {
+        // test the queued leaves
+        if (nq > 0 && (size == 0 || qtris >= 64 || nq > kWideQueue - 64)) {
+            const float bound_t = key_t(best);
+            // drop leaves now behind the closest hit; prefix of the kept sizes
+            uint32_t run = 0;
+            for (int q0 = 0; q0 < nq; q0 += 32) {
+                const int q = q0 + lane;
+                int c = 0;
+                if (q < nq) {
+                    c = qcnt[q];
+                    if (qt0[q] > bound_t || qpos[q] < 0 || c < 0 || (uint32_t)qpos[q] + (uint32_t)c > tr_.n) c = 0;
+                }
+                uint32_t incl = (uint32_t)c;
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const uint32_t y = __shfl_up_sync(kFull, incl, off);
+                    if (lane >= off) incl += y;
+                }
+                if (q < nq) qincl[q] = run + incl;
+                run += __shfl_sync(kFull, incl, 31);
+            }
+            __syncwarp();
+            const uint32_t total = run;
+            for (uint32_t base = 0; base < total; base += 32) {
+                const uint32_t p = base + lane;
+                uint64_t key = ~0ull;
+                float kt = 0.0f, ku = 0.0f, kv = 0.0f;
+                if (p < total) {
+                    // queued leaf holding pair p: the first with inclusive prefix > p
+                    int lo = 0, hi = nq - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (qincl[mid] > p) hi = mid; else lo = mid + 1;
+                    }
+                    const uint32_t ex = lo > 0 ? qincl[lo - 1] : 0u;
+                    const float4* tp = tr_.tris + 3 * (size_t)(qpos[lo] + (int)(p - ex));
+                    const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                    const int id = __float_as_int(a.w);
+                    float u, v, t;
+                    if (id != r.exclude && tri_test(r, a, b, c, &u, &v, &t)) {
+                        const uint64_t k = hit_key(t, id);
+                        if (k < best) {
+                            key = k;
+                            kt = t;
+                            ku = u;
+                            kv = v;
+                        }
+                    }
+                }
+                const uint64_t kmin = warp_min_u64(key);
+                if (kmin < best) {
+                    const int w = __ffs(__ballot_sync(kFull, key == kmin)) - 1;
+                    best = kmin;
+                    bt = __shfl_sync(kFull, kt, w);
+                    bu = __shfl_sync(kFull, ku, w);
+                    bv = __shfl_sync(kFull, kv, w);
+                    if (any_hit) break;
+                }
+            }
+            nq = 0;
+            qtris = 0;
+            __syncwarp();
+            if (any_hit && best < init) stop = true;
+            continue;
+        }
+        // pop up to 32 internal nodes from the top
+        const int k = min(32, size);
+        const float bound_t = key_t(best);
+        uint32_t nd = 0;
+        bool live = false;
+        if (lane < k) {
+            nd = snode[size - 1 - lane];
+            live = !(st0[size - 1 - lane] > bound_t);
+        }
+        size -= k;
+        __syncwarp();
+        // children of each popped node
+        bool push_l = false, push_r = false, leaf_l = false, leaf_r = false;
+        float tl = 0.0f, tr = 0.0f;
+        float4 l1 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = l1;
+        uint32_t c0 = 0;
+        if (live) {
+            c0 = nd << 1;
+            if (c0 + 1 >= tr_.num_nodes) {
+                atomicOr(tr_.err, RT_DEVERR_BOUNDS);
+            } else {
+                const float4* p = reinterpret_cast<const float4*>(tr_.nodes + c0);
+                const float4 l0 = __ldg(p), r0 = __ldg(p + 2);
+                l1 = __ldg(p + 1);
+                r1 = __ldg(p + 3);
+                push_l = box_enter<EXACT>(r, l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, bound_t, &tl);
+                push_r = box_enter<EXACT>(r, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, bound_t, &tr);
+                leaf_l = push_l && (__float_as_int(l1.z) & 4);
+                leaf_r = push_r && (__float_as_int(r1.z) & 4);
+            }
+        }
+        // internal children onto the stack, leaves into the queue
+        const uint32_t lt = (1u << lane) - 1u;
+        const int ni = (push_l && !leaf_l) + (push_r && !leaf_r);
+        const int nl = leaf_l + leaf_r;
+        const uint32_t ib0 = __ballot_sync(kFull, ni >= 1), ib1 = __ballot_sync(kFull, ni >= 2);
+        const uint32_t lb0 = __ballot_sync(kFull, nl >= 1), lb1 = __ballot_sync(kFull, nl >= 2);
+        const int ioff = size + __popc(ib0 & lt) + __popc(ib1 & lt);
+        const int loff = nq + __popc(lb0 & lt) + __popc(lb1 & lt);
+        const int itotal = __popc(ib0) + __popc(ib1), ltotal = __popc(lb0) + __popc(lb1);
+        if (size + itotal > kWideStack) {  // cannot happen with depth <= 26; stop rather than overflow
+            if (lane == 0) atomicOr(tr_.err, RT_DEVERR_BOUNDS);
+            stop = true;
+            break;
+        }
+        int io = ioff, lo_ = loff;
+        if (push_l) {
+            if (leaf_l) {
+                qpos[lo_] = __float_as_int(l1.w);
+                qcnt[lo_] = __float_as_int(l1.z) >> 3;
+                qt0[lo_] = tl;
+                ++lo_;
+            } else {
+                snode[io] = c0;
+                st0[io] = tl;
+                ++io;
+            }
+        }
+        if (push_r) {
+            if (leaf_r) {
+                qpos[lo_] = __float_as_int(r1.w);
+                qcnt[lo_] = __float_as_int(r1.z) >> 3;
+                qt0[lo_] = tr;
+            } else {
+                snode[io] = c0 | 1u;
+                st0[io] = tr;
+            }
+        }
+        int lt_tris = (leaf_l ? (__float_as_int(l1.z) >> 3) : 0) + (leaf_r ? (__float_as_int(r1.z) >> 3) : 0);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) lt_tris += __shfl_xor_sync(kFull, lt_tris, off);
+        size += itotal;
+        nq += ltotal;
+        qtris += lt_tris;
+        __syncwarp();
+    }
     Hit h;
-    h.id = __shfl_sync(kFull, b.id, w);
-    h.u = __shfl_sync(kFull, b.u, w);
-    h.v = __shfl_sync(kFull, b.v, w);
-    h.t = __shfl_sync(kFull, b.t, w);
+    if (best < init) {
+        h.id = (int)(uint32_t)best;
+        h.t = bt;
+        h.u = bu;
+        h.v = bv;
+    } else {
+        h.id = -1;
+        h.u = -1.0f;
+        h.v = -1.0f;
+        h.t = r.tmax;
+    }
+    __syncwarp();
     return h;
 }
 
