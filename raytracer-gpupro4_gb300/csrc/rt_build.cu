@@ -676,7 +676,7 @@ __global__ void __launch_bounds__(kEmitThreads) k_emit_leaves(const uint32_t* __
     // pre-gather in sorted order (A.xyz,id | B.xyz,0 | C.xyz,0), lane-contiguous
     // so that the 48-byte records of a warp are written as one contiguous run
     const uint32_t tbase = blockIdx.x * kEmitTile;
-#pragma unroll 2
+#pragma unroll 4
     for (int q = 0; q < kEmitItems; ++q) {
         const uint32_t k = tbase + q * kEmitThreads + threadIdx.x;
         if (k < n) {
@@ -738,8 +738,8 @@ __device__ __forceinline__ void leaf_boxes(int64_t gpos, int cnt, const float4* 
     const uint32_t total = __shfl_sync(kFull, incl, 31);
     const uint32_t excl = incl - (uint32_t)cnt;
     const uint32_t glo = (uint32_t)gpos, ghi = (uint32_t)(gpos >> 32);
-    for (uint32_t base = 0; base < total; base += 32) {
-        const uint32_t p = base + lane;
+    // owner of pair p and the address of its triangle
+    auto locate = [&](uint32_t p, int* owner) -> const float4* {
         int o = 0;
 #pragma unroll
         for (int step = 16; step > 0; step >>= 1) {
@@ -749,10 +749,35 @@ __device__ __forceinline__ void leaf_boxes(int64_t gpos, int cnt, const float4* 
         const uint32_t o_excl = __shfl_sync(kFull, excl, o);
         const int64_t o_gpos =
             (int64_t)(((uint64_t)__shfl_sync(kFull, ghi, o) << 32) | __shfl_sync(kFull, glo, o));
+        *owner = o;
+        return sorted_tris + 3 * (o_gpos + (int64_t)(p - o_excl));
+    };
+    // software pipelined: the next batch's triangles are loaded while the
+    // current batch is reduced
+    int on = 0;
+    float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = na, nc = na;
+    if (total > 0) {
+        const float4* tp = locate(lane, &on);
+        if ((uint32_t)lane < total) {
+            na = __ldg(tp);
+            nb = __ldg(tp + 1);
+            nc = __ldg(tp + 2);
+        }
+    }
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t p = base + lane;
+        const int o = on;
+        const float4 a = na, b = nb, c = nc;
+        if (base + 32 < total) {
+            const float4* tp = locate(p + 32, &on);
+            if (p + 32 < total) {
+                na = __ldg(tp);
+                nb = __ldg(tp + 1);
+                nc = __ldg(tp + 2);
+            }
+        }
         float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
         if (p < total) {
-            const float4* tp = sorted_tris + 3 * (o_gpos + (int64_t)(p - o_excl));
-            const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
             lo[0] = fminf(a.x, fminf(b.x, c.x)); hi[0] = fmaxf(a.x, fmaxf(b.x, c.x));
             lo[1] = fminf(a.y, fminf(b.y, c.y)); hi[1] = fmaxf(a.y, fmaxf(b.y, c.y));
             lo[2] = fminf(a.z, fminf(b.z, c.z)); hi[2] = fmaxf(a.z, fmaxf(b.z, c.z));
