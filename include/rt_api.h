@@ -191,6 +191,13 @@ rt_status rt_trace_rays(rt_ctx* ctx, const rt_lbvh* lbvh, const rt_ray* d_rays, 
 rt_status rt_render_frame_host(rt_ctx* ctx, rt_lbvh* lbvh, const float* h_tris, uint32_t n,
                                const rt_camera* cam, const float light[3], rt_hit* h_primary,
                                uint8_t* h_vis, rt_hit* h_mirror);
+/* The same frame, queued on the context stream without waiting: the host
+ * buffers must stay untouched until rt_ctx_sync (pinned memory makes the
+ * copies asynchronous).  Two contexts on two streams, used for alternate
+ * frames, overlap one frame's copies with the other frame's kernels. */
+rt_status rt_render_frame_host_async(rt_ctx* ctx, rt_lbvh* lbvh, const float* h_tris, uint32_t n,
+                                     const rt_camera* cam, const float light[3], rt_hit* h_primary,
+                                     uint8_t* h_vis, rt_hit* h_mirror);
 
 /* ---- one frame as a CUDA graph ------------------------------------- */
 /* The dynamic per-frame path (RayTracerCS::Render with dynamic=1,

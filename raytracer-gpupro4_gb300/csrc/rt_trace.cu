@@ -418,13 +418,13 @@ extern "C" rt_status rt_trace_rays(rt_ctx* ctx, const rt_lbvh* l, const rt_ray* 
     return launch_heavy(ctx, sp, a);
 }
 
-extern "C" rt_status rt_render_frame_host(rt_ctx* ctx, rt_lbvh* l, const float* h_tris, uint32_t n,
-                                          const rt_camera* cam, const float light[3], rt_hit* h_primary,
-                                          uint8_t* h_vis, rt_hit* h_mirror) {
+static rt_status render_frame_host(rt_ctx* ctx, rt_lbvh* l, const float* h_tris, uint32_t n, const rt_camera* cam,
+                                   const float light[3], rt_hit* h_primary, uint8_t* h_vis, rt_hit* h_mirror,
+                                   bool sync, const char* who) {
     if (!ctx) return RT_ERR_INVALID;
-    if (!l || !h_tris || !cam || !light) return rt_fail(ctx, RT_ERR_INVALID, "rt_render_frame_host: null argument");
+    if (!l || !h_tris || !cam || !light) return rt_fail(ctx, RT_ERR_INVALID, "%s: null argument", who);
     const size_t px = (size_t)cam->width * cam->height;
-    if (px == 0 || px > (1ull << 31)) return rt_fail(ctx, RT_ERR_INVALID, "rt_render_frame_host: bad image size");
+    if (px == 0 || px > (1ull << 31)) return rt_fail(ctx, RT_ERR_INVALID, "%s: bad image size", who);
     if (px > l->f_pixels) {  // frame buffers grow on the first call at a new size
         RT_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         if (l->f_primary) cudaFree(l->f_primary);
@@ -447,8 +447,21 @@ extern "C" rt_status rt_render_frame_host(rt_ctx* ctx, rt_lbvh* l, const float* 
     if (h_primary) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_primary, l->f_primary, sizeof(rt_hit) * px, cudaMemcpyDeviceToHost, st));
     if (h_vis) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_vis, l->f_vis, px, cudaMemcpyDeviceToHost, st));
     if (h_mirror) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_mirror, l->f_mirror, sizeof(rt_hit) * px, cudaMemcpyDeviceToHost, st));
-    RT_CHECK_CUDA(ctx, cudaStreamSynchronize(st));
+    if (sync) RT_CHECK_CUDA(ctx, cudaStreamSynchronize(st));
     return RT_OK;
+}
+
+extern "C" rt_status rt_render_frame_host(rt_ctx* ctx, rt_lbvh* l, const float* h_tris, uint32_t n,
+                                          const rt_camera* cam, const float light[3], rt_hit* h_primary,
+                                          uint8_t* h_vis, rt_hit* h_mirror) {
+    return render_frame_host(ctx, l, h_tris, n, cam, light, h_primary, h_vis, h_mirror, true, "rt_render_frame_host");
+}
+
+extern "C" rt_status rt_render_frame_host_async(rt_ctx* ctx, rt_lbvh* l, const float* h_tris, uint32_t n,
+                                                const rt_camera* cam, const float light[3], rt_hit* h_primary,
+                                                uint8_t* h_vis, rt_hit* h_mirror) {
+    return render_frame_host(ctx, l, h_tris, n, cam, light, h_primary, h_vis, h_mirror, false,
+                             "rt_render_frame_host_async");
 }
 
 // ---------------------------------------------------------------------------

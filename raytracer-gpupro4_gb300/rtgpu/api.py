@@ -220,11 +220,14 @@ class RayTracer:
         return (hits, st) if stats else hits
 
     def render_frame_host(self, lbvh: LBVH, tris: np.ndarray, cam: L.Camera, light, primary: np.ndarray,
-                          vis: np.ndarray, mirror: np.ndarray):
+                          vis: np.ndarray, mirror: np.ndarray, wait: bool = True):
+        """One frame from and to host buffers; wait=False queues it on the
+        context stream (rt_render_frame_host_async; the buffers stay in use
+        until Context.sync)."""
         lf = (C.c_float * 3)(*light)
-        L.check(L.lib().rt_render_frame_host(self.ctx.h, lbvh.h, _host_ptr(tris), len(tris), C.byref(cam), lf,
-                                             _host_ptr(primary), _host_ptr(vis), _host_ptr(mirror)),
-                self.ctx.h, "rt_render_frame_host")
+        fn = L.lib().rt_render_frame_host if wait else L.lib().rt_render_frame_host_async
+        L.check(fn(self.ctx.h, lbvh.h, _host_ptr(tris), len(tris), C.byref(cam), lf, _host_ptr(primary),
+                   _host_ptr(vis), _host_ptr(mirror)), self.ctx.h, "rt_render_frame_host")
 
     def pathtrace(self, lbvh: LBVH, albedo: torch.Tensor, emission: torch.Tensor, cam: L.Camera, spp: int,
                   bounces: int, seed: int, sky=(1.0, 1.0, 1.0), out: torch.Tensor | None = None) -> torch.Tensor:

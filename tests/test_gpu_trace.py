@@ -144,8 +144,9 @@ def test_render_frame_host_equals_device_path(gpu_ctx, torus_scene):
 
 
 def test_shared_traversal_matches_oracle(gpu_ctx, oracle_mod, torus_scene):
-    """The production traversal (no counters: idle lanes take over stacked
-    subtrees of busy lanes) gives the oracle's hits bit for bit."""
+    """The production traversal (no counters: serial and pooled leaf parts,
+    rays over the work budget handed to the warp-per-ray pass) gives the
+    oracle's hits bit for bit."""
     from rtgpu import scenes
     from rtgpu.api import RayTracer, hits_to_numpy
     tris, lb, dt, nodes, ids = torus_scene
@@ -244,3 +245,36 @@ def test_heavy_ray_handover_generic_rays(gpu_ctx, oracle_mod, any_hit):
         assert np.array_equal(g["id"] >= 0, oh["id"] >= 0)
     else:
         assert_hits_equal(g, oh, "rays")
+
+
+def test_render_frame_host_async_two_streams(gpu_ctx, torus_scene):
+    """rt_render_frame_host_async on two contexts / streams, alternate frames,
+    gives the synchronous call's results."""
+    import torch
+    from rtgpu import scenes
+    from rtgpu._lib import HIT_DTYPE
+    from rtgpu.api import LBVH, Context, RayTracer
+    tris, lb, dt, nodes, ids = torus_scene
+    cam = scenes.torus_camera(256, 160)
+    npx = cam.width * cam.height
+    rt = RayTracer(gpu_ctx)
+    lbs = LBVH(gpu_ctx, len(tris), 20)
+    ref = [np.zeros(npx, HIT_DTYPE), np.zeros(npx, np.uint8), np.zeros(npx, HIT_DTYPE)]
+    rt.render_frame_host(lbs, tris, cam, scenes.TORUS_LIGHT, *ref)
+    lanes = []
+    for _ in range(2):
+        ctx = Context(0, stream=torch.cuda.Stream())
+        outs = [torch.empty(npx * 4, dtype=torch.int32).pin_memory(), torch.empty(npx, dtype=torch.uint8).pin_memory(),
+                torch.empty(npx * 4, dtype=torch.int32).pin_memory()]
+        lanes.append((ctx, LBVH(ctx, len(tris), 20), RayTracer(ctx), outs))
+    soup = torch.from_numpy(tris).pin_memory().numpy()
+    for k in range(4):
+        ctx, lbq, rtq, outs = lanes[k % 2]
+        ctx.sync()
+        rtq.render_frame_host(lbq, soup, cam, scenes.TORUS_LIGHT, outs[0].numpy().view(HIT_DTYPE), outs[1].numpy(),
+                              outs[2].numpy().view(HIT_DTYPE), wait=False)
+    for ctx, lbq, rtq, outs in lanes:
+        ctx.check()
+        assert np.array_equal(outs[0].numpy().view(HIT_DTYPE), ref[0])
+        assert np.array_equal(outs[1].numpy(), ref[1])
+        assert np.array_equal(outs[2].numpy().view(HIT_DTYPE), ref[2])
