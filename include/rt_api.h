@@ -94,6 +94,12 @@ rt_status rt_ctx_set_stream(rt_ctx* ctx, void* stream);
  * handed to a second kernel that traces it with a whole warp (same hit).
  * 0 turns the hand-over off.  Default 384.  Path tracing never hands over. */
 rt_status rt_ctx_set_trace_budget(rt_ctx* ctx, uint32_t budget);
+/* Heavy-first tile order: for each trace kind in `kinds` (bit 0 primary
+ * rays, bit 1 shadow / mirror rays, bit 2 rt_trace_rays) a call first
+ * traces the tiles that were the most expensive in the previous call of the
+ * same kind on this context, then the rest in image order.  Results do not
+ * depend on the order.  Default: primary rays only (1). */
+rt_status rt_ctx_set_tile_order(rt_ctx* ctx, uint32_t kinds);
 rt_status rt_ctx_sync(rt_ctx* ctx);
 /* Synchronises, then reports a device-side error flag raised since the
  * last check (RT_ERR_TIMEOUT, RT_ERR_NONFINITE) and clears it. */

@@ -46,9 +46,12 @@ extern "C" rt_status rt_ctx_create(int device, void* stream, rt_ctx** out) {
     if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
         cudaMalloc((void**)&c->d_words, 64 * sizeof(uint32_t)) != cudaSuccess ||
         cudaMemset(c->d_words, 0, 64 * sizeof(uint32_t)) != cudaSuccess ||
-        cudaMalloc((void**)&c->d_spill, sizeof(uint32_t) * kSpillCap) != cudaSuccess) {
+        cudaMalloc((void**)&c->d_spill, sizeof(uint32_t) * kSpillCap) != cudaSuccess ||
+        cudaMalloc((void**)&c->d_order, sizeof(uint32_t) * kOrderKinds * kOrderWords) != cudaSuccess ||
+        cudaMemset(c->d_order, 0, sizeof(uint32_t) * kOrderKinds * kOrderWords) != cudaSuccess) {
         if (c->d_words) cudaFree(c->d_words);
         if (c->d_spill) cudaFree(c->d_spill);
+        if (c->d_order) cudaFree(c->d_order);
         delete c;
         return RT_ERR_CUDA;
     }
@@ -63,6 +66,7 @@ extern "C" rt_status rt_ctx_destroy(rt_ctx* ctx) {
     if (!ctx) return RT_OK;
     if (ctx->d_words) cudaFree(ctx->d_words);
     if (ctx->d_spill) cudaFree(ctx->d_spill);
+    if (ctx->d_order) cudaFree(ctx->d_order);
     delete ctx;
     return RT_OK;
 }
@@ -76,6 +80,13 @@ extern "C" rt_status rt_ctx_set_stream(rt_ctx* ctx, void* stream) {
 extern "C" rt_status rt_ctx_set_trace_budget(rt_ctx* ctx, uint32_t budget) {
     if (!ctx) return RT_ERR_INVALID;
     ctx->trace_budget = budget;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_ctx_set_tile_order(rt_ctx* ctx, uint32_t kinds) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (kinds > 7u) return rt_fail(ctx, RT_ERR_INVALID, "rt_ctx_set_tile_order: kinds is a 3-bit mask");
+    ctx->tile_order = kinds;
     return RT_OK;
 }
 

@@ -87,6 +87,11 @@ constexpr uint32_t kMaxTris = (1u << 29);
 // hands the ray to the warp-per-ray kernel.
 constexpr uint32_t kSpillCap = 1u << 20;
 constexpr uint32_t kDefaultTraceBudget = 384;
+// Heavy-first tile order (TileOrder in rt_traverse.cuh): per trace kind two
+// lists of kOrderCap tiles and two bitmaps, in one allocation.
+constexpr uint32_t kOrderCap = 1u << 20;
+constexpr size_t kOrderWords = 2 * (size_t)kOrderCap + 2 * (size_t)(kOrderCap / 32);
+constexpr int kOrderKinds = 3;
 
 struct rt_ctx {
     int device = 0;
@@ -97,7 +102,9 @@ struct rt_ctx {
     uint32_t* d_spill_count = nullptr;  // heavy-ray list length (d_words[32])
     uint32_t* d_words = nullptr; // 64 device words
     uint32_t* d_spill = nullptr; // heavy-ray list, kSpillCap entries
+    uint32_t* d_order = nullptr; // heavy-first tile order, kOrderKinds x kOrderWords (parity / counts: d_words[40..])
     uint32_t trace_budget = kDefaultTraceBudget;  // 0: no hand-over
+    uint32_t tile_order = 1u;  // heavy-first tile order per kind: bit 0 primary, 1 shading, 2 generic rays
     int num_sms = 0;
 };
 

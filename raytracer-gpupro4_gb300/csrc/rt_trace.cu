@@ -40,8 +40,10 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_
                                                                  rt_hit* __restrict__ hits,
                                                                  uint32_t* __restrict__ stats, uint32_t* work,
                                                                  uint32_t num_tiles, Spill spill,
-                                                                 uint32_t* __restrict__ list) {
-    for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
+                                                                 uint32_t* __restrict__ list, TileOrder ord) {
+    const uint32_t wbuf = *ord.parity, rbuf = wbuf ^ 1u, heavy = min(ord.counts[rbuf], ord.cap);
+    for (uint32_t tile = next_ordered_tile(work, ord, rbuf, heavy, num_tiles); tile < num_tiles;
+         tile = next_ordered_tile(work, ord, rbuf, heavy, num_tiles)) {
         uint32_t i, j;
         const bool valid = tile_pixel(tile, threadIdx.x & 31, cam.width, cam.height, &i, &j);
         if (!valid) i = j = 0;  // lanes past the image edge only help the warp
@@ -62,6 +64,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_
                 stats[2 * p + 1] = nt;
             }
         }
+        record_tile_cost(ord, wbuf, tile, nb + nt);
     }
 }
 
@@ -125,7 +128,7 @@ __device__ __forceinline__ void secondary_pixel(const TreeRef& tr, const float* 
                                                 uint8_t* __restrict__ vis, rt_hit* __restrict__ mirror,
                                                 uint32_t* __restrict__ sstats, uint32_t* __restrict__ mstats,
                                                 bool valid, uint32_t i, uint32_t j, const Spill* spill,
-                                                uint32_t* __restrict__ list) {
+                                                uint32_t* __restrict__ list, uint32_t* tests = nullptr) {
     const size_t p = (size_t)j * cam.width + i;
     const ShadeRays s = shade_rays(soup, cam, lx, ly, lz, ph, valid, i, j, mirror != nullptr);
     uint32_t snb = 0, snt = 0, mnb = 0, mnt = 0;
@@ -152,6 +155,7 @@ __device__ __forceinline__ void secondary_pixel(const TreeRef& tr, const float* 
         if (sstats) { sstats[2 * p] = snb; sstats[2 * p + 1] = snt; }
         if (mstats) { mstats[2 * p] = mnb; mstats[2 * p + 1] = mnt; }
     }
+    if (tests) *tests = snb + snt + mnb + mnt;
 }
 
 template <bool STATS>
@@ -159,15 +163,19 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_secondary(
     TreeRef tr, const float* __restrict__ soup, rt_camera cam, float lx, float ly, float lz,
     const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis, rt_hit* __restrict__ mirror,
     uint32_t* __restrict__ sstats, uint32_t* __restrict__ mstats, uint32_t* work, uint32_t num_tiles, Spill spill,
-    uint32_t* __restrict__ list) {
-    for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
+    uint32_t* __restrict__ list, TileOrder ord) {
+    const uint32_t wbuf = *ord.parity, rbuf = wbuf ^ 1u, heavy = min(ord.counts[rbuf], ord.cap);
+    for (uint32_t tile = next_ordered_tile(work, ord, rbuf, heavy, num_tiles); tile < num_tiles;
+         tile = next_ordered_tile(work, ord, rbuf, heavy, num_tiles)) {
         uint32_t i, j;
         const bool valid = tile_pixel(tile, threadIdx.x & 31, cam.width, cam.height, &i, &j);
         if (!valid) i = j = 0;
         int4 ph = make_int4(-1, 0, 0, 0);
         if (valid) ph = __ldg(reinterpret_cast<const int4*>(prim + (size_t)j * cam.width + i));
+        uint32_t tests = 0;
         secondary_pixel<STATS>(tr, soup, cam, lx, ly, lz, ph, vis, mirror, sstats, mstats, valid, i, j, &spill,
-                               list);
+                               list, &tests);
+        record_tile_cost(ord, wbuf, tile, tests);
     }
 }
 
@@ -184,9 +192,12 @@ template <bool STATS>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_rays(TreeRef tr, const rt_ray* __restrict__ rays, uint32_t n,
                                                               int any_hit, rt_hit* __restrict__ hits,
                                                               uint32_t* __restrict__ stats, uint32_t* work,
-                                                              Spill spill, uint32_t* __restrict__ list) {
+                                                              Spill spill, uint32_t* __restrict__ list,
+                                                              TileOrder ord) {
     const uint32_t num_tiles = (n + 31) / 32;
-    for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
+    const uint32_t wbuf = *ord.parity, rbuf = wbuf ^ 1u, heavy = min(ord.counts[rbuf], ord.cap);
+    for (uint32_t tile = next_ordered_tile(work, ord, rbuf, heavy, num_tiles); tile < num_tiles;
+         tile = next_ordered_tile(work, ord, rbuf, heavy, num_tiles)) {
         const uint32_t k = tile * 32 + (threadIdx.x & 31);
         const bool valid = k < n;
         const RayState r = load_ray(rays, k, valid);
@@ -204,6 +215,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_rays(TreeRef tr, const 
                 stats[2 * k + 1] = nt;
             }
         }
+        record_tile_cost(ord, wbuf, tile, nb + nt);
     }
 }
 
@@ -317,6 +329,44 @@ rt_status launch_heavy(rt_ctx* ctx, const Spill& sp, HeavyArgs a) {
     return RT_OK;
 }
 
+__global__ void k_order_begin(TileOrder o) {
+    __shared__ uint32_t s_w;
+    if (threadIdx.x == 0) {
+        const uint32_t w = *o.parity ^ 1u;
+        *o.parity = w;
+        s_w = w;
+    }
+    __syncthreads();
+    const uint32_t w = s_w;
+    const uint32_t n = min(o.counts[w], o.cap);
+    __syncthreads();
+    // the buffer this call writes was read two calls ago: clear its bits
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint32_t t = o.lists[(size_t)w * o.cap + i];
+        if (t < o.cap) o.bits[(size_t)w * (o.cap / 32) + t / 32] = 0u;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) o.counts[w] = 0u;
+}
+
+// Tile order of one trace kind (0 primary, 1 shading, 2 generic rays),
+// advanced to this call; enabled == false gives image order (cap 0: no list
+// is read or written).
+rt_status order_begin(rt_ctx* ctx, int kind, bool enabled, TileOrder* out) {
+    TileOrder o;
+    o.cap = enabled ? kOrderCap : 0u;
+    o.parity = ctx->d_words + 40 + 4 * kind;
+    o.counts = o.parity + 1;
+    o.lists = ctx->d_order + (size_t)kind * kOrderWords;
+    o.bits = o.lists + 2 * (size_t)kOrderCap;
+    if (enabled) {
+        k_order_begin<<<1, 256, 0, ctx->stream>>>(o);
+        RT_CHECK_LAUNCH(ctx, "k_order_begin");
+    }
+    *out = o;
+    return RT_OK;
+}
+
 HeavyArgs heavy_args(rt_ctx* ctx, const rt_lbvh* l) {
     HeavyArgs a;
     memset(&a, 0, sizeof(a));
@@ -334,16 +384,18 @@ extern "C" rt_status rt_trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_ca
     if ((s = reset_work(ctx, kWorkPrimary)) != RT_OK) return s;
     const Spill sp = spill_of(ctx, !d_stats && (uint64_t)cam->width * cam->height <= kHeavyIndexMask);
     if ((s = reset_spill(ctx, sp)) != RT_OK) return s;
+    TileOrder ord;
+    if ((s = order_begin(ctx, 0, ctx->tile_order & 1u, &ord)) != RT_OK) return s;
     const uint32_t tiles = pixel_tiles(cam);
     uint32_t* work = ctx->d_work + kWorkPrimary;
     if (d_stats) {
         auto k = k_trace_primary<true>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), *cam, d_hits, d_stats, work, tiles, sp, ctx->d_spill);
+            tree_ref(ctx, l), *cam, d_hits, d_stats, work, tiles, sp, ctx->d_spill, ord);
     } else {
         auto k = k_trace_primary<false>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), *cam, d_hits, nullptr, work, tiles, sp, ctx->d_spill);
+            tree_ref(ctx, l), *cam, d_hits, nullptr, work, tiles, sp, ctx->d_spill, ord);
     }
     RT_CHECK_LAUNCH(ctx, "k_trace_primary");
     HeavyArgs a = heavy_args(ctx, l);
@@ -363,18 +415,20 @@ extern "C" rt_status rt_trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const
     const bool stats = d_shadow_stats || d_mirror_stats;
     const Spill sp = spill_of(ctx, !stats && (uint64_t)cam->width * cam->height <= kHeavyIndexMask);
     if ((s = reset_spill(ctx, sp)) != RT_OK) return s;
+    TileOrder ord;
+    if ((s = order_begin(ctx, 1, ctx->tile_order & 2u, &ord)) != RT_OK) return s;
     const uint32_t tiles = pixel_tiles(cam);
     uint32_t* work = ctx->d_work + kWorkSecondary;
     if (stats) {
         auto k = k_trace_secondary<true>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
             tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_vis, d_mirror,
-            d_shadow_stats, d_mirror_stats, work, tiles, sp, ctx->d_spill);
+            d_shadow_stats, d_mirror_stats, work, tiles, sp, ctx->d_spill, ord);
     } else {
         auto k = k_trace_secondary<false>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
             tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_vis, d_mirror, nullptr,
-            nullptr, work, tiles, sp, ctx->d_spill);
+            nullptr, work, tiles, sp, ctx->d_spill, ord);
     }
     RT_CHECK_LAUNCH(ctx, "k_trace_secondary");
     HeavyArgs a = heavy_args(ctx, l);
@@ -399,16 +453,18 @@ extern "C" rt_status rt_trace_rays(rt_ctx* ctx, const rt_lbvh* l, const rt_ray* 
     if (s != RT_OK) return s;
     const Spill sp = spill_of(ctx, !d_stats && n <= kHeavyIndexMask);
     if ((s = reset_spill(ctx, sp)) != RT_OK) return s;
+    TileOrder ord;
+    if ((s = order_begin(ctx, 2, ctx->tile_order & 4u, &ord)) != RT_OK) return s;
     const uint32_t tiles = (n + 31) / 32;
     uint32_t* work = ctx->d_work + kWorkRays;
     if (d_stats) {
         auto k = k_trace_rays<true>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), d_rays, n, any_hit, d_hits, d_stats, work, sp, ctx->d_spill);
+            tree_ref(ctx, l), d_rays, n, any_hit, d_hits, d_stats, work, sp, ctx->d_spill, ord);
     } else {
         auto k = k_trace_rays<false>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), d_rays, n, any_hit, d_hits, nullptr, work, sp, ctx->d_spill);
+            tree_ref(ctx, l), d_rays, n, any_hit, d_hits, nullptr, work, sp, ctx->d_spill, ord);
     }
     RT_CHECK_LAUNCH(ctx, "k_trace_rays");
     HeavyArgs a = heavy_args(ctx, l);

@@ -443,10 +443,8 @@ __device__ __forceinline__ Hit traverse(const RayState& r, bool active, const Tr
             }
         }
     }
-    if (STATS) {
-        *nbox_out = nbox;
-        *ntri_out = ntri;
-    }
+    if (nbox_out) *nbox_out = nbox;
+    if (ntri_out) *ntri_out = ntri;
     if (slot_out) *slot_out = slot;
     Hit h;
     h.id = b.id;
@@ -747,6 +745,58 @@ __device__ __forceinline__ bool tile_pixel(uint32_t tile, uint32_t lane, uint32_
     *i = tx * 8 + (lane & 7);
     *j = ty * 4 + (lane >> 3);
     return *i < w && *j < h;
+}
+
+// Heavy-first tile order.  A trace call records the tiles whose rays spent
+// more than kHeavyTileTests box + triangle tests in all (a list and a bitmap,
+// written by call c into buffer w = parity); call c + 1 hands those tiles out
+// first (buffer 1 - w), then every other tile in image order, skipping the
+// ones already handed out.  Frames are coherent, so the tiles that made the
+// last call's tail start first; the order changes no result, and a stale or
+// foreign list (another image, another scene) only changes the order: every
+// tile is still traced exactly once.  The parity word is flipped on the
+// device (k_order_begin), so a replayed CUDA graph alternates too.
+constexpr uint32_t kHeavyTileTests = 4096;
+
+struct TileOrder {
+    uint32_t* parity;      // device word: the buffer this call writes
+    uint32_t* lists;       // 2 x cap tile indices
+    uint32_t* counts;      // 2 words
+    uint32_t* bits;        // 2 x (cap / 32) words
+    uint32_t cap;
+};
+
+// Next tile of this warp (all lanes call; returns num_tiles when done).
+__device__ __forceinline__ uint32_t next_ordered_tile(uint32_t* work, const TileOrder& ord, uint32_t rbuf,
+                                                      uint32_t heavy, uint32_t num_tiles) {
+    for (;;) {
+        const uint32_t v = next_tile(work);
+        if (v < heavy) {
+            const uint32_t t = __ldg(ord.lists + (size_t)rbuf * ord.cap + v);
+            if (t < num_tiles) return t;
+            continue;  // a tile of another image
+        }
+        const uint32_t t = v - heavy;
+        if (t >= num_tiles) return num_tiles;
+        if (t < ord.cap && heavy > 0 && ((__ldg(ord.bits + (size_t)rbuf * (ord.cap / 32) + t / 32) >> (t % 32)) & 1u))
+            continue;  // handed out first
+        return t;
+    }
+}
+
+// Records tile t as heavy for the next call when the warp's tests exceed the
+// threshold (lane 0 of the warp).
+__device__ __forceinline__ void record_tile_cost(const TileOrder& ord, uint32_t wbuf, uint32_t t, uint32_t tests) {
+    uint32_t sum = tests;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+    if ((threadIdx.x & 31) == 0 && sum > kHeavyTileTests && t < ord.cap) {
+        const uint32_t k = atomicAdd(ord.counts + wbuf, 1u);
+        if (k < ord.cap) {
+            ord.lists[(size_t)wbuf * ord.cap + k] = t;
+            atomicOr(ord.bits + (size_t)wbuf * (ord.cap / 32) + t / 32, 1u << (t % 32));
+        }
+    }
 }
 
 }  // namespace rt

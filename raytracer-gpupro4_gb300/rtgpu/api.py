@@ -62,6 +62,10 @@ class Context:
     def sync(self):
         L.check(L.lib().rt_ctx_sync(self.h), self.h, "rt_ctx_sync")
 
+    def set_tile_order(self, kinds: int):
+        """Heavy-first tile order per trace kind (bit 0 primary, 1 shading, 2 generic rays)."""
+        L.check(L.lib().rt_ctx_set_tile_order(self.h, int(kinds)), self.h, "rt_ctx_set_tile_order")
+
     def set_trace_budget(self, budget: int):
         """Box + triangle tests a ray may spend in the per-lane traversal before
         it is handed to the warp-per-ray pass (0: never)."""

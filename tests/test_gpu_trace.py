@@ -278,3 +278,29 @@ def test_render_frame_host_async_two_streams(gpu_ctx, torus_scene):
         assert np.array_equal(outs[0].numpy().view(HIT_DTYPE), ref[0])
         assert np.array_equal(outs[1].numpy(), ref[1])
         assert np.array_equal(outs[2].numpy().view(HIT_DTYPE), ref[2])
+
+
+def test_heavy_first_tile_order_keeps_results(gpu_ctx, oracle_mod, torus_scene):
+    """With the heavy-first order on for every kind, calls that follow calls
+    on other images (a foreign tile list) and on the same image (its own list)
+    still give the oracle's results."""
+    from rtgpu import scenes
+    from rtgpu.api import RayTracer, hits_to_numpy
+    tris, lb, dt, nodes, ids = torus_scene
+    rt = RayTracer(gpu_ctx)
+    gpu_ctx.set_tile_order(7)
+    try:
+        big = scenes.torus_camera(512, 512)
+        rt.shadow_mirror(lb, big, scenes.TORUS_LIGHT, rt.primary(lb, big))
+        cam = scenes.look_at((2.2, 0.3, 0.4), (0.0, 0.0, 0.0), width=320, height=200)
+        for _ in range(3):
+            hits = rt.primary(lb, cam)
+            vis, mirror = rt.shadow_mirror(lb, cam, scenes.TORUS_LIGHT, hits)
+        gpu_ctx.check()
+    finally:
+        gpu_ctx.set_tile_order(1)
+    oh = oracle_mod.trace(nodes, 20, ids, tris, oracle_mod.primary_rays(cam))
+    ovis, omir = oracle_mod.shadow_mirror(nodes, 20, ids, tris, cam, scenes.TORUS_LIGHT, oh)
+    assert_hits_equal(hits_to_numpy(hits), oh, "primary")
+    assert np.array_equal(vis.cpu().numpy(), ovis)
+    assert_hits_equal(hits_to_numpy(mirror), omir, "mirror")
