@@ -70,6 +70,11 @@ extern "C" rt_status rt_frame_capture(rt_ctx* ctx, rt_lbvh* l, const float* d_tr
     if (!ctx) return RT_ERR_INVALID;
     if (!l || !d_tris || !cam || !light || !d_primary || !out)
         return rt_fail(ctx, RT_ERR_INVALID, "rt_frame_capture: null argument");
+    // buffers the frame's calls would otherwise allocate inside the capture
+    if ((d_vis || d_mirror) && cam->width && cam->height) {
+        const rt_status es = ensure_shade_lists(ctx, l, (size_t)cam->width * cam->height);
+        if (es != RT_OK) return es;
+    }
     return capture_frame(
         ctx, "rt_frame_capture",
         [&]() {

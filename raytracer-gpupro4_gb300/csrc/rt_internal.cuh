@@ -134,6 +134,9 @@ struct rt_lbvh {
     rt_hit* f_mirror = nullptr;
     uint8_t* f_vis = nullptr;
     size_t f_pixels = 0;
+    // compacted shading-ray lists (shadow pixels, then mirror pixels), 2 x s_pixels
+    uint32_t* s_lists = nullptr;
+    size_t s_pixels = 0;
 };
 
 // Many independent scenes built in one pass of the build kernels and traced
@@ -209,8 +212,14 @@ enum : int {
     kWorkPath = 3,
     kWorkAdjoint = 4,
     kWorkBatch = 5,
-    kWorkHeavy = 6
+    kWorkHeavy = 6,
+    kWorkShade = 7,
+    kShadeCounts = 8  // two words: shadow-list and mirror-list lengths
 };
+
+// Grows the compacted shading-ray lists of l to px pixels (synchronises the
+// context stream when it allocates; call before a stream capture).
+rt_status ensure_shade_lists(rt_ctx* ctx, rt_lbvh* l, size_t px);
 
 inline rt_status reset_work(rt_ctx* ctx, int slot) {
     RT_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_work + slot, 0, sizeof(uint32_t), ctx->stream));

@@ -179,6 +179,88 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_secondary(
     }
 }
 
+// Production path of the shading rays, in two passes.  k_shade_setup runs
+// over the pixels in 8x4-tile order, writes the results that need no ray (no
+// primary hit: visibility 0 and the mirror miss record; light behind the
+// surface: visibility 1) and appends the pixels that cast a shadow ray and
+// those that cast a mirror ray to two lists, a warp's pixels in order, so
+// neighbouring rays stay neighbours.  k_trace_shade then traces the lists
+// 32 rays per warp with every lane busy (the tile pass leaves the lanes of
+// sky pixels and of pixels without a cast ray idle), rebuilding each ray from
+// its pixel exactly as the tile pass does.
+__device__ __forceinline__ void append_pixel(bool take, uint32_t p, uint32_t* list, uint32_t cap, uint32_t* count) {
+    const uint32_t m = __ballot_sync(0xffffffffu, take);
+    if (!m) return;
+    uint32_t base = 0;
+    if ((threadIdx.x & 31) == 0) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    const uint32_t k = base + __popc(m & ((1u << (threadIdx.x & 31)) - 1u));
+    if (take && k < cap) list[k] = p;
+}
+
+__global__ void __launch_bounds__(256) k_shade_setup(const float* __restrict__ soup, rt_camera cam, float lx, float ly,
+                                                     float lz, const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis,
+                                                     rt_hit* __restrict__ mirror, uint32_t* __restrict__ lists,
+                                                     uint32_t cap, uint32_t* counts, uint32_t num_tiles) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t t = warp; t < num_tiles; t += nwarps) {
+        uint32_t i, j;
+        const bool valid = tile_pixel(t, lane, cam.width, cam.height, &i, &j);
+        if (!valid) i = j = 0;
+        const size_t p = (size_t)j * cam.width + i;
+        int4 ph = make_int4(-1, 0, 0, 0);
+        if (valid) ph = __ldg(reinterpret_cast<const int4*>(prim + p));
+        const ShadeRays s = shade_rays(soup, cam, lx, ly, lz, ph, valid, i, j, false);
+        if (valid) {
+            if (vis && !(s.has && s.cast)) vis[p] = vis_code(s.has, s.cast, false);
+            if (mirror && !s.has) {
+                Hit mh;
+                mh.id = -2; mh.u = -1.0f; mh.v = -1.0f; mh.t = 0.0f;
+                store_hit(mirror + p, mh);
+            }
+        }
+        append_pixel(vis && valid && s.has && s.cast, (uint32_t)p, lists, cap, counts);
+        append_pixel(mirror && valid && s.has, (uint32_t)p, lists + cap, cap, counts + 1);
+    }
+}
+
+__global__ void __launch_bounds__(kTraceThreads) k_trace_shade(
+    TreeRef tr, const float* __restrict__ soup, rt_camera cam, float lx, float ly, float lz,
+    const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis, rt_hit* __restrict__ mirror,
+    const uint32_t* __restrict__ lists, uint32_t cap, const uint32_t* counts, uint32_t* work, Spill spill,
+    uint32_t* __restrict__ list) {
+    const uint32_t ns = min(counts[0], cap), nm = min(counts[1], cap);
+    const uint32_t cs = (ns + 31) / 32, cm = (nm + 31) / 32;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t c = next_tile(work); c < cs + cm; c = next_tile(work)) {
+        const bool shadow = c < cs;  // uniform across the warp
+        const uint32_t k = (shadow ? c : c - cs) * 32 + lane;
+        const bool valid = k < (shadow ? ns : nm);
+        uint32_t p = 0;
+        if (valid) p = __ldg(lists + (shadow ? 0u : cap) + k);
+        const uint32_t i = p % cam.width, j = p / cam.width;
+        int4 ph = make_int4(-1, 0, 0, 0);
+        if (valid) ph = __ldg(reinterpret_cast<const int4*>(prim + p));
+        const ShadeRays s = shade_rays(soup, cam, lx, ly, lz, ph, valid, i, j, !shadow);
+        uint32_t nb = 0, nt = 0;
+        int slot = -1;
+        if (shadow) {
+            const Hit h = trace_ray<false>(s.shadow, valid && s.cast, tr, true, &nb, &nt, &spill, &slot);
+            if (valid) {
+                if (slot >= 0) spill_record(list, slot, kHeavyShadow, p);
+                else vis[p] = vis_code(s.has, s.cast, h.id >= 0);
+            }
+        } else {
+            const Hit h = trace_ray<false>(s.mirror, valid && s.has, tr, false, &nb, &nt, &spill, &slot);
+            if (valid) {
+                if (slot >= 0) spill_record(list, slot, kHeavyMirror, p);
+                else store_hit(mirror + p, h);
+            }
+        }
+    }
+}
+
 __device__ __forceinline__ RayState load_ray(const rt_ray* __restrict__ rays, uint32_t k, bool valid) {
     float4 a = make_float4(0.f, 0.f, 0.f, __int_as_float(-1)), b = make_float4(0.f, 0.f, 1.f, 1.f);
     if (valid) {
@@ -284,6 +366,17 @@ rt_status check_trace_args(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, 
 }
 
 }  // namespace
+
+rt_status ensure_shade_lists(rt_ctx* ctx, rt_lbvh* l, size_t px) {
+    if (px <= l->s_pixels) return RT_OK;
+    RT_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (l->s_lists) cudaFree(l->s_lists);
+    l->s_lists = nullptr;
+    l->s_pixels = 0;
+    RT_CHECK_CUDA(ctx, cudaMalloc((void**)&l->s_lists, 2 * sizeof(uint32_t) * px));
+    l->s_pixels = px;
+    return RT_OK;
+}
 
 TreeRef tree_ref(const rt_ctx* ctx, const rt_lbvh* l) {
     TreeRef t;
@@ -415,22 +508,36 @@ extern "C" rt_status rt_trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const
     const bool stats = d_shadow_stats || d_mirror_stats;
     const Spill sp = spill_of(ctx, !stats && (uint64_t)cam->width * cam->height <= kHeavyIndexMask);
     if ((s = reset_spill(ctx, sp)) != RT_OK) return s;
-    TileOrder ord;
-    if ((s = order_begin(ctx, 1, ctx->tile_order & 2u, &ord)) != RT_OK) return s;
     const uint32_t tiles = pixel_tiles(cam);
-    uint32_t* work = ctx->d_work + kWorkSecondary;
-    if (stats) {
+    if (stats) {  // per-pixel counts in the oracle's order: the tile pass
+        TileOrder ord;
+        if ((s = order_begin(ctx, 1, ctx->tile_order & 2u, &ord)) != RT_OK) return s;
+        uint32_t* work = ctx->d_work + kWorkSecondary;
         auto k = k_trace_secondary<true>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
             tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_vis, d_mirror,
             d_shadow_stats, d_mirror_stats, work, tiles, sp, ctx->d_spill, ord);
-    } else {
-        auto k = k_trace_secondary<false>;
-        k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_vis, d_mirror, nullptr,
-            nullptr, work, tiles, sp, ctx->d_spill, ord);
+        RT_CHECK_LAUNCH(ctx, "k_trace_secondary");
+    } else {  // compacted shading-ray lists
+        const size_t px = (size_t)cam->width * cam->height;
+        if ((s = ensure_shade_lists(ctx, const_cast<rt_lbvh*>(l), px)) != RT_OK) return s;
+        uint32_t* counts = ctx->d_work + kShadeCounts;
+        RT_CHECK_CUDA(ctx, cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), ctx->stream));
+        if ((s = reset_work(ctx, kWorkShade)) != RT_OK) return s;
+        const uint32_t cap = (uint32_t)l->s_pixels;
+        const uint32_t sblocks = std::max(1u, std::min((tiles + 7) / 8, (uint32_t)ctx->num_sms * 8));
+        k_shade_setup<<<sblocks, 256, 0, ctx->stream>>>(l->src_tris, *cam, light[0], light[1], light[2], d_primary,
+                                                         d_vis, d_mirror, l->s_lists, cap, counts, tiles);
+        RT_CHECK_LAUNCH(ctx, "k_shade_setup");
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_shade, kTraceThreads, 0) != cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+        k_trace_shade<<<(uint32_t)per_sm * ctx->num_sms, kTraceThreads, 0, ctx->stream>>>(
+            tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_vis, d_mirror, l->s_lists,
+            cap, counts, ctx->d_work + kWorkShade, sp, ctx->d_spill);
+        RT_CHECK_LAUNCH(ctx, "k_trace_shade");
     }
-    RT_CHECK_LAUNCH(ctx, "k_trace_secondary");
     HeavyArgs a = heavy_args(ctx, l);
     a.soup = l->src_tris;
     a.cam = *cam;
