@@ -89,6 +89,12 @@ class Dist:
         return float(t.item())
 
 
+def replica_rate(dist: "Dist", local_units: float, local_seconds: float) -> float:
+    """Whole-job throughput of independent replicas: the units every rank
+    processed over the slowest rank's time (units per second)."""
+    return dist.sum(float(local_units)) / dist.max(float(local_seconds))
+
+
 class Clocks:
     """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
 
@@ -277,9 +283,8 @@ def run_ours(args, dist: Dist):
     dist.barrier()
     ctx.check()
     step_ms = np.array([e[0].elapsed_time(e[1]) for e in gevs])
-    t_total = dist.max(float(step_ms.sum()) / 1e3)
     frames_done = dist.sum(float(args.steps))
-    value = frames_done * n / t_total / 1e6
+    value = replica_rate(dist, args.steps * n, float(step_ms.sum()) / 1e3) / 1e6
     for g in graphs:
         g.close()
 
@@ -497,8 +502,7 @@ def run_batch(args, dist: Dist):
     with Clocks(dist.local) as clk:
         step_ms = timed(frame.launch, args.steps)
     dist.barrier()
-    t_total = dist.max(float(step_ms.sum()) / 1e3)
-    value = dist.sum(float(args.steps)) * total / t_total / 1e6
+    value = replica_rate(dist, args.steps * total, float(step_ms.sum()) / 1e3) / 1e6
 
     # e2e: pinned host soup in, hits + visibility out, inside the timed region.
     # Two batches on two streams take alternate frames (upload, graph launch,
@@ -823,9 +827,7 @@ def run_pt(args, dist: Dist, adjoint: bool = False):
     ctx.check()
     per = np.array([[e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])] for e in evs])  # ms: build+forward, backward
     step_ms = per.sum(1)
-    t_total = dist.max(float(step_ms.sum()) / 1e3)
-    samples = W * H * spp * dist.sum(float(args.steps))
-    value = samples / t_total / 1e6
+    value = replica_rate(dist, W * H * spp * args.steps, float(step_ms.sum()) / 1e3) / 1e6
     name = (f"GI box {n} tris, {W}x{H}, {spp} spp, {bounces} bounces" +
             (", forward + L2 loss + adjoint (albedo x3, emitter radiance)" if adjoint else ""))
     out = {"metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": dist.world,
