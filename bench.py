@@ -372,7 +372,9 @@ def run_ours(args, dist: Dist):
                        "wall_s": round(wall, 3)},
         "roofline": roofline,
         "e2e": e2e,
-        "gpu_launches": 14 * args.steps,  # 10 build kernels + 2 x (trace kernel + k_trace_heavy) per graph
+        # per graph: 10 build kernels; k_order_begin, k_trace_primary, k_trace_heavy;
+        # k_shade_setup, k_trace_shade, k_trace_heavy
+        "gpu_launches": 16 * args.steps,
     }
     out["clocks"] = clk.summary()
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
