@@ -116,6 +116,7 @@ rt_status rt_lbvh_create(rt_ctx* ctx, uint32_t max_tris, uint32_t depth, rt_lbvh
 rt_status rt_lbvh_destroy(rt_lbvh* lbvh);
 
 #define RT_BUILD_CLEAR_UNREACHED 1u  /* write RT_NODE_SENTINEL to unreached slots */
+#define RT_BUILD_COMPACT 2u          /* also build the compact layout (rt_lbvh_compact_get) and trace it */
 
 /* Full rebuild from a device triangle soup (n x 9 floats: A, B, C):
  * scene bounds, 30-bit Morton codes, stable LSD radix sort, node emission,
@@ -165,6 +166,13 @@ typedef struct rt_lbvh_view {
     uint32_t node_size;        /* 32 (GetSizeOfElement) */
 } rt_lbvh_view;
 rt_status rt_lbvh_view_get(const rt_lbvh* lbvh, rt_lbvh_view* out);
+/* The compact node layout that rt_lbvh_build with RT_BUILD_COMPACT adds and
+ * the traversal then uses (the heap above stays the reference layout): slot 1 = root, the reachable nodes in
+ * sibling pairs at even slots, and in an internal node PrimPos holds the slot
+ * of its children pair instead of its first primitive.  *slots = the
+ * capacity of the array (2 + 2 x internal nodes are used).  RT_ERR_INVALID
+ * when the last build did not make it (imported trees are traced in the heap). */
+rt_status rt_lbvh_compact_get(const rt_lbvh* lbvh, const rt_node** d_nodes, uint32_t* slots);
 /* WorldBound() = root box (LBVH.h:115).  Synchronous. */
 rt_status rt_lbvh_world_bound(rt_ctx* ctx, const rt_lbvh* lbvh, float out_min_max[6]);
 /* Synchronous copies to host; any pointer may be NULL. */

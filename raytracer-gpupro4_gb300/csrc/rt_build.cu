@@ -817,7 +817,7 @@ __device__ __forceinline__ void leaf_boxes(int64_t gpos, int cnt, const float4* 
 __device__ __forceinline__ void refit_walk(uint32_t h, int32_t pos, int32_t end, const float mn_in[3],
                                            const float mx_in[3], const uint32_t* __restrict__ keys, uint32_t n,
                                            uint32_t depth, rt_node* nodes, uint32_t* arrive, uint32_t epoch,
-                                           uint32_t* err) {
+                                           uint32_t* err, uint32_t* inner = nullptr) {
     const int32_t count = end - pos + 1;
     // leaf axis = the reference's round-robin counter at the call that made
     // the leaf: entry with bit (d_parent - 1) -> (31 - d_parent) % 3; a run
@@ -864,6 +864,7 @@ __device__ __forceinline__ void refit_walk(uint32_t h, int32_t pos, int32_t end,
         nd.prim_pos = lpos;
         h >>= 1;
         nodes[h] = nd;
+        if (inner) atomicOr(inner + (h >> 5), 1u << (h & 31));
     }
 }
 
@@ -871,7 +872,8 @@ __global__ void __launch_bounds__(256) k_emit_refit(const uint32_t* __restrict__
                                                     uint32_t n, uint32_t depth, rt_node* nodes,
                                                     const uint32_t* __restrict__ leaf_list,
                                                     const uint32_t* leaf_count, uint32_t* arrive,
-                                                    const uint32_t* epoch_word, uint32_t* err) {
+                                                    const uint32_t* epoch_word, uint32_t* err,
+                                                    uint32_t* inner = nullptr) {
     const uint32_t nleaves = min(*leaf_count, n);
     const uint32_t epoch = *epoch_word;
     const uint32_t lane = threadIdx.x & 31;
@@ -888,9 +890,75 @@ __global__ void __launch_bounds__(256) k_emit_refit(const uint32_t* __restrict__
         }
         float mn[3], mx[3];
         leaf_boxes(pos, ok ? end - pos + 1 : 0, sorted_tris, mn, mx);
-        if (ok) refit_walk(h, pos, end, mn, mx, keys, n, depth, nodes, arrive, epoch, err);
+        if (ok) refit_walk(h, pos, end, mn, mx, keys, n, depth, nodes, arrive, epoch, err, inner);
     }
 }
+
+// Compact layout (rt_lbvh.cnodes) from the heap: inner_rank = exclusive
+// popcount prefix of the internal-node bitmap (one block), then every
+// reachable internal node x writes its two children at slots 2 rank(x) + 2
+// and + 3, an internal child's PrimPos replaced by the slot of its own pair.
+constexpr int kRankThreads = 1024;
+
+__global__ void __launch_bounds__(kRankThreads) k_inner_rank(const uint32_t* __restrict__ inner, uint32_t words,
+                                                             uint32_t* __restrict__ rank) {
+    __shared__ uint32_t s_w[kRankThreads / 32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const uint32_t per = (words + kRankThreads - 1) / kRankThreads;
+    const uint32_t lo = min(words, (uint32_t)t * per), hi = min(words, lo + per);
+    uint32_t sum = 0;
+    for (uint32_t q = lo; q < hi; ++q) sum += __popc(inner[q]);
+    uint32_t incl = sum;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, incl, off);
+        if (lane >= off) incl += y;
+    }
+    if (lane == 31) s_w[w] = incl;
+    __syncthreads();
+    uint32_t run = incl - sum;
+    for (int q = 0; q < w; ++q) run += s_w[q];
+    for (uint32_t q = lo; q < hi; ++q) {
+        rank[q] = run;
+        run += __popc(inner[q]);
+    }
+}
+
+__device__ __forceinline__ uint32_t inner_slot(const uint32_t* inner, const uint32_t* rank, uint32_t x) {
+    return 2u * (rank[x >> 5] + __popc(inner[x >> 5] & ((1u << (x & 31)) - 1u))) + 2u;
+}
+
+__global__ void __launch_bounds__(256) k_compact(const rt_node* __restrict__ nodes, const uint32_t* __restrict__ inner,
+                                                 const uint32_t* __restrict__ rank, uint32_t words, uint32_t num_nodes,
+                                                 rt_node* __restrict__ cnodes, uint32_t ccap, uint32_t* err) {
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    if (gtid == 0) {  // the root at slot 1
+        rt_node root = nodes[1];
+        if (inner[0] & 2u) root.prim_pos = 2;
+        cnodes[1] = root;
+    }
+    for (uint32_t w = gtid; w < words; w += gs) {
+        uint32_t m = inner[w];
+        while (m) {
+            const uint32_t b = __ffs(m) - 1;
+            m &= m - 1u;
+            const uint32_t x = w * 32 + b;
+            const uint32_t slot = inner_slot(inner, rank, x);
+            if (2 * x + 1 >= num_nodes || slot + 1 >= ccap) {
+                atomicOr(err, RT_DEVERR_BOUNDS);
+                continue;
+            }
+#pragma unroll
+            for (uint32_t q = 0; q < 2; ++q) {
+                const uint32_t y = 2 * x + q;
+                rt_node nd = nodes[y];
+                if (!(nd.prim_count & 4)) nd.prim_pos = (int32_t)inner_slot(inner, rank, y);
+                cnodes[slot + q] = nd;
+            }
+        }
+    }
+}
+
 
 // Pre-gather for imported trees (ids + soup uploaded from the host).
 __global__ void k_gather_tris(const uint32_t* __restrict__ ids, const float* __restrict__ tris, uint32_t n,
@@ -936,6 +1004,10 @@ extern "C" rt_status rt_lbvh_create(rt_ctx* ctx, uint32_t max_tris, uint32_t dep
     alloc((void**)&l->keys_alt, 4 * cap);
     alloc((void**)&l->ids_alt, 4 * cap);
     alloc((void**)&l->sorted_tris, sizeof(float4) * 3 * cap);
+    l->ccap = (uint32_t)std::min<uint64_t>((uint64_t)l->num_nodes + 2, 2ull * cap + 2);
+    alloc((void**)&l->cnodes, sizeof(rt_node) * l->ccap);
+    alloc((void**)&l->inner, sizeof(uint32_t) * std::max(1u, l->num_nodes / 32));
+    alloc((void**)&l->inner_rank, sizeof(uint32_t) * std::max(1u, l->num_nodes / 32));
     alloc((void**)&l->tris, sizeof(float) * 9 * cap);
     alloc((void**)&l->scene, sizeof(SceneInfo));
     alloc((void**)&l->partials, sizeof(float) * 8 * l->bounds_blocks);
@@ -961,7 +1033,7 @@ extern "C" rt_status rt_lbvh_destroy(rt_lbvh* l) {
     void* ptrs[] = {l->nodes,    l->keys,     l->ids,      l->keys_alt,  l->ids_alt, l->sorted_tris,
                     l->tris,     l->scene,    l->partials, l->counters,  l->hist,    l->lookback,
                     l->scan,     l->leaf_list, l->arrive,  l->f_primary, l->f_mirror, l->f_vis,
-                    l->s_lists};
+                    l->s_lists,  l->cnodes,   l->inner,    l->inner_rank};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete l;
@@ -1001,10 +1073,22 @@ static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint
                                                        l->sorted_tris, l->leaf_list, l->counters + 5, ctx->d_err);
     RT_CHECK_LAUNCH(ctx, "k_emit_leaves");
     const uint32_t rblocks = std::max(1u, std::min(ceil_div(n, 256), (uint32_t)ctx->num_sms * 8));
+    const bool compact = (flags & RT_BUILD_COMPACT) != 0;
+    const uint32_t words = std::max(1u, l->num_nodes / 32);
+    if (compact) RT_CHECK_CUDA(ctx, cudaMemsetAsync(l->inner, 0, sizeof(uint32_t) * words, st));
     k_emit_refit<<<rblocks, 256, 0, st>>>(l->keys, l->sorted_tris, n, l->depth, l->nodes, l->leaf_list,
-                                          l->counters + 5, l->arrive, l->counters + 6, ctx->d_err);
+                                          l->counters + 5, l->arrive, l->counters + 6, ctx->d_err,
+                                          compact ? l->inner : nullptr);
     RT_CHECK_LAUNCH(ctx, "k_emit_refit");
+    if (compact) {
+        k_inner_rank<<<1, kRankThreads, 0, st>>>(l->inner, words, l->inner_rank);
+        RT_CHECK_LAUNCH(ctx, "k_inner_rank");
+        k_compact<<<std::max(1u, std::min(ceil_div(words, 256), (uint32_t)ctx->num_sms * 8)), 256, 0, st>>>(
+            l->nodes, l->inner, l->inner_rank, words, l->num_nodes, l->cnodes, l->ccap, ctx->d_err);
+        RT_CHECK_LAUNCH(ctx, "k_compact");
+    }
     l->built_keys = true;
+    l->compact_valid = compact;
     return RT_OK;
 }
 
@@ -1039,6 +1123,7 @@ extern "C" rt_status rt_lbvh_import_host(rt_ctx* ctx, rt_lbvh* l, const rt_node*
     l->n = n;
     l->src_tris = l->tris;
     l->built_keys = false;
+    l->compact_valid = false;  // an imported tree is traversed in its heap layout
     return RT_OK;
 }
 
@@ -1052,6 +1137,14 @@ extern "C" rt_status rt_lbvh_view_get(const rt_lbvh* l, rt_lbvh_view* v) {
     v->depth = l->depth;
     v->num_nodes = l->num_nodes;
     v->node_size = (uint32_t)sizeof(rt_node);
+    return RT_OK;
+}
+
+extern "C" rt_status rt_lbvh_compact_get(const rt_lbvh* l, const rt_node** d_nodes, uint32_t* slots) {
+    if (!l || !d_nodes || !slots) return RT_ERR_INVALID;
+    if (!l->compact_valid) return RT_ERR_INVALID;
+    *d_nodes = l->cnodes;
+    *slots = l->ccap;
     return RT_OK;
 }
 

@@ -117,6 +117,14 @@ struct rt_lbvh {
     uint32_t* keys_alt = nullptr;
     uint32_t* ids_alt = nullptr;
     float4* sorted_tris = nullptr;  // 3 x float4 per triangle
+    // compact layout used by the traversal: slot 1 = root, the children of
+    // internal node x at slots 2 r + 2, 2 r + 3 with r = the rank of x among
+    // the reachable internal nodes in heap order (its PrimPos holds 2 r + 2)
+    rt_node* cnodes = nullptr;
+    uint32_t ccap = 0;              // slots of cnodes
+    uint32_t* inner = nullptr;      // bitmap of reachable internal heap slots (num_nodes / 32 words, >= 1)
+    uint32_t* inner_rank = nullptr; // exclusive popcount prefix of inner
+    bool compact_valid = false;     // cnodes describe the current tree
     float* tris = nullptr;          // device copy of the soup (host builds / imports)
     const float* src_tris = nullptr; // soup of the last build / import, indexed by triangle id (borrowed)
     // build scratch

@@ -380,9 +380,10 @@ rt_status ensure_shade_lists(rt_ctx* ctx, rt_lbvh* l, size_t px) {
 
 TreeRef tree_ref(const rt_ctx* ctx, const rt_lbvh* l) {
     TreeRef t;
-    t.nodes = l->nodes;
+    t.compact = l->compact_valid;
+    t.nodes = t.compact ? l->cnodes : l->nodes;
+    t.num_nodes = t.compact ? l->ccap : l->num_nodes;
     t.tris = l->sorted_tris;
-    t.num_nodes = l->num_nodes;
     t.n = l->n;
     t.err = ctx->d_err;
     return t;
@@ -663,6 +664,7 @@ __global__ void __launch_bounds__(256) k_batch_trace(BatchTraceArgs a, uint32_t*
             const uint32_t tile = a.order ? g / a.S : g % a.tiles_per_scene;
             const uint32_t toff = __ldg(a.tri_off + s);
             TreeRef tr;
+            tr.compact = false;
             tr.nodes = a.nodes + ((size_t)s << a.depth);
             tr.tris = a.sorted_tris + 3 * (size_t)toff;
             tr.num_nodes = 1u << a.depth;

@@ -34,7 +34,16 @@ struct TreeRef {
     uint32_t num_nodes;
     uint32_t n;
     uint32_t* err;
+    // compact layout: the children of an internal node are the pair at
+    // slots PrimPos, PrimPos + 1 (even), not at heap slots 2i, 2i + 1
+    bool compact;
 };
+
+// First slot of the children pair of internal node `node` whose record's
+// fourth float4 lane (PrimPos) is pp.
+__device__ __forceinline__ uint32_t child_pair(const TreeRef& tr, uint32_t node, float pp) {
+    return tr.compact ? (uint32_t)__float_as_int(pp) : node << 1;
+}
 
 struct RayState {
     f3 o, d, inv;
@@ -309,7 +318,7 @@ __device__ __forceinline__ bool descend(const TreeRef& tr_, const RayState& r, f
     const rt_node* __restrict__ nodes = tr_.nodes;
     while (!(__float_as_int(cur.b.z) & 4)) {
         const int pc = __float_as_int(cur.b.z);
-        const uint32_t c0 = node << 1;
+        const uint32_t c0 = child_pair(tr_, node, cur.b.w);
         if (c0 + 1 >= tr_.num_nodes) {
             atomicOr(tr_.err, RT_DEVERR_BOUNDS);
             return false;
@@ -464,8 +473,9 @@ __device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
 }
 
 // One ray traced by the whole warp (every lane passes the same ray): a
-// frontier walk.  The warp keeps a stack of internal nodes the ray enters
-// (node, entry distance) and a queue of leaves in shared memory.  Each step
+// frontier walk.  The warp keeps a stack of the internal nodes the ray enters
+// (as the slot of their children pair, with the entry distance) and a queue
+// of leaves in shared memory.  Each step
 // pops up to 32 nodes from the top (the deepest: the walk stays depth-first
 // at the scale of a warp, which bounds the stack by 32 entries per level),
 // tests both children of each, and pushes the entered internal children and
@@ -528,7 +538,7 @@ __device__ __forceinline__ Hit traverse_wide(const RayState& r, const TreeRef& t
                 qtris = __float_as_int(root.b.z) >> 3;
             } else {
                 if (lane == 0) {
-                    snode[0] = 1;
+                    snode[0] = child_pair(tr_, 1, root.b.w);  // the stack holds children-pair slots
                     st0[0] = t0;
                 }
                 size = 1;
@@ -619,7 +629,7 @@ __device__ __forceinline__ Hit traverse_wide(const RayState& r, const TreeRef& t
         float4 l1 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = l1;
         uint32_t c0 = 0;
         if (live) {
-            c0 = nd << 1;
+            c0 = nd;
             if (c0 + 1 >= tr_.num_nodes) {
                 atomicOr(tr_.err, RT_DEVERR_BOUNDS);
             } else {
@@ -655,7 +665,7 @@ __device__ __forceinline__ Hit traverse_wide(const RayState& r, const TreeRef& t
                 qt0[lo_] = tl;
                 ++lo_;
             } else {
-                snode[io] = c0;
+                snode[io] = child_pair(tr_, c0, l1.w);
                 st0[io] = tl;
                 ++io;
             }
@@ -666,7 +676,7 @@ __device__ __forceinline__ Hit traverse_wide(const RayState& r, const TreeRef& t
                 qcnt[lo_] = __float_as_int(r1.z) >> 3;
                 qt0[lo_] = tr;
             } else {
-                snode[io] = c0 | 1u;
+                snode[io] = child_pair(tr_, c0 | 1u, r1.w);
                 st0[io] = tr;
             }
         }

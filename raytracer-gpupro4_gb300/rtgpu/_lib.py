@@ -14,6 +14,7 @@ from .build import LIB
 
 RT_OK, RT_ERR_INVALID, RT_ERR_CAPACITY, RT_ERR_CUDA, RT_ERR_TIMEOUT, RT_ERR_NONFINITE = range(6)
 RT_BUILD_CLEAR_UNREACHED = 1
+RT_BUILD_COMPACT = 2
 RT_NOALLOC_MAX_TRIS = 262144
 RT_NOALLOC_MAX_DEPTH = 20
 RT_NODE_SENTINEL = -2147483647
@@ -28,7 +29,7 @@ EXPORTED = [
     "rt_api_version", "rt_status_string", "rt_ctx_create", "rt_ctx_destroy", "rt_ctx_set_stream", "rt_ctx_sync",
     "rt_ctx_set_trace_budget", "rt_ctx_set_tile_order",
     "rt_ctx_check", "rt_last_error", "rt_lbvh_create", "rt_lbvh_destroy", "rt_lbvh_build", "rt_lbvh_build_host",
-    "rt_lbvh_import_host", "rt_lbvh_view_get", "rt_lbvh_world_bound", "rt_lbvh_download", "rt_trace_primary",
+    "rt_lbvh_import_host", "rt_lbvh_view_get", "rt_lbvh_compact_get", "rt_lbvh_world_bound", "rt_lbvh_download", "rt_trace_primary",
     "rt_trace_shadow_mirror", "rt_trace_rays", "rt_render_frame_host", "rt_render_frame_host_async", "rt_pathtrace", "rt_pathtrace_adjoint",
     "rt_lbvh_build_noalloc", "rt_frame_capture", "rt_frame_launch", "rt_frame_node_count", "rt_frame_destroy",
     "rt_batch_create", "rt_batch_destroy", "rt_batch_scene_count", "rt_batch_build", "rt_batch_view_get",
@@ -85,6 +86,7 @@ def lib() -> C.CDLL:
         "rt_lbvh_build_host": (i32, [vp, vp, vp, u32, u32]),
         "rt_lbvh_import_host": (i32, [vp, vp, vp, vp, vp, u32]),
         "rt_lbvh_view_get": (i32, [vp, C.POINTER(LbvhView)]),
+        "rt_lbvh_compact_get": (i32, [vp, C.POINTER(vp), C.POINTER(u32)]),
         "rt_lbvh_world_bound": (i32, [vp, vp, fp]),
         "rt_lbvh_download": (i32, [vp, vp, vp, vp, vp]),
         "rt_trace_primary": (i32, [vp, vp, C.POINTER(Camera), vp, vp]),

@@ -304,3 +304,35 @@ def test_heavy_first_tile_order_keeps_results(gpu_ctx, oracle_mod, torus_scene):
     assert_hits_equal(hits_to_numpy(hits), oh, "primary")
     assert np.array_equal(vis.cpu().numpy(), ovis)
     assert_hits_equal(hits_to_numpy(mirror), omir, "mirror")
+
+
+def test_compact_layout_traversal(gpu_ctx, oracle_mod):
+    """RT_BUILD_COMPACT: the heap export is unchanged, the compact layout is
+    reported, and the traversal over it gives the oracle's hits."""
+    import ctypes as C
+    import torch
+    from rtgpu import _lib as L
+    from rtgpu import scenes
+    from rtgpu.api import LBVH, RayTracer, hits_to_numpy
+    tris = scenes.torus(128, 64)
+    lb = LBVH(gpu_ctx, len(tris), 18).Build(torch.from_numpy(tris).cuda(), L.RT_BUILD_COMPACT)
+    ptr, slots = C.c_void_p(), C.c_uint32()
+    assert L.lib().rt_lbvh_compact_get(lb.h, C.byref(ptr), C.byref(slots)) == L.RT_OK
+    assert ptr.value and slots.value >= 2
+    nodes, ids, keys = lb.download(True, True, True)
+    onodes, oids, okeys, reached = oracle_mod.lbvh_build(tris, 18)
+    r = np.nonzero(reached)[0]
+    assert np.array_equal(nodes[r], onodes[r]) and np.array_equal(ids, oids)
+    cam = scenes.look_at((2.2, 0.3, 0.4), (0.0, 0.0, 0.0), width=320, height=200)
+    rt = RayTracer(gpu_ctx)
+    hits = rt.primary(lb, cam)
+    vis, mirror = rt.shadow_mirror(lb, cam, scenes.TORUS_LIGHT, hits)
+    gpu_ctx.check()
+    oh = oracle_mod.trace(onodes, 18, oids, tris, oracle_mod.primary_rays(cam))
+    ovis, omir = oracle_mod.shadow_mirror(onodes, 18, oids, tris, cam, scenes.TORUS_LIGHT, oh)
+    assert_hits_equal(hits_to_numpy(hits), oh, "primary")
+    assert np.array_equal(vis.cpu().numpy(), ovis)
+    assert_hits_equal(hits_to_numpy(mirror), omir, "mirror")
+    # a build without the flag reports no compact layout
+    lb.Build(torch.from_numpy(tris).cuda())
+    assert L.lib().rt_lbvh_compact_get(lb.h, C.byref(ptr), C.byref(slots)) == L.RT_ERR_INVALID
