@@ -229,6 +229,13 @@ def rlib() -> C.CDLL:
         L.ref_copy_ids.argtypes = [vp, vp]
         L.ref_world_bound.argtypes = [vp, vp]
         L.ref_intersect.argtypes = [vp, vp, C.c_long, vp, vp, vp, vp, i32]
+        L.ref_obj_load.argtypes = [C.c_char_p]
+        L.ref_obj_load.restype = i32
+        L.ref_obj_fetch.argtypes = [vp, vp]
+        L.ref_obj_material_count.restype = i32
+        L.ref_txt_load.argtypes = [C.c_char_p]
+        L.ref_txt_load.restype = i32
+        L.ref_obj_fetch_materials.argtypes = [vp]
         _rlib = L
     return _rlib
 
@@ -300,3 +307,29 @@ def reachable_mask(nodes: np.ndarray) -> np.ndarray:
         m[lo:hi] = m[par] & ~leaf[par]
         lo = hi
     return m
+
+
+def ref_load_model(path):
+    """(soup n x 9 float32, material id per triangle) of a model file: .obj
+    through the reference's vendored loader + normalize(), .txt through a
+    restatement of Model::LoadFile's .txt branch; both then through the
+    reference's own Model::Scale (oracle/ref/ref_shim.cpp ref_obj_load,
+    ref_txt_load)."""
+    L = rlib()
+    p = str(path)
+    n = (L.ref_txt_load if ".txt" in p or ".TXT" in p else L.ref_obj_load)(p.encode())
+    if n < 0:
+        raise OSError(f"reference loader could not read {path}")
+    soup = np.zeros((n, 9), np.float32)
+    mat = np.zeros(n, np.int32)
+    L.ref_obj_fetch(_ptr(soup), _ptr(mat))
+    return soup, mat
+
+
+def ref_obj_materials():
+    """Materials of the file ref_load_model read last: (m, 14) float32 rows of
+    ambient[4], diffuse[4], specular[4], shininess, alpha."""
+    L = rlib()
+    out = np.zeros((L.ref_obj_material_count(), 14), np.float32)
+    L.ref_obj_fetch_materials(_ptr(out))
+    return out

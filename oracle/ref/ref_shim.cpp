@@ -10,11 +10,15 @@
 // objects and exposes plain C entry points for the parity tests and the CPU
 // baseline.  Nothing here is used by the GPU product path.
 #include <cstdio>
+#include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 #include <chrono>
 #include "LBVH.h"
 #include "bvh.h"
+#include "model_obj.h"
+#include "model_scale_stub.h"
 
 namespace {
 
@@ -117,6 +121,130 @@ void ref_intersect(void* hp, const float* rays, long n, int* id, float* t, float
         id[i] = hit.IDTr;
         t[i] = hit.t; u[i] = hit.u; v[i] = hit.v;
     }
+}
+
+// Model ingestion: the reference's vendored OBJ loader
+// (Common/Scenes/Loaders/model_obj.cpp: ModelOBJ::import + normalize(), as
+// Model::LoadFile calls them, Model.cpp:266-274) followed by the reference's
+// own Model::Scale (Model.cpp:647-710, compiled against
+// shim/model_scale_stub.h) on the loader's vertex buffer.  Output: the
+// triangle soup (ntris x 9 floats) in index-buffer order and the material id
+// of each triangle (its mesh's material, Model.cpp:355-372).  Two calls:
+// ref_obj_load / ref_txt_load return the triangle count (or -1), then
+// ref_obj_fetch copies the result.
+static std::vector<float> g_obj_soup;
+static std::vector<int> g_obj_mat;
+static std::vector<float> g_obj_materials;  // 14 floats per material
+
+// Model::Scale on x y z triples, through a Model holding them as Vertex.
+static void reference_scale(std::vector<float>& pos) {
+    const int nv = int(pos.size() / 3);
+    std::vector<Vertex> v(nv);
+    for (int i = 0; i < nv; ++i) v[i] = Vertex(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+    Model model;
+    model.m_pVertices = v.data();
+    model.m_uiNumVertices = unsigned(nv);
+    model.Scale();
+    for (int i = 0; i < nv; ++i) {
+        pos[3 * i] = v[i].Pos.x;
+        pos[3 * i + 1] = v[i].Pos.y;
+        pos[3 * i + 2] = v[i].Pos.z;
+    }
+}
+
+int ref_obj_load(const char* path) {
+    ModelOBJ m;
+    if (!m.import(path)) return -1;
+    m.normalize();
+    const int nv = m.getNumberOfVertices(), nt = m.getNumberOfTriangles();
+    std::vector<float> pos(size_t(nv) * 3);
+    for (int i = 0; i < nv; ++i)
+        for (int c = 0; c < 3; ++c) pos[3 * i + c] = m.getVertexBuffer()[i].position[c];
+    reference_scale(pos);
+    g_obj_soup.assign(size_t(nt) * 9, 0.0f);
+    g_obj_mat.assign(size_t(nt), 0);
+    const int* ib = m.getIndexBuffer();
+    for (int t = 0; t < nt; ++t)
+        for (int k = 0; k < 3; ++k)
+            for (int c = 0; c < 3; ++c) g_obj_soup[9 * size_t(t) + 3 * k + c] = pos[3 * ib[3 * t + k] + c];
+    // the materials as the loader holds them (its default one when the file
+    // names none): ambient, diffuse, specular (4 each), shininess, alpha
+    const int nm = std::max(1, m.getNumberOfMaterials());
+    g_obj_materials.assign(size_t(nm) * 14, 0.0f);
+    for (int i = 0; i < nm; ++i) {
+        const ModelOBJ::Material& mt = m.getMaterial(i);
+        float* o = &g_obj_materials[14 * size_t(i)];
+        for (int c = 0; c < 4; ++c) {
+            o[c] = mt.ambient[c];
+            o[4 + c] = mt.diffuse[c];
+            o[8 + c] = mt.specular[c];
+        }
+        o[12] = mt.shininess;
+        o[13] = mt.alpha;
+    }
+    if (m.getNumberOfMaterials() > 1) {
+        for (int i = 0; i < m.getNumberOfMeshes(); ++i) {
+            const ModelOBJ::Mesh& mesh = m.getMesh(i);
+            const int id = m.getMaterialCache()[mesh.pMaterial->name];
+            for (int j = 0; j < mesh.triangleCount; ++j) g_obj_mat[mesh.startIndex / 3 + j] = id;
+        }
+    }
+    return nt;
+}
+
+void ref_obj_fetch(float* soup, int* material) {
+    memcpy(soup, g_obj_soup.data(), sizeof(float) * g_obj_soup.size());
+    memcpy(material, g_obj_mat.data(), sizeof(int) * g_obj_mat.size());
+}
+
+// The .txt branch of Model::LoadFile (Model.cpp:215-262) restated for
+// positions: vertex count, triangle count, 8 floats per vertex (position,
+// normal, u, v), 3 indices per triangle; then the reference's Model::Scale
+// over every vertex.
+int ref_txt_load(const char* path) {
+    FILE* f = fopen(path, "r");
+    if (!f) return -1;
+    int nv = 0, nt = 0;
+    if (fscanf(f, "%d", &nv) != 1 || fscanf(f, "%d", &nt) != 1 || nv <= 0 || nt <= 0) {
+        fclose(f);
+        return -1;
+    }
+    std::vector<float> pos(size_t(nv) * 3);
+    for (int i = 0; i < nv; ++i) {
+        float p[8];
+        if (fscanf(f, "%f %f %f %f %f %f %f %f", &p[0], &p[1], &p[2], &p[3], &p[4], &p[5], &p[6], &p[7]) != 8) {
+            fclose(f);
+            return -1;
+        }
+        pos[3 * i] = p[0];
+        pos[3 * i + 1] = p[1];
+        pos[3 * i + 2] = p[2];
+    }
+    std::vector<int> idx(size_t(nt) * 3);
+    for (int t = 0; t < nt; ++t)
+        if (fscanf(f, "%d %d %d", &idx[3 * t], &idx[3 * t + 1], &idx[3 * t + 2]) != 3) {
+            fclose(f);
+            return -1;
+        }
+    fclose(f);
+    for (int k : idx)
+        if (k < 0 || k >= nv) return -1;
+    reference_scale(pos);
+    g_obj_soup.assign(size_t(nt) * 9, 0.0f);
+    g_obj_mat.assign(size_t(nt), 0);
+    for (int t = 0; t < nt; ++t)
+        for (int k = 0; k < 3; ++k)
+            for (int c = 0; c < 3; ++c) g_obj_soup[9 * size_t(t) + 3 * k + c] = pos[3 * idx[3 * t + k] + c];
+    g_obj_materials.assign(14, 0.0f);
+    const float dflt[14] = {0.2f, 0.2f, 0.2f, 1.0f, 0.8f, 0.8f, 0.8f, 1.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 1.0f};
+    memcpy(g_obj_materials.data(), dflt, sizeof(dflt));
+    return nt;
+}
+
+int ref_obj_material_count() { return int(g_obj_materials.size() / 14); }
+
+void ref_obj_fetch_materials(float* out) {
+    memcpy(out, g_obj_materials.data(), sizeof(float) * g_obj_materials.size());
 }
 
 }  // extern "C"

@@ -5,13 +5,17 @@
 // the Python binding of the same C ABI.
 //
 //   rt_frame_demo <soup.f32> <n> <camera.f32> <width> <height> <lx> <ly> <lz> <depth> <frames> <out_prefix>
+//   rt_frame_demo <model.obj|model.txt> 0 <camera.f32> ...
 //
-// soup.f32: n x 9 float32; camera.f32: eye, right, up, fwd (3 floats each),
-// tan(fovy/2).  Writes <out_prefix>.primary / .vis / .mirror (raw rt_hit /
-// uint8 arrays of the last frame) and prints one JSON summary line.
+// soup.f32: n x 9 float32, or a model file loaded through Model (Model::
+// LoadFile + Model::Scale; n is then the model's triangle count);
+// camera.f32: eye, right, up, fwd (3 floats each), tan(fovy/2).  Writes
+// <out_prefix>.primary / .vis / .mirror (raw rt_hit / uint8 arrays of the
+// last frame) and prints one JSON summary line.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "rt_stages.h"
@@ -42,8 +46,21 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "usage: %s soup n camera width height lx ly lz depth frames out_prefix\n", argv[0]);
         return 2;
     }
-    const unsigned n = (unsigned)std::strtoul(argv[2], nullptr, 10);
-    std::vector<float> soup = read_floats(argv[1], (size_t)n * 9);
+    unsigned n = (unsigned)std::strtoul(argv[2], nullptr, 10);
+    std::vector<float> soup;
+    const char* src = argv[1];
+    if (std::strstr(src, ".obj") || std::strstr(src, ".OBJ") || std::strstr(src, ".txt") || std::strstr(src, ".TXT")) {
+        try {
+            rtgb::Model model(src);
+            n = model.GetNumPrimitives();
+            soup.assign(model.GetSoup(), model.GetSoup() + (size_t)n * 9);
+        } catch (const rtgb::Error& e) {
+            std::fprintf(stderr, "%s\n", e.what());
+            return 2;
+        }
+    } else {
+        soup = read_floats(src, (size_t)n * 9);
+    }
     std::vector<float> c = read_floats(argv[3], 13);
     rt_camera cam;
     for (int k = 0; k < 3; ++k) {

@@ -26,6 +26,19 @@ void Context::Sync() { check(rt_ctx_sync(ctx_), ctx_, "rt_ctx_sync"); }
 void Context::Check() { check(rt_ctx_check(ctx_), ctx_, "rt_ctx_check"); }
 
 // ---------------------------------------------------------------------------
+Model::Model(const std::string& sFileName) : m_sName(sFileName.substr(0, sFileName.find('.'))) {
+    char err[512] = {0};
+    const rt_status s = rt_model_load(sFileName.c_str(), &m_model, err, sizeof(err));
+    if (s != RT_OK) throw Error(s, std::string("rt_model_load: ") + err);
+}
+Model::~Model() { rt_model_free(m_model); }
+const rt_material& Model::GetMaterial(unsigned int i) const {
+    const rt_material* m = rt_model_material(m_model, i);
+    if (!m) throw Error(RT_ERR_INVALID, "Model::GetMaterial: index out of range");
+    return *m;
+}
+
+// ---------------------------------------------------------------------------
 DeviceBuffer::DeviceBuffer(size_t bytes) { resize(bytes); }
 DeviceBuffer::~DeviceBuffer() {
     if (p_) cudaFree(p_);

@@ -8,6 +8,8 @@
 //   StructureConstruction  RayTracerCS/StructureConstruction.h:67-91
 //   RayTracerCS            RayTracerCS/RayTracerCS.h:64-144 (headless: the
 //                          swap chain becomes device hit buffers)
+//   Model                  Common/Scenes/Model.h:35-80 (file -> triangle soup
+//                          through include/rt_model.h; no Direct3D objects)
 // The geometry types mirror Common/Geometry (Vector3, BBox, Ray,
 // TIntersection) and the 32-byte LBVHNode (LBVH.h:25-28).
 //
@@ -22,6 +24,7 @@
 #include <vector>
 
 #include "rt_api.h"
+#include "rt_model.h"
 
 namespace rtgb {
 
@@ -173,6 +176,29 @@ class StructureConstruction {
 struct Scene {
     const float* soup = nullptr;  // host, n x 9 floats
     unsigned int numPrimitives = 0;
+};
+
+// Model (Model.h:35-80): the constructor loads the file (Model::LoadFile,
+// .obj or .txt) and applies Model::Scale; the primitives are the triangle
+// soup the acceleration structures take.  The path is used as given (the
+// reference prefixed "./Models/").
+class Model {
+   public:
+    explicit Model(const std::string& sFileName);
+    ~Model();
+    Model(const Model&) = delete;
+    Model& operator=(const Model&) = delete;
+    unsigned int GetNumPrimitives() const { return rt_model_triangle_count(m_model); }
+    unsigned int GetNumMaterials() const { return rt_model_material_count(m_model); }
+    const float* GetSoup() const { return rt_model_soup(m_model); }  // n x 9 floats
+    const int32_t* GetMaterialIds() const { return rt_model_material_ids(m_model); }
+    const rt_material& GetMaterial(unsigned int i) const;
+    const std::string& GetName() const { return m_sName; }
+    Scene GetScene() const { return Scene{GetSoup(), GetNumPrimitives()}; }
+
+   private:
+    rt_model* m_model = nullptr;
+    std::string m_sName;
 };
 
 // RayTracerCS::Render (RayTracerCS.cpp:241-311) without a window: per frame,

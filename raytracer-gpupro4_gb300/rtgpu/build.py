@@ -4,7 +4,8 @@
   compiled by nvcc for sm_103a only.
 * ``host/_build/librthost.so`` and ``host/_build/rt_frame_demo``: the C++
   stage classes that mirror the reference's AccelerationStructure /
-  StructureConstruction / RayTracerCS interface on top of the C ABI.
+  StructureConstruction / RayTracerCS interface on top of the C ABI, and the
+  model loader (``include/rt_model.h``).
 
 Translation units are compiled in parallel processes and linked once; a
 library is rebuilt only when one of its sources is newer than it.
@@ -101,9 +102,9 @@ def build_host(force: bool = False) -> Path | None:
     inc = ["-I", str(INCLUDE), "-I", str(HOST), "-I", str(cuda / "include")]
     cudart = ["-L", str(cuda / "lib64"), "-lcudart", f"-Wl,-rpath,{cuda / 'lib64'}"]
     HOST_BUILD.mkdir(parents=True, exist_ok=True)
-    if force or _newer(lib_srcs + hdrs + [INCLUDE / "rt_api.h", LIB], HOST_LIB):
+    if force or _newer(lib_srcs + hdrs + [INCLUDE / "rt_api.h", INCLUDE / "rt_model.h", LIB], HOST_LIB):
         tmp = HOST_LIB.with_suffix(".so.tmp")
-        _run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", *inc, *map(str, lib_srcs), "-o", str(tmp),
+        _run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", *inc, *map(str, lib_srcs), "-o", str(tmp),
               "-L", str(BUILD), "-lrtgb300", f"-Wl,-rpath,{BUILD}", *cudart])
         os.replace(tmp, HOST_LIB)
     demo_src = HOST / "rt_frame_demo.cpp"

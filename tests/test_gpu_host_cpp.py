@@ -52,3 +52,26 @@ def test_cpp_stage_classes(gpu_ctx, oracle_mod, tmp_path):
     ray = oracle_mod.rays_array(eye, (c - eye)[None], 1e16, -1)
     oh = oracle_mod.trace(nodes, depth, ids, tris, ray)
     assert summary["single_ray_id"] == int(oh["id"][0])
+
+
+def test_cpp_model_input(gpu_ctx, oracle_mod, tmp_path):
+    """rt_frame_demo with a model file: Model (Model::LoadFile + Scale)
+    feeds the same stage classes; the primary hits match the oracle traced
+    over the reference loader's soup of that file."""
+    from conftest import GOLDEN
+    from rtgpu import build, scenes
+    from rtgpu._lib import HIT_DTYPE
+    build.build_host()
+    soup = np.load(GOLDEN / "models" / "expected.npz")["torus_OBJ__soup"]
+    cam = scenes.look_at((0.3, -1.2, 0.9), (0.0, 0.0, 0.0), width=160, height=120)
+    np.array([*cam.eye, *cam.right, *cam.up, *cam.fwd, cam.tan_half_fovy], np.float32).tofile(tmp_path / "cam.f32")
+    depth = 12
+    r = subprocess.run([str(build.DEMO), str(GOLDEN / "models" / "torus.OBJ"), "0", str(tmp_path / "cam.f32"),
+                        str(cam.width), str(cam.height), "1", "1", "1", str(depth), "1", str(tmp_path / "m")],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    prim = np.fromfile(str(tmp_path / "m") + ".primary", HIT_DTYPE)
+    nodes, ids, _, _ = oracle_mod.lbvh_build(soup, depth)
+    oh = oracle_mod.trace(nodes, depth, ids, soup, oracle_mod.primary_rays(cam))
+    assert (oh["id"] >= 0).sum() > 1000
+    assert np.array_equal(prim["id"], oh["id"]) and np.array_equal(prim["t"], oh["t"])
