@@ -211,14 +211,18 @@ def run_ours(args, dist: Dist):
     lb = LBVH(ctx, n, args.depth)
     rt = RayTracer(ctx)
     hits = torch.empty((npx, 4), dtype=torch.int32, device=dev)
+    leaves = torch.empty(npx, dtype=torch.int32, device=dev)
     mirror = torch.empty((npx, 4), dtype=torch.int32, device=dev)
+    mleaves = torch.empty(npx, dtype=torch.int32, device=dev)
     vis = torch.empty(npx, dtype=torch.uint8, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
 
-    # algorithmic trace bytes of frame 0 from the per-ray test counters
+    # algorithmic trace bytes of frame 0 from the per-ray test counters of the
+    # frame path's walks (shading rays restarted at the primary leaves)
     lb.Build(dfr[0])
-    _, pst = rt.primary(lb, cam, stats=True, out=hits)
-    _, _, sst, mst = rt.shadow_mirror(lb, cam, light, hits, stats=True, vis=vis, mirror=mirror)
+    _, _, pst = rt.primary_leaves(lb, cam, stats=True, out=hits, leaves=leaves)
+    _, _, _, sst, mst = rt.shadow_mirror_from(lb, cam, light, hits, leaves, stats=True, vis=vis, mirror=mirror,
+                                              mirror_leaves=mleaves)
     ctx.check()
     pst, sst, mst = (x.to(torch.int64).sum(0).tolist() for x in (pst, sst, mst))
     visn = vis.cpu().numpy()
@@ -238,10 +242,10 @@ def run_ours(args, dist: Dist):
         lb.Build(f)
         if evs:
             evs[1].record(stream)
-        rt.primary(lb, cam, out=hits)
+        rt.primary_leaves(lb, cam, out=hits, leaves=leaves)
         if evs:
             evs[2].record(stream)
-        rt.shadow_mirror(lb, cam, light, hits, vis=vis, mirror=mirror)
+        rt.shadow_mirror_from(lb, cam, light, hits, leaves, vis=vis, mirror=mirror, mirror_leaves=mleaves)
         if evs:
             evs[3].record(stream)
 

@@ -199,9 +199,32 @@ rt_status rt_trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* lbvh, const rt_came
 rt_status rt_trace_rays(rt_ctx* ctx, const rt_lbvh* lbvh, const rt_ray* d_rays, uint32_t n, int any_hit,
                         rt_hit* d_hits, uint32_t* d_stats);
 
+/* Traversal restart: the iRoot of LBVH_IntersectP(ray, nodeNum)
+ * (LBVH.hlsl:363-376), which the reference feeds with the leaf where the
+ * previous intersection was found (CSIntersections.hlsl:32,
+ * CSComputeColorRT.hlsl:160).  A walk started at heap node k visits k's
+ * subtree and the siblings of k's ancestors, which together hold every
+ * triangle, so the hits equal a walk from the root (up to the order
+ * dependence every walk has between two triangles hit within an ulp of each
+ * other); a ray leaving a surface near its last hit reaches fewer boxes.  A start of 0 or 1 is the root; any
+ * other start must be a node the current build reached, such as a leaf one
+ * of these calls reported (1 is reported for a miss, for a ray handed to the
+ * warp-per-ray pass, and for every ray when the compact layout is built).
+ * d_leaves / d_mirror_leaves (nullable): the heap node whose triangles gave
+ * each closest hit. */
+rt_status rt_trace_primary_leaves(rt_ctx* ctx, const rt_lbvh* lbvh, const rt_camera* cam, rt_hit* d_hits,
+                                  uint32_t* d_leaves, uint32_t* d_stats);
+rt_status rt_trace_shadow_mirror_from(rt_ctx* ctx, const rt_lbvh* lbvh, const rt_camera* cam,
+                                      const float light[3], const rt_hit* d_primary,
+                                      const uint32_t* d_primary_leaves, uint8_t* d_vis, rt_hit* d_mirror,
+                                      uint32_t* d_mirror_leaves, uint32_t* d_shadow_stats, uint32_t* d_mirror_stats);
+rt_status rt_trace_rays_from(rt_ctx* ctx, const rt_lbvh* lbvh, const rt_ray* d_rays, uint32_t n, int any_hit,
+                             const uint32_t* d_starts, rt_hit* d_hits, uint32_t* d_leaves, uint32_t* d_stats);
+
 /* One frame of the dynamic path (RayTracerCS::Render with dynamic=1,
  * RayTracerCS.cpp:258-295): rebuild from a host soup, primary, shadow and
- * mirror rays, results copied back to host buffers (any may be NULL). */
+ * mirror rays (started at the primary hits' leaves), results copied back to
+ * host buffers (any may be NULL). */
 rt_status rt_render_frame_host(rt_ctx* ctx, rt_lbvh* lbvh, const float* h_tris, uint32_t n,
                                const rt_camera* cam, const float light[3], rt_hit* h_primary,
                                uint8_t* h_vis, rt_hit* h_mirror);

@@ -85,8 +85,11 @@ def olib() -> C.CDLL:
         L.or_lbvh_emit.argtypes = [vp, vp, vp, u32, u32, vp, vp]
         L.or_lbvh_build.argtypes = [vp, u32, u32, vp, vp, vp, vp]
         L.or_trace.argtypes = [vp, u32, vp, vp, vp, u32, vp, vp, i32, i32]
+        L.or_trace_from.argtypes = [vp, u32, vp, vp, vp, u32, vp, vp, vp, vp, i32, i32]
         L.or_primary_rays.argtypes = [C.POINTER(OrCamera), vp]
         L.or_shadow_mirror.argtypes = [vp, u32, vp, vp, C.POINTER(OrCamera), vp, vp, vp, vp, vp, vp, i32]
+        L.or_shadow_mirror_from.argtypes = [vp, u32, vp, vp, C.POINTER(OrCamera), vp, vp, vp, vp, vp, vp, vp, vp,
+                                            i32]
         L.or_pathtrace.argtypes = [vp, u32, vp, vp, vp, vp, C.POINTER(OrCamera), C.POINTER(OrPtParams), vp, i32]
         L.or_pathtrace_adjoint.argtypes = [vp, u32, vp, vp, vp, vp, C.POINTER(OrCamera), C.POINTER(OrPtParams),
                                            vp, vp, vp, i32]
@@ -155,6 +158,22 @@ def trace(nodes, depth, ids, tris, rays, any_hit=False, nthreads=None, stats=Fal
     return (hits, st) if stats else hits
 
 
+def trace_from(nodes, depth, ids, tris, rays, starts=None, any_hit=False, nthreads=None, stats=False):
+    """or_trace_from: the walk of each ray starts at heap node starts[i]
+    (None: the root).  Returns (hits, leaves[, stats]); leaves[i] = the node
+    whose triangles gave the closest hit (1 for a miss)."""
+    rays = np.ascontiguousarray(rays, np.float32)
+    n = len(rays)
+    hits = np.zeros(n, HIT_DTYPE)
+    leaves = np.zeros(n, np.uint32)
+    st = np.zeros((n, 2), np.uint32) if stats else None
+    sp = None if starts is None else np.ascontiguousarray(starts, np.uint32)
+    olib().or_trace_from(_ptr(nodes), depth, _ptr(ids), _ptr(np.ascontiguousarray(tris, np.float32)), _ptr(rays), n,
+                         _ptr(sp) if sp is not None else None, _ptr(hits), _ptr(leaves),
+                         _ptr(st) if stats else None, int(any_hit), nthreads or nthreads_default())
+    return (hits, leaves, st) if stats else (hits, leaves)
+
+
 def primary_rays(cam) -> np.ndarray:
     oc = to_or_camera(cam)
     r = np.zeros((cam.width * cam.height, 8), np.float32)
@@ -174,6 +193,25 @@ def shadow_mirror(nodes, depth, ids, tris, cam, light, prim, nthreads=None, stat
                             _ptr(mirror), _ptr(ss) if stats else None, _ptr(ms) if stats else None,
                             nthreads or nthreads_default())
     return (vis, mirror, ss, ms) if stats else (vis, mirror)
+
+
+def shadow_mirror_from(nodes, depth, ids, tris, cam, light, prim, prim_leaves, nthreads=None, stats=False):
+    """or_shadow_mirror_from: shading rays started at the primary hits'
+    leaves.  Returns (vis, mirror, mirror_leaves[, shadow_stats, mirror_stats])."""
+    oc = to_or_camera(cam)
+    npx = cam.width * cam.height
+    vis = np.zeros(npx, np.uint8)
+    mirror = np.zeros(npx, HIT_DTYPE)
+    ml = np.zeros(npx, np.uint32)
+    ss = np.zeros((npx, 2), np.uint32) if stats else None
+    ms = np.zeros((npx, 2), np.uint32) if stats else None
+    pl = None if prim_leaves is None else np.ascontiguousarray(prim_leaves, np.uint32)
+    olib().or_shadow_mirror_from(_ptr(nodes), depth, _ptr(ids), _ptr(np.ascontiguousarray(tris, np.float32)),
+                                 C.byref(oc), _ptr(np.asarray(light, np.float32)), _ptr(np.ascontiguousarray(prim)),
+                                 _ptr(pl) if pl is not None else None, _ptr(vis), _ptr(mirror), _ptr(ml),
+                                 _ptr(ss) if stats else None, _ptr(ms) if stats else None,
+                                 nthreads or nthreads_default())
+    return (vis, mirror, ml, ss, ms) if stats else (vis, mirror, ml)
 
 
 def pathtrace(nodes, depth, ids, tris, albedo, emission, cam, spp, bounces, seed, sky=(1.0, 1.0, 1.0), nthreads=None):

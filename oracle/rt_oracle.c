@@ -260,9 +260,25 @@ static inline int tri_test(const float* A, const float* B, const float* C, const
  * Walk: both children of an entered internal node (heap slots 2i, 2i+1) are
  * box-tested together, the near one is entered, a hit far one is pushed with
  * its entry distance and re-checked against the closest t when popped.
- * Box tests are counted as 1 (root) + 2 per entered internal node. */
-static void trace_one(const or_node* nodes, const uint32_t* ids, const float* tris, const float* r,
-                      or_hit* out, uint32_t* stats, int any_hit) {
+ * Box tests are counted as 1 (root) + 2 per entered internal node.
+ *
+ * Restart (the iRoot argument of LBVH_IntersectP, LBVH.hlsl:363-376, fed
+ * from the previous intersection's leaf at CSIntersections.hlsl:32 and
+ * CSComputeColorRT.hlsl:160): with start > 1 the walk begins at heap node
+ * `start` instead of the root.  The reference's trail bits then visit
+ * start, its sibling, the parent's sibling and so on up to level 1, which
+ * together cover the whole heap; here the siblings of start's ancestors are
+ * box-tested first (one test each, deepest on top of the stack) and start's
+ * own box next.  A box that contains a child's box admits the child's rays
+ * (the slab arithmetic is monotone in the bounds), so the closest hit is the
+ * one a walk from the root finds, except where two triangles are hit within
+ * an ulp of each other and a box entry distance rounded past the nearer one
+ * lets the order decide (as between any two walk orders).  start must
+ * be a node the build reached (a leaf a trace of the same tree returned).
+ * *leaf_out = the heap node whose triangles gave the closest hit (the
+ * reference's iRoot, LBVH.hlsl:422), or 1 when nothing was hit. */
+static void trace_one_from(const or_node* nodes, const uint32_t* ids, const float* tris, const float* r,
+                           or_hit* out, uint32_t* stats, int any_hit, uint32_t start, uint32_t* leaf_out) {
     const float o[3] = {r[0], r[1], r[2]};
     const float d[3] = {r[3], r[4], r[5]};
     const int exclude = (int)r[7];
@@ -270,14 +286,26 @@ static void trace_one(const or_node* nodes, const uint32_t* ids, const float* tr
     int sgn[3] = {d[0] < 0.0f, d[1] < 0.0f, d[2] < 0.0f};
     float best_t = r[6], best_u = -1.0f, best_v = -1.0f;
     int best_id = -1;
+    uint32_t best_leaf = 1;
     uint32_t nbox = 1, ntri = 0;
     uint32_t stack_node[64];
     float stack_t0[64];
     int sp = 0;
     float T0, T1;
-    box_interval(&nodes[1], o, inv, &T0, &T1);
-    int have = !(T1 < 0.0f) && !(T0 > best_t);
     uint32_t node = 1;
+    if (start > 1) {
+        const int D = hb32(start);
+        for (int k = 1; k <= D; ++k) {
+            const uint32_t sib = (start >> (D - k)) ^ 1u;
+            box_interval(&nodes[sib], o, inv, &T0, &T1);
+            ++nbox;
+            if (r[6] > 0.0f && !(T1 < 0.0f) && !(T0 > best_t)) { stack_node[sp] = sib; stack_t0[sp] = T0; ++sp; }
+        }
+        node = start;
+    }
+    box_interval(&nodes[node], o, inv, &T0, &T1);
+    /* no t satisfies 0 <= t < tmax when tmax <= 0 or is NaN */
+    int have = r[6] > 0.0f && !(T1 < 0.0f) && !(T0 > best_t);
     for (;;) {
         if (have) {
             const or_node* nd = &nodes[node];
@@ -292,7 +320,7 @@ static void trace_one(const or_node* nodes, const uint32_t* ids, const float* tr
                     float u, v, tt;
                     if (tri_test(t, t + 3, t + 6, o, d, &u, &v, &tt)) {
                         if (tt < best_t || (tt == best_t && best_id >= 0 && id < best_id)) {
-                            best_t = tt; best_u = u; best_v = v; best_id = id;
+                            best_t = tt; best_u = u; best_v = v; best_id = id; best_leaf = node;
                         }
                     }
                 }
@@ -332,6 +360,12 @@ static void trace_one(const or_node* nodes, const uint32_t* ids, const float* tr
     out->v = best_v;
     out->t = best_t;
     if (stats) { stats[0] = nbox; stats[1] = ntri; }
+    if (leaf_out) *leaf_out = best_leaf;
+}
+
+static void trace_one(const or_node* nodes, const uint32_t* ids, const float* tris, const float* r,
+                      or_hit* out, uint32_t* stats, int any_hit) {
+    trace_one_from(nodes, ids, tris, r, out, stats, any_hit, 1u, NULL);
 }
 
 void or_trace(const or_node* nodes, uint32_t depth, const uint32_t* ids, const float* tris,
@@ -342,6 +376,17 @@ void or_trace(const or_node* nodes, uint32_t depth, const uint32_t* ids, const f
 #pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
     for (long i = 0; i < (long)nrays; ++i)
         trace_one(nodes, ids, tris, rays + 8 * i, &hits[i], stats ? stats + 2 * i : NULL, any_hit);
+}
+
+void or_trace_from(const or_node* nodes, uint32_t depth, const uint32_t* ids, const float* tris,
+                   const float* rays, uint32_t nrays, const uint32_t* starts, or_hit* hits, uint32_t* leaves,
+                   uint32_t* stats, int any_hit, int nthreads) {
+    (void)depth;
+    if (nthreads <= 0) nthreads = 1;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+    for (long i = 0; i < (long)nrays; ++i)
+        trace_one_from(nodes, ids, tris, rays + 8 * i, &hits[i], stats ? stats + 2 * i : NULL, any_hit,
+                       starts ? starts[i] : 1u, leaves ? leaves + i : NULL);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -417,6 +462,18 @@ static void secondary(const float* tris, const float* r, const or_hit* h, const 
 void or_shadow_mirror(const or_node* nodes, uint32_t depth, const uint32_t* ids, const float* tris,
                       const or_camera* cam, const float light[3], const or_hit* prim, uint8_t* vis,
                       or_hit* mirror, uint32_t* shadow_stats, uint32_t* mirror_stats, int nthreads) {
+    or_shadow_mirror_from(nodes, depth, ids, tris, cam, light, prim, NULL, vis, mirror, NULL, shadow_stats,
+                          mirror_stats, nthreads);
+}
+
+/* The shading rays started at the primary hit's leaf (prim_leaves, the
+ * iRoot the colour stage passes to LBVH_IntersectP, CSComputeColorRT.hlsl:160,
+ * and the next intersection stage, CSIntersections.hlsl:32); NULL: the root.
+ * mirror_leaves (nullable) receives the mirror hit's leaf. */
+void or_shadow_mirror_from(const or_node* nodes, uint32_t depth, const uint32_t* ids, const float* tris,
+                           const or_camera* cam, const float light[3], const or_hit* prim,
+                           const uint32_t* prim_leaves, uint8_t* vis, or_hit* mirror, uint32_t* mirror_leaves,
+                           uint32_t* shadow_stats, uint32_t* mirror_stats, int nthreads) {
     (void)depth;
     const long npx = (long)cam->width * cam->height;
     if (nthreads <= 0) nthreads = 1;
@@ -426,11 +483,13 @@ void or_shadow_mirror(const or_node* nodes, uint32_t depth, const uint32_t* ids,
         uint32_t i = (uint32_t)(p % cam->width), j = (uint32_t)(p / cam->width);
         if (shadow_stats) { shadow_stats[2 * p] = 0; shadow_stats[2 * p + 1] = 0; }
         if (mirror_stats) { mirror_stats[2 * p] = 0; mirror_stats[2 * p + 1] = 0; }
+        if (mirror_leaves) mirror_leaves[p] = 1;
         if (prim[p].id < 0) {
             vis[p] = 0;
             mirror[p].id = -2; mirror[p].u = -1.0f; mirror[p].v = -1.0f; mirror[p].t = 0.0f;
             continue;
         }
+        const uint32_t start = prim_leaves ? prim_leaves[p] : 1u;
         float r[8];
         float x = (float)(2 * (int)i + 1 - (int)cam->width) * inv;
         float y = -((float)(2 * (int)j + 1 - (int)cam->height) * inv);
@@ -442,12 +501,13 @@ void or_shadow_mirror(const or_node* nodes, uint32_t depth, const uint32_t* ids,
         secondary(tris, r, &prim[p], light, sr, mr, &cast);
         if (cast) {
             or_hit sh;
-            trace_one(nodes, ids, tris, sr, &sh, shadow_stats ? shadow_stats + 2 * p : NULL, 1);
+            trace_one_from(nodes, ids, tris, sr, &sh, shadow_stats ? shadow_stats + 2 * p : NULL, 1, start, NULL);
             vis[p] = (sh.id >= 0) ? 2 : 3;
         } else {
             vis[p] = 1;
         }
-        trace_one(nodes, ids, tris, mr, &mirror[p], mirror_stats ? mirror_stats + 2 * p : NULL, 0);
+        trace_one_from(nodes, ids, tris, mr, &mirror[p], mirror_stats ? mirror_stats + 2 * p : NULL, 0, start,
+                       mirror_leaves ? mirror_leaves + p : NULL);
     }
 }
 

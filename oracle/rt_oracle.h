@@ -65,6 +65,14 @@ void or_trace(const or_node* nodes, uint32_t depth, const uint32_t* ids, const f
               const float* rays, uint32_t nrays, or_hit* hits, uint32_t* stats, int any_hit,
               int nthreads);
 
+/* The same with the walk started at heap node starts[i] (NULL or values
+ * <= 1: the root), the iRoot restart of LBVH_IntersectP (LBVH.hlsl:363-376);
+ * leaves (nullable) receives the node whose triangles gave each closest hit
+ * (1 for a miss).  A start must be a node the build reached. */
+void or_trace_from(const or_node* nodes, uint32_t depth, const uint32_t* ids, const float* tris,
+                   const float* rays, uint32_t nrays, const uint32_t* starts, or_hit* hits, uint32_t* leaves,
+                   uint32_t* stats, int any_hit, int nthreads);
+
 /* --- ray generation and shading rays (CSPrimaryRays.hlsl, CSComputeColorRT.hlsl) */
 void or_primary_rays(const or_camera* cam, float* rays /* w*h x 8 */);
 /* From primary hits: shadow-ray visibility code per pixel
@@ -75,6 +83,14 @@ void or_shadow_mirror(const or_node* nodes, uint32_t depth, const uint32_t* ids,
                       const or_camera* cam, const float light[3], const or_hit* prim,
                       uint8_t* vis, or_hit* mirror, uint32_t* shadow_stats, uint32_t* mirror_stats,
                       int nthreads);
+
+/* The same with each pixel's shading rays started at its primary hit's leaf
+ * (prim_leaves from or_trace_from; NULL: the root); mirror_leaves
+ * (nullable) receives the mirror hit's leaf.  Hits equal or_shadow_mirror's. */
+void or_shadow_mirror_from(const or_node* nodes, uint32_t depth, const uint32_t* ids, const float* tris,
+                           const or_camera* cam, const float light[3], const or_hit* prim,
+                           const uint32_t* prim_leaves, uint8_t* vis, or_hit* mirror, uint32_t* mirror_leaves,
+                           uint32_t* shadow_stats, uint32_t* mirror_stats, int nthreads);
 
 /* --- path tracer (CSComputeColorGI.hlsl:19-238, ConstantBuffers.h:85-110) */
 typedef struct or_pt_params {

@@ -79,9 +79,7 @@ extern "C" rt_status rt_frame_capture(rt_ctx* ctx, rt_lbvh* l, const float* d_tr
         ctx, "rt_frame_capture",
         [&]() {
             rt_status s = rt_lbvh_build(ctx, l, d_tris, n, flags);
-            if (s == RT_OK) s = rt_trace_primary(ctx, l, cam, d_primary, nullptr);
-            if (s == RT_OK && (d_vis || d_mirror))
-                s = rt_trace_shadow_mirror(ctx, l, cam, light, d_primary, d_vis, d_mirror, nullptr, nullptr);
+            if (s == RT_OK) s = trace_frame(ctx, l, cam, light, d_primary, d_vis, d_mirror, "rt_frame_capture");
             return s;
         },
         out);

@@ -228,6 +228,10 @@ enum : int {
 // Grows the compacted shading-ray lists of l to px pixels (synchronises the
 // context stream when it allocates; call before a stream capture).
 rt_status ensure_shade_lists(rt_ctx* ctx, rt_lbvh* l, size_t px);
+// Primary rays, then (d_vis or d_mirror set) the shading rays started at the
+// primary leaves; the shading lists must hold the image (ensure_shade_lists).
+rt_status trace_frame(rt_ctx* ctx, rt_lbvh* l, const rt_camera* cam, const float light[3], rt_hit* d_primary,
+                      uint8_t* d_vis, rt_hit* d_mirror, const char* who);
 
 inline rt_status reset_work(rt_ctx* ctx, int slot) {
     RT_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_work + slot, 0, sizeof(uint32_t), ctx->stream));

@@ -38,6 +38,7 @@ __device__ __forceinline__ void spill_record(uint32_t* list, int slot, uint32_t 
 template <bool STATS>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_camera cam,
                                                                  rt_hit* __restrict__ hits,
+                                                                 uint32_t* __restrict__ leaves,
                                                                  uint32_t* __restrict__ stats, uint32_t* work,
                                                                  uint32_t num_tiles, Spill spill,
                                                                  uint32_t* __restrict__ list, TileOrder ord) {
@@ -49,15 +50,16 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_
         if (!valid) i = j = 0;  // lanes past the image edge only help the warp
         const f3 d = primary_dir(cam, i, j);
         const RayState r = make_ray(mk3(cam.eye[0], cam.eye[1], cam.eye[2]), d, 1e16f, -1);
-        uint32_t nb = 0, nt = 0;
+        uint32_t nb = 0, nt = 0, leaf = 1;
         int slot = -1;
-        const Hit h = trace_ray<STATS>(r, valid, tr, false, &nb, &nt, &spill, &slot);
+        const Hit h = trace_ray<STATS>(r, valid, tr, false, &nb, &nt, &spill, &slot, 1u, &leaf);
         if (valid) {
             const size_t p = (size_t)j * cam.width + i;
             if (slot >= 0) {
                 spill_record(list, slot, kHeavyPrimary, p);
             } else {
                 store_hit(hits + p, h);
+                if (leaves) leaves[p] = leaf;
             }
             if (STATS) {
                 stats[2 * p] = nb;
@@ -128,13 +130,14 @@ __device__ __forceinline__ void secondary_pixel(const TreeRef& tr, const float* 
                                                 uint8_t* __restrict__ vis, rt_hit* __restrict__ mirror,
                                                 uint32_t* __restrict__ sstats, uint32_t* __restrict__ mstats,
                                                 bool valid, uint32_t i, uint32_t j, const Spill* spill,
-                                                uint32_t* __restrict__ list, uint32_t* tests = nullptr) {
+                                                uint32_t* __restrict__ list, uint32_t* tests, uint32_t start,
+                                                uint32_t* __restrict__ mirror_leaves) {
     const size_t p = (size_t)j * cam.width + i;
     const ShadeRays s = shade_rays(soup, cam, lx, ly, lz, ph, valid, i, j, mirror != nullptr);
     uint32_t snb = 0, snt = 0, mnb = 0, mnt = 0;
     if (vis) {  // uniform across the warp
         int slot = -1;
-        const Hit sh = trace_ray<STATS>(s.shadow, s.cast, tr, true, &snb, &snt, spill, &slot);
+        const Hit sh = trace_ray<STATS>(s.shadow, s.cast, tr, true, &snb, &snt, spill, &slot, start);
         if (valid) {
             if (slot >= 0) spill_record(list, slot, kHeavyShadow, p);
             else vis[p] = vis_code(s.has, s.cast, sh.id >= 0);
@@ -142,13 +145,18 @@ __device__ __forceinline__ void secondary_pixel(const TreeRef& tr, const float* 
     }
     if (mirror) {
         int slot = -1;
-        Hit mh = trace_ray<STATS>(s.mirror, s.has, tr, false, &mnb, &mnt, spill, &slot);
+        uint32_t leaf = 1;
+        Hit mh = trace_ray<STATS>(s.mirror, s.has, tr, false, &mnb, &mnt, spill, &slot, start, &leaf);
         if (!s.has) {
             mh.id = -2; mh.u = -1.0f; mh.v = -1.0f; mh.t = 0.0f;
         }
         if (valid) {
-            if (slot >= 0) spill_record(list, slot, kHeavyMirror, p);
-            else store_hit(mirror + p, mh);
+            if (slot >= 0) {
+                spill_record(list, slot, kHeavyMirror, p);
+            } else {
+                store_hit(mirror + p, mh);
+                if (mirror_leaves) mirror_leaves[p] = leaf;
+            }
         }
     }
     if (STATS && valid) {
@@ -158,12 +166,19 @@ __device__ __forceinline__ void secondary_pixel(const TreeRef& tr, const float* 
     if (tests) *tests = snb + snt + mnb + mnt;
 }
 
+// Restart node of a pixel's shading rays: its primary hit's leaf, or the root.
+__device__ __forceinline__ uint32_t shade_start(const uint32_t* __restrict__ prim_leaves, int4 ph, bool valid,
+                                                size_t p) {
+    return (prim_leaves && valid && ph.x >= 0) ? __ldg(prim_leaves + p) : 1u;
+}
+
 template <bool STATS>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_secondary(
     TreeRef tr, const float* __restrict__ soup, rt_camera cam, float lx, float ly, float lz,
-    const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis, rt_hit* __restrict__ mirror,
-    uint32_t* __restrict__ sstats, uint32_t* __restrict__ mstats, uint32_t* work, uint32_t num_tiles, Spill spill,
-    uint32_t* __restrict__ list, TileOrder ord) {
+    const rt_hit* __restrict__ prim, const uint32_t* __restrict__ prim_leaves, uint8_t* __restrict__ vis,
+    rt_hit* __restrict__ mirror, uint32_t* __restrict__ mirror_leaves, uint32_t* __restrict__ sstats,
+    uint32_t* __restrict__ mstats, uint32_t* work, uint32_t num_tiles, Spill spill, uint32_t* __restrict__ list,
+    TileOrder ord) {
     const uint32_t wbuf = *ord.parity, rbuf = wbuf ^ 1u, heavy = min(ord.counts[rbuf], ord.cap);
     for (uint32_t tile = next_ordered_tile(work, ord, rbuf, heavy, num_tiles); tile < num_tiles;
          tile = next_ordered_tile(work, ord, rbuf, heavy, num_tiles)) {
@@ -174,7 +189,8 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_secondary(
         if (valid) ph = __ldg(reinterpret_cast<const int4*>(prim + (size_t)j * cam.width + i));
         uint32_t tests = 0;
         secondary_pixel<STATS>(tr, soup, cam, lx, ly, lz, ph, vis, mirror, sstats, mstats, valid, i, j, &spill,
-                               list, &tests);
+                               list, &tests, shade_start(prim_leaves, ph, valid, (size_t)j * cam.width + i),
+                               mirror_leaves);
         record_tile_cost(ord, wbuf, tile, tests);
     }
 }
@@ -200,8 +216,9 @@ __device__ __forceinline__ void append_pixel(bool take, uint32_t p, uint32_t* li
 
 __global__ void __launch_bounds__(256) k_shade_setup(const float* __restrict__ soup, rt_camera cam, float lx, float ly,
                                                      float lz, const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis,
-                                                     rt_hit* __restrict__ mirror, uint32_t* __restrict__ lists,
-                                                     uint32_t cap, uint32_t* counts, uint32_t num_tiles) {
+                                                     rt_hit* __restrict__ mirror, uint32_t* __restrict__ mirror_leaves,
+                                                     uint32_t* __restrict__ lists, uint32_t cap, uint32_t* counts,
+                                                     uint32_t num_tiles) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t t = warp; t < num_tiles; t += nwarps) {
@@ -218,6 +235,7 @@ __global__ void __launch_bounds__(256) k_shade_setup(const float* __restrict__ s
                 Hit mh;
                 mh.id = -2; mh.u = -1.0f; mh.v = -1.0f; mh.t = 0.0f;
                 store_hit(mirror + p, mh);
+                if (mirror_leaves) mirror_leaves[p] = 1u;
             }
         }
         append_pixel(vis && valid && s.has && s.cast, (uint32_t)p, lists, cap, counts);
@@ -227,9 +245,9 @@ __global__ void __launch_bounds__(256) k_shade_setup(const float* __restrict__ s
 
 __global__ void __launch_bounds__(kTraceThreads) k_trace_shade(
     TreeRef tr, const float* __restrict__ soup, rt_camera cam, float lx, float ly, float lz,
-    const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis, rt_hit* __restrict__ mirror,
-    const uint32_t* __restrict__ lists, uint32_t cap, const uint32_t* counts, uint32_t* work, Spill spill,
-    uint32_t* __restrict__ list) {
+    const rt_hit* __restrict__ prim, const uint32_t* __restrict__ prim_leaves, uint8_t* __restrict__ vis,
+    rt_hit* __restrict__ mirror, uint32_t* __restrict__ mirror_leaves, const uint32_t* __restrict__ lists,
+    uint32_t cap, const uint32_t* counts, uint32_t* work, Spill spill, uint32_t* __restrict__ list) {
     const uint32_t ns = min(counts[0], cap), nm = min(counts[1], cap);
     const uint32_t cs = (ns + 31) / 32, cm = (nm + 31) / 32;
     const uint32_t lane = threadIdx.x & 31;
@@ -243,19 +261,24 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_shade(
         int4 ph = make_int4(-1, 0, 0, 0);
         if (valid) ph = __ldg(reinterpret_cast<const int4*>(prim + p));
         const ShadeRays s = shade_rays(soup, cam, lx, ly, lz, ph, valid, i, j, !shadow);
-        uint32_t nb = 0, nt = 0;
+        const uint32_t start = shade_start(prim_leaves, ph, valid, p);
+        uint32_t nb = 0, nt = 0, leaf = 1;
         int slot = -1;
         if (shadow) {
-            const Hit h = trace_ray<false>(s.shadow, valid && s.cast, tr, true, &nb, &nt, &spill, &slot);
+            const Hit h = trace_ray<false>(s.shadow, valid && s.cast, tr, true, &nb, &nt, &spill, &slot, start);
             if (valid) {
                 if (slot >= 0) spill_record(list, slot, kHeavyShadow, p);
                 else vis[p] = vis_code(s.has, s.cast, h.id >= 0);
             }
         } else {
-            const Hit h = trace_ray<false>(s.mirror, valid && s.has, tr, false, &nb, &nt, &spill, &slot);
+            const Hit h = trace_ray<false>(s.mirror, valid && s.has, tr, false, &nb, &nt, &spill, &slot, start, &leaf);
             if (valid) {
-                if (slot >= 0) spill_record(list, slot, kHeavyMirror, p);
-                else store_hit(mirror + p, h);
+                if (slot >= 0) {
+                    spill_record(list, slot, kHeavyMirror, p);
+                } else {
+                    store_hit(mirror + p, h);
+                    if (mirror_leaves) mirror_leaves[p] = leaf;
+                }
             }
         }
     }
@@ -272,7 +295,8 @@ __device__ __forceinline__ RayState load_ray(const rt_ray* __restrict__ rays, ui
 
 template <bool STATS>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_rays(TreeRef tr, const rt_ray* __restrict__ rays, uint32_t n,
-                                                              int any_hit, rt_hit* __restrict__ hits,
+                                                              int any_hit, const uint32_t* __restrict__ starts,
+                                                              rt_hit* __restrict__ hits, uint32_t* __restrict__ leaves,
                                                               uint32_t* __restrict__ stats, uint32_t* work,
                                                               Spill spill, uint32_t* __restrict__ list,
                                                               TileOrder ord) {
@@ -283,14 +307,16 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_rays(TreeRef tr, const 
         const uint32_t k = tile * 32 + (threadIdx.x & 31);
         const bool valid = k < n;
         const RayState r = load_ray(rays, k, valid);
-        uint32_t nb = 0, nt = 0;
+        const uint32_t start = (starts && valid) ? __ldg(starts + k) : 1u;
+        uint32_t nb = 0, nt = 0, leaf = 1;
         int slot = -1;
-        const Hit h = trace_ray<STATS>(r, valid, tr, any_hit != 0, &nb, &nt, &spill, &slot);
+        const Hit h = trace_ray<STATS>(r, valid, tr, any_hit != 0, &nb, &nt, &spill, &slot, start, &leaf);
         if (valid) {
             if (slot >= 0) {
                 spill_record(list, slot, kHeavyRay, k);
             } else {
                 store_hit(hits + k, h);
+                if (leaves) leaves[k] = leaf;
             }
             if (STATS) {
                 stats[2 * k] = nb;
@@ -315,6 +341,8 @@ struct HeavyArgs {
     rt_hit* mirror;
     const rt_ray* rays;
     int any_hit;          // generic rays
+    uint32_t* leaves;     // primary / generic-ray leaf output (nullable)
+    uint32_t* mirror_leaves;
     const uint32_t* list;
     const uint32_t* count;
     uint32_t cap;
@@ -332,11 +360,17 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_heavy(HeavyArgs a) {
             const RayState r = make_ray(mk3(a.cam.eye[0], a.cam.eye[1], a.cam.eye[2]), primary_dir(a.cam, i, j),
                                         1e16f, -1);
             const Hit h = trace_wide(r, a.tr, false);
-            if (lane == 0) store_hit(a.hits + idx, h);
+            if (lane == 0) {
+                store_hit(a.hits + idx, h);
+                if (a.leaves) a.leaves[idx] = 1u;  // the root: a valid restart node
+            }
         } else if (kind == kHeavyRay) {
             const RayState r = load_ray(a.rays, idx, true);
             const Hit h = trace_wide(r, a.tr, a.any_hit != 0);
-            if (lane == 0) store_hit(a.hits + idx, h);
+            if (lane == 0) {
+                store_hit(a.hits + idx, h);
+                if (a.leaves) a.leaves[idx] = 1u;
+            }
         } else {
             const uint32_t i = idx % a.cam.width, j = idx / a.cam.width;
             const int4 ph = __ldg(reinterpret_cast<const int4*>(a.prim + idx));
@@ -346,7 +380,10 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_heavy(HeavyArgs a) {
                 if (lane == 0) a.vis[idx] = vis_code(s.has, s.cast, h.id >= 0);
             } else {
                 const Hit h = trace_wide(s.mirror, a.tr, false);
-                if (lane == 0) store_hit(a.mirror + idx, h);
+                if (lane == 0) {
+                    store_hit(a.mirror + idx, h);
+                    if (a.mirror_leaves) a.mirror_leaves[idx] = 1u;
+                }
             }
         }
     }
@@ -373,7 +410,8 @@ rt_status ensure_shade_lists(rt_ctx* ctx, rt_lbvh* l, size_t px) {
     if (l->s_lists) cudaFree(l->s_lists);
     l->s_lists = nullptr;
     l->s_pixels = 0;
-    RT_CHECK_CUDA(ctx, cudaMalloc((void**)&l->s_lists, 2 * sizeof(uint32_t) * px));
+    // shadow-ray pixels, mirror-ray pixels, primary leaves of a frame
+    RT_CHECK_CUDA(ctx, cudaMalloc((void**)&l->s_lists, 3 * sizeof(uint32_t) * px));
     l->s_pixels = px;
     return RT_OK;
 }
@@ -470,11 +508,13 @@ HeavyArgs heavy_args(rt_ctx* ctx, const rt_lbvh* l) {
 
 }  // namespace
 
-extern "C" rt_status rt_trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, rt_hit* d_hits,
-                                      uint32_t* d_stats) {
-    rt_status s = check_trace_args(ctx, l, cam, "rt_trace_primary");
+namespace {
+
+rt_status trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, rt_hit* d_hits, uint32_t* d_leaves,
+                        uint32_t* d_stats, const char* who) {
+    rt_status s = check_trace_args(ctx, l, cam, who);
     if (s != RT_OK) return s;
-    if (!d_hits) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_primary: null output");
+    if (!d_hits) return rt_fail(ctx, RT_ERR_INVALID, "%s: null output", who);
     if ((s = reset_work(ctx, kWorkPrimary)) != RT_OK) return s;
     const Spill sp = spill_of(ctx, !d_stats && (uint64_t)cam->width * cam->height <= kHeavyIndexMask);
     if ((s = reset_spill(ctx, sp)) != RT_OK) return s;
@@ -485,26 +525,28 @@ extern "C" rt_status rt_trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_ca
     if (d_stats) {
         auto k = k_trace_primary<true>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), *cam, d_hits, d_stats, work, tiles, sp, ctx->d_spill, ord);
+            tree_ref(ctx, l), *cam, d_hits, d_leaves, d_stats, work, tiles, sp, ctx->d_spill, ord);
     } else {
         auto k = k_trace_primary<false>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), *cam, d_hits, nullptr, work, tiles, sp, ctx->d_spill, ord);
+            tree_ref(ctx, l), *cam, d_hits, d_leaves, nullptr, work, tiles, sp, ctx->d_spill, ord);
     }
     RT_CHECK_LAUNCH(ctx, "k_trace_primary");
     HeavyArgs a = heavy_args(ctx, l);
     a.cam = *cam;
     a.hits = d_hits;
+    a.leaves = d_leaves;
     return launch_heavy(ctx, sp, a);
 }
 
-extern "C" rt_status rt_trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, const float light[3],
-                                            const rt_hit* d_primary, uint8_t* d_vis, rt_hit* d_mirror,
-                                            uint32_t* d_shadow_stats, uint32_t* d_mirror_stats) {
-    rt_status s = check_trace_args(ctx, l, cam, "rt_trace_shadow_mirror");
+rt_status trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, const float light[3],
+                              const rt_hit* d_primary, const uint32_t* d_prim_leaves, uint8_t* d_vis,
+                              rt_hit* d_mirror, uint32_t* d_mirror_leaves, uint32_t* d_shadow_stats,
+                              uint32_t* d_mirror_stats, const char* who) {
+    rt_status s = check_trace_args(ctx, l, cam, who);
     if (s != RT_OK) return s;
-    if (!light || !d_primary) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_shadow_mirror: null argument");
-    if (!l->src_tris) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_shadow_mirror: no triangle soup bound");
+    if (!light || !d_primary) return rt_fail(ctx, RT_ERR_INVALID, "%s: null argument", who);
+    if (!l->src_tris) return rt_fail(ctx, RT_ERR_INVALID, "%s: no triangle soup bound", who);
     if ((s = reset_work(ctx, kWorkSecondary)) != RT_OK) return s;
     const bool stats = d_shadow_stats || d_mirror_stats;
     const Spill sp = spill_of(ctx, !stats && (uint64_t)cam->width * cam->height <= kHeavyIndexMask);
@@ -516,8 +558,8 @@ extern "C" rt_status rt_trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const
         uint32_t* work = ctx->d_work + kWorkSecondary;
         auto k = k_trace_secondary<true>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_vis, d_mirror,
-            d_shadow_stats, d_mirror_stats, work, tiles, sp, ctx->d_spill, ord);
+            tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_prim_leaves, d_vis,
+            d_mirror, d_mirror_leaves, d_shadow_stats, d_mirror_stats, work, tiles, sp, ctx->d_spill, ord);
         RT_CHECK_LAUNCH(ctx, "k_trace_secondary");
     } else {  // compacted shading-ray lists
         const size_t px = (size_t)cam->width * cam->height;
@@ -528,15 +570,16 @@ extern "C" rt_status rt_trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const
         const uint32_t cap = (uint32_t)l->s_pixels;
         const uint32_t sblocks = std::max(1u, std::min((tiles + 7) / 8, (uint32_t)ctx->num_sms * 8));
         k_shade_setup<<<sblocks, 256, 0, ctx->stream>>>(l->src_tris, *cam, light[0], light[1], light[2], d_primary,
-                                                         d_vis, d_mirror, l->s_lists, cap, counts, tiles);
+                                                         d_vis, d_mirror, d_mirror_leaves, l->s_lists, cap, counts,
+                                                         tiles);
         RT_CHECK_LAUNCH(ctx, "k_shade_setup");
         int per_sm = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_shade, kTraceThreads, 0) != cudaSuccess ||
             per_sm < 1)
             per_sm = 1;
         k_trace_shade<<<(uint32_t)per_sm * ctx->num_sms, kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_vis, d_mirror, l->s_lists,
-            cap, counts, ctx->d_work + kWorkShade, sp, ctx->d_spill);
+            tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_prim_leaves, d_vis,
+            d_mirror, d_mirror_leaves, l->s_lists, cap, counts, ctx->d_work + kWorkShade, sp, ctx->d_spill);
         RT_CHECK_LAUNCH(ctx, "k_trace_shade");
     }
     HeavyArgs a = heavy_args(ctx, l);
@@ -548,14 +591,16 @@ extern "C" rt_status rt_trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const
     a.prim = d_primary;
     a.vis = d_vis;
     a.mirror = d_mirror;
+    a.mirror_leaves = d_mirror_leaves;
     return launch_heavy(ctx, sp, a);
 }
 
-extern "C" rt_status rt_trace_rays(rt_ctx* ctx, const rt_lbvh* l, const rt_ray* d_rays, uint32_t n, int any_hit,
-                                   rt_hit* d_hits, uint32_t* d_stats) {
+rt_status trace_rays(rt_ctx* ctx, const rt_lbvh* l, const rt_ray* d_rays, uint32_t n, int any_hit,
+                     const uint32_t* d_starts, rt_hit* d_hits, uint32_t* d_leaves, uint32_t* d_stats,
+                     const char* who) {
     if (!ctx) return RT_ERR_INVALID;
-    if (!l || !d_rays || !d_hits) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_rays: null argument");
-    if (l->n == 0) return rt_fail(ctx, RT_ERR_INVALID, "rt_trace_rays: the LBVH has not been built");
+    if (!l || !d_rays || !d_hits) return rt_fail(ctx, RT_ERR_INVALID, "%s: null argument", who);
+    if (l->n == 0) return rt_fail(ctx, RT_ERR_INVALID, "%s: the LBVH has not been built", who);
     if (n == 0) return RT_OK;
     rt_status s = reset_work(ctx, kWorkRays);
     if (s != RT_OK) return s;
@@ -568,18 +613,71 @@ extern "C" rt_status rt_trace_rays(rt_ctx* ctx, const rt_lbvh* l, const rt_ray* 
     if (d_stats) {
         auto k = k_trace_rays<true>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), d_rays, n, any_hit, d_hits, d_stats, work, sp, ctx->d_spill, ord);
+            tree_ref(ctx, l), d_rays, n, any_hit, d_starts, d_hits, d_leaves, d_stats, work, sp, ctx->d_spill, ord);
     } else {
         auto k = k_trace_rays<false>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), d_rays, n, any_hit, d_hits, nullptr, work, sp, ctx->d_spill, ord);
+            tree_ref(ctx, l), d_rays, n, any_hit, d_starts, d_hits, d_leaves, nullptr, work, sp, ctx->d_spill, ord);
     }
     RT_CHECK_LAUNCH(ctx, "k_trace_rays");
     HeavyArgs a = heavy_args(ctx, l);
     a.rays = d_rays;
     a.any_hit = any_hit;
     a.hits = d_hits;
+    a.leaves = d_leaves;
     return launch_heavy(ctx, sp, a);
+}
+
+}  // namespace
+
+extern "C" rt_status rt_trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, rt_hit* d_hits,
+                                      uint32_t* d_stats) {
+    return trace_primary(ctx, l, cam, d_hits, nullptr, d_stats, "rt_trace_primary");
+}
+
+extern "C" rt_status rt_trace_primary_leaves(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, rt_hit* d_hits,
+                                             uint32_t* d_leaves, uint32_t* d_stats) {
+    return trace_primary(ctx, l, cam, d_hits, d_leaves, d_stats, "rt_trace_primary_leaves");
+}
+
+extern "C" rt_status rt_trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, const float light[3],
+                                            const rt_hit* d_primary, uint8_t* d_vis, rt_hit* d_mirror,
+                                            uint32_t* d_shadow_stats, uint32_t* d_mirror_stats) {
+    return trace_shadow_mirror(ctx, l, cam, light, d_primary, nullptr, d_vis, d_mirror, nullptr, d_shadow_stats,
+                               d_mirror_stats, "rt_trace_shadow_mirror");
+}
+
+extern "C" rt_status rt_trace_shadow_mirror_from(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam,
+                                                 const float light[3], const rt_hit* d_primary,
+                                                 const uint32_t* d_primary_leaves, uint8_t* d_vis, rt_hit* d_mirror,
+                                                 uint32_t* d_mirror_leaves, uint32_t* d_shadow_stats,
+                                                 uint32_t* d_mirror_stats) {
+    return trace_shadow_mirror(ctx, l, cam, light, d_primary, d_primary_leaves, d_vis, d_mirror, d_mirror_leaves,
+                               d_shadow_stats, d_mirror_stats, "rt_trace_shadow_mirror_from");
+}
+
+extern "C" rt_status rt_trace_rays(rt_ctx* ctx, const rt_lbvh* l, const rt_ray* d_rays, uint32_t n, int any_hit,
+                                   rt_hit* d_hits, uint32_t* d_stats) {
+    return trace_rays(ctx, l, d_rays, n, any_hit, nullptr, d_hits, nullptr, d_stats, "rt_trace_rays");
+}
+
+extern "C" rt_status rt_trace_rays_from(rt_ctx* ctx, const rt_lbvh* l, const rt_ray* d_rays, uint32_t n, int any_hit,
+                                        const uint32_t* d_starts, rt_hit* d_hits, uint32_t* d_leaves,
+                                        uint32_t* d_stats) {
+    return trace_rays(ctx, l, d_rays, n, any_hit, d_starts, d_hits, d_leaves, d_stats, "rt_trace_rays_from");
+}
+
+// The trace stages of one frame: primary rays, then the shading rays started
+// at each primary hit's leaf (the iRoot restart; the leaves live in the third
+// segment of the shading lists, which the caller has sized).
+rt_status trace_frame(rt_ctx* ctx, rt_lbvh* l, const rt_camera* cam, const float light[3], rt_hit* d_primary,
+                      uint8_t* d_vis, rt_hit* d_mirror, const char* who) {
+    const size_t px = (size_t)cam->width * cam->height;
+    uint32_t* leaves = (d_vis || d_mirror) && l->s_pixels >= px ? l->s_lists + 2 * l->s_pixels : nullptr;
+    rt_status s = trace_primary(ctx, l, cam, d_primary, leaves, nullptr, who);
+    if (s == RT_OK && (d_vis || d_mirror))
+        s = trace_shadow_mirror(ctx, l, cam, light, d_primary, leaves, d_vis, d_mirror, nullptr, nullptr, nullptr, who);
+    return s;
 }
 
 static rt_status render_frame_host(rt_ctx* ctx, rt_lbvh* l, const float* h_tris, uint32_t n, const rt_camera* cam,
@@ -600,13 +698,14 @@ static rt_status render_frame_host(rt_ctx* ctx, rt_lbvh* l, const float* h_tris,
         RT_CHECK_CUDA(ctx, cudaMalloc((void**)&l->f_vis, px));
         l->f_pixels = px;
     }
-    rt_status s = rt_lbvh_build_host(ctx, l, h_tris, n, 0);
-    if (s != RT_OK) return s;
-    s = rt_trace_primary(ctx, l, cam, l->f_primary, nullptr);
-    if (s != RT_OK) return s;
-    s = rt_trace_shadow_mirror(ctx, l, cam, light, l->f_primary, h_vis ? l->f_vis : nullptr,
-                               h_mirror ? l->f_mirror : nullptr, nullptr, nullptr);
-    if (s != RT_OK) return s;
+    rt_status s = RT_OK;
+    if (h_vis || h_mirror) {
+        if ((s = ensure_shade_lists(ctx, l, px)) != RT_OK) return s;
+    }
+    if ((s = rt_lbvh_build_host(ctx, l, h_tris, n, 0)) != RT_OK) return s;
+    if ((s = trace_frame(ctx, l, cam, light, l->f_primary, h_vis ? l->f_vis : nullptr, h_mirror ? l->f_mirror : nullptr,
+                         who)) != RT_OK)
+        return s;
     cudaStream_t st = ctx->stream;
     if (h_primary) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_primary, l->f_primary, sizeof(rt_hit) * px, cudaMemcpyDeviceToHost, st));
     if (h_vis) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_vis, l->f_vis, px, cudaMemcpyDeviceToHost, st));
@@ -676,15 +775,16 @@ __global__ void __launch_bounds__(256) k_batch_trace(BatchTraceArgs a, uint32_t*
             if (!valid) i = j = 0;
             const f3 d = primary_dir(cam, i, j);
             const RayState r = make_ray(mk3(cam.eye[0], cam.eye[1], cam.eye[2]), d, 1e16f, -1);
-            uint32_t nb = 0, nt = 0;
-            const Hit h = trace_ray<false>(r, valid, tr, false, &nb, &nt);
+            uint32_t nb = 0, nt = 0, leaf = 1;
+            const Hit h = trace_ray<false>(r, valid, tr, false, &nb, &nt, nullptr, nullptr, 1u, &leaf);
             const size_t p = (size_t)j * a.width + i;
             if (valid) store_hit(a.hits + s * px + p, h);
-            if (a.vis) {  // uniform across the grid
+            if (a.vis) {  // uniform across the grid; the shadow ray restarts at the primary leaf
                 const int4 ph = make_int4(h.id, __float_as_int(h.u), __float_as_int(h.v), __float_as_int(h.t));
                 secondary_pixel<false>(tr, a.soup + 9 * (size_t)toff, cam, __ldg(a.lights + 3 * s),
                                        __ldg(a.lights + 3 * s + 1), __ldg(a.lights + 3 * s + 2), ph,
-                                       a.vis + s * px, nullptr, nullptr, nullptr, valid, i, j, nullptr, nullptr);
+                                       a.vis + s * px, nullptr, nullptr, nullptr, valid, i, j, nullptr, nullptr,
+                                       nullptr, h.id >= 0 ? leaf : 1u, nullptr);
             }
         }
     }

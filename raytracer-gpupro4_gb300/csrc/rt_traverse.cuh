@@ -155,6 +155,7 @@ struct Best {
     uint64_t key;
     float t, u, v;
     int id;
+    uint32_t leaf;  // node whose triangles gave the hit (the reference's iRoot)
 };
 
 __device__ __forceinline__ float key_t(uint64_t key) { return __uint_as_float((uint32_t)(key >> 32)); }
@@ -169,7 +170,7 @@ __device__ __forceinline__ float key_t(uint64_t key) { return __uint_as_float((u
 // returns true when b (and the bound) improved.
 template <bool STATS>
 __device__ __forceinline__ bool leaf_phase(const TreeRef& tr_, const RayState& r, bool have, const NodeBox& cur,
-                                           uint64_t& bound, Best& b, uint32_t& ntri) {
+                                           uint32_t node, uint64_t& bound, Best& b, uint32_t& ntri) {
     constexpr uint32_t kFull = 0xffffffffu;
     const float4* __restrict__ tris = tr_.tris;
     const int lane = threadIdx.x & 31;
@@ -222,6 +223,7 @@ __device__ __forceinline__ bool leaf_phase(const TreeRef& tr_, const RayState& r
                     b.u = u;
                     b.v = v;
                     b.id = id;
+                    b.leaf = node;
                     improved = true;
                 }
             }
@@ -298,6 +300,7 @@ __device__ __forceinline__ bool leaf_phase(const TreeRef& tr_, const RayState& r
             b.u = hu;
             b.v = hv;
             b.id = (int)(uint32_t)hk;
+            b.leaf = node;
             improved = true;
         }
     }
@@ -401,10 +404,22 @@ struct Spill {
 // warp tests the held leaves' triangles together.  Without a budget, hits and
 // box / triangle test counts equal the oracle's.  *slot_out = the heavy-list
 // slot of a ray handed over (its hit is then not valid), else -1.
+//
+// Restart (the iRoot argument of LBVH_IntersectP, LBVH.hlsl:363-376): with
+// start > 1 the walk begins at heap node `start`.  The siblings of start's
+// ancestors are box-tested first and stacked with their entry distances
+// (the deepest on top), then start itself is entered; together they cover
+// the heap, and since a parent's box admits every ray its children's boxes
+// admit, the closest hit is the root walk's (except where two triangles are
+// hit within an ulp and a rounded box entry lets the order decide, as it
+// does between any two walk orders).  Only the heap layout can be
+// restarted (with the compact layout the walk starts at the root).  start
+// must be a node the build reached, e.g. a leaf a trace of the same tree
+// reported through *leaf_out (1 when nothing was hit).
 template <bool EXACT, bool STATS>
 __device__ __forceinline__ Hit traverse(const RayState& r, bool active, const TreeRef& tr_, bool any_hit,
                                         uint32_t* nbox_out, uint32_t* ntri_out, const Spill* spill,
-                                        int* slot_out) {
+                                        int* slot_out, uint32_t start = 1u, uint32_t* leaf_out = nullptr) {
     constexpr uint32_t kFull = 0xffffffffu;
     Best b;
     b.key = hit_key(r.tmax, 0);
@@ -412,6 +427,7 @@ __device__ __forceinline__ Hit traverse(const RayState& r, bool active, const Tr
     b.u = -1.0f;
     b.v = -1.0f;
     b.t = r.tmax;
+    b.leaf = 1u;
     uint64_t bound = b.key;
     uint32_t nbox = 0, ntri = 0;
     uint32_t stack_node[kStackSize];
@@ -425,16 +441,37 @@ __device__ __forceinline__ Hit traverse(const RayState& r, bool active, const Tr
     int slot = -1;
     bool budgeted = !STATS && spill != nullptr && spill->count != nullptr;
     if (active) {
-        cur = load_node(tr_.nodes, 1);
+        // no t satisfies 0 <= t < tmax when tmax <= 0 or is NaN
+        const bool live = r.tmax > 0.0f;
+        if (start > 1u && !tr_.compact) {
+            if (start >= tr_.num_nodes) {
+                atomicOr(tr_.err, RT_DEVERR_BOUNDS);
+            } else {
+                const int D = 31 - __clz(start);  // <= kMaxDepth < kStackSize
+                for (int k = 1; k <= D; ++k) {
+                    const uint32_t sib = (start >> (D - k)) ^ 1u;
+                    const NodeBox sb = load_node(tr_.nodes, sib);
+                    ++nbox;
+                    float t0;
+                    if (live && box_enter<EXACT>(r, sb.a.x, sb.a.y, sb.a.z, sb.a.w, sb.b.x, sb.b.y, b.t, &t0)) {
+                        stack_node[sp & (kStackSize - 1)] = sib;
+                        stack_t0[sp & (kStackSize - 1)] = t0;
+                        ++sp;
+                    }
+                }
+                node = start;
+            }
+        }
+        cur = load_node(tr_.nodes, node);
         ++nbox;
         float t0;
-        // no t satisfies 0 <= t < tmax when tmax <= 0 or is NaN
-        have = r.tmax > 0.0f && box_enter<EXACT>(r, cur.a.x, cur.a.y, cur.a.z, cur.a.w, cur.b.x, cur.b.y, b.t, &t0);
+        have = live && box_enter<EXACT>(r, cur.a.x, cur.a.y, cur.a.z, cur.a.w, cur.b.x, cur.b.y, b.t, &t0);
+        if (!have) have = pop_node(tr_, b.t, node, cur, stack_node, stack_t0, sp, 0u);
     }
     while (__any_sync(kFull, have)) {
         if (have) have = descend<EXACT, STATS>(tr_, r, b.t, node, cur, stack_node, stack_t0, sp, 0u, nbox);
         __syncwarp();
-        leaf_phase<STATS>(tr_, r, have, cur, bound, b, ntri);
+        leaf_phase<STATS>(tr_, r, have, cur, node, bound, b, ntri);
         if (have) {
             if (any_hit && b.id >= 0) {
                 have = false;
@@ -455,6 +492,7 @@ __device__ __forceinline__ Hit traverse(const RayState& r, bool active, const Tr
     if (nbox_out) *nbox_out = nbox;
     if (ntri_out) *ntri_out = ntri;
     if (slot_out) *slot_out = slot;
+    if (leaf_out) *leaf_out = tr_.compact ? 1u : b.leaf;
     Hit h;
     h.id = b.id;
     h.u = b.u;
@@ -710,10 +748,10 @@ __device__ __forceinline__ Hit traverse_wide(const RayState& r, const TreeRef& t
 template <bool STATS>
 __device__ __forceinline__ Hit trace_ray(const RayState& r, bool active, const TreeRef& tr, bool any_hit,
                                          uint32_t* nbox, uint32_t* ntri, const Spill* spill = nullptr,
-                                         int* slot = nullptr) {
+                                         int* slot = nullptr, uint32_t start = 1u, uint32_t* leaf = nullptr) {
     if (__any_sync(0xffffffffu, active && r.exact))
-        return traverse<true, STATS>(r, active, tr, any_hit, nbox, ntri, spill, slot);
-    return traverse<false, STATS>(r, active, tr, any_hit, nbox, ntri, spill, slot);
+        return traverse<true, STATS>(r, active, tr, any_hit, nbox, ntri, spill, slot, start, leaf);
+    return traverse<false, STATS>(r, active, tr, any_hit, nbox, ntri, spill, slot, start, leaf);
 }
 
 // One ray traced by the whole warp; every lane passes the same ray.

@@ -209,6 +209,7 @@ RayTracerCS::RayTracerCS(Context& ctx, const Scene& scene, const rt_camera& came
     std::memcpy(m_light, light, sizeof(m_light));
     const size_t px = (size_t)camera.width * camera.height;
     m_primary.resize(sizeof(rt_hit) * px);
+    m_roots.resize(sizeof(uint32_t) * px);
     m_vis.resize(px);
     m_mirror.resize(sizeof(rt_hit) * px);
     UpdateScene(scene.soup);
@@ -223,18 +224,21 @@ void RayTracerCS::UpdateScene(const float* soup) {
 
 void RayTracerCS::Render() {
     // Render (RayTracerCS.cpp:258-295): rebuild when dynamic, then primary
-    // rays and the colour stage's shadow + mirror rays
+    // rays and the colour stage's shadow + mirror rays, which start their
+    // walks at the primary hit's leaf (the iRoot the reference keeps in
+    // g_uIntersections, CSComputeColorRT.hlsl:160)
     if (m_dynamic || !m_built) {
         m_construction.GPUBuildStructure(m_depth, static_cast<const float*>(m_soup.data()), m_scene.numPrimitives);
         m_built = true;
     }
     rt_lbvh* l = m_construction.lbvh();
-    check(rt_trace_primary(m_ctx.get(), l, &m_camera, static_cast<rt_hit*>(m_primary.data()), nullptr), m_ctx.get(),
-          "rt_trace_primary");
-    check(rt_trace_shadow_mirror(m_ctx.get(), l, &m_camera, m_light, static_cast<const rt_hit*>(m_primary.data()),
-                                 static_cast<uint8_t*>(m_vis.data()), static_cast<rt_hit*>(m_mirror.data()), nullptr,
-                                 nullptr),
-          m_ctx.get(), "rt_trace_shadow_mirror");
+    uint32_t* roots = static_cast<uint32_t*>(m_roots.data());
+    check(rt_trace_primary_leaves(m_ctx.get(), l, &m_camera, static_cast<rt_hit*>(m_primary.data()), roots, nullptr),
+          m_ctx.get(), "rt_trace_primary_leaves");
+    check(rt_trace_shadow_mirror_from(m_ctx.get(), l, &m_camera, m_light, static_cast<const rt_hit*>(m_primary.data()),
+                                      roots, static_cast<uint8_t*>(m_vis.data()), static_cast<rt_hit*>(m_mirror.data()),
+                                      nullptr, nullptr, nullptr),
+          m_ctx.get(), "rt_trace_shadow_mirror_from");
     ++m_NumMuestras;
 }
 

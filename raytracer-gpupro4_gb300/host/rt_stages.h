@@ -226,7 +226,7 @@ class RayTracerCS {
     bool m_dynamic;
     bool m_built = false;
     StructureConstruction m_construction;
-    DeviceBuffer m_soup, m_primary, m_vis, m_mirror;
+    DeviceBuffer m_soup, m_primary, m_roots, m_vis, m_mirror;
     unsigned int m_NumMuestras = 0;
 };
 

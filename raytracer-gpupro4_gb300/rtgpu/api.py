@@ -214,6 +214,53 @@ class RayTracer:
                 "rt_trace_shadow_mirror")
         return (vis, mirror, ss, ms) if stats else (vis, mirror)
 
+    def primary_leaves(self, lbvh: LBVH, cam: L.Camera, stats: bool = False, out: torch.Tensor | None = None,
+                       leaves: torch.Tensor | None = None):
+        """Primary hits and the heap leaf of each hit (the reference's iRoot,
+        rt_trace_primary_leaves).  Returns (hits, leaves[, stats])."""
+        npx = cam.width * cam.height
+        hits = out if out is not None else self._alloc_hits(npx)
+        if leaves is None:
+            leaves = torch.empty(npx, dtype=torch.int32, device=self.ctx.torch_device)
+        st = torch.empty((npx, 2), dtype=torch.int32, device=self.ctx.torch_device) if stats else None
+        L.check(L.lib().rt_trace_primary_leaves(self.ctx.h, lbvh.h, C.byref(cam), _dev_ptr(hits), _dev_ptr(leaves),
+                                                _dev_ptr(st) if stats else None), self.ctx.h,
+                "rt_trace_primary_leaves")
+        return (hits, leaves, st) if stats else (hits, leaves)
+
+    def shadow_mirror_from(self, lbvh: LBVH, cam: L.Camera, light, primary: torch.Tensor, leaves: torch.Tensor,
+                           stats: bool = False, vis: torch.Tensor | None = None, mirror: torch.Tensor | None = None,
+                           mirror_leaves: torch.Tensor | None = None):
+        """Shading rays started at the primary leaves (rt_trace_shadow_mirror_from).
+        Returns (vis, mirror, mirror_leaves[, shadow_stats, mirror_stats])."""
+        npx = cam.width * cam.height
+        dev = self.ctx.torch_device
+        vis = vis if vis is not None else torch.empty(npx, dtype=torch.uint8, device=dev)
+        mirror = mirror if mirror is not None else self._alloc_hits(npx)
+        ml = mirror_leaves if mirror_leaves is not None else torch.empty(npx, dtype=torch.int32, device=dev)
+        ss = torch.empty((npx, 2), dtype=torch.int32, device=dev) if stats else None
+        ms = torch.empty((npx, 2), dtype=torch.int32, device=dev) if stats else None
+        lf = (C.c_float * 3)(*light)
+        L.check(L.lib().rt_trace_shadow_mirror_from(self.ctx.h, lbvh.h, C.byref(cam), lf, _dev_ptr(primary),
+                                                    _dev_ptr(leaves), _dev_ptr(vis), _dev_ptr(mirror), _dev_ptr(ml),
+                                                    _dev_ptr(ss) if stats else None, _dev_ptr(ms) if stats else None),
+                self.ctx.h, "rt_trace_shadow_mirror_from")
+        return (vis, mirror, ml, ss, ms) if stats else (vis, mirror, ml)
+
+    def rays_from(self, lbvh: LBVH, rays: torch.Tensor, starts: torch.Tensor | None, any_hit: bool = False,
+                  stats: bool = False):
+        """rt_trace_rays_from: each ray's walk starts at heap node starts[i]
+        (None: the root).  Returns (hits, leaves[, stats])."""
+        n = rays.shape[0]
+        hits = self._alloc_hits(n)
+        leaves = torch.empty(n, dtype=torch.int32, device=self.ctx.torch_device)
+        st = torch.empty((n, 2), dtype=torch.int32, device=self.ctx.torch_device) if stats else None
+        L.check(L.lib().rt_trace_rays_from(self.ctx.h, lbvh.h, _dev_ptr(rays), n, int(any_hit),
+                                           _dev_ptr(starts) if starts is not None else None, _dev_ptr(hits),
+                                           _dev_ptr(leaves), _dev_ptr(st) if stats else None), self.ctx.h,
+                "rt_trace_rays_from")
+        return (hits, leaves, st) if stats else (hits, leaves)
+
     def rays(self, lbvh: LBVH, rays: torch.Tensor, any_hit: bool = False, stats: bool = False):
         """rays: (n, 8) float32 device tensor laid out as rt_ray {o, exclude(int bits), d, tmax}."""
         n = rays.shape[0]

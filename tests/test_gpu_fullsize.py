@@ -46,6 +46,14 @@ def test_full_frame_build_and_trace(gpu_ctx, oracle_mod, frames):
         assert np.array_equal(vis.cpu().numpy(), ovis)
         assert_hits_equal(hits_to_numpy(mirror), omir, "mirror")
         assert (oh["id"] >= 0).sum() > 300_000 and (ovis == 3).sum() > 100_000
+    # the shading rays started at the primary leaves (the frame path's walk)
+    hits, leaves = rt.primary_leaves(lb, cam)
+    vis, mirror, _ = rt.shadow_mirror_from(lb, cam, light, hits, leaves)
+    gpu_ctx.check()
+    oh, ol = oracle_mod.trace_from(onodes, 20, oids, tris, oracle_mod.primary_rays(cam))
+    ovis, omir, _ = oracle_mod.shadow_mirror_from(onodes, 20, oids, tris, cam, light, oh, ol)
+    assert np.array_equal(vis.cpu().numpy(), ovis)
+    assert_hits_equal(hits_to_numpy(mirror), omir, "mirror from leaves")
     # the captured frame (rebuild + both passes in one graph) gives the same images
     h2 = torch.empty((npx, 4), dtype=torch.int32, device="cuda")
     v2 = torch.empty(npx, dtype=torch.uint8, device="cuda")

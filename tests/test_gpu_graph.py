@@ -32,8 +32,8 @@ def test_graph_frames_equal_direct_calls(gpu_ctx):
             gp, gv, gm = hits_to_numpy(prim), vis.cpu().numpy(), hits_to_numpy(mir)
             g_nodes, g_ids, g_keys = lb_g.download(True, True, True)
             lb_d.Build(f)
-            dp = rt.primary(lb_d, cam)
-            dv, dm = rt.shadow_mirror(lb_d, cam, light, dp)
+            dp, dl = rt.primary_leaves(lb_d, cam)
+            dv, dm, _ = rt.shadow_mirror_from(lb_d, cam, light, dp, dl)
             gpu_ctx.check()
             d_nodes, d_ids, d_keys = lb_d.download(True, True, True)
             assert np.array_equal(g_keys, d_keys) and np.array_equal(g_ids, d_ids)

@@ -37,8 +37,8 @@ def test_cpp_stage_classes(gpu_ctx, oracle_mod, tmp_path):
     # same frame through the Python binding
     lb = LBVH(gpu_ctx, len(tris), depth).Build(torch.from_numpy(tris).cuda())
     rt = RayTracer(gpu_ctx)
-    hits = rt.primary(lb, cam)
-    pv, pm = rt.shadow_mirror(lb, cam, light, hits)
+    hits, leaves = rt.primary_leaves(lb, cam)
+    pv, pm, _ = rt.shadow_mirror_from(lb, cam, light, hits, leaves)
     assert np.array_equal(prim, hits_to_numpy(hits))
     assert np.array_equal(vis, pv.cpu().numpy())
     assert np.array_equal(mir, hits_to_numpy(pm))

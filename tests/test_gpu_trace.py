@@ -131,8 +131,9 @@ def test_render_frame_host_equals_device_path(gpu_ctx, torus_scene):
     tris, lb, dt, nodes, ids = torus_scene
     cam = scenes.torus_camera(320, 200)
     rt = RayTracer(gpu_ctx)
-    hits = rt.primary(lb, cam)
-    vis, mirror = rt.shadow_mirror(lb, cam, scenes.TORUS_LIGHT, hits)
+    # the frame call starts the shading rays at the primary leaves
+    hits, leaves = rt.primary_leaves(lb, cam)
+    vis, mirror, _ = rt.shadow_mirror_from(lb, cam, scenes.TORUS_LIGHT, hits, leaves)
     lb2 = LBVH(gpu_ctx, len(tris), 20)
     hp = np.zeros(cam.width * cam.height, HIT_DTYPE)
     hv = np.zeros(cam.width * cam.height, np.uint8)
