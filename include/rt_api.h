@@ -221,6 +221,45 @@ rt_status rt_trace_shadow_mirror_from(rt_ctx* ctx, const rt_lbvh* lbvh, const rt
 rt_status rt_trace_rays_from(rt_ctx* ctx, const rt_lbvh* lbvh, const rt_ray* d_rays, uint32_t n, int any_hit,
                              const uint32_t* d_starts, rt_hit* d_hits, uint32_t* d_leaves, uint32_t* d_stats);
 
+/* ---- colour stage ---------------------------------------------------- */
+/* Material (Structures.hlsl:69-78; the MTL colours of Model::LoadFile):
+ * shininess = Ns / 1000, alpha = d or 1 - Tr (the probability of the mirror
+ * bounce), ambient[3] = the refraction index of the refracted bounce. */
+typedef struct rt_material {
+    float ambient[4];
+    float diffuse[4];
+    float specular[4];
+    float shininess;
+    float alpha;
+} rt_material;
+
+/* Switches of the colour stage (cbInputOutput, ConstantBuffers.h:35-70). */
+typedef struct rt_shade_params {
+    uint32_t bounces;       /* num_reflex: colour stages run = bounces + 1 */
+    int32_t shadows;        /* bIsShadowOn */
+    int32_t phong;          /* bIsPhongShadingOn: interpolate d_normals (flat when NULL) */
+    int32_t gloss_mapping;  /* bIsGlossMappingOn: keep specular.w */
+    int32_t env_mapping;    /* iEnvMapping: -1 a miss takes env_color and ends the ray; 0 it shows 1 */
+    float env_color[3];     /* stands in for the environment cube map */
+    uint32_t seed;          /* the mirror / refraction choice (stands in for the random texture) */
+} rt_shade_params;
+
+/* RayTracerCS::Render without global illumination (RayTracerCS.cpp:284-295):
+ * primary rays, then bounces + 1 times the intersection stage
+ * (CSIntersections.hlsl:18-39, each walk restarted at the pixel's previous
+ * leaf) and the colour stage (CSComputeColorRT.hlsl:18-262 without textures
+ * or normal maps: flat or Phong normal, shadow ray, specular^49 and diffuse
+ * terms, mirror or refracted next ray, environment colour on a miss).
+ * d_material_ids (nullable: all 0): n; d_materials: num_materials (>= 1);
+ * d_normals (nullable): n x 9 per-corner normals.  d_accum / d_result
+ * (w*h x 4 floats, row-major; d_result nullable): g_uAccumulation and
+ * g_uResultTexture after the last bounce.  The triangles are the soup of
+ * the last build (indexed by triangle id); the walks use the heap layout. */
+rt_status rt_render_whitted(rt_ctx* ctx, const rt_lbvh* lbvh, const rt_camera* cam, const float light[3],
+                            const rt_shade_params* params, const int32_t* d_material_ids,
+                            const rt_material* d_materials, uint32_t num_materials, const float* d_normals,
+                            float* d_accum, float* d_result);
+
 /* One frame of the dynamic path (RayTracerCS::Render with dynamic=1,
  * RayTracerCS.cpp:258-295): rebuild from a host soup, primary, shadow and
  * mirror rays (started at the primary hits' leaves), results copied back to

@@ -35,13 +35,7 @@ extern "C" {
 
 typedef struct rt_model rt_model;
 
-typedef struct rt_material {
-    float ambient[4];
-    float diffuse[4];
-    float specular[4];
-    float shininess; /* Ns / 1000 */
-    float alpha;     /* d, or 1 - Tr */
-} rt_material;
+/* rt_material (include/rt_api.h): the MTL colours, Ns / 1000, and d or 1 - Tr. */
 
 /* Loads `path` (.obj / .txt by extension, either case).  On failure returns
  * RT_ERR_INVALID and, when err is not NULL, a message in err[0 .. errlen). */

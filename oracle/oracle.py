@@ -35,6 +35,11 @@ class OrPtParams(C.Structure):
     _fields_ = [("spp", C.c_uint32), ("bounces", C.c_uint32), ("seed", C.c_uint64), ("sky", C.c_float * 3)]
 
 
+class OrShadeParams(C.Structure):
+    _fields_ = [("bounces", C.c_uint32), ("shadows", C.c_int32), ("phong", C.c_int32), ("gloss_mapping", C.c_int32),
+                ("env_mapping", C.c_int32), ("env_color", C.c_float * 3), ("seed", C.c_uint32)]
+
+
 def build_oracle() -> Path:
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
     return ORACLE_LIB
@@ -93,6 +98,10 @@ def olib() -> C.CDLL:
         L.or_pathtrace.argtypes = [vp, u32, vp, vp, vp, vp, C.POINTER(OrCamera), C.POINTER(OrPtParams), vp, i32]
         L.or_pathtrace_adjoint.argtypes = [vp, u32, vp, vp, vp, vp, C.POINTER(OrCamera), C.POINTER(OrPtParams),
                                            vp, vp, vp, i32]
+        L.or_render_whitted.argtypes = [vp, u32, vp, vp, vp, vp, vp, u32, C.POINTER(OrCamera), vp,
+                                        C.POINTER(OrShadeParams), vp, vp, i32]
+        L.or_whitted_rand.argtypes = [u32, u32, u32]
+        L.or_whitted_rand.restype = C.c_float
         L.or_pcg32_first.argtypes = [C.c_uint64, C.c_uint64, u32, vp]
         L.or_pcg32_first.restype = u32
         _olib = L
@@ -212,6 +221,28 @@ def shadow_mirror_from(nodes, depth, ids, tris, cam, light, prim, prim_leaves, n
                                  _ptr(ss) if stats else None, _ptr(ms) if stats else None,
                                  nthreads or nthreads_default())
     return (vis, mirror, ml, ss, ms) if stats else (vis, mirror, ml)
+
+
+def render_whitted(nodes, depth, ids, tris, cam, light, materials, material_ids=None, normals=None, bounces=0,
+                   shadows=True, phong=False, gloss_mapping=False, env_mapping=-1, env_color=(1.0, 1.0, 1.0), seed=0,
+                   nthreads=None):
+    """or_render_whitted: the colour stage and its bounce loop.  materials:
+    (m, 14) float32 rows (ambient 4, diffuse 4, specular 4, shininess,
+    alpha).  Returns (accum, result), each (w*h, 4) float32."""
+    oc = to_or_camera(cam)
+    sp = OrShadeParams(bounces, int(shadows), int(phong), int(gloss_mapping), env_mapping,
+                       (C.c_float * 3)(*env_color), seed)
+    mats = np.ascontiguousarray(materials, np.float32).reshape(-1, 14)
+    mid = None if material_ids is None else np.ascontiguousarray(material_ids, np.int32)
+    nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
+    npx = cam.width * cam.height
+    acc = np.zeros((npx, 4), np.float32)
+    res = np.zeros((npx, 4), np.float32)
+    olib().or_render_whitted(_ptr(nodes), depth, _ptr(ids), _ptr(np.ascontiguousarray(tris, np.float32)),
+                             _ptr(nrm) if nrm is not None else None, _ptr(mid) if mid is not None else None,
+                             _ptr(mats), len(mats), C.byref(oc), _ptr(np.asarray(light, np.float32)), C.byref(sp),
+                             _ptr(acc), _ptr(res), nthreads or nthreads_default())
+    return acc, res
 
 
 def pathtrace(nodes, depth, ids, tris, albedo, emission, cam, spp, bounces, seed, sky=(1.0, 1.0, 1.0), nthreads=None):

@@ -729,3 +729,176 @@ void or_pathtrace_adjoint(const or_node* nodes, uint32_t depth, const uint32_t* 
     }
     for (int c = 0; c < 3; ++c) d_emission_scale[c] = dle[c];
 }
+
+/* ------------------------------------------------------------------------ */
+/* The ray-tracing colour stage and its bounce loop: RayTracerCS::Render
+ * (RayTracerCS.cpp:284-295) runs CSGeneratePrimaryRays, then bounces + 1
+ * times CSComputeIntersections (CSIntersections.hlsl:18-39) and
+ * CSComputeColor (CSComputeColorRT.hlsl:18-262), without textures or normal
+ * maps.  Per pixel, in the reference's operation order:
+ *   N   = normalize(cross(B-A, C-A)), or with Phong normalize(nA*w + nB*u +
+ *         nC*v), w = 1 - (u+v) (Vec3BaryCentric, Intersection.hlsl:98-108)
+ *   NM  = -N if dot(N, d) > 0                              (:126-131)
+ *   P = o + t d; L = (P - light) / |P - light|             (:134-138)
+ *   R   = normalize(reflect(d, NM))                        (:141-142)
+ *   lit when dot(N,L)*dot(N,d) > 0 and (shadows off or the shadow ray from P
+ *   towards the light, excluding the hit triangle, restarted at the hit's
+ *   leaf, reaches the light)                               (:145-169)
+ *   spec = max(0, -dot(L, R))^49, diff = max(0, -dot(NM, L))  (:164-175)
+ *   colour = (amb + diff*kd.w)*kd + spec*(1 - kd.w)*ks', ks'.w = ks.w*gloss,
+ *   times (factor, 1)                                      (:183-200)
+ *   next ray: from P; with probability alpha the mirror ray R and factor *=
+ *   ks.xyz, else refract(d, NM, eta) with eta = amb.w (1/amb.w entering),
+ *   normalised, factor *= kd.xyz, or R on total internal reflection (:203-231)
+ *   a miss: colour = (factor * env, 1) and the ray ends (:233-245)
+ *   accumulation += colour, result = accumulation          (:255-256)
+ * A pixel whose intersection id is below the environment flag (a miss with
+ * the flag 0) gets result 1 and keeps its ray, so every later bounce finds
+ * the same miss (:29-35).  The random texture sample of :204-207 is a hash
+ * of (seed, pixel, bounce); normalize divides by the length (as Geometry.h
+ * does) and pow(x, 49) is x^32 * x^16 * x, so the CUDA kernels can match
+ * these values bit for bit. */
+static inline uint32_t lowbias32(uint32_t x) {
+    x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+    return x;
+}
+
+float or_whitted_rand(uint32_t seed, uint32_t pixel, uint32_t bounce) {
+    const uint32_t h = lowbias32(pixel ^ lowbias32(seed ^ (0x9e3779b9U * (bounce + 1U))));
+    return (float)(h >> 8) * (1.0f / 16777216.0f);
+}
+
+static inline float pow49(float x) {
+    float x2 = x * x, x4 = x2 * x2, x8 = x4 * x4, x16 = x8 * x8, x32 = x16 * x16;
+    return (x32 * x16) * x;
+}
+
+static inline void normalize3v(float v[3]) {
+    float l = sqrtf(dot3(v, v));
+    v[0] /= l; v[1] /= l; v[2] /= l;
+}
+
+static void whitted_pixel(const or_node* nodes, const uint32_t* ids, const float* tris, const float* normals,
+                          const int32_t* mat_ids, const or_material* mats, uint32_t nmat, const or_camera* cam,
+                          const float light[3], const or_shade_params* sp, uint32_t i, uint32_t j, float acc[4],
+                          float res[4]) {
+    const uint32_t pixel = j * cam->width + i;
+    const float inv = 1.0f / (float)cam->height;
+    float o[3] = {cam->eye[0], cam->eye[1], cam->eye[2]}, d[3];
+    float x = (float)(2 * (int)i + 1 - (int)cam->width) * inv;
+    float y = -((float)(2 * (int)j + 1 - (int)cam->height) * inv);
+    camera_dir(cam, x, y, d);
+    float factor[3] = {1.0f, 1.0f, 1.0f};
+    int exclude = -1;
+    uint32_t start = 1;
+    for (int c = 0; c < 4; ++c) { acc[c] = 0.0f; res[c] = 0.0f; }
+    for (uint32_t b = 0; b <= sp->bounces; ++b) {
+        float r[8] = {o[0], o[1], o[2], d[0], d[1], d[2], 1e16f, (float)exclude};
+        or_hit h;
+        uint32_t leaf = 1;
+        trace_one_from(nodes, ids, tris, r, &h, NULL, 0, start, &leaf);
+        const int id = h.id;
+        if (id < sp->env_mapping) {
+            if (id > -2) for (int c = 0; c < 4; ++c) res[c] = 1.0f;
+            return;  /* the same miss at every later bounce */
+        }
+        float fin[4] = {0.0f, 0.0f, 0.0f, 1.0f};
+        if (id < 0) {
+            for (int c = 0; c < 3; ++c) fin[c] = factor[c] * sp->env_color[c];
+            for (int c = 0; c < 4; ++c) acc[c] += fin[c];
+            for (int c = 0; c < 4; ++c) res[c] = acc[c];
+            return;  /* the ray ends */
+        }
+        const float* t = tris + 9 * (size_t)id;
+        float E1[3] = {t[3] - t[0], t[4] - t[1], t[5] - t[2]};
+        float E2[3] = {t[6] - t[0], t[7] - t[1], t[8] - t[2]};
+        float N[3] = {(E1[1] * E2[2]) - (E1[2] * E2[1]), (E1[2] * E2[0]) - (E1[0] * E2[2]),
+                      (E1[0] * E2[1]) - (E1[1] * E2[0])};
+        normalize3v(N);
+        if (sp->phong && normals) {
+            const float* nn = normals + 9 * (size_t)id;
+            const float w = 1.0f - (h.u + h.v);
+            for (int c = 0; c < 3; ++c) N[c] = (nn[c] * w + nn[3 + c] * h.u) + nn[6 + c] * h.v;
+            normalize3v(N);
+        }
+        float NM[3] = {N[0], N[1], N[2]};
+        int inverse = 0;
+        if (dot3(NM, d) > 0.0f) { NM[0] = -NM[0]; NM[1] = -NM[1]; NM[2] = -NM[2]; inverse = 1; }
+        float P[3], L[3];
+        for (int c = 0; c < 3; ++c) P[c] = o[c] + h.t * d[c];
+        for (int c = 0; c < 3; ++c) L[c] = P[c] - light[c];
+        const float dist = sqrtf(dot3(L, L));
+        L[0] /= dist; L[1] /= dist; L[2] /= dist;
+        const float k2 = 2.0f * dot3(d, NM);
+        float R[3] = {d[0] - k2 * NM[0], d[1] - k2 * NM[1], d[2] - k2 * NM[2]};
+        normalize3v(R);
+        const float ls = dot3(N, L), rs = dot3(N, d);
+        float spec = 0.0f, diff = 0.0f, spec_w = 1.0f, diff_w = 1.0f;
+        if (ls * rs > 0.0f) {
+            int lit = 1;
+            if (sp->shadows) {
+                float s[8] = {P[0], P[1], P[2], -L[0], -L[1], -L[2], dist, (float)id};
+                or_hit sh;
+                trace_one_from(nodes, ids, tris, s, &sh, NULL, 1, leaf, NULL);
+                lit = sh.id < 0;
+            }
+            if (lit) {
+                spec = pow49(fmaxf(0.0f, -dot3(L, R)));
+                diff = fmaxf(0.0f, -dot3(NM, L));
+                spec_w = spec;
+                diff_w = diff;
+            }
+        }
+        uint32_t m = mat_ids ? (uint32_t)mat_ids[id] : 0u;
+        if (m >= nmat) m = 0;
+        const or_material* mt = &mats[m];
+        float ks[4] = {mt->specular[0], mt->specular[1], mt->specular[2], mt->specular[3] * (float)sp->gloss_mapping};
+        const float* amb = mt->ambient;
+        const float* kd = mt->diffuse;
+        const float dv[4] = {diff, diff, diff, diff_w}, sv[4] = {spec, spec, spec, spec_w};
+        for (int c = 0; c < 4; ++c) {
+            const float dc = (amb[c] + dv[c] * kd[3]) * kd[c];
+            const float sc = (sv[c] * (1.0f - kd[3])) * ks[c];
+            fin[c] = dc + sc;
+        }
+        for (int c = 0; c < 3; ++c) fin[c] *= factor[c];
+        for (int c = 0; c < 4; ++c) acc[c] += fin[c];
+        for (int c = 0; c < 4; ++c) res[c] = acc[c];
+        /* the next ray */
+        float nd[3] = {R[0], R[1], R[2]};
+        if (mt->alpha >= or_whitted_rand(sp->seed, pixel, b)) {
+            for (int c = 0; c < 3; ++c) factor[c] *= ks[c];
+        } else {
+            float eta = amb[3];
+            if (!inverse) eta = 1.0f / eta;
+            const float ci = dot3(NM, d);
+            const float kk = 1.0f - (eta * eta) * (1.0f - ci * ci);
+            float T[3] = {0.0f, 0.0f, 0.0f};
+            if (!(kk < 0.0f)) {
+                const float sq = eta * ci + sqrtf(kk);
+                for (int c = 0; c < 3; ++c) T[c] = eta * d[c] - sq * NM[c];
+            }
+            const float tl = sqrtf(dot3(T, T));
+            if (!(tl < 0.000001f)) {
+                for (int c = 0; c < 3; ++c) nd[c] = T[c] / tl;
+                for (int c = 0; c < 3; ++c) factor[c] *= kd[c];
+            }
+        }
+        for (int c = 0; c < 3; ++c) { o[c] = P[c]; d[c] = nd[c]; }
+        exclude = id;
+        start = leaf;
+    }
+}
+
+void or_render_whitted(const or_node* nodes, uint32_t depth, const uint32_t* ids, const float* tris,
+                       const float* normals, const int32_t* mat_ids, const or_material* mats, uint32_t nmat,
+                       const or_camera* cam, const float light[3], const or_shade_params* sp, float* accum,
+                       float* result, int nthreads) {
+    (void)depth;
+    const long npx = (long)cam->width * cam->height;
+    if (nthreads <= 0) nthreads = 1;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+    for (long p = 0; p < npx; ++p)
+        whitted_pixel(nodes, ids, tris, normals, mat_ids, mats, nmat, cam, light, sp, (uint32_t)(p % cam->width),
+                      (uint32_t)(p / cam->width), accum + 4 * p, result + 4 * p);
+}

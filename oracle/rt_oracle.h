@@ -112,6 +112,33 @@ void or_pathtrace_adjoint(const or_node* nodes, uint32_t depth, const uint32_t* 
                           const or_pt_params* p, const float* d_image,
                           double* d_albedo, double* d_emission_scale, int nthreads);
 
+/* --- colour stage with its bounce loop (CSComputeColorRT.hlsl:18-262,
+ * RayTracerCS.cpp:284-295), no textures ------------------------------- */
+typedef struct or_material {  /* Material, Structures.hlsl:69-78 */
+    float ambient[4];
+    float diffuse[4];
+    float specular[4];
+    float shininess;
+    float alpha;
+} or_material;
+typedef struct or_shade_params {
+    uint32_t bounces;        /* colour stages run = bounces + 1 */
+    int32_t shadows;         /* g_bIsShadowOn */
+    int32_t phong;           /* g_bIsPhongShadingOn (needs per-corner normals) */
+    int32_t gloss_mapping;   /* g_bIsGlossMappingOn */
+    int32_t env_mapping;     /* g_iEnvMappingFlag: -1 on, 0 off */
+    float env_color[3];      /* the environment map's colour */
+    uint32_t seed;           /* reflection / refraction choice */
+} or_shade_params;
+/* normals (nullable): n x 9 per-corner normals; mat_ids (nullable): n;
+ * accum / result: w*h x 4 (g_uAccumulation, g_uResultTexture). */
+void or_render_whitted(const or_node* nodes, uint32_t depth, const uint32_t* ids, const float* tris,
+                       const float* normals, const int32_t* mat_ids, const or_material* mats, uint32_t nmat,
+                       const or_camera* cam, const float light[3], const or_shade_params* sp, float* accum,
+                       float* result, int nthreads);
+/* The uniform number of the reflection / refraction choice. */
+float or_whitted_rand(uint32_t seed, uint32_t pixel, uint32_t bounce);
+
 /* PCG32 helpers shared with the tests (O'Neill, pcg-random.org, pcg32_srandom_r). */
 uint32_t or_pcg32_first(uint64_t initstate, uint64_t initseq, uint32_t count, uint32_t* out);
 

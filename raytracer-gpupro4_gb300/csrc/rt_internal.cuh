@@ -142,9 +142,12 @@ struct rt_lbvh {
     rt_hit* f_mirror = nullptr;
     uint8_t* f_vis = nullptr;
     size_t f_pixels = 0;
-    // compacted shading-ray lists (shadow pixels, then mirror pixels), 2 x s_pixels
+    // compacted shading-ray lists (shadow pixels, mirror pixels, primary leaves), 3 x s_pixels
     uint32_t* s_lists = nullptr;
     size_t s_pixels = 0;
+    // per-pixel state of the colour stage's bounce loop (rt_render_whitted)
+    void* w_buf = nullptr;
+    size_t w_pixels = 0;
 };
 
 // Many independent scenes built in one pass of the build kernels and traced

@@ -31,7 +31,7 @@ EXPORTED = [
     "rt_ctx_check", "rt_last_error", "rt_lbvh_create", "rt_lbvh_destroy", "rt_lbvh_build", "rt_lbvh_build_host",
     "rt_lbvh_import_host", "rt_lbvh_view_get", "rt_lbvh_compact_get", "rt_lbvh_world_bound", "rt_lbvh_download", "rt_trace_primary",
     "rt_trace_shadow_mirror", "rt_trace_rays", "rt_trace_primary_leaves", "rt_trace_shadow_mirror_from",
-    "rt_trace_rays_from", "rt_render_frame_host", "rt_render_frame_host_async", "rt_pathtrace", "rt_pathtrace_adjoint",
+    "rt_trace_rays_from", "rt_render_whitted", "rt_render_frame_host", "rt_render_frame_host_async", "rt_pathtrace", "rt_pathtrace_adjoint",
     "rt_lbvh_build_noalloc", "rt_frame_capture", "rt_frame_launch", "rt_frame_node_count", "rt_frame_destroy",
     "rt_batch_create", "rt_batch_destroy", "rt_batch_scene_count", "rt_batch_build", "rt_batch_view_get",
     "rt_batch_download", "rt_batch_set_views", "rt_batch_trace", "rt_batch_set_tuning", "rt_batch_get_tuning", "rt_batch_frame_capture",
@@ -52,6 +52,21 @@ class LbvhView(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("threads", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("grab", C.c_uint32), ("order", C.c_uint32)]
+
+
+class Material(C.Structure):
+    """rt_material (Structures.hlsl:69-78)."""
+    _fields_ = [("ambient", C.c_float * 4), ("diffuse", C.c_float * 4), ("specular", C.c_float * 4),
+                ("shininess", C.c_float), ("alpha", C.c_float)]
+
+
+class ShadeParams(C.Structure):
+    """rt_shade_params (cbInputOutput, ConstantBuffers.h:35-70)."""
+    _fields_ = [("bounces", C.c_uint32), ("shadows", C.c_int32), ("phong", C.c_int32), ("gloss_mapping", C.c_int32),
+                ("env_mapping", C.c_int32), ("env_color", C.c_float * 3), ("seed", C.c_uint32)]
+
+
+assert C.sizeof(Material) == 56 and C.sizeof(ShadeParams) == 36
 
 
 class PtParams(C.Structure):
@@ -96,6 +111,7 @@ def lib() -> C.CDLL:
         "rt_trace_primary_leaves": (i32, [vp, vp, C.POINTER(Camera), vp, vp, vp]),
         "rt_trace_shadow_mirror_from": (i32, [vp, vp, C.POINTER(Camera), fp, vp, vp, vp, vp, vp, vp, vp]),
         "rt_trace_rays_from": (i32, [vp, vp, vp, u32, i32, vp, vp, vp, vp]),
+        "rt_render_whitted": (i32, [vp, vp, C.POINTER(Camera), fp, C.POINTER(ShadeParams), vp, vp, u32, vp, vp, vp]),
         "rt_render_frame_host": (i32, [vp, vp, vp, u32, C.POINTER(Camera), fp, vp, vp, vp]),
         "rt_render_frame_host_async": (i32, [vp, vp, vp, u32, C.POINTER(Camera), fp, vp, vp, vp]),
         "rt_pathtrace": (i32, [vp, vp, vp, vp, C.POINTER(Camera), C.POINTER(PtParams), vp]),

@@ -261,6 +261,33 @@ class RayTracer:
                 "rt_trace_rays_from")
         return (hits, leaves, st) if stats else (hits, leaves)
 
+    def whitted(self, lbvh: LBVH, cam: L.Camera, light, materials, material_ids: torch.Tensor | None = None,
+                normals: torch.Tensor | None = None, bounces: int = 0, shadows: bool = True, phong: bool = False,
+                gloss_mapping: bool = False, env_mapping: int = -1, env_color=(1.0, 1.0, 1.0), seed: int = 0,
+                result: bool = True):
+        """The colour stage with its bounce loop (rt_render_whitted).
+        materials: (m, 14) float32 rows (ambient 4, diffuse 4, specular 4,
+        shininess, alpha), host or device; material_ids: (n,) int32 device
+        tensor; normals: (n, 9) float32 device tensor (Phong).  Returns
+        (accum, result) as (w*h, 4) float32 device tensors (result None when
+        result=False)."""
+        dev = self.ctx.torch_device
+        mats = torch.as_tensor(np.ascontiguousarray(materials, np.float32).reshape(-1, 14) if not isinstance(
+            materials, torch.Tensor) else materials, device=dev).to(torch.float32).contiguous()
+        npx = cam.width * cam.height
+        acc = torch.empty((npx, 4), dtype=torch.float32, device=dev)
+        res = torch.empty((npx, 4), dtype=torch.float32, device=dev) if result else None
+        p = L.ShadeParams(bounces, int(shadows), int(phong), int(gloss_mapping), env_mapping,
+                          (C.c_float * 3)(*env_color), seed)
+        lf = (C.c_float * 3)(*light)
+        L.check(L.lib().rt_render_whitted(self.ctx.h, lbvh.h, C.byref(cam), lf, C.byref(p),
+                                          _dev_ptr(material_ids) if material_ids is not None else None,
+                                          _dev_ptr(mats), mats.shape[0],
+                                          _dev_ptr(normals) if normals is not None else None, _dev_ptr(acc),
+                                          _dev_ptr(res) if res is not None else None), self.ctx.h,
+                "rt_render_whitted")
+        return acc, res
+
     def rays(self, lbvh: LBVH, rays: torch.Tensor, any_hit: bool = False, stats: bool = False):
         """rays: (n, 8) float32 device tensor laid out as rt_ray {o, exclude(int bits), d, tmax}."""
         n = rays.shape[0]
