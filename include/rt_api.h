@@ -221,6 +221,37 @@ rt_status rt_trace_shadow_mirror_from(rt_ctx* ctx, const rt_lbvh* lbvh, const rt
 rt_status rt_trace_rays_from(rt_ctx* ctx, const rt_lbvh* lbvh, const rt_ray* d_rays, uint32_t n, int any_hit,
                              const uint32_t* d_starts, rt_hit* d_hits, uint32_t* d_leaves, uint32_t* d_stats);
 
+/* ---- the reference's SAH BVH: a second structure ---------------------- */
+/* BVH (AccelerationStructures/BVH/bvh.h, PBRT's SAH build) keeps its tree as
+ * a depth-first LinearBVHNode array (FlattenBVHTree, bvh.cpp:272-293), the
+ * same 32-byte record as rt_node: prim_count = nPrimitives (> 0: a leaf of
+ * that many entries of the ordered primitive ids from prim_pos; <= 0: an
+ * interior node split on axis -prim_count whose first child is the next
+ * record and whose second child is at prim_pos).  An rt_bvh holds such a
+ * tree on the device, and BVH_IntersectP (BVH.hlsl:124-217) traces it:
+ * visited node boxes tested with IntersectBox, the child on the ray's
+ * negative side of the split axis first.  All leaf triangles are tested
+ * (the shader tests a leaf's first one only, which is the same for the
+ * one-primitive leaves it supports); ties at equal t keep the smaller id. */
+typedef struct rt_bvh rt_bvh;
+rt_status rt_bvh_create(rt_ctx* ctx, uint32_t max_nodes, uint32_t max_tris, rt_bvh** out);
+rt_status rt_bvh_destroy(rt_bvh* bvh);
+/* Uploads a tree the reference built (BVH::GetPtrToElements,
+ * GetOrderedElementsIds) and the soup it was built over (host pointers,
+ * n x 9 floats).  The tree is checked first: every child inside the array
+ * and after its parent, every leaf range inside the ids, every id below n,
+ * split axes 0..2 (RT_ERR_INVALID otherwise). */
+rt_status rt_bvh_import_host(rt_ctx* ctx, rt_bvh* bvh, const rt_node* h_nodes, uint32_t num_nodes,
+                             const uint32_t* h_ids, const float* h_tris, uint32_t n);
+/* The tracing calls of the LBVH, over the BVH. */
+rt_status rt_bvh_trace_primary(rt_ctx* ctx, const rt_bvh* bvh, const rt_camera* cam, rt_hit* d_hits,
+                               uint32_t* d_stats);
+rt_status rt_bvh_trace_shadow_mirror(rt_ctx* ctx, const rt_bvh* bvh, const rt_camera* cam, const float light[3],
+                                     const rt_hit* d_primary, uint8_t* d_vis, rt_hit* d_mirror,
+                                     uint32_t* d_shadow_stats, uint32_t* d_mirror_stats);
+rt_status rt_bvh_trace_rays(rt_ctx* ctx, const rt_bvh* bvh, const rt_ray* d_rays, uint32_t n, int any_hit,
+                            rt_hit* d_hits, uint32_t* d_stats);
+
 /* ---- colour stage ---------------------------------------------------- */
 /* Material (Structures.hlsl:69-78; the MTL colours of Model::LoadFile):
  * shininess = Ns / 1000, alpha = d or 1 - Tr (the probability of the mirror

@@ -102,6 +102,8 @@ def olib() -> C.CDLL:
                                         C.POINTER(OrShadeParams), vp, vp, i32]
         L.or_whitted_rand.argtypes = [u32, u32, u32]
         L.or_whitted_rand.restype = C.c_float
+        L.or_bvh_trace.argtypes = [vp, u32, vp, u32, vp, vp, u32, vp, vp, i32, i32]
+        L.or_bvh_shadow_mirror.argtypes = [vp, u32, vp, u32, vp, C.POINTER(OrCamera), vp, vp, vp, vp, vp, vp, i32]
         L.or_pcg32_first.argtypes = [C.c_uint64, C.c_uint64, u32, vp]
         L.or_pcg32_first.restype = u32
         _olib = L
@@ -245,6 +247,38 @@ def render_whitted(nodes, depth, ids, tris, cam, light, materials, material_ids=
     return acc, res
 
 
+def bvh_trace(nodes, ids, tris, rays, any_hit=False, nthreads=None, stats=False):
+    """or_bvh_trace: BVH_IntersectP over a flattened SAH BVH (nodes in the
+    LinearBVHNode = NODE_DTYPE layout, ids = ordered primitive ids)."""
+    rays = np.ascontiguousarray(rays, np.float32)
+    nodes = np.ascontiguousarray(nodes)
+    ids = np.ascontiguousarray(ids, np.uint32)
+    n = len(rays)
+    hits = np.zeros(n, HIT_DTYPE)
+    st = np.zeros((n, 2), np.uint32) if stats else None
+    olib().or_bvh_trace(_ptr(nodes), len(nodes), _ptr(ids), len(ids), _ptr(np.ascontiguousarray(tris, np.float32)),
+                        _ptr(rays), n, _ptr(hits), _ptr(st) if stats else None, int(any_hit),
+                        nthreads or nthreads_default())
+    return (hits, st) if stats else hits
+
+
+def bvh_shadow_mirror(nodes, ids, tris, cam, light, prim, nthreads=None, stats=False):
+    oc = to_or_camera(cam)
+    npx = cam.width * cam.height
+    nodes = np.ascontiguousarray(nodes)
+    ids = np.ascontiguousarray(ids, np.uint32)
+    vis = np.zeros(npx, np.uint8)
+    mirror = np.zeros(npx, HIT_DTYPE)
+    ss = np.zeros((npx, 2), np.uint32) if stats else None
+    ms = np.zeros((npx, 2), np.uint32) if stats else None
+    olib().or_bvh_shadow_mirror(_ptr(nodes), len(nodes), _ptr(ids), len(ids),
+                                _ptr(np.ascontiguousarray(tris, np.float32)), C.byref(oc),
+                                _ptr(np.asarray(light, np.float32)), _ptr(np.ascontiguousarray(prim)), _ptr(vis),
+                                _ptr(mirror), _ptr(ss) if stats else None, _ptr(ms) if stats else None,
+                                nthreads or nthreads_default())
+    return (vis, mirror, ss, ms) if stats else (vis, mirror)
+
+
 def pathtrace(nodes, depth, ids, tris, albedo, emission, cam, spp, bounces, seed, sky=(1.0, 1.0, 1.0), nthreads=None):
     oc = to_or_camera(cam)
     p = OrPtParams(spp, bounces, seed, (C.c_float * 3)(*sky))
@@ -335,10 +369,11 @@ class RefStructure:
     def nodes(self) -> np.ndarray:
         L = rlib()
         n = L.ref_num_elements(self.h)
-        assert L.ref_element_size(self.h) == 32 or self.kind != "lbvh"
-        raw = np.zeros(n * L.ref_element_size(self.h), np.uint8)
+        esize = L.ref_element_size(self.h)
+        assert esize == 32  # LBVHNode and LinearBVHNode: bounds, count, offset
+        raw = np.zeros(n * esize, np.uint8)
         L.ref_copy_elements(self.h, _ptr(raw))
-        return raw.view(NODE_DTYPE) if self.kind == "lbvh" else raw
+        return raw.view(NODE_DTYPE)
 
     def ids(self) -> np.ndarray:
         out = np.zeros(self.n, np.uint32)

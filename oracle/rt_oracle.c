@@ -902,3 +902,122 @@ void or_render_whitted(const or_node* nodes, uint32_t depth, const uint32_t* ids
         whitted_pixel(nodes, ids, tris, normals, mat_ids, mats, nmat, cam, light, sp, (uint32_t)(p % cam->width),
                       (uint32_t)(p / cam->width), accum + 4 * p, result + 4 * p);
 }
+
+/* ------------------------------------------------------------------------ */
+/* Closest hit over the reference's flattened SAH BVH (LinearBVHNode array of
+ * BVH::FlattenBVHTree, bvh.cpp:272-293; the same 32-byte record as the LBVH
+ * node: bounds, nPrimitives, offset): BVH_IntersectP (BVH.hlsl:124-217).
+ * A visited node's box is tested (IntersectBox) and pruned when T1 < 0 or
+ * T0 > closest t; a leaf (nPrimitives > 0) tests its triangles ids[offset ..
+ * offset + nPrimitives); an interior node (nPrimitives = -split axis) goes
+ * to its second child (offset) first when the ray direction is negative on
+ * the split axis, else to its first child (the next record), and stacks the
+ * other.  Box tests count visited nodes.  Differences from the shader, none
+ * of which changes a closest hit: a leaf's triangles are all tested (the
+ * shader tests its first one nPrimitives + 1 times, which is the same for
+ * the one-primitive leaves it supports), and equal-t ties keep the smaller
+ * id.  Rays with tmax <= 0 or NaN walk nothing. */
+static void bvh_trace_one(const or_node* nodes, uint32_t num_nodes, const uint32_t* ids, uint32_t n,
+                          const float* tris, const float* r, or_hit* out, uint32_t* stats, int any_hit) {
+    const float o[3] = {r[0], r[1], r[2]};
+    const float d[3] = {r[3], r[4], r[5]};
+    const int exclude = (int)r[7];
+    float inv[3] = {1.0f / d[0], 1.0f / d[1], 1.0f / d[2]};
+    float best_t = r[6], best_u = -1.0f, best_v = -1.0f;
+    int best_id = -1;
+    uint32_t nbox = 0, ntri = 0;
+    uint32_t stack[128];
+    int sp = 0;
+    uint32_t node = 0;
+    int live = r[6] > 0.0f && num_nodes > 0;
+    while (live) {
+        const or_node* nd = &nodes[node];
+        float T0, T1;
+        box_interval(nd, o, inv, &T0, &T1);
+        ++nbox;
+        int next = 0;
+        if (!(T1 < 0.0f) && !(T0 > best_t)) {
+            if (nd->prim_count > 0) {
+                for (int i = 0; i < nd->prim_count; ++i) {
+                    const uint32_t k = (uint32_t)nd->prim_pos + (uint32_t)i;
+                    if (k >= n) break;
+                    ++ntri;
+                    const int id = (int)ids[k];
+                    if (id == exclude) continue;
+                    const float* t = tris + 9 * (size_t)id;
+                    float u, v, tt;
+                    if (tri_test(t, t + 3, t + 6, o, d, &u, &v, &tt)) {
+                        if (tt < best_t || (tt == best_t && best_id >= 0 && id < best_id)) {
+                            best_t = tt; best_u = u; best_v = v; best_id = id;
+                        }
+                    }
+                }
+                if (any_hit && best_id >= 0) break;
+            } else {
+                const int axis = -nd->prim_count;
+                const int neg = (axis >= 0 && axis < 3) ? (inv[axis] < 0.0f) : 0;
+                const uint32_t first = node + 1, second = (uint32_t)nd->prim_pos;
+                if (sp >= 128 || first >= num_nodes || second >= num_nodes) break;
+                stack[sp++] = neg ? first : second;
+                node = neg ? second : first;
+                next = 1;
+            }
+        }
+        if (!next) {
+            if (sp == 0) break;
+            node = stack[--sp];
+        }
+    }
+    out->id = best_id;
+    out->u = best_u;
+    out->v = best_v;
+    out->t = best_t;
+    if (stats) { stats[0] = nbox; stats[1] = ntri; }
+}
+
+void or_bvh_trace(const or_node* nodes, uint32_t num_nodes, const uint32_t* ids, uint32_t n, const float* tris,
+                  const float* rays, uint32_t nrays, or_hit* hits, uint32_t* stats, int any_hit, int nthreads) {
+    if (nthreads <= 0) nthreads = 1;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+    for (long i = 0; i < (long)nrays; ++i)
+        bvh_trace_one(nodes, num_nodes, ids, n, tris, rays + 8 * i, &hits[i], stats ? stats + 2 * i : NULL, any_hit);
+}
+
+/* or_shadow_mirror over the BVH: the same shading rays, traced by
+ * bvh_trace_one. */
+void or_bvh_shadow_mirror(const or_node* nodes, uint32_t num_nodes, const uint32_t* ids, uint32_t n,
+                          const float* tris, const or_camera* cam, const float light[3], const or_hit* prim,
+                          uint8_t* vis, or_hit* mirror, uint32_t* shadow_stats, uint32_t* mirror_stats,
+                          int nthreads) {
+    const long npx = (long)cam->width * cam->height;
+    if (nthreads <= 0) nthreads = 1;
+    const float inv = 1.0f / (float)cam->height;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+    for (long p = 0; p < npx; ++p) {
+        uint32_t i = (uint32_t)(p % cam->width), j = (uint32_t)(p / cam->width);
+        if (shadow_stats) { shadow_stats[2 * p] = 0; shadow_stats[2 * p + 1] = 0; }
+        if (mirror_stats) { mirror_stats[2 * p] = 0; mirror_stats[2 * p + 1] = 0; }
+        if (prim[p].id < 0) {
+            vis[p] = 0;
+            mirror[p].id = -2; mirror[p].u = -1.0f; mirror[p].v = -1.0f; mirror[p].t = 0.0f;
+            continue;
+        }
+        float r[8];
+        float x = (float)(2 * (int)i + 1 - (int)cam->width) * inv;
+        float y = -((float)(2 * (int)j + 1 - (int)cam->height) * inv);
+        camera_dir(cam, x, y, r + 3);
+        r[0] = cam->eye[0]; r[1] = cam->eye[1]; r[2] = cam->eye[2];
+        r[6] = 1e16f; r[7] = -1.0f;
+        float sr[8], mr[8];
+        int cast;
+        secondary(tris, r, &prim[p], light, sr, mr, &cast);
+        if (cast) {
+            or_hit sh;
+            bvh_trace_one(nodes, num_nodes, ids, n, tris, sr, &sh, shadow_stats ? shadow_stats + 2 * p : NULL, 1);
+            vis[p] = (sh.id >= 0) ? 2 : 3;
+        } else {
+            vis[p] = 1;
+        }
+        bvh_trace_one(nodes, num_nodes, ids, n, tris, mr, &mirror[p], mirror_stats ? mirror_stats + 2 * p : NULL, 0);
+    }
+}

@@ -139,6 +139,15 @@ void or_render_whitted(const or_node* nodes, uint32_t depth, const uint32_t* ids
 /* The uniform number of the reflection / refraction choice. */
 float or_whitted_rand(uint32_t seed, uint32_t pixel, uint32_t bounce);
 
+/* --- the reference's SAH BVH (LinearBVHNode, bvh.cpp:272-293), traced as
+ * BVH_IntersectP (BVH.hlsl:124-217) ----------------------------------- */
+void or_bvh_trace(const or_node* nodes, uint32_t num_nodes, const uint32_t* ids, uint32_t n, const float* tris,
+                  const float* rays, uint32_t nrays, or_hit* hits, uint32_t* stats, int any_hit, int nthreads);
+void or_bvh_shadow_mirror(const or_node* nodes, uint32_t num_nodes, const uint32_t* ids, uint32_t n,
+                          const float* tris, const or_camera* cam, const float light[3], const or_hit* prim,
+                          uint8_t* vis, or_hit* mirror, uint32_t* shadow_stats, uint32_t* mirror_stats,
+                          int nthreads);
+
 /* PCG32 helpers shared with the tests (O'Neill, pcg-random.org, pcg32_srandom_r). */
 uint32_t or_pcg32_first(uint64_t initstate, uint64_t initseq, uint32_t count, uint32_t* out);
 

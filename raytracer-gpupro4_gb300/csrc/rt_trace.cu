@@ -70,55 +70,6 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_
     }
 }
 
-// The shading rays of one pixel whose primary hit is ph (CSComputeColorRT.hlsl,
-// flat normal, no textures): the shadow ray towards the point light, cast
-// only when the light and the viewer are on the same side of the surface,
-// and the mirror ray.  has = the primary ray hit something.
-struct ShadeRays {
-    RayState shadow, mirror;
-    bool has, cast;
-};
-
-__device__ __forceinline__ ShadeRays shade_rays(const float* __restrict__ soup, const rt_camera& cam, float lx,
-                                                float ly, float lz, int4 ph, bool valid, uint32_t i, uint32_t j,
-                                                bool want_mirror) {
-    ShadeRays s;
-    const int id = valid ? ph.x : -1;
-    s.has = valid && id >= 0;
-    s.cast = false;
-    f3 N = mk3(0.f, 0.f, 1.f), Nf = N, P = mk3(0.f, 0.f, 0.f), L = mk3(0.f, 0.f, 1.f), d = mk3(0.f, 0.f, 1.f);
-    float dist = 1.0f;
-    if (s.has) {
-        const float t = __int_as_float(ph.w);
-        d = primary_dir(cam, i, j);
-        const f3 o = mk3(cam.eye[0], cam.eye[1], cam.eye[2]);
-        const float* tp = soup + 9 * (size_t)id;
-        const f3 A = mk3(__ldg(tp), __ldg(tp + 1), __ldg(tp + 2));
-        const f3 B = mk3(__ldg(tp + 3), __ldg(tp + 4), __ldg(tp + 5));
-        const f3 C = mk3(__ldg(tp + 6), __ldg(tp + 7), __ldg(tp + 8));
-        N = normalize3(cross3(sub3(B, A), sub3(C, A)));            // CSComputeColorRT.hlsl:61-63,75
-        Nf = N;
-        if (dot3(Nf, d) > 0.0f) Nf = mk3(-N.x, -N.y, -N.z);        // :126-131
-        P = mk3(fadd(o.x, fmul(t, d.x)), fadd(o.y, fmul(t, d.y)), fadd(o.z, fmul(t, d.z)));  // :134-135
-        L = mk3(fsub(P.x, lx), fsub(P.y, ly), fsub(P.z, lz));      // :136
-        dist = fsqrt(dot3(L, L));                                  // :137
-        L = mk3(fdiv(L.x, dist), fdiv(L.y, dist), fdiv(L.z, dist)); // :138
-        const float ls = dot3(N, L), rs = dot3(N, d);              // :145-146
-        s.cast = fmul(ls, rs) > 0.0f;                              // :147
-    }
-    s.shadow = make_ray(P, mk3(-L.x, -L.y, -L.z), dist, id);      // :149-153
-    f3 R = mk3(0.f, 0.f, 1.f);
-    if (want_mirror && s.has) {
-        const float k = fmul(2.0f, dot3(d, Nf));                   // reflect(d, N) = d - 2*dot(d,N)*N
-        R = normalize3(mk3(fsub(d.x, fmul(k, Nf.x)), fsub(d.y, fmul(k, Nf.y)), fsub(d.z, fmul(k, Nf.z))));
-    }
-    s.mirror = make_ray(P, R, 1e16f, id);
-    return s;
-}
-
-__device__ __forceinline__ uint8_t vis_code(bool has, bool cast, bool occluded) {
-    return !has ? 0 : (!cast ? 1 : (occluded ? 2 : 3));
-}
 
 // Shadow (any hit) and mirror (closest hit) rays of one pixel whose primary
 // hit is ph.  Called by all lanes of the warp together (valid == false for

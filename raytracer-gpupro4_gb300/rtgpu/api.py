@@ -163,6 +163,39 @@ class LBVH:
         return np.array(out[:], np.float32)
 
 
+class BVH:
+    """The reference's SAH BVH on the device (rt_bvh): a flattened
+    LinearBVHNode array (bvh.cpp:272-293, NODE_DTYPE layout) with its
+    ordered primitive ids, imported from the reference's CPU build and traced
+    as BVH_IntersectP (BVH.hlsl:124-217).  RayTracer's primary,
+    shadow_mirror and rays accept it in place of an LBVH."""
+
+    def __init__(self, ctx: Context, max_nodes: int, max_tris: int):
+        self.ctx = ctx
+        h = C.c_void_p()
+        L.check(L.lib().rt_bvh_create(ctx.h, max_nodes, max_tris, C.byref(h)), ctx.h, "rt_bvh_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            L.lib().rt_bvh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def Import(self, nodes: np.ndarray, ids: np.ndarray, tris: np.ndarray) -> "BVH":
+        nodes = np.ascontiguousarray(nodes).view(L.NODE_DTYPE)
+        ids = np.ascontiguousarray(ids, np.uint32)
+        tris = np.ascontiguousarray(tris, np.float32)
+        L.check(L.lib().rt_bvh_import_host(self.ctx.h, self.h, _host_ptr(nodes), len(nodes), _host_ptr(ids),
+                                           _host_ptr(tris), len(tris)), self.ctx.h, "rt_bvh_import_host")
+        return self
+
+
 class StructureConstruction:
     """GPUBuildStructure(depth) over a device soup (StructureConstruction.cpp:86-131)."""
 
@@ -190,8 +223,9 @@ class RayTracer:
         npx = cam.width * cam.height
         hits = out if out is not None else self._alloc_hits(npx)
         st = torch.empty((npx, 2), dtype=torch.int32, device=self.ctx.torch_device) if stats else None
-        L.check(L.lib().rt_trace_primary(self.ctx.h, lbvh.h, C.byref(cam), _dev_ptr(hits),
-                                         _dev_ptr(st) if stats else None), self.ctx.h, "rt_trace_primary")
+        fn = L.lib().rt_bvh_trace_primary if isinstance(lbvh, BVH) else L.lib().rt_trace_primary
+        L.check(fn(self.ctx.h, lbvh.h, C.byref(cam), _dev_ptr(hits), _dev_ptr(st) if stats else None), self.ctx.h,
+                "rt_trace_primary")
         return (hits, st) if stats else hits
 
     def shadow_mirror(self, lbvh: LBVH, cam: L.Camera, light, primary: torch.Tensor, stats: bool = False,
@@ -207,11 +241,10 @@ class RayTracer:
         ss = torch.empty((npx, 2), dtype=torch.int32, device=self.ctx.torch_device) if stats else None
         ms = torch.empty((npx, 2), dtype=torch.int32, device=self.ctx.torch_device) if stats and with_mirror else None
         lf = (C.c_float * 3)(*light)
-        L.check(L.lib().rt_trace_shadow_mirror(self.ctx.h, lbvh.h, C.byref(cam), lf, _dev_ptr(primary),
-                                               _dev_ptr(vis), _dev_ptr(mirror) if mirror is not None else None,
-                                               _dev_ptr(ss) if stats else None,
-                                               _dev_ptr(ms) if ms is not None else None), self.ctx.h,
-                "rt_trace_shadow_mirror")
+        fn = L.lib().rt_bvh_trace_shadow_mirror if isinstance(lbvh, BVH) else L.lib().rt_trace_shadow_mirror
+        L.check(fn(self.ctx.h, lbvh.h, C.byref(cam), lf, _dev_ptr(primary), _dev_ptr(vis),
+                   _dev_ptr(mirror) if mirror is not None else None, _dev_ptr(ss) if stats else None,
+                   _dev_ptr(ms) if ms is not None else None), self.ctx.h, "rt_trace_shadow_mirror")
         return (vis, mirror, ss, ms) if stats else (vis, mirror)
 
     def primary_leaves(self, lbvh: LBVH, cam: L.Camera, stats: bool = False, out: torch.Tensor | None = None,
@@ -293,8 +326,9 @@ class RayTracer:
         n = rays.shape[0]
         hits = self._alloc_hits(n)
         st = torch.empty((n, 2), dtype=torch.int32, device=self.ctx.torch_device) if stats else None
-        L.check(L.lib().rt_trace_rays(self.ctx.h, lbvh.h, _dev_ptr(rays), n, int(any_hit), _dev_ptr(hits),
-                                      _dev_ptr(st) if stats else None), self.ctx.h, "rt_trace_rays")
+        fn = L.lib().rt_bvh_trace_rays if isinstance(lbvh, BVH) else L.lib().rt_trace_rays
+        L.check(fn(self.ctx.h, lbvh.h, _dev_ptr(rays), n, int(any_hit), _dev_ptr(hits),
+                   _dev_ptr(st) if stats else None), self.ctx.h, "rt_trace_rays")
         return (hits, st) if stats else hits
 
     def render_frame_host(self, lbvh: LBVH, tris: np.ndarray, cam: L.Camera, light, primary: np.ndarray,
