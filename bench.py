@@ -158,15 +158,18 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str):
-    """Per-launch DRAM traffic of a kernel from the committed ncu summary."""
+def ncu_traffic(*kernels: str):
+    """Per-launch DRAM traffic (read + write bytes) of a stage's kernels, summed,
+    from the committed ncu summary; None when one of them was not captured."""
     p = ROOT / "profiles" / "ncu_traffic.json"
     if not p.exists():
         return None
     try:
-        return json.loads(p.read_text()).get(kernel)
+        d = json.loads(p.read_text())
     except (ValueError, OSError):
         return None
+    vals = [d.get(k) for k in kernels]
+    return None if any(v is None for v in vals) else int(sum(vals))
 
 
 # ---------------------------------------------------------------------------
@@ -217,15 +220,15 @@ def run_ours(args, dist: Dist):
     vis = torch.empty(npx, dtype=torch.uint8, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
 
-    # algorithmic trace bytes of frame 0 from the per-ray test counters of the
-    # frame path's walks (shading rays restarted at the primary leaves)
+    # algorithmic trace bytes of frame 0: per-ray node visits and triangle
+    # tests of the reference's own walk (LBVH_IntersectP in the shader's order,
+    # shadow and mirror rays restarted at the primary leaf, closest hit for
+    # both), the counts the trace bytes are defined on
     lb.Build(dfr[0])
-    _, _, pst = rt.primary_leaves(lb, cam, stats=True, out=hits, leaves=leaves)
-    _, _, _, sst, mst = rt.shadow_mirror_from(lb, cam, light, hits, leaves, stats=True, vis=vis, mirror=mirror,
-                                              mirror_leaves=mleaves)
+    _, svis, _, pst, sst, mst = rt.frame_shader_order(lb, cam, light, stats=True)
     ctx.check()
     pst, sst, mst = (x.to(torch.int64).sum(0).tolist() for x in (pst, sst, mst))
-    visn = vis.cpu().numpy()
+    visn = svis.cpu().numpy()
     n_prim = npx
     n_shadow = int((visn >= 2).sum())
     n_mirror = int((visn >= 1).sum())
@@ -292,11 +295,12 @@ def run_ours(args, dist: Dist):
     for g in graphs:
         g.close()
 
-    # e2e: the public C ABI call with host buffers, copies inside the timed
-    # region.  Two contexts on two streams take alternate frames
-    # (rt_render_frame_host_async), so one frame's copies overlap the other
-    # frame's kernels; every frame's soup upload and result download is inside
-    # the timed region.
+    # e2e: the public C ABI with host buffers, copies inside the timed region.
+    # Two contexts on two streams take alternate frames, each frame one launch
+    # of a graph captured by rt_frame_capture_host (pinned soup upload,
+    # rebuild, trace, read-back of hits / visibility / mirror hits into pinned
+    # host buffers), so one frame's copies overlap the other frame's kernels;
+    # every frame's upload and read-back is inside the timed region.
     e2e = None
     if not args.no_e2e:
         lanes = []
@@ -304,19 +308,16 @@ def run_ours(args, dist: Dist):
             st_q = torch.cuda.Stream(dev)
             ctx_q = Context(dist.local, stream=st_q)
             lb_q = LBVH(ctx_q, n, args.depth)
-            bufs = []
-            for _ in range(3):
-                t = torch.empty(npx * 4, dtype=torch.int32).pin_memory()
-                bufs.append(t)
+            hp_t = torch.empty((npx, 4), dtype=torch.int32).pin_memory()
+            hm_t = torch.empty((npx, 4), dtype=torch.int32).pin_memory()
             hv_t = torch.empty(npx, dtype=torch.uint8).pin_memory()
-            lanes.append((ctx_q, lb_q, RayTracer(ctx_q), bufs[0].numpy().view(L.HIT_DTYPE), hv_t.numpy(),
-                          bufs[1].numpy().view(L.HIT_DTYPE), bufs, hv_t))
-        hosts = [host[k].numpy() for k in range(len(frames))]
+            fr_q = [Frame(ctx_q, lb_q, host[k], cam, light, hp_t, hv_t, hm_t, host=True) for k in range(len(frames))]
+            lanes.append((ctx_q, lb_q, fr_q, hp_t, hv_t, hm_t))
 
         def e2e_frame(k):
-            ctx_q, lb_q, rt_q, hp2, hv2, hm2 = lanes[k % 2][:6]
-            ctx_q.sync()  # this lane's previous frame is done with its buffers
-            rt_q.render_frame_host(lb_q, hosts[k % len(frames)], cam, light, hp2, hv2, hm2, wait=False)
+            ctx_q, _, fr_q = lanes[k % 2][:3]
+            ctx_q.sync()  # this lane's previous frame is done with its host buffers
+            fr_q[k % len(frames)].launch()
 
         for k in range(args.warmup):
             e2e_frame(k)
@@ -334,29 +335,34 @@ def run_ours(args, dist: Dist):
             lanes[q][0].check()
         # the last frame read back equals the last graph frame (same soup)
         last = lanes[(args.warmup + args.steps - 1) % 2][3]
-        e2e_ok = bool(np.array_equal(last.view(np.int32).reshape(-1, 4), hits.cpu().numpy()))
+        e2e_ok = bool(np.array_equal(last.numpy(), hits.cpu().numpy()))
         e2e = {"value": round(frames_done * n / te / 1e6, 3), "unit": "Mtri/s",
                "h2d_bytes_per_step": int(n * 36), "d2h_bytes_per_step": int(npx * (16 + 1 + 16)),
                "ms_per_step": round(te / args.steps * 1e3, 3),
-               "call": "rt_render_frame_host_async on two contexts / streams, alternate frames "
+               "call": "rt_frame_capture_host graphs on two contexts / streams, alternate frames "
                        "(pinned host soup in, hits / visibility / mirror hits out)",
                "matches_device_path": e2e_ok}
         for q in range(2):
+            for f in lanes[q][2]:
+                f.close()
             lanes[q][1].close()
             lanes[q][0].close()
 
     peak, peak_kind = measured_peaks()
-    groups = {"k_trace_primary (+ k_trace_heavy)": (prim_ms, bytes_primary),
-              "k_trace_secondary (+ k_trace_heavy)": (sec_ms, bytes_secondary),
-              "build (10 kernels)": (build_ms, BUILD_BYTES_PER_TRI * n)}
+    # stage: (ms, algorithmic bytes, kernels of the stage's ncu traffic)
+    groups = {"k_trace_primary (+ k_trace_heavy)": (prim_ms, bytes_primary, ("k_trace_primary", "k_trace_heavy")),
+              "k_trace_shade (+ k_shade_setup, k_trace_heavy)": (sec_ms, bytes_secondary,
+                                                                 ("k_trace_shade", "k_shade_setup", "k_trace_heavy")),
+              "build (10 kernels)": (build_ms, BUILD_BYTES_PER_TRI * n, ("k_bounds", "k_morton_hist", "k_onesweep",
+                                                                          "k_emit_leaves", "k_emit_refit"))}
     dom = max(groups, key=lambda g: groups[g][0])
-    ms, byts = groups[dom]
+    ms, byts, kern = groups[dom]
     achieved = byts / (ms / 1e3) / 1e9
     frame_bytes = BUILD_BYTES_PER_TRI * n + bytes_primary + bytes_secondary
     frame_ms = float(step_ms.mean())
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                "traffic": ncu_traffic(dom.split(" ")[0]), "algorithmic_bytes_per_launch": int(byts),
+                "traffic": ncu_traffic(*kern), "algorithmic_bytes_per_launch": int(byts),
                 "avg_launch_ms": round(float(ms), 4),
                 "frame": {"algorithmic_bytes": int(frame_bytes), "ms": round(frame_ms, 4),
                           "achieved": round(frame_bytes / (frame_ms / 1e3) / 1e9, 1),
@@ -436,16 +442,16 @@ def run_batch(args, dist: Dist):
     lb = LBVH(ctx, int(sizes.max()), args.depth)
     rt = RayTracer(ctx)
     phits = torch.empty((S, npx, 4), dtype=torch.int32, device=dev)
+    pleaves = torch.empty(npx, dtype=torch.int32, device=dev)
     pvis = torch.empty((S, npx), dtype=torch.uint8, device=dev)
     nb = nt = 0
     n_shadow = 0
-    for s in range(S):
+    for s in range(S):  # counts of the reference's own walk (LBVH_IntersectP order), per scene
         lb.Build(dsoup[off[s]:off[s + 1]])
-        _, pst = rt.primary(lb, cams[s], stats=True, out=phits[s])
-        _, _, sst, _ = rt.shadow_mirror(lb, cams[s], lights[s], phits[s], stats=True, vis=pvis[s], with_mirror=False)
+        _, svis, _, pst, sst, _ = rt.frame_shader_order(lb, cams[s], lights[s], stats=True, with_mirror=False)
         nb += int(pst[:, 0].sum() + sst[:, 0].sum())
         nt += int(pst[:, 1].sum() + sst[:, 1].sum())
-        n_shadow += int((pvis[s] >= 2).sum())
+        n_shadow += int((svis >= 2).sum())
     ctx.check()
     rays = S * npx + n_shadow
     trace_bytes = 32 * nb + 40 * nt + 32 * rays
@@ -453,8 +459,8 @@ def run_batch(args, dist: Dist):
     def plain_step():
         for s in range(S):
             lb.Build(dsoup[off[s]:off[s + 1]])
-            rt.primary(lb, cams[s], out=phits[s])
-            rt.shadow_mirror(lb, cams[s], lights[s], phits[s], vis=pvis[s], with_mirror=False)
+            rt.primary_leaves(lb, cams[s], out=phits[s], leaves=pleaves)
+            rt.shadow_mirror_from(lb, cams[s], lights[s], phits[s], pleaves, vis=pvis[s], with_mirror=False)
 
     def timed(fn, steps):
         evs = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(steps)]

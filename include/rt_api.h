@@ -291,6 +291,21 @@ rt_status rt_render_whitted(rt_ctx* ctx, const rt_lbvh* lbvh, const rt_camera* c
                             const rt_material* d_materials, uint32_t num_materials, const float* d_normals,
                             float* d_accum, float* d_result);
 
+/* A frame (primary, shadow, mirror rays) traced in the reference's own walk
+ * order: LBVH_IntersectP (LBVH.hlsl:363-440) as the shader runs it, a
+ * stackless trail walk with one box test per visited node, the child picked
+ * by the stored axis field first, closest hit for every ray (the shadow ray
+ * too, as CSComputeColorRT.hlsl:160 issues it) and exact ties resolved as
+ * the shader resolves them (the first triangle tested stays); the shading
+ * rays restart at the primary hit's leaf.  One lane per ray: slower than
+ * rt_trace_primary + rt_trace_shadow_mirror, which keep the smaller id on
+ * an exact tie.  The optional stats are the shader's iVisitedNodes per ray
+ * {visited nodes, triangle tests}; the trace's algorithmic bytes are
+ * defined on them.  vis / mirror may be NULL. */
+rt_status rt_trace_frame_shader_order(rt_ctx* ctx, const rt_lbvh* lbvh, const rt_camera* cam, const float light[3],
+                                      rt_hit* d_primary, uint8_t* d_vis, rt_hit* d_mirror, uint32_t* d_primary_stats,
+                                      uint32_t* d_shadow_stats, uint32_t* d_mirror_stats);
+
 /* One frame of the dynamic path (RayTracerCS::Render with dynamic=1,
  * RayTracerCS.cpp:258-295): rebuild from a host soup, primary, shadow and
  * mirror rays (started at the primary hits' leaves), results copied back to
@@ -321,6 +336,15 @@ rt_status rt_frame_capture(rt_ctx* ctx, rt_lbvh* lbvh, const float* d_tris, uint
 rt_status rt_frame_launch(rt_ctx* ctx, rt_frame* frame);
 uint32_t rt_frame_node_count(const rt_frame* frame);
 rt_status rt_frame_destroy(rt_frame* frame);
+/* rt_frame_capture with host buffers: the upload of the pinned host soup,
+ * the rebuild, the trace and the read-back of the results into pinned host
+ * buffers (any output may be NULL), captured as one graph; every launch of
+ * it is one frame of rt_render_frame_host.  All host buffers must be
+ * page-locked (RT_ERR_INVALID otherwise); the caller writes the next frame's
+ * vertices into h_tris between launches. */
+rt_status rt_frame_capture_host(rt_ctx* ctx, rt_lbvh* lbvh, const float* h_tris, uint32_t n, uint32_t flags,
+                                const rt_camera* cam, const float light[3], rt_hit* h_primary, uint8_t* h_vis,
+                                rt_hit* h_mirror, rt_frame** out);
 
 /* ---- batched scenes ------------------------------------------------- */
 /* Up to 256 independent scenes rebuilt and traced together: one pass of the

@@ -91,6 +91,8 @@ def olib() -> C.CDLL:
         L.or_lbvh_build.argtypes = [vp, u32, u32, vp, vp, vp, vp]
         L.or_trace.argtypes = [vp, u32, vp, vp, vp, u32, vp, vp, i32, i32]
         L.or_trace_from.argtypes = [vp, u32, vp, vp, vp, u32, vp, vp, vp, vp, i32, i32]
+        L.or_trace_hlsl.argtypes = [vp, u32, vp, vp, vp, u32, vp, vp, vp, vp, i32]
+        L.or_shadow_mirror_hlsl.argtypes = [vp, u32, vp, vp, C.POINTER(OrCamera), vp, vp, vp, vp, vp, vp, vp, i32]
         L.or_primary_rays.argtypes = [C.POINTER(OrCamera), vp]
         L.or_shadow_mirror.argtypes = [vp, u32, vp, vp, C.POINTER(OrCamera), vp, vp, vp, vp, vp, vp, i32]
         L.or_shadow_mirror_from.argtypes = [vp, u32, vp, vp, C.POINTER(OrCamera), vp, vp, vp, vp, vp, vp, vp, vp,
@@ -183,6 +185,38 @@ def trace_from(nodes, depth, ids, tris, rays, starts=None, any_hit=False, nthrea
                          _ptr(sp) if sp is not None else None, _ptr(hits), _ptr(leaves),
                          _ptr(st) if stats else None, int(any_hit), nthreads or nthreads_default())
     return (hits, leaves, st) if stats else (hits, leaves)
+
+
+def trace_hlsl(nodes, depth, ids, tris, rays, starts=None, nthreads=None):
+    """or_trace_hlsl: the reference's own LBVH_IntersectP walk.  Returns
+    (hits, leaves, stats) with stats = {visited nodes, triangle tests}."""
+    rays = np.ascontiguousarray(rays, np.float32)
+    n = len(rays)
+    hits = np.zeros(n, HIT_DTYPE)
+    leaves = np.zeros(n, np.uint32)
+    st = np.zeros((n, 2), np.uint32)
+    sp = None if starts is None else np.ascontiguousarray(starts, np.uint32)
+    olib().or_trace_hlsl(_ptr(nodes), depth, _ptr(ids), _ptr(np.ascontiguousarray(tris, np.float32)), _ptr(rays), n,
+                         _ptr(sp) if sp is not None else None, _ptr(hits), _ptr(leaves), _ptr(st),
+                         nthreads or nthreads_default())
+    return hits, leaves, st
+
+
+def frame_hlsl(nodes, depth, ids, tris, cam, light, nthreads=None):
+    """A frame in the reference's own walk order (or_trace_hlsl +
+    or_shadow_mirror_hlsl).  Returns (prim, vis, mirror, prim_stats,
+    shadow_stats, mirror_stats)."""
+    prim, leaves, pst = trace_hlsl(nodes, depth, ids, tris, primary_rays(cam), nthreads=nthreads)
+    oc = to_or_camera(cam)
+    npx = cam.width * cam.height
+    vis = np.zeros(npx, np.uint8)
+    mirror = np.zeros(npx, HIT_DTYPE)
+    ss = np.zeros((npx, 2), np.uint32)
+    ms = np.zeros((npx, 2), np.uint32)
+    olib().or_shadow_mirror_hlsl(_ptr(nodes), depth, _ptr(ids), _ptr(np.ascontiguousarray(tris, np.float32)),
+                                 C.byref(oc), _ptr(np.asarray(light, np.float32)), _ptr(prim), _ptr(leaves),
+                                 _ptr(vis), _ptr(mirror), _ptr(ss), _ptr(ms), nthreads or nthreads_default())
+    return prim, vis, mirror, pst, ss, ms
 
 
 def primary_rays(cam) -> np.ndarray:

@@ -1021,3 +1021,112 @@ void or_bvh_shadow_mirror(const or_node* nodes, uint32_t num_nodes, const uint32
         bvh_trace_one(nodes, num_nodes, ids, n, tris, mr, &mirror[p], mirror_stats ? mirror_stats + 2 * p : NULL, 0);
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* The reference's own walk, LBVH_IntersectP (LBVH.hlsl:363-440): a stackless
+ * walk over the heap driven by a trail word (the `iRoot` restart sets
+ * trail = 1 << firstbithigh(node), as if every ancestor had been entered by
+ * its first child), one box test per visited node (IntersectBox), the child
+ * picked by dirIsNeg[axis field] entered first, each visited leaf's
+ * triangles tested in order, a candidate accepted when it is not the
+ * excluded triangle, passes RayTriangleTest and is strictly nearer (so on
+ * an exact tie the first one tested stays), and fMaxT lowered to it.  It is
+ * a closest-hit walk for every ray, shadow rays included
+ * (CSComputeColorRT.hlsl:160).  stats = {visited nodes, triangle tests}: the
+ * two halves of the shader's iVisitedNodes counter (result++ per node,
+ * += 65536 per triangle, :389, :404). */
+static void hlsl_walk(const or_node* nodes, const uint32_t* ids, const float* tris, const float* r,
+                      uint32_t node, or_hit* out, uint32_t* stats, uint32_t* leaf_out) {
+    const float o[3] = {r[0], r[1], r[2]};
+    const float d[3] = {r[3], r[4], r[5]};
+    const int exclude = (int)r[7];
+    const float inv[3] = {1.0f / d[0], 1.0f / d[1], 1.0f / d[2]};
+    const int neg[3] = {inv[0] < 0.0f, inv[1] < 0.0f, inv[2] < 0.0f};
+    float best_t = r[6], best_u = -1.0f, best_v = -1.0f;
+    int best_id = -1;
+    uint32_t root = 1, visits = 0, ntri = 0;
+    if (node < 1) node = 1;
+    uint32_t trail = 1u << hb32(node);
+    do {
+        float T0, T1;
+        box_interval(&nodes[node], o, inv, &T0, &T1);
+        const int p = __builtin_ctz(trail + 1u);
+        ++visits;
+        if (T0 > best_t || T1 < 0.0f) {
+            trail = (trail >> p) + 1u;
+            node = (node >> p) ^ 1u;
+        } else if (nodes[node].prim_count & 4) {
+            const int cnt = nodes[node].prim_count >> 3, pos = nodes[node].prim_pos;
+            for (int i = 0; i < cnt; ++i) {
+                ++ntri;
+                const int id = (int)ids[pos + i];
+                const float* t = tris + 9 * (size_t)id;
+                float u, v, tt;
+                if (id != exclude && tri_test(t, t + 3, t + 6, o, d, &u, &v, &tt) && tt < best_t) {
+                    best_t = tt; best_u = u; best_v = v; best_id = id; root = node;
+                }
+            }
+            trail = (trail >> p) + 1u;
+            node = (node >> p) ^ 1u;
+        } else {
+            trail <<= 1;
+            node = (node << 1) | (uint32_t)neg[nodes[node].prim_count & 3];
+        }
+    } while (trail > 1u);
+    out->id = best_id; out->u = best_u; out->v = best_v; out->t = best_t;
+    if (stats) { stats[0] = visits; stats[1] = ntri; }
+    if (leaf_out) *leaf_out = root;
+}
+
+void or_trace_hlsl(const or_node* nodes, uint32_t depth, const uint32_t* ids, const float* tris,
+                   const float* rays, uint32_t nrays, const uint32_t* starts, or_hit* hits, uint32_t* leaves,
+                   uint32_t* stats, int nthreads) {
+    (void)depth;
+    if (nthreads <= 0) nthreads = 1;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+    for (long i = 0; i < (long)nrays; ++i)
+        hlsl_walk(nodes, ids, tris, rays + 8 * i, starts ? starts[i] : 1u, &hits[i], stats ? stats + 2 * i : NULL,
+                  leaves ? leaves + i : NULL);
+}
+
+/* The shading rays of or_shadow_mirror traced with the reference's own walk
+ * (hlsl_walk), restarted at the primary hit's leaf from or_trace_hlsl; the
+ * shadow ray is a closest-hit walk as CSComputeColorRT.hlsl:160 issues it. */
+void or_shadow_mirror_hlsl(const or_node* nodes, uint32_t depth, const uint32_t* ids, const float* tris,
+                           const or_camera* cam, const float light[3], const or_hit* prim, const uint32_t* prim_leaves,
+                           uint8_t* vis, or_hit* mirror, uint32_t* shadow_stats, uint32_t* mirror_stats,
+                           int nthreads) {
+    (void)depth;
+    const long npx = (long)cam->width * cam->height;
+    if (nthreads <= 0) nthreads = 1;
+    const float inv = 1.0f / (float)cam->height;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+    for (long p = 0; p < npx; ++p) {
+        uint32_t i = (uint32_t)(p % cam->width), j = (uint32_t)(p / cam->width);
+        if (shadow_stats) { shadow_stats[2 * p] = 0; shadow_stats[2 * p + 1] = 0; }
+        if (mirror_stats) { mirror_stats[2 * p] = 0; mirror_stats[2 * p + 1] = 0; }
+        if (prim[p].id < 0) {
+            vis[p] = 0;
+            mirror[p].id = -2; mirror[p].u = -1.0f; mirror[p].v = -1.0f; mirror[p].t = 0.0f;
+            continue;
+        }
+        float r[8];
+        float x = (float)(2 * (int)i + 1 - (int)cam->width) * inv;
+        float y = -((float)(2 * (int)j + 1 - (int)cam->height) * inv);
+        camera_dir(cam, x, y, r + 3);
+        r[0] = cam->eye[0]; r[1] = cam->eye[1]; r[2] = cam->eye[2];
+        r[6] = 1e16f; r[7] = -1.0f;
+        float sr[8], mr[8];
+        int cast;
+        secondary(tris, r, &prim[p], light, sr, mr, &cast);
+        const uint32_t start = prim_leaves[p];
+        if (cast) {
+            or_hit sh;
+            hlsl_walk(nodes, ids, tris, sr, start, &sh, shadow_stats ? shadow_stats + 2 * p : NULL, NULL);
+            vis[p] = (sh.id >= 0) ? 2 : 3;
+        } else {
+            vis[p] = 1;
+        }
+        hlsl_walk(nodes, ids, tris, mr, start, &mirror[p], mirror_stats ? mirror_stats + 2 * p : NULL, NULL);
+    }
+}

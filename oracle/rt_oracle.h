@@ -73,6 +73,19 @@ void or_trace_from(const or_node* nodes, uint32_t depth, const uint32_t* ids, co
                    const float* rays, uint32_t nrays, const uint32_t* starts, or_hit* hits, uint32_t* leaves,
                    uint32_t* stats, int any_hit, int nthreads);
 
+/* The reference's own walk order, LBVH_IntersectP (LBVH.hlsl:363-440): the
+ * stackless trail walk started at heap node starts[i] (NULL: the root), a
+ * closest-hit walk whose exact ties keep the first triangle it tests;
+ * stats = {visited nodes, triangle tests} (its iVisitedNodes counter). */
+void or_trace_hlsl(const or_node* nodes, uint32_t depth, const uint32_t* ids, const float* tris,
+                   const float* rays, uint32_t nrays, const uint32_t* starts, or_hit* hits, uint32_t* leaves,
+                   uint32_t* stats, int nthreads);
+
+void or_shadow_mirror_hlsl(const or_node* nodes, uint32_t depth, const uint32_t* ids, const float* tris,
+                           const or_camera* cam, const float light[3], const or_hit* prim, const uint32_t* prim_leaves,
+                           uint8_t* vis, or_hit* mirror, uint32_t* shadow_stats, uint32_t* mirror_stats,
+                           int nthreads);
+
 /* --- ray generation and shading rays (CSPrimaryRays.hlsl, CSComputeColorRT.hlsl) */
 void or_primary_rays(const or_camera* cam, float* rays /* w*h x 8 */);
 /* From primary hits: shadow-ray visibility code per pixel

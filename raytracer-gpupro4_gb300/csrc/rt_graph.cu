@@ -85,6 +85,53 @@ extern "C" rt_status rt_frame_capture(rt_ctx* ctx, rt_lbvh* l, const float* d_tr
         out);
 }
 
+// A host buffer a captured copy may use: page-locked (cudaHostAlloc /
+// cudaHostRegister) or managed.
+static bool pinned(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged;
+}
+
+extern "C" rt_status rt_frame_capture_host(rt_ctx* ctx, rt_lbvh* l, const float* h_tris, uint32_t n, uint32_t flags,
+                                           const rt_camera* cam, const float light[3], rt_hit* h_primary,
+                                           uint8_t* h_vis, rt_hit* h_mirror, rt_frame** out) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (!l || !h_tris || !cam || !light || !out) return rt_fail(ctx, RT_ERR_INVALID, "rt_frame_capture_host: null argument");
+    if (n == 0 || n > l->cap) return rt_fail(ctx, RT_ERR_CAPACITY, "rt_frame_capture_host: n=%u (capacity %u)", n, l->cap);
+    const size_t px = (size_t)cam->width * cam->height;
+    if (px == 0 || px > (1ull << 31)) return rt_fail(ctx, RT_ERR_INVALID, "rt_frame_capture_host: bad image size");
+    const void* host[] = {h_tris, h_primary, h_vis, h_mirror};
+    for (const void* h : host)
+        if (h && !pinned(h))
+            return rt_fail(ctx, RT_ERR_INVALID, "rt_frame_capture_host: host buffers must be page-locked");
+    // buffers the frame's calls would otherwise allocate inside the capture
+    rt_status es = ensure_frame_buffers(ctx, l, px);
+    if (es == RT_OK && (h_vis || h_mirror)) es = ensure_shade_lists(ctx, l, px);
+    if (es != RT_OK) return es;
+    return capture_frame(
+        ctx, "rt_frame_capture_host",
+        [&]() {
+            cudaStream_t st = ctx->stream;
+            RT_CHECK_CUDA(ctx, cudaMemcpyAsync(l->tris, h_tris, sizeof(float) * 9 * (size_t)n, cudaMemcpyHostToDevice, st));
+            rt_status s = rt_lbvh_build(ctx, l, l->tris, n, flags);
+            if (s == RT_OK)
+                s = trace_frame(ctx, l, cam, light, l->f_primary, h_vis ? l->f_vis : nullptr,
+                                h_mirror ? l->f_mirror : nullptr, "rt_frame_capture_host");
+            if (s != RT_OK) return s;
+            if (h_primary)
+                RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_primary, l->f_primary, sizeof(rt_hit) * px, cudaMemcpyDeviceToHost, st));
+            if (h_vis) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_vis, l->f_vis, px, cudaMemcpyDeviceToHost, st));
+            if (h_mirror)
+                RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_mirror, l->f_mirror, sizeof(rt_hit) * px, cudaMemcpyDeviceToHost, st));
+            return RT_OK;
+        },
+        out);
+}
+
 extern "C" rt_status rt_batch_frame_capture(rt_ctx* ctx, rt_batch* b, const float* d_tris, uint32_t flags,
                                             rt_hit* d_hits, uint8_t* d_vis, rt_frame** out) {
     if (!ctx) return RT_ERR_INVALID;

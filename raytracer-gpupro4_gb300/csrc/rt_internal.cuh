@@ -231,6 +231,9 @@ enum : int {
 // Grows the compacted shading-ray lists of l to px pixels (synchronises the
 // context stream when it allocates; call before a stream capture).
 rt_status ensure_shade_lists(rt_ctx* ctx, rt_lbvh* l, size_t px);
+// Grows the per-frame result buffers of l (f_primary, f_vis, f_mirror) to px
+// pixels (synchronises the context stream when it allocates).
+rt_status ensure_frame_buffers(rt_ctx* ctx, rt_lbvh* l, size_t px);
 // Primary rays, then (d_vis or d_mirror set) the shading rays started at the
 // primary leaves; the shading lists must hold the image (ensure_shade_lists).
 rt_status trace_frame(rt_ctx* ctx, rt_lbvh* l, const rt_camera* cam, const float light[3], rt_hit* d_primary,

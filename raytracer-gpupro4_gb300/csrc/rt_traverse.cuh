@@ -387,6 +387,54 @@ __device__ __forceinline__ bool pop_node(const TreeRef& tr_, float bt, uint32_t&
     return false;
 }
 
+// Start of a walk at heap node `start` (<= 1: the root; see traverse): the
+// siblings of start's ancestors are box-tested and stacked, then start's own
+// box is tested; a missed start pops the stack.  Returns true when the lane
+// holds a node to enter.
+template <bool EXACT>
+__device__ __forceinline__ bool start_walk(const RayState& r, const TreeRef& tr_, uint32_t start, float bt,
+                                           uint32_t* stack_node, float* stack_t0, uint32_t& sp, uint32_t& node,
+                                           NodeBox& cur, uint32_t& nbox) {
+    // no t satisfies 0 <= t < tmax when tmax <= 0 or is NaN
+    const bool live = r.tmax > 0.0f;
+    node = 1;
+    if (start > 1u && !tr_.compact) {
+        if (start >= tr_.num_nodes) {
+            atomicOr(tr_.err, RT_DEVERR_BOUNDS);
+        } else {
+            const int D = 31 - __clz(start);  // <= kMaxDepth < kStackSize
+            for (int k = 1; k <= D; ++k) {
+                const uint32_t sib = (start >> (D - k)) ^ 1u;
+                const NodeBox sb = load_node(tr_.nodes, sib);
+                ++nbox;
+                float t0;
+                if (live && box_enter<EXACT>(r, sb.a.x, sb.a.y, sb.a.z, sb.a.w, sb.b.x, sb.b.y, bt, &t0)) {
+                    stack_node[sp & (kStackSize - 1)] = sib;
+                    stack_t0[sp & (kStackSize - 1)] = t0;
+                    ++sp;
+                }
+            }
+            node = start;
+        }
+    }
+    cur = load_node(tr_.nodes, node);
+    ++nbox;
+    float t0;
+    bool have = live && box_enter<EXACT>(r, cur.a.x, cur.a.y, cur.a.z, cur.a.w, cur.b.x, cur.b.y, bt, &t0);
+    if (!have) {
+        while (sp != 0) {  // pop_node, declared below
+            --sp;
+            if (!(stack_t0[sp & (kStackSize - 1)] > bt)) {
+                node = stack_node[sp & (kStackSize - 1)];
+                cur = load_node(tr_.nodes, node);
+                have = true;
+                break;
+            }
+        }
+    }
+    return have;
+}
+
 // Hand-over of rays that exceed a work budget.  A lane whose ray has spent
 // more than `budget` box + triangle tests takes a slot of the heavy-ray list
 // (atomicAdd on *count) and stops; the caller records the ray in that slot,
@@ -440,34 +488,7 @@ __device__ __forceinline__ Hit traverse(const RayState& r, bool active, const Tr
     uint32_t node = 1;
     int slot = -1;
     bool budgeted = !STATS && spill != nullptr && spill->count != nullptr;
-    if (active) {
-        // no t satisfies 0 <= t < tmax when tmax <= 0 or is NaN
-        const bool live = r.tmax > 0.0f;
-        if (start > 1u && !tr_.compact) {
-            if (start >= tr_.num_nodes) {
-                atomicOr(tr_.err, RT_DEVERR_BOUNDS);
-            } else {
-                const int D = 31 - __clz(start);  // <= kMaxDepth < kStackSize
-                for (int k = 1; k <= D; ++k) {
-                    const uint32_t sib = (start >> (D - k)) ^ 1u;
-                    const NodeBox sb = load_node(tr_.nodes, sib);
-                    ++nbox;
-                    float t0;
-                    if (live && box_enter<EXACT>(r, sb.a.x, sb.a.y, sb.a.z, sb.a.w, sb.b.x, sb.b.y, b.t, &t0)) {
-                        stack_node[sp & (kStackSize - 1)] = sib;
-                        stack_t0[sp & (kStackSize - 1)] = t0;
-                        ++sp;
-                    }
-                }
-                node = start;
-            }
-        }
-        cur = load_node(tr_.nodes, node);
-        ++nbox;
-        float t0;
-        have = live && box_enter<EXACT>(r, cur.a.x, cur.a.y, cur.a.z, cur.a.w, cur.b.x, cur.b.y, b.t, &t0);
-        if (!have) have = pop_node(tr_, b.t, node, cur, stack_node, stack_t0, sp, 0u);
-    }
+    if (active) have = start_walk<EXACT>(r, tr_, start, b.t, stack_node, stack_t0, sp, node, cur, nbox);
     while (__any_sync(kFull, have)) {
         if (have) have = descend<EXACT, STATS>(tr_, r, b.t, node, cur, stack_node, stack_t0, sp, 0u, nbox);
         __syncwarp();

@@ -31,9 +31,9 @@ EXPORTED = [
     "rt_ctx_check", "rt_last_error", "rt_lbvh_create", "rt_lbvh_destroy", "rt_lbvh_build", "rt_lbvh_build_host",
     "rt_lbvh_import_host", "rt_lbvh_view_get", "rt_lbvh_compact_get", "rt_lbvh_world_bound", "rt_lbvh_download", "rt_trace_primary",
     "rt_trace_shadow_mirror", "rt_trace_rays", "rt_trace_primary_leaves", "rt_trace_shadow_mirror_from",
-    "rt_trace_rays_from", "rt_render_whitted", "rt_bvh_create", "rt_bvh_destroy", "rt_bvh_import_host",
+    "rt_trace_rays_from", "rt_trace_frame_shader_order", "rt_render_whitted", "rt_bvh_create", "rt_bvh_destroy", "rt_bvh_import_host",
     "rt_bvh_trace_primary", "rt_bvh_trace_shadow_mirror", "rt_bvh_trace_rays", "rt_render_frame_host", "rt_render_frame_host_async", "rt_pathtrace", "rt_pathtrace_adjoint",
-    "rt_lbvh_build_noalloc", "rt_frame_capture", "rt_frame_launch", "rt_frame_node_count", "rt_frame_destroy",
+    "rt_lbvh_build_noalloc", "rt_frame_capture_host", "rt_frame_capture", "rt_frame_launch", "rt_frame_node_count", "rt_frame_destroy",
     "rt_batch_create", "rt_batch_destroy", "rt_batch_scene_count", "rt_batch_build", "rt_batch_view_get",
     "rt_batch_download", "rt_batch_set_views", "rt_batch_trace", "rt_batch_set_tuning", "rt_batch_get_tuning", "rt_batch_frame_capture",
 ]
@@ -112,6 +112,7 @@ def lib() -> C.CDLL:
         "rt_trace_primary_leaves": (i32, [vp, vp, C.POINTER(Camera), vp, vp, vp]),
         "rt_trace_shadow_mirror_from": (i32, [vp, vp, C.POINTER(Camera), fp, vp, vp, vp, vp, vp, vp, vp]),
         "rt_trace_rays_from": (i32, [vp, vp, vp, u32, i32, vp, vp, vp, vp]),
+        "rt_trace_frame_shader_order": (i32, [vp, vp, C.POINTER(Camera), fp, vp, vp, vp, vp, vp, vp]),
         "rt_render_whitted": (i32, [vp, vp, C.POINTER(Camera), fp, C.POINTER(ShadeParams), vp, vp, u32, vp, vp, vp]),
         "rt_bvh_create": (i32, [vp, u32, u32, C.POINTER(vp)]),
         "rt_bvh_destroy": (i32, [vp]),
@@ -125,6 +126,7 @@ def lib() -> C.CDLL:
         "rt_pathtrace_adjoint": (i32, [vp, vp, vp, vp, C.POINTER(Camera), C.POINTER(PtParams), vp, vp, vp]),
         "rt_lbvh_build_noalloc": (i32, [vp, vp, vp, u32, u32, u32, vp, vp, vp, vp]),
         "rt_frame_capture": (i32, [vp, vp, vp, u32, u32, C.POINTER(Camera), fp, vp, vp, vp, C.POINTER(vp)]),
+        "rt_frame_capture_host": (i32, [vp, vp, vp, u32, u32, C.POINTER(Camera), fp, vp, vp, vp, C.POINTER(vp)]),
         "rt_frame_launch": (i32, [vp, vp]),
         "rt_frame_node_count": (u32, [vp]),
         "rt_frame_destroy": (i32, [vp]),

@@ -263,20 +263,25 @@ class RayTracer:
 
     def shadow_mirror_from(self, lbvh: LBVH, cam: L.Camera, light, primary: torch.Tensor, leaves: torch.Tensor,
                            stats: bool = False, vis: torch.Tensor | None = None, mirror: torch.Tensor | None = None,
-                           mirror_leaves: torch.Tensor | None = None):
+                           mirror_leaves: torch.Tensor | None = None, with_mirror: bool = True):
         """Shading rays started at the primary leaves (rt_trace_shadow_mirror_from).
-        Returns (vis, mirror, mirror_leaves[, shadow_stats, mirror_stats])."""
+        Returns (vis, mirror, mirror_leaves[, shadow_stats, mirror_stats]);
+        with_mirror=False traces the shadow rays only (mirror outputs None)."""
         npx = cam.width * cam.height
         dev = self.ctx.torch_device
         vis = vis if vis is not None else torch.empty(npx, dtype=torch.uint8, device=dev)
-        mirror = mirror if mirror is not None else self._alloc_hits(npx)
-        ml = mirror_leaves if mirror_leaves is not None else torch.empty(npx, dtype=torch.int32, device=dev)
+        if with_mirror:
+            mirror = mirror if mirror is not None else self._alloc_hits(npx)
+            ml = mirror_leaves if mirror_leaves is not None else torch.empty(npx, dtype=torch.int32, device=dev)
+        else:
+            mirror = ml = None
         ss = torch.empty((npx, 2), dtype=torch.int32, device=dev) if stats else None
-        ms = torch.empty((npx, 2), dtype=torch.int32, device=dev) if stats else None
+        ms = torch.empty((npx, 2), dtype=torch.int32, device=dev) if stats and with_mirror else None
         lf = (C.c_float * 3)(*light)
+        opt = lambda t: _dev_ptr(t) if t is not None else None  # noqa: E731
         L.check(L.lib().rt_trace_shadow_mirror_from(self.ctx.h, lbvh.h, C.byref(cam), lf, _dev_ptr(primary),
-                                                    _dev_ptr(leaves), _dev_ptr(vis), _dev_ptr(mirror), _dev_ptr(ml),
-                                                    _dev_ptr(ss) if stats else None, _dev_ptr(ms) if stats else None),
+                                                    _dev_ptr(leaves), _dev_ptr(vis), opt(mirror), opt(ml), opt(ss),
+                                                    opt(ms)),
                 self.ctx.h, "rt_trace_shadow_mirror_from")
         return (vis, mirror, ml, ss, ms) if stats else (vis, mirror, ml)
 
@@ -321,6 +326,26 @@ class RayTracer:
                 "rt_render_whitted")
         return acc, res
 
+    def frame_shader_order(self, lbvh: LBVH, cam: L.Camera, light, stats: bool = False, with_mirror: bool = True):
+        """rt_trace_frame_shader_order: primary, shadow and mirror rays in the
+        reference shader's own walk order and tie rule.  Returns (primary, vis,
+        mirror[, primary_stats, shadow_stats, mirror_stats]); mirror outputs are
+        None with with_mirror=False."""
+        npx = cam.width * cam.height
+        dev = self.ctx.torch_device
+        prim = self._alloc_hits(npx)
+        vis = torch.empty(npx, dtype=torch.uint8, device=dev)
+        mirror = self._alloc_hits(npx) if with_mirror else None
+        st = [torch.zeros((npx, 2), dtype=torch.int32, device=dev) for _ in range(3)] if stats else [None] * 3
+        if not with_mirror:
+            st[2] = None
+        lf = (C.c_float * 3)(*light)
+        opt = lambda t: _dev_ptr(t) if t is not None else None  # noqa: E731
+        L.check(L.lib().rt_trace_frame_shader_order(self.ctx.h, lbvh.h, C.byref(cam), lf, _dev_ptr(prim),
+                                                    _dev_ptr(vis), opt(mirror), opt(st[0]), opt(st[1]), opt(st[2])),
+                self.ctx.h, "rt_trace_frame_shader_order")
+        return (prim, vis, mirror, *st) if stats else (prim, vis, mirror)
+
     def rays(self, lbvh: LBVH, rays: torch.Tensor, any_hit: bool = False, stats: bool = False):
         """rays: (n, 8) float32 device tensor laid out as rt_ray {o, exclude(int bits), d, tmax}."""
         n = rays.shape[0]
@@ -363,18 +388,26 @@ class RayTracer:
 
 class Frame:
     """One frame of the dynamic path (rebuild + primary + shadow + mirror)
-    captured as a CUDA graph (rt_frame_capture); launch() replays it."""
+    captured as a CUDA graph (rt_frame_capture); launch() replays it.  With
+    host=True the tensors are pinned host tensors and the graph also holds
+    the soup upload and the result read-back (rt_frame_capture_host)."""
 
     def __init__(self, ctx: Context, lbvh: LBVH, tris: torch.Tensor, cam: L.Camera, light, primary: torch.Tensor,
-                 vis: torch.Tensor | None, mirror: torch.Tensor | None, flags: int = 0):
+                 vis: torch.Tensor | None, mirror: torch.Tensor | None, flags: int = 0, host: bool = False):
         self.ctx = ctx
         self._keep = (tris, primary, vis, mirror)
         h = C.c_void_p()
         lf = (C.c_float * 3)(*light)
-        L.check(L.lib().rt_frame_capture(ctx.h, lbvh.h, _dev_ptr(tris), tris.shape[0], flags, C.byref(cam), lf,
-                                         _dev_ptr(primary), _dev_ptr(vis) if vis is not None else None,
-                                         _dev_ptr(mirror) if mirror is not None else None, C.byref(h)),
-                ctx.h, "rt_frame_capture")
+        fn = L.lib().rt_frame_capture_host if host else L.lib().rt_frame_capture
+
+        def ptr(t):
+            if t is None:
+                return None
+            assert t.is_contiguous() and t.is_cuda != host  # host buffers: rt_frame_capture_host checks pinning
+            return C.c_void_p(t.data_ptr())
+
+        L.check(fn(ctx.h, lbvh.h, ptr(tris), tris.shape[0], flags, C.byref(cam), lf, ptr(primary), ptr(vis),
+                   ptr(mirror), C.byref(h)), ctx.h, "rt_frame_capture_host" if host else "rt_frame_capture")
         self.h = h
         lbvh.n = tris.shape[0]
         lbvh._tris = tris

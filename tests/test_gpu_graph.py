@@ -43,3 +43,42 @@ def test_graph_frames_equal_direct_calls(gpu_ctx):
             assert np.array_equal(gm, hits_to_numpy(dm))
     for g in graphs:
         g.close()
+
+
+def test_host_frame_graph(gpu_ctx):
+    """rt_frame_capture_host: upload, rebuild, trace and read-back as one
+    graph; each replay reads the soup's current contents and writes the same
+    results as the device frame graph; pageable host buffers are refused."""
+    import torch
+    from rtgpu import scenes
+    from rtgpu._lib import RtError
+    from rtgpu.api import LBVH, Frame
+    s = scenes.icosphere(freq=40)
+    soups = [torch.from_numpy(s.frame(k)) for k in range(2)]
+    cam = scenes.sphere_camera(320, 180)
+    light = scenes.TORUS_LIGHT
+    n, npx = soups[0].shape[0], cam.width * cam.height
+    # device reference
+    lb_d = LBVH(gpu_ctx, n, 16)
+    dp = torch.empty((npx, 4), dtype=torch.int32, device="cuda")
+    dv = torch.empty(npx, dtype=torch.uint8, device="cuda")
+    dm = torch.empty((npx, 4), dtype=torch.int32, device="cuda")
+    # host graph over one pinned soup buffer whose contents change per frame
+    hs = torch.empty_like(soups[0]).pin_memory()
+    hp = torch.empty((npx, 4), dtype=torch.int32).pin_memory()
+    hv = torch.empty(npx, dtype=torch.uint8).pin_memory()
+    hm = torch.empty((npx, 4), dtype=torch.int32).pin_memory()
+    lb_h = LBVH(gpu_ctx, n, 16)
+    fh = Frame(gpu_ctx, lb_h, hs, cam, light, hp, hv, hm, host=True)
+    for k in range(2):
+        hs.copy_(soups[k])
+        fh.launch()
+        gpu_ctx.sync()
+        fd = Frame(gpu_ctx, lb_d, soups[k].cuda(), cam, light, dp, dv, dm)
+        fd.launch()
+        gpu_ctx.check()
+        assert torch.equal(hp, dp.cpu()) and torch.equal(hv, dv.cpu()) and torch.equal(hm, dm.cpu())
+        fd.close()
+    fh.close()
+    with pytest.raises(RtError):
+        Frame(gpu_ctx, lb_h, soups[0].clone(), cam, light, hp, hv, hm, host=True)  # pageable soup

