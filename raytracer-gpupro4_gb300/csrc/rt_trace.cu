@@ -372,6 +372,7 @@ struct HeavyArgs {
     int any_hit;          // generic rays
     uint32_t* leaves;     // primary / generic-ray leaf output (nullable)
     uint32_t* mirror_leaves;
+    uint32_t wide_cap;    // frontier-stack entries per warp (wide_stack_entries of the tree depth)
     const uint32_t* list;
     const uint32_t* count;
     uint32_t cap;
@@ -388,14 +389,14 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_heavy(HeavyArgs a) {
             const uint32_t i = idx % a.cam.width, j = idx / a.cam.width;
             const RayState r = make_ray(mk3(a.cam.eye[0], a.cam.eye[1], a.cam.eye[2]), primary_dir(a.cam, i, j),
                                         1e16f, -1);
-            const Hit h = trace_wide(r, a.tr, false);
+            const Hit h = trace_wide(r, a.tr, false, a.wide_cap);
             if (lane == 0) {
                 store_hit(a.hits + idx, h);
                 if (a.leaves) a.leaves[idx] = 1u;  // the root: a valid restart node
             }
         } else if (kind == kHeavyRay) {
             const RayState r = load_ray(a.rays, idx, true);
-            const Hit h = trace_wide(r, a.tr, a.any_hit != 0);
+            const Hit h = trace_wide(r, a.tr, a.any_hit != 0, a.wide_cap);
             if (lane == 0) {
                 store_hit(a.hits + idx, h);
                 if (a.leaves) a.leaves[idx] = 1u;
@@ -405,10 +406,10 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_heavy(HeavyArgs a) {
             const int4 ph = __ldg(reinterpret_cast<const int4*>(a.prim + idx));
             const ShadeRays s = shade_rays(a.soup, a.cam, a.lx, a.ly, a.lz, ph, true, i, j, kind == kHeavyMirror);
             if (kind == kHeavyShadow) {
-                const Hit h = trace_wide(s.shadow, a.tr, true);
+                const Hit h = trace_wide(s.shadow, a.tr, true, a.wide_cap);
                 if (lane == 0) a.vis[idx] = vis_code(s.has, s.cast, h.id >= 0);
             } else {
-                const Hit h = trace_wide(s.mirror, a.tr, false);
+                const Hit h = trace_wide(s.mirror, a.tr, false, a.wide_cap);
                 if (lane == 0) {
                     store_hit(a.mirror + idx, h);
                     if (a.mirror_leaves) a.mirror_leaves[idx] = 1u;
@@ -481,11 +482,12 @@ rt_status launch_heavy(rt_ctx* ctx, const Spill& sp, HeavyArgs a) {
     a.count = ctx->d_spill_count;
     a.cap = kSpillCap;
     a.work = ctx->d_work + kWorkHeavy;
+    const size_t smem = wide_smem_bytes(a.wide_cap);
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_heavy, kTraceThreads, 0) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_heavy, kTraceThreads, smem) != cudaSuccess ||
         per_sm < 1)
         per_sm = 1;
-    k_trace_heavy<<<(uint32_t)per_sm * ctx->num_sms, kTraceThreads, 0, ctx->stream>>>(a);
+    k_trace_heavy<<<(uint32_t)per_sm * ctx->num_sms, kTraceThreads, smem, ctx->stream>>>(a);
     RT_CHECK_LAUNCH(ctx, "k_trace_heavy");
     return RT_OK;
 }
@@ -532,6 +534,7 @@ HeavyArgs heavy_args(rt_ctx* ctx, const rt_lbvh* l) {
     HeavyArgs a;
     memset(&a, 0, sizeof(a));
     a.tr = tree_ref(ctx, l);
+    a.wide_cap = wide_stack_entries(l->depth);
     return a;
 }
 

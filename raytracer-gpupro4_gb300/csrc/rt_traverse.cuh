@@ -544,37 +544,38 @@ __device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
 // (t, id) keys becomes the shared bound.  The closest hit under the tie rule
 // does not depend on the order of the tests, so the hit equals traverse()'s.
 // For any_hit the walk stops at the first accepted hit.
-constexpr int kWideStack = 1024;   // entries per warp (a depth-26 tree needs at most 26 x 32 + 32)
-constexpr int kWideQueue = 128;    // queued leaves per warp
-constexpr int kWideWarps = 4;          // blocks of at most 128 threads
+// Each step pops the newest 32 entries, so every group of pushed children
+// leaves at most 32 entries behind, one group per tree level: a tree of
+// depth D needs at most 32 (D + 1) entries, and wide_stack_entries adds one
+// more group.  The stack lives in dynamic shared memory sized per launch.
+constexpr int kWideStackMax = 1024;  // entries per warp for depth <= 29
+constexpr int kWideQueue = 128;      // queued leaves per warp
+constexpr int kWideWarps = 4;        // blocks of at most 128 threads
 
-struct WideSmem {
-    uint32_t node[kWideWarps][kWideStack];
-    float t0[kWideWarps][kWideStack];
-    int32_t qpos[kWideWarps][kWideQueue];
-    int32_t qcnt[kWideWarps][kWideQueue];
-    float qt0[kWideWarps][kWideQueue];
-    uint32_t qincl[kWideWarps][kWideQueue];
-};
+__host__ __device__ constexpr uint32_t wide_stack_entries(uint32_t depth) {
+    return (depth + 2u) * 32u < (uint32_t)kWideStackMax ? (depth + 2u) * 32u : (uint32_t)kWideStackMax;
+}
 
-// One block-wide instance shared by both instantiations of traverse_wide.
-__device__ __forceinline__ WideSmem& wide_smem() {
-    __shared__ WideSmem sm;
-    return sm;
+// Dynamic shared memory of a block running traverse_wide with `cap` stack
+// entries per warp: stack nodes and entry distances, then the leaf queue.
+__host__ __device__ constexpr size_t wide_smem_bytes(uint32_t cap) {
+    return (size_t)kWideWarps * (cap * 8u + kWideQueue * 16u);
 }
 
 template <bool EXACT>
-__device__ __forceinline__ Hit traverse_wide(const RayState& r, const TreeRef& tr_, bool any_hit) {
+__device__ __forceinline__ Hit traverse_wide(const RayState& r, const TreeRef& tr_, bool any_hit, uint32_t cap) {
     constexpr uint32_t kFull = 0xffffffffu;
-    WideSmem& sm = wide_smem();
+    extern __shared__ uint4 wide_dyn[];
+    uint8_t* base8 = reinterpret_cast<uint8_t*>(wide_dyn);
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    uint32_t* snode = sm.node[wib];
-    float* st0 = sm.t0[wib];
-    int32_t* qpos = sm.qpos[wib];
-    int32_t* qcnt = sm.qcnt[wib];
-    float* qt0 = sm.qt0[wib];
-    uint32_t* qincl = sm.qincl[wib];
+    uint32_t* snode = reinterpret_cast<uint32_t*>(base8) + (size_t)wib * cap;
+    float* st0 = reinterpret_cast<float*>(base8 + (size_t)kWideWarps * cap * 4u) + (size_t)wib * cap;
+    uint8_t* qbase = base8 + (size_t)kWideWarps * cap * 8u;
+    int32_t* qpos = reinterpret_cast<int32_t*>(qbase) + wib * kWideQueue;
+    int32_t* qcnt = reinterpret_cast<int32_t*>(qbase) + (kWideWarps + wib) * kWideQueue;
+    float* qt0 = reinterpret_cast<float*>(qbase) + (2 * kWideWarps + wib) * kWideQueue;
+    uint32_t* qincl = reinterpret_cast<uint32_t*>(qbase) + (3 * kWideWarps + wib) * kWideQueue;
     const uint64_t init = hit_key(r.tmax, 0);
     uint64_t best = init;  // uniform across the warp
     float bu = -1.0f, bv = -1.0f, bt = r.tmax;
@@ -711,7 +712,7 @@ __device__ __forceinline__ Hit traverse_wide(const RayState& r, const TreeRef& t
         const int ioff = size + __popc(ib0 & lt) + __popc(ib1 & lt);
         const int loff = nq + __popc(lb0 & lt) + __popc(lb1 & lt);
         const int itotal = __popc(ib0) + __popc(ib1), ltotal = __popc(lb0) + __popc(lb1);
-        if (size + itotal > kWideStack) {  // cannot happen with depth <= 26; stop rather than overflow
+        if (size + itotal > (int)cap) {  // cannot happen within the tree's depth; stop rather than overflow
             if (lane == 0) atomicOr(tr_.err, RT_DEVERR_BOUNDS);
             stop = true;
             break;
@@ -776,9 +777,9 @@ __device__ __forceinline__ Hit trace_ray(const RayState& r, bool active, const T
 }
 
 // One ray traced by the whole warp; every lane passes the same ray.
-__device__ __forceinline__ Hit trace_wide(const RayState& r, const TreeRef& tr, bool any_hit) {
-    if (r.exact) return traverse_wide<true>(r, tr, any_hit);
-    return traverse_wide<false>(r, tr, any_hit);
+__device__ __forceinline__ Hit trace_wide(const RayState& r, const TreeRef& tr, bool any_hit, uint32_t cap) {
+    if (r.exact) return traverse_wide<true>(r, tr, any_hit, cap);
+    return traverse_wide<false>(r, tr, any_hit, cap);
 }
 
 // Primary ray of pixel (i, j): CSPrimaryRays.hlsl:36-56 with the basis camera.
