@@ -92,8 +92,12 @@ rt_status rt_ctx_set_stream(rt_ctx* ctx, void* stream);
 /* Work budget of the camera, shading and generic ray traces: a ray that has
  * spent more than `budget` box + triangle tests in the per-lane traversal is
  * handed to a second kernel that traces it with a whole warp (same hit).
- * 0 turns the hand-over off.  Default 384.  Path tracing never hands over. */
+ * 0 turns the hand-over off.  rt_ctx_set_trace_budget sets every kind;
+ * rt_ctx_set_trace_budget_kind one (0 primary rays, 1 shadow / mirror rays,
+ * 2 rt_trace_rays).  Defaults: 384, 768, 384 (the fastest on a 2.1 M-triangle
+ * frame).  Path tracing never hands over. */
 rt_status rt_ctx_set_trace_budget(rt_ctx* ctx, uint32_t budget);
+rt_status rt_ctx_set_trace_budget_kind(rt_ctx* ctx, uint32_t kind, uint32_t budget);
 /* Heavy-first tile order: for each trace kind in `kinds` (bit 0 primary
  * rays, bit 1 shadow / mirror rays, bit 2 rt_trace_rays) a call first
  * traces the tiles that were the most expensive in the previous call of the

@@ -79,7 +79,14 @@ extern "C" rt_status rt_ctx_set_stream(rt_ctx* ctx, void* stream) {
 
 extern "C" rt_status rt_ctx_set_trace_budget(rt_ctx* ctx, uint32_t budget) {
     if (!ctx) return RT_ERR_INVALID;
-    ctx->trace_budget = budget;
+    for (uint32_t& b : ctx->trace_budget) b = budget;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_ctx_set_trace_budget_kind(rt_ctx* ctx, uint32_t kind, uint32_t budget) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (kind > 2u) return rt_fail(ctx, RT_ERR_INVALID, "rt_ctx_set_trace_budget_kind: kind is 0, 1 or 2");
+    ctx->trace_budget[kind] = budget;
     return RT_OK;
 }
 

@@ -87,6 +87,7 @@ constexpr uint32_t kMaxTris = (1u << 29);
 // hands the ray to the warp-per-ray kernel.
 constexpr uint32_t kSpillCap = 1u << 20;
 constexpr uint32_t kDefaultTraceBudget = 384;
+constexpr uint32_t kDefaultShadeBudget = 768;
 // Heavy-first tile order (TileOrder in rt_traverse.cuh): per trace kind two
 // lists of kOrderCap tiles and two bitmaps, in one allocation.
 constexpr uint32_t kOrderCap = 1u << 20;
@@ -103,7 +104,8 @@ struct rt_ctx {
     uint32_t* d_words = nullptr; // 64 device words
     uint32_t* d_spill = nullptr; // heavy-ray list, kSpillCap entries
     uint32_t* d_order = nullptr; // heavy-first tile order, kOrderKinds x kOrderWords (parity / counts: d_words[40..])
-    uint32_t trace_budget = kDefaultTraceBudget;  // 0: no hand-over
+    // hand-over budget per trace kind (0 primary, 1 shading, 2 generic rays); 0: no hand-over
+    uint32_t trace_budget[3] = {kDefaultTraceBudget, kDefaultShadeBudget, kDefaultTraceBudget};
     uint32_t tile_order = 1u;  // heavy-first tile order per kind: bit 0 primary, 1 shading, 2 generic rays
     int num_sms = 0;
 };

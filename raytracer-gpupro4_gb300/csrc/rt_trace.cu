@@ -462,11 +462,11 @@ namespace {
 // Heavy-ray hand-over of one trace call: the list is emptied before the
 // first pass (budget 0 or a counting pass: no hand-over), and the second pass
 // drains it.
-Spill spill_of(rt_ctx* ctx, bool enabled) {
+Spill spill_of(rt_ctx* ctx, bool enabled, int kind) {
     Spill sp;
-    sp.count = (enabled && ctx->trace_budget) ? ctx->d_spill_count : nullptr;
+    sp.budget = ctx->trace_budget[kind];
+    sp.count = (enabled && sp.budget) ? ctx->d_spill_count : nullptr;
     sp.cap = kSpillCap;
-    sp.budget = ctx->trace_budget;
     return sp;
 }
 
@@ -548,7 +548,7 @@ rt_status trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, rt_
     if (s != RT_OK) return s;
     if (!d_hits) return rt_fail(ctx, RT_ERR_INVALID, "%s: null output", who);
     if ((s = reset_work(ctx, kWorkPrimary)) != RT_OK) return s;
-    const Spill sp = spill_of(ctx, !d_stats && (uint64_t)cam->width * cam->height <= kHeavyIndexMask);
+    const Spill sp = spill_of(ctx, !d_stats && (uint64_t)cam->width * cam->height <= kHeavyIndexMask, 0);
     if ((s = reset_spill(ctx, sp)) != RT_OK) return s;
     TileOrder ord;
     if ((s = order_begin(ctx, 0, ctx->tile_order & 1u, &ord)) != RT_OK) return s;
@@ -581,7 +581,7 @@ rt_status trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* ca
     if (!l->src_tris) return rt_fail(ctx, RT_ERR_INVALID, "%s: no triangle soup bound", who);
     if ((s = reset_work(ctx, kWorkSecondary)) != RT_OK) return s;
     const bool stats = d_shadow_stats || d_mirror_stats;
-    const Spill sp = spill_of(ctx, !stats && (uint64_t)cam->width * cam->height <= kHeavyIndexMask);
+    const Spill sp = spill_of(ctx, !stats && (uint64_t)cam->width * cam->height <= kHeavyIndexMask, 1);
     if ((s = reset_spill(ctx, sp)) != RT_OK) return s;
     const uint32_t tiles = pixel_tiles(cam);
     if (stats) {  // per-pixel counts in the oracle's order: the tile pass
@@ -636,7 +636,7 @@ rt_status trace_rays(rt_ctx* ctx, const rt_lbvh* l, const rt_ray* d_rays, uint32
     if (n == 0) return RT_OK;
     rt_status s = reset_work(ctx, kWorkRays);
     if (s != RT_OK) return s;
-    const Spill sp = spill_of(ctx, !d_stats && n <= kHeavyIndexMask);
+    const Spill sp = spill_of(ctx, !d_stats && n <= kHeavyIndexMask, 2);
     if ((s = reset_spill(ctx, sp)) != RT_OK) return s;
     TileOrder ord;
     if ((s = order_begin(ctx, 2, ctx->tile_order & 4u, &ord)) != RT_OK) return s;

@@ -66,10 +66,22 @@ class Context:
         """Heavy-first tile order per trace kind (bit 0 primary, 1 shading, 2 generic rays)."""
         L.check(L.lib().rt_ctx_set_tile_order(self.h, int(kinds)), self.h, "rt_ctx_set_tile_order")
 
-    def set_trace_budget(self, budget: int):
+    DEFAULT_BUDGETS = (384, 768, 384)  # primary, shadow / mirror, generic rays
+
+    def set_trace_budget(self, budget: int | None, kind: int | None = None):
         """Box + triangle tests a ray may spend in the per-lane traversal before
-        it is handed to the warp-per-ray pass (0: never)."""
-        L.check(L.lib().rt_ctx_set_trace_budget(self.h, int(budget)), self.h, "rt_ctx_set_trace_budget")
+        it is handed to the warp-per-ray pass (0: never) for one trace kind
+        (0 primary, 1 shadow / mirror, 2 generic rays) or all; None restores
+        the defaults."""
+        if budget is None:
+            for k, b in enumerate(self.DEFAULT_BUDGETS):
+                self.set_trace_budget(b, k)
+            return
+        if kind is None:
+            L.check(L.lib().rt_ctx_set_trace_budget(self.h, int(budget)), self.h, "rt_ctx_set_trace_budget")
+        else:
+            L.check(L.lib().rt_ctx_set_trace_budget_kind(self.h, int(kind), int(budget)), self.h,
+                    "rt_ctx_set_trace_budget_kind")
 
 
 class LBVH:

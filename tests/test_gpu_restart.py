@@ -64,7 +64,7 @@ def test_production_shading_rays_from_leaves(gpu_ctx, oracle_mod, sphere, budget
         vis, mir, ml = rt.shadow_mirror_from(lb, cam, light, hits, leaves)
         gpu_ctx.check()
     finally:
-        gpu_ctx.set_trace_budget(384)
+        gpu_ctx.set_trace_budget(None)
     oh, ol = oracle_mod.trace_from(nodes, 18, ids, tris, oracle_mod.primary_rays(cam))
     ovis, omir, oml = oracle_mod.shadow_mirror_from(nodes, 18, ids, tris, cam, light, oh, ol)
     assert_hits_equal(hits_to_numpy(hits), oh, "primary")

@@ -211,7 +211,7 @@ def test_heavy_ray_handover_matches_oracle(gpu_ctx, oracle_mod, torus_scene, bud
         vis, mirror = rt.shadow_mirror(lb, cam, scenes.TORUS_LIGHT, hits)
         gpu_ctx.check()
     finally:
-        gpu_ctx.set_trace_budget(384)
+        gpu_ctx.set_trace_budget(None)
     oh = oracle_mod.trace(nodes, 20, ids, tris, oracle_mod.primary_rays(cam))
     ovis, omir = oracle_mod.shadow_mirror(nodes, 20, ids, tris, cam, scenes.TORUS_LIGHT, oh)
     assert_hits_equal(hits_to_numpy(hits), oh, "primary")
@@ -239,7 +239,7 @@ def test_heavy_ray_handover_generic_rays(gpu_ctx, oracle_mod, any_hit):
         hits = RayTracer(gpu_ctx).rays(lb, rays_tensor(o, d, tmax, excl, "cuda"), any_hit=any_hit)
         gpu_ctx.check()
     finally:
-        gpu_ctx.set_trace_budget(384)
+        gpu_ctx.set_trace_budget(None)
     oh = oracle_mod.trace(nodes, 16, ids, tris, oracle_mod.rays_array(o, d, tmax, excl), any_hit=any_hit)
     g = hits_to_numpy(hits)
     if any_hit:
