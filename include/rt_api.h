@@ -339,6 +339,11 @@ rt_status rt_frame_capture(rt_ctx* ctx, rt_lbvh* lbvh, const float* d_tris, uint
                            rt_hit* d_mirror, rt_frame** out);
 rt_status rt_frame_launch(rt_ctx* ctx, rt_frame* frame);
 uint32_t rt_frame_node_count(const rt_frame* frame);
+/* A captured frame holds a reference on its rt_lbvh (rt_batch): while it
+ * exists the structure's grow-on-demand buffers keep their size (a call that
+ * would grow them fails with RT_ERR_CAPACITY), and rt_lbvh_destroy /
+ * rt_batch_destroy only marks the structure; the last rt_frame_destroy frees
+ * it. */
 rt_status rt_frame_destroy(rt_frame* frame);
 /* rt_frame_capture with host buffers: the upload of the pinned host soup,
  * the rebuild, the trace and the read-back of the results into pinned host

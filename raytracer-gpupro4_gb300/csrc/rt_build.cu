@@ -1030,6 +1030,15 @@ extern "C" rt_status rt_lbvh_create(rt_ctx* ctx, uint32_t max_tris, uint32_t dep
 
 extern "C" rt_status rt_lbvh_destroy(rt_lbvh* l) {
     if (!l) return RT_OK;
+    if (l->graph_refs > 0) {  // a captured frame still points into l: the last frame destroy frees it
+        l->destroy_pending = true;
+        return RT_OK;
+    }
+    free_lbvh(l);
+    return RT_OK;
+}
+
+void free_lbvh(rt_lbvh* l) {
     void* ptrs[] = {l->nodes,    l->keys,     l->ids,      l->keys_alt,  l->ids_alt, l->sorted_tris,
                     l->tris,     l->scene,    l->partials, l->counters,  l->hist,    l->lookback,
                     l->scan,     l->leaf_list, l->arrive,  l->f_primary, l->f_mirror, l->f_vis,
@@ -1037,7 +1046,6 @@ extern "C" rt_status rt_lbvh_destroy(rt_lbvh* l) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete l;
-    return RT_OK;
 }
 
 static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint32_t n, uint32_t flags) {
@@ -1632,13 +1640,21 @@ __global__ void __launch_bounds__(256) kb_emit_refit(const uint32_t* __restrict_
 
 extern "C" rt_status rt_batch_destroy(rt_batch* b) {
     if (!b) return RT_OK;
+    if (b->graph_refs > 0) {  // a captured frame still points into b: the last frame destroy frees it
+        b->destroy_pending = true;
+        return RT_OK;
+    }
+    free_batch(b);
+    return RT_OK;
+}
+
+void free_batch(rt_batch* b) {
     void* ptrs[] = {b->tri_off, b->node_off, b->chunks, b->nodes, b->keys, b->ids, b->keys_alt, b->ids_alt,
                     b->ids_local, b->sorted_tris, b->sbounds, b->counters, b->hist, b->lookback, b->scan,
                     b->leaf_list, b->arrive, b->cams, b->lights};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete b;
-    return RT_OK;
 }
 
 extern "C" rt_status rt_batch_create(rt_ctx* ctx, uint32_t n_scenes, const uint32_t* h_tri_counts, uint32_t depth,

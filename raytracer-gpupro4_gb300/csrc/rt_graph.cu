@@ -14,7 +14,19 @@ struct rt_frame {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     uint32_t nodes = 0;
+    rt_lbvh* lbvh = nullptr;    // the structure whose buffers the graph points into (a reference)
+    rt_batch* batch = nullptr;
 };
+
+// The frame keeps l's (b's) buffers alive and at their size until it is destroyed.
+static void hold(rt_frame* f, rt_lbvh* l) {
+    f->lbvh = l;
+    ++l->graph_refs;
+}
+static void hold(rt_frame* f, rt_batch* b) {
+    f->batch = b;
+    ++b->graph_refs;
+}
 
 // Records what `record` issues on the context stream into a graph: the
 // context stream is swapped for a private non-blocking stream (the legacy
@@ -75,7 +87,7 @@ extern "C" rt_status rt_frame_capture(rt_ctx* ctx, rt_lbvh* l, const float* d_tr
         const rt_status es = ensure_shade_lists(ctx, l, (size_t)cam->width * cam->height);
         if (es != RT_OK) return es;
     }
-    return capture_frame(
+    const rt_status s = capture_frame(
         ctx, "rt_frame_capture",
         [&]() {
             rt_status s = rt_lbvh_build(ctx, l, d_tris, n, flags);
@@ -83,6 +95,8 @@ extern "C" rt_status rt_frame_capture(rt_ctx* ctx, rt_lbvh* l, const float* d_tr
             return s;
         },
         out);
+    if (s == RT_OK) hold(*out, l);
+    return s;
 }
 
 // A host buffer a captured copy may use: page-locked (cudaHostAlloc /
@@ -112,7 +126,7 @@ extern "C" rt_status rt_frame_capture_host(rt_ctx* ctx, rt_lbvh* l, const float*
     rt_status es = ensure_frame_buffers(ctx, l, px);
     if (es == RT_OK && (h_vis || h_mirror)) es = ensure_shade_lists(ctx, l, px);
     if (es != RT_OK) return es;
-    return capture_frame(
+    const rt_status cs = capture_frame(
         ctx, "rt_frame_capture_host",
         [&]() {
             cudaStream_t st = ctx->stream;
@@ -130,6 +144,8 @@ extern "C" rt_status rt_frame_capture_host(rt_ctx* ctx, rt_lbvh* l, const float*
             return RT_OK;
         },
         out);
+    if (cs == RT_OK) hold(*out, l);
+    return cs;
 }
 
 extern "C" rt_status rt_batch_frame_capture(rt_ctx* ctx, rt_batch* b, const float* d_tris, uint32_t flags,
@@ -137,7 +153,7 @@ extern "C" rt_status rt_batch_frame_capture(rt_ctx* ctx, rt_batch* b, const floa
     if (!ctx) return RT_ERR_INVALID;
     if (!b || !d_tris || !d_hits || !out) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_frame_capture: null argument");
     if (b->width == 0) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_frame_capture: no views set (rt_batch_set_views)");
-    return capture_frame(
+    const rt_status cs = capture_frame(
         ctx, "rt_batch_frame_capture",
         [&]() {
             rt_status s = rt_batch_build(ctx, b, d_tris, flags);
@@ -145,6 +161,8 @@ extern "C" rt_status rt_batch_frame_capture(rt_ctx* ctx, rt_batch* b, const floa
             return s;
         },
         out);
+    if (cs == RT_OK) hold(*out, b);
+    return cs;
 }
 
 extern "C" rt_status rt_frame_launch(rt_ctx* ctx, rt_frame* f) {
@@ -160,6 +178,12 @@ extern "C" rt_status rt_frame_destroy(rt_frame* f) {
     if (!f) return RT_OK;
     if (f->exec) cudaGraphExecDestroy(f->exec);
     if (f->graph) cudaGraphDestroy(f->graph);
+    if (rt_lbvh* l = f->lbvh) {
+        if (--l->graph_refs == 0 && l->destroy_pending) free_lbvh(l);
+    }
+    if (rt_batch* b = f->batch) {
+        if (--b->graph_refs == 0 && b->destroy_pending) free_batch(b);
+    }
     delete f;
     return RT_OK;
 }

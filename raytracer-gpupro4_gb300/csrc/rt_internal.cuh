@@ -150,13 +150,24 @@ struct rt_lbvh {
     // per-pixel state of the colour stage's bounce loop (rt_render_whitted)
     void* w_buf = nullptr;
     size_t w_pixels = 0;
+    // captured frames that point into this structure's buffers: while any
+    // exists the grow-on-demand buffers keep their size, and a destroy
+    // waits for the last one
+    uint32_t graph_refs = 0;
+    bool destroy_pending = false;
 };
+
+// Frees an rt_lbvh / rt_batch and its device buffers.
+void free_lbvh(rt_lbvh* l);
+void free_batch(rt_batch* b);
 
 // Many independent scenes built in one pass of the build kernels and traced
 // by one persistent kernel.  Scene s owns triangles [tri_off[s], tri_off[s+1])
 // of the concatenated soup and heap slots [node_off[s], node_off[s+1]).
 struct rt_batch {
     uint32_t S = 0, depth = 0, total = 0;
+    uint32_t graph_refs = 0;       // captured frames pointing into the batch (see rt_lbvh)
+    bool destroy_pending = false;
     std::vector<uint32_t> h_tri_off;
     uint32_t* tri_off = nullptr;   // S + 1
     uint32_t* node_off = nullptr;  // S + 1

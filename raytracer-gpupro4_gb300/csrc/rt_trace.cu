@@ -436,6 +436,10 @@ rt_status check_trace_args(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, 
 
 rt_status ensure_shade_lists(rt_ctx* ctx, rt_lbvh* l, size_t px) {
     if (px <= l->s_pixels) return RT_OK;
+    if (l->graph_refs > 0)
+        return rt_fail(ctx, RT_ERR_CAPACITY,
+                       "shading lists of %zu pixels cannot grow to %zu while a captured frame uses them",
+                       l->s_pixels, px);
     RT_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (l->s_lists) cudaFree(l->s_lists);
     l->s_lists = nullptr;
@@ -714,6 +718,10 @@ rt_status trace_frame(rt_ctx* ctx, rt_lbvh* l, const rt_camera* cam, const float
 
 rt_status ensure_frame_buffers(rt_ctx* ctx, rt_lbvh* l, size_t px) {
     if (px <= l->f_pixels) return RT_OK;  // frame buffers grow on the first call at a new size
+    if (l->graph_refs > 0)
+        return rt_fail(ctx, RT_ERR_CAPACITY,
+                       "frame buffers of %zu pixels cannot grow to %zu while a captured frame uses them",
+                       l->f_pixels, px);
     RT_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (l->f_primary) cudaFree(l->f_primary);
     if (l->f_mirror) cudaFree(l->f_mirror);

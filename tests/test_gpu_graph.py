@@ -82,3 +82,36 @@ def test_host_frame_graph(gpu_ctx):
     fh.close()
     with pytest.raises(RtError):
         Frame(gpu_ctx, lb_h, soups[0].clone(), cam, light, hp, hv, hm, host=True)  # pageable soup
+
+
+def test_frame_holds_its_structure(gpu_ctx):
+    """A captured frame keeps its LBVH's buffers: a call that would grow them
+    fails while the frame exists, destroying the LBVH first is deferred to
+    the last frame destroy, and the frame still replays in between."""
+    import torch
+    from rtgpu import scenes
+    from rtgpu._lib import RtError
+    from rtgpu.api import LBVH, Frame, RayTracer
+    s = scenes.icosphere(freq=30)
+    tris = torch.from_numpy(s.frame(0)).cuda()
+    cam = scenes.sphere_camera(160, 90)
+    big = scenes.sphere_camera(320, 180)
+    npx = cam.width * cam.height
+    lb = LBVH(gpu_ctx, tris.shape[0], 14)
+    prim = torch.empty((npx, 4), dtype=torch.int32, device="cuda")
+    vis = torch.empty(npx, dtype=torch.uint8, device="cuda")
+    mir = torch.empty((npx, 4), dtype=torch.int32, device="cuda")
+    f = Frame(gpu_ctx, lb, tris, cam, scenes.TORUS_LIGHT, prim, vis, mir)
+    f.launch()
+    gpu_ctx.check()
+    ref = (prim.clone(), vis.clone(), mir.clone())
+    rt = RayTracer(gpu_ctx)
+    hb = rt.primary(lb, big)
+    with pytest.raises(RtError):
+        rt.shadow_mirror(lb, big, scenes.TORUS_LIGHT, hb)  # would grow the shading lists
+    lb.close()  # deferred: the frame still owns the buffers
+    prim.zero_()
+    f.launch()
+    gpu_ctx.check()
+    assert torch.equal(prim, ref[0]) and torch.equal(vis, ref[1]) and torch.equal(mir, ref[2])
+    f.close()  # frees the LBVH
