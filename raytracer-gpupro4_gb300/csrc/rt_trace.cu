@@ -35,13 +35,58 @@ __device__ __forceinline__ void spill_record(uint32_t* list, int slot, uint32_t 
     list[slot] = (kind << 30) | (uint32_t)index;
 }
 
+// Warp-aggregated append of the lanes' pixels to a list (a warp's pixels in
+// lane order, so neighbouring rays stay neighbours).
+__device__ __forceinline__ void append_pixel(bool take, uint32_t p, uint32_t* list, uint32_t cap, uint32_t* count) {
+    const uint32_t m = __ballot_sync(0xffffffffu, take);
+    if (!m) return;
+    uint32_t base = 0;
+    if ((threadIdx.x & 31) == 0) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    const uint32_t k = base + __popc(m & ((1u << (threadIdx.x & 31)) - 1u));
+    if (take && k < cap) list[k] = p;
+}
+
+// The shading-ray lists of a frame (shadow pixels, then mirror pixels) and
+// the results that need no ray.  A frame's primary pass fills them as it
+// goes (lists != nullptr), so no separate pass re-reads the primary hits.
+struct ShadeLists {
+    const float* soup;
+    float lx, ly, lz;
+    uint8_t* vis;
+    rt_hit* mirror;
+    uint32_t* lists;
+    uint32_t cap;
+    uint32_t* counts;  // 2 words
+};
+
+// One pixel's shading-ray setup from its primary hit ph (all lanes call):
+// visibility 0 (no hit) or 1 (light behind the surface) and the mirror
+// miss record are written, the pixels that cast a shadow ray and those that
+// cast a mirror ray are appended to the two lists.
+__device__ __forceinline__ void shade_setup_pixel(const ShadeLists& sl, const rt_camera& cam, int4 ph, bool valid,
+                                                  uint32_t i, uint32_t j, size_t p) {
+    const ShadeRays s = shade_rays(sl.soup, cam, sl.lx, sl.ly, sl.lz, ph, valid, i, j, false);
+    if (valid) {
+        if (sl.vis && !(s.has && s.cast)) sl.vis[p] = vis_code(s.has, s.cast, false);
+        if (sl.mirror && !s.has) {
+            Hit mh;
+            mh.id = -2; mh.u = -1.0f; mh.v = -1.0f; mh.t = 0.0f;
+            store_hit(sl.mirror + p, mh);
+        }
+    }
+    append_pixel(sl.vis && valid && s.has && s.cast, (uint32_t)p, sl.lists, sl.cap, sl.counts);
+    append_pixel(sl.mirror && valid && s.has, (uint32_t)p, sl.lists + sl.cap, sl.cap, sl.counts + 1);
+}
+
 template <bool STATS>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_camera cam,
                                                                  rt_hit* __restrict__ hits,
                                                                  uint32_t* __restrict__ leaves,
                                                                  uint32_t* __restrict__ stats, uint32_t* work,
                                                                  uint32_t num_tiles, Spill spill,
-                                                                 uint32_t* __restrict__ list, TileOrder ord) {
+                                                                 uint32_t* __restrict__ list, TileOrder ord,
+                                                                 ShadeLists sl) {
     const uint32_t wbuf = *ord.parity, rbuf = wbuf ^ 1u, heavy = min(ord.counts[rbuf], ord.cap);
     for (uint32_t tile = next_ordered_tile(work, ord, rbuf, heavy, num_tiles); tile < num_tiles;
          tile = next_ordered_tile(work, ord, rbuf, heavy, num_tiles)) {
@@ -53,8 +98,8 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_
         uint32_t nb = 0, nt = 0, leaf = 1;
         int slot = -1;
         const Hit h = trace_ray<STATS>(r, valid, tr, false, &nb, &nt, &spill, &slot, 1u, &leaf);
+        const size_t p = (size_t)j * cam.width + i;
         if (valid) {
-            const size_t p = (size_t)j * cam.width + i;
             if (slot >= 0) {
                 spill_record(list, slot, kHeavyPrimary, p);
             } else {
@@ -65,6 +110,10 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_
                 stats[2 * p] = nb;
                 stats[2 * p + 1] = nt;
             }
+        }
+        if (sl.lists) {  // uniform; a handed-over pixel is set up by the warp-per-ray pass
+            const int4 ph = make_int4(h.id, __float_as_int(h.u), __float_as_int(h.v), __float_as_int(h.t));
+            shade_setup_pixel(sl, cam, ph, valid && slot < 0, i, j, p);
         }
         record_tile_cost(ord, wbuf, tile, nb + nt);
     }
@@ -155,16 +204,6 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_secondary(
 // 32 rays per warp with every lane busy (the tile pass leaves the lanes of
 // sky pixels and of pixels without a cast ray idle), rebuilding each ray from
 // its pixel exactly as the tile pass does.
-__device__ __forceinline__ void append_pixel(bool take, uint32_t p, uint32_t* list, uint32_t cap, uint32_t* count) {
-    const uint32_t m = __ballot_sync(0xffffffffu, take);
-    if (!m) return;
-    uint32_t base = 0;
-    if ((threadIdx.x & 31) == 0) base = atomicAdd(count, (uint32_t)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    const uint32_t k = base + __popc(m & ((1u << (threadIdx.x & 31)) - 1u));
-    if (take && k < cap) list[k] = p;
-}
-
 __global__ void __launch_bounds__(256) k_shade_setup(const float* __restrict__ soup, rt_camera cam, float lx, float ly,
                                                      float lz, const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis,
                                                      rt_hit* __restrict__ mirror, uint32_t* __restrict__ mirror_leaves,
@@ -179,18 +218,9 @@ __global__ void __launch_bounds__(256) k_shade_setup(const float* __restrict__ s
         const size_t p = (size_t)j * cam.width + i;
         int4 ph = make_int4(-1, 0, 0, 0);
         if (valid) ph = __ldg(reinterpret_cast<const int4*>(prim + p));
-        const ShadeRays s = shade_rays(soup, cam, lx, ly, lz, ph, valid, i, j, false);
-        if (valid) {
-            if (vis && !(s.has && s.cast)) vis[p] = vis_code(s.has, s.cast, false);
-            if (mirror && !s.has) {
-                Hit mh;
-                mh.id = -2; mh.u = -1.0f; mh.v = -1.0f; mh.t = 0.0f;
-                store_hit(mirror + p, mh);
-                if (mirror_leaves) mirror_leaves[p] = 1u;
-            }
-        }
-        append_pixel(vis && valid && s.has && s.cast, (uint32_t)p, lists, cap, counts);
-        append_pixel(mirror && valid && s.has, (uint32_t)p, lists + cap, cap, counts + 1);
+        const ShadeLists sl{soup, lx, ly, lz, vis, mirror, lists, cap, counts};
+        shade_setup_pixel(sl, cam, ph, valid, i, j, p);
+        if (valid && mirror_leaves && ph.x < 0) mirror_leaves[p] = 1u;
     }
 }
 
@@ -373,6 +403,7 @@ struct HeavyArgs {
     uint32_t* leaves;     // primary / generic-ray leaf output (nullable)
     uint32_t* mirror_leaves;
     uint32_t wide_cap;    // frontier-stack entries per warp (wide_stack_entries of the tree depth)
+    ShadeLists sl;        // primary entries: set up their pixel's shading rays too (sl.lists != nullptr)
     const uint32_t* list;
     const uint32_t* count;
     uint32_t cap;
@@ -393,6 +424,10 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_heavy(HeavyArgs a) {
             if (lane == 0) {
                 store_hit(a.hits + idx, h);
                 if (a.leaves) a.leaves[idx] = 1u;  // the root: a valid restart node
+            }
+            if (a.sl.lists) {
+                const int4 ph = make_int4(h.id, __float_as_int(h.u), __float_as_int(h.v), __float_as_int(h.t));
+                shade_setup_pixel(a.sl, a.cam, ph, lane == 0, i, j, idx);
             }
         } else if (kind == kHeavyRay) {
             const RayState r = load_ray(a.rays, idx, true);
@@ -546,8 +581,10 @@ HeavyArgs heavy_args(rt_ctx* ctx, const rt_lbvh* l) {
 
 namespace {
 
+// sl (nullable): a frame's shading lists, filled by this pass as it goes
+// (counts zeroed by the caller); the statistics variant never fills them.
 rt_status trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, rt_hit* d_hits, uint32_t* d_leaves,
-                        uint32_t* d_stats, const char* who) {
+                        uint32_t* d_stats, const char* who, const ShadeLists* sl = nullptr) {
     rt_status s = check_trace_args(ctx, l, cam, who);
     if (s != RT_OK) return s;
     if (!d_hits) return rt_fail(ctx, RT_ERR_INVALID, "%s: null output", who);
@@ -558,27 +595,33 @@ rt_status trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, rt_
     if ((s = order_begin(ctx, 0, ctx->tile_order & 1u, &ord)) != RT_OK) return s;
     const uint32_t tiles = pixel_tiles(cam);
     uint32_t* work = ctx->d_work + kWorkPrimary;
+    ShadeLists none;
+    memset(&none, 0, sizeof(none));
+    const ShadeLists lists = (sl && !d_stats) ? *sl : none;
     if (d_stats) {
         auto k = k_trace_primary<true>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), *cam, d_hits, d_leaves, d_stats, work, tiles, sp, ctx->d_spill, ord);
+            tree_ref(ctx, l), *cam, d_hits, d_leaves, d_stats, work, tiles, sp, ctx->d_spill, ord, none);
     } else {
         auto k = k_trace_primary<false>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), *cam, d_hits, d_leaves, nullptr, work, tiles, sp, ctx->d_spill, ord);
+            tree_ref(ctx, l), *cam, d_hits, d_leaves, nullptr, work, tiles, sp, ctx->d_spill, ord, lists);
     }
     RT_CHECK_LAUNCH(ctx, "k_trace_primary");
     HeavyArgs a = heavy_args(ctx, l);
     a.cam = *cam;
     a.hits = d_hits;
     a.leaves = d_leaves;
+    a.sl = lists;
     return launch_heavy(ctx, sp, a);
 }
 
+// prebuilt: the frame's primary pass has filled the shading lists (and the
+// results that need no ray), so the setup pass is skipped.
 rt_status trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, const float light[3],
                               const rt_hit* d_primary, const uint32_t* d_prim_leaves, uint8_t* d_vis,
                               rt_hit* d_mirror, uint32_t* d_mirror_leaves, uint32_t* d_shadow_stats,
-                              uint32_t* d_mirror_stats, const char* who) {
+                              uint32_t* d_mirror_stats, const char* who, bool prebuilt = false) {
     rt_status s = check_trace_args(ctx, l, cam, who);
     if (s != RT_OK) return s;
     if (!light || !d_primary) return rt_fail(ctx, RT_ERR_INVALID, "%s: null argument", who);
@@ -601,14 +644,16 @@ rt_status trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* ca
         const size_t px = (size_t)cam->width * cam->height;
         if ((s = ensure_shade_lists(ctx, const_cast<rt_lbvh*>(l), px)) != RT_OK) return s;
         uint32_t* counts = ctx->d_work + kShadeCounts;
-        RT_CHECK_CUDA(ctx, cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), ctx->stream));
         if ((s = reset_work(ctx, kWorkShade)) != RT_OK) return s;
         const uint32_t cap = (uint32_t)l->s_pixels;
-        const uint32_t sblocks = std::max(1u, std::min((tiles + 7) / 8, (uint32_t)ctx->num_sms * 8));
-        k_shade_setup<<<sblocks, 256, 0, ctx->stream>>>(l->src_tris, *cam, light[0], light[1], light[2], d_primary,
-                                                         d_vis, d_mirror, d_mirror_leaves, l->s_lists, cap, counts,
-                                                         tiles);
-        RT_CHECK_LAUNCH(ctx, "k_shade_setup");
+        if (!prebuilt) {
+            RT_CHECK_CUDA(ctx, cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), ctx->stream));
+            const uint32_t sblocks = std::max(1u, std::min((tiles + 7) / 8, (uint32_t)ctx->num_sms * 8));
+            k_shade_setup<<<sblocks, 256, 0, ctx->stream>>>(l->src_tris, *cam, light[0], light[1], light[2], d_primary,
+                                                             d_vis, d_mirror, d_mirror_leaves, l->s_lists, cap, counts,
+                                                             tiles);
+            RT_CHECK_LAUNCH(ctx, "k_shade_setup");
+        }
         int per_sm = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_shade, kTraceThreads, 0) != cudaSuccess ||
             per_sm < 1)
@@ -710,9 +755,16 @@ rt_status trace_frame(rt_ctx* ctx, rt_lbvh* l, const rt_camera* cam, const float
                       uint8_t* d_vis, rt_hit* d_mirror, const char* who) {
     const size_t px = (size_t)cam->width * cam->height;
     uint32_t* leaves = (d_vis || d_mirror) && l->s_pixels >= px ? l->s_lists + 2 * l->s_pixels : nullptr;
-    rt_status s = trace_primary(ctx, l, cam, d_primary, leaves, nullptr, who);
-    if (s == RT_OK && (d_vis || d_mirror))
-        s = trace_shadow_mirror(ctx, l, cam, light, d_primary, leaves, d_vis, d_mirror, nullptr, nullptr, nullptr, who);
+    if (!leaves) return trace_primary(ctx, l, cam, d_primary, nullptr, nullptr, who);
+    if (!l->src_tris) return rt_fail(ctx, RT_ERR_INVALID, "%s: no triangle soup bound", who);
+    // the primary pass (and its warp-per-ray pass) fills the shading lists
+    ShadeLists sl{l->src_tris, light[0], light[1], light[2], d_vis, d_mirror, l->s_lists, (uint32_t)l->s_pixels,
+                  ctx->d_work + kShadeCounts};
+    RT_CHECK_CUDA(ctx, cudaMemsetAsync(sl.counts, 0, 2 * sizeof(uint32_t), ctx->stream));
+    rt_status s = trace_primary(ctx, l, cam, d_primary, leaves, nullptr, who, &sl);
+    if (s == RT_OK)
+        s = trace_shadow_mirror(ctx, l, cam, light, d_primary, leaves, d_vis, d_mirror, nullptr, nullptr, nullptr, who,
+                                true);
     return s;
 }
 
