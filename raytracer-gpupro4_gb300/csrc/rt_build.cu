@@ -99,6 +99,7 @@ __global__ void __launch_bounds__(256) k_bounds(const float* __restrict__ tris, 
                                                 float* partials, uint32_t* counters, uint32_t* hist,
                                                 uint32_t* lookback, uint32_t lookback_words, rt_node* nodes,
                                                 uint32_t num_nodes, int clear_nodes) {
+    grid_dep_wait();
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t gstride = gridDim.x * blockDim.x;
 
@@ -235,6 +236,7 @@ __global__ void __launch_bounds__(kMortonThreads) k_morton_hist(const float* __r
                                                                 uint32_t* __restrict__ keys,
                                                                 uint32_t* __restrict__ ids, uint32_t* hist,
                                                                 uint32_t* err) {
+    grid_dep_wait();
     __shared__ float s_tri[kMortonThreads * 9];
     __shared__ uint32_t s_hist[4][256];
     for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0u;
@@ -336,6 +338,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
                                                            uint32_t* tile_counter, uint32_t* err,
                                                            const uint32_t* __restrict__ scene_off = nullptr,
                                                            uint32_t S = 0) {
+    grid_dep_wait();
     __shared__ uint32_t s_keys[kSortTile];
     __shared__ uint32_t s_ids[kSortTile];
     __shared__ uint32_t s_warp[kSortThreads / 32][256];
@@ -537,6 +540,7 @@ __device__ __forceinline__ void load_chunk(const uint32_t* __restrict__ keys, ui
 __global__ void __launch_bounds__(kEmitThreads) k_emit_tiles(const uint32_t* __restrict__ keys, uint32_t n,
                                                              uint32_t* scan, uint32_t* arrive, uint32_t arrive_words,
                                                              const uint32_t* epoch_word) {
+    grid_dep_wait();
     // epoch 1 means the first build or a wrapped epoch counter: the refit's
     // arrival words may hold any old epoch and are cleared before k_emit_refit
     if (*epoch_word == 1u)
@@ -570,6 +574,7 @@ __global__ void __launch_bounds__(kEmitThreads) k_emit_tiles(const uint32_t* __r
 constexpr int kPrefixThreads = 1024;
 
 __global__ void __launch_bounds__(kPrefixThreads) k_emit_prefix(uint32_t* scan, uint32_t tiles) {
+    grid_dep_wait();
     __shared__ uint32_t s_f[kPrefixThreads / 32], s_b[kPrefixThreads / 32];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     const uint32_t per = (tiles + kPrefixThreads - 1) / kPrefixThreads;
@@ -619,6 +624,7 @@ __global__ void __launch_bounds__(kEmitThreads) k_emit_leaves(const uint32_t* __
                                                               rt_node* nodes, float4* __restrict__ sorted_tris,
                                                               uint32_t* leaf_list, uint32_t* leaf_count,
                                                               uint32_t* err) {
+    grid_dep_wait();
     __shared__ uint32_t s_f[8], s_b[8];
     const uint32_t s = blockIdx.x * kEmitTile + threadIdx.x * kEmitItems;
     EmitChunk e;
@@ -874,6 +880,7 @@ __global__ void __launch_bounds__(256) k_emit_refit(const uint32_t* __restrict__
                                                     const uint32_t* leaf_count, uint32_t* arrive,
                                                     const uint32_t* epoch_word, uint32_t* err,
                                                     uint32_t* inner = nullptr) {
+    grid_dep_wait();
     const uint32_t nleaves = min(*leaf_count, n);
     const uint32_t epoch = *epoch_word;
     const uint32_t lane = threadIdx.x & 31;
@@ -1056,35 +1063,35 @@ static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint
     const uint32_t emit_tiles = ceil_div(n, kEmitTile);
     const uint32_t lb_words = kSortPasses * 256 * sort_tiles;
     const uint32_t bblocks = std::max(1u, std::min(ceil_div(3ull * n, 256), l->bounds_blocks));
-    k_bounds<<<bblocks, 256, 0, st>>>(d_tris, n, l->scene, l->partials, l->counters, l->hist, l->lookback,
+    launch_pdl(k_bounds, bblocks, 256, 0, st, d_tris, n, l->scene, l->partials, l->counters, l->hist, l->lookback,
                                       lb_words, l->nodes, l->num_nodes, (flags & RT_BUILD_CLEAR_UNREACHED) ? 1 : 0);
     RT_CHECK_LAUNCH(ctx, "k_bounds");
     const uint32_t mblocks = std::max(1u, std::min(ceil_div(n, kMortonThreads), (uint32_t)ctx->num_sms * 4));
-    k_morton_hist<<<mblocks, kMortonThreads, 0, st>>>(d_tris, n, l->scene, l->keys, l->ids, l->hist, ctx->d_err);
+    launch_pdl(k_morton_hist, mblocks, kMortonThreads, 0, st, d_tris, n, l->scene, l->keys, l->ids, l->hist, ctx->d_err);
     RT_CHECK_LAUNCH(ctx, "k_morton_hist");
     uint32_t *kin = l->keys, *iin = l->ids, *kout = l->keys_alt, *iout = l->ids_alt;
     for (int p = 0; p < kSortPasses; ++p) {
-        k_onesweep<false><<<sort_tiles, kSortThreads, 0, st>>>(kin, iin, kout, iout, n, p, l->hist,
-                                                        l->lookback + (size_t)p * 256 * sort_tiles,
-                                                        l->counters + 1 + p, ctx->d_err);
+        launch_pdl(k_onesweep<false>, sort_tiles, kSortThreads, 0, st, (const uint32_t*)kin, (const uint32_t*)iin,
+                   kout, iout, n, p, (const uint32_t*)l->hist, l->lookback + (size_t)p * 256 * sort_tiles,
+                   l->counters + 1 + p, ctx->d_err, (const uint32_t*)nullptr, 0u);
         RT_CHECK_LAUNCH(ctx, "k_onesweep");
         std::swap(kin, kout);
         std::swap(iin, iout);
     }
     // four passes: sorted pairs are back in keys / ids
-    k_emit_tiles<<<emit_tiles, kEmitThreads, 0, st>>>(l->keys, n, l->scan, l->arrive, std::max(1u, l->num_nodes >> 1),
+    launch_pdl(k_emit_tiles, emit_tiles, kEmitThreads, 0, st, l->keys, n, l->scan, l->arrive, std::max(1u, l->num_nodes >> 1),
                                                       l->counters + 6);
     RT_CHECK_LAUNCH(ctx, "k_emit_tiles");
-    k_emit_prefix<<<1, kPrefixThreads, 0, st>>>(l->scan, emit_tiles);
+    launch_pdl(k_emit_prefix, 1, kPrefixThreads, 0, st, l->scan, emit_tiles);
     RT_CHECK_LAUNCH(ctx, "k_emit_prefix");
-    k_emit_leaves<<<emit_tiles, kEmitThreads, 0, st>>>(l->keys, l->ids, d_tris, n, l->depth, l->scan, l->nodes,
+    launch_pdl(k_emit_leaves, emit_tiles, kEmitThreads, 0, st, l->keys, l->ids, d_tris, n, l->depth, l->scan, l->nodes,
                                                        l->sorted_tris, l->leaf_list, l->counters + 5, ctx->d_err);
     RT_CHECK_LAUNCH(ctx, "k_emit_leaves");
     const uint32_t rblocks = std::max(1u, std::min(ceil_div(n, 256), (uint32_t)ctx->num_sms * 8));
     const bool compact = (flags & RT_BUILD_COMPACT) != 0;
     const uint32_t words = std::max(1u, l->num_nodes / 32);
     if (compact) RT_CHECK_CUDA(ctx, cudaMemsetAsync(l->inner, 0, sizeof(uint32_t) * words, st));
-    k_emit_refit<<<rblocks, 256, 0, st>>>(l->keys, l->sorted_tris, n, l->depth, l->nodes, l->leaf_list,
+    launch_pdl(k_emit_refit, rblocks, 256, 0, st, l->keys, l->sorted_tris, n, l->depth, l->nodes, l->leaf_list,
                                           l->counters + 5, l->arrive, l->counters + 6, ctx->d_err,
                                           compact ? l->inner : nullptr);
     RT_CHECK_LAUNCH(ctx, "k_emit_refit");

@@ -198,6 +198,30 @@ struct rt_batch {
 // error plumbing (host)
 rt_status rt_fail(rt_ctx* ctx, rt_status s, const char* fmt, ...);
 
+// Programmatic dependent launch.  A kernel launched with launch_pdl may be
+// scheduled while the kernel before it on the stream drains (in a captured
+// graph the edge between the two becomes a programmatic one), which hides
+// the launch and block-scheduling gap between dependent kernels.  Every
+// kernel launched this way begins with grid_dep_wait(): it returns once the
+// previous kernel has completed and its writes are visible (at once for an
+// ordinary launch), so the stream order of memory effects is unchanged.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... P, typename... A>
+inline void launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);  // an error is left for RT_CHECK_LAUNCH
+}
+
 #define RT_CHECK_CUDA(ctx, call)                                                               \
     do {                                                                                       \
         cudaError_t e_ = (call);                                                               \

@@ -87,6 +87,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_
                                                                  uint32_t num_tiles, Spill spill,
                                                                  uint32_t* __restrict__ list, TileOrder ord,
                                                                  ShadeLists sl) {
+    grid_dep_wait();
     const uint32_t wbuf = *ord.parity, rbuf = wbuf ^ 1u, heavy = min(ord.counts[rbuf], ord.cap);
     for (uint32_t tile = next_ordered_tile(work, ord, rbuf, heavy, num_tiles); tile < num_tiles;
          tile = next_ordered_tile(work, ord, rbuf, heavy, num_tiles)) {
@@ -240,6 +241,7 @@ __global__ void __launch_bounds__(kTraceThreads, 7) k_trace_shade(
     const rt_hit* __restrict__ prim, const uint32_t* __restrict__ prim_leaves, uint8_t* __restrict__ vis,
     rt_hit* __restrict__ mirror, uint32_t* __restrict__ mirror_leaves, const uint32_t* __restrict__ lists,
     uint32_t cap, const uint32_t* counts, uint32_t* work, Spill spill, uint32_t* __restrict__ list) {
+    grid_dep_wait();
     constexpr uint32_t kFull = 0xffffffffu;
     const uint32_t ns = min(counts[0], cap), nm = min(counts[1], cap), total = ns + nm;
     const int lane = threadIdx.x & 31;
@@ -411,6 +413,7 @@ struct HeavyArgs {
 };
 
 __global__ void __launch_bounds__(kTraceThreads) k_trace_heavy(HeavyArgs a) {
+    grid_dep_wait();
     const uint32_t n = min(*a.count, a.cap);
     const int lane = threadIdx.x & 31;
     for (uint32_t e = next_tile(a.work); e < n; e = next_tile(a.work)) {
@@ -509,10 +512,31 @@ Spill spill_of(rt_ctx* ctx, bool enabled, int kind) {
     return sp;
 }
 
-rt_status reset_spill(rt_ctx* ctx, const Spill& sp) {
-    if (!sp.count) return RT_OK;
-    RT_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_spill_count, 0, sizeof(uint32_t), ctx->stream));
-    return reset_work(ctx, kWorkHeavy);
+// A trace call zeroes its counters (words of ctx->d_words) in one small
+// kernel launched before its first pass, k_order_begin where the call has a
+// tile order to advance, k_reset_words otherwise: one graph node instead of a
+// memset per counter, and a programmatic edge to the pass.
+uint64_t word_bit(const rt_ctx* ctx, const uint32_t* p) { return 1ull << (uint32_t)(p - ctx->d_words); }
+
+// The list length and the warp-per-ray pass's claim counter.
+uint64_t spill_reset_bits(const rt_ctx* ctx, const Spill& sp) {
+    return sp.count ? word_bit(ctx, ctx->d_spill_count) | word_bit(ctx, ctx->d_work + kWorkHeavy) : 0ull;
+}
+
+__device__ __forceinline__ void zero_words(uint32_t* words, unsigned long long mask) {
+    if (threadIdx.x < 64 && ((mask >> threadIdx.x) & 1ull)) words[threadIdx.x] = 0u;
+}
+
+__global__ void k_reset_words(uint32_t* words, unsigned long long mask) {
+    grid_dep_wait();
+    zero_words(words, mask);
+}
+
+rt_status reset_words(rt_ctx* ctx, uint64_t mask) {
+    if (!mask) return RT_OK;
+    launch_pdl(k_reset_words, 1, 64, 0, ctx->stream, ctx->d_words, (unsigned long long)mask);
+    RT_CHECK_LAUNCH(ctx, "k_reset_words");
+    return RT_OK;
 }
 
 rt_status launch_heavy(rt_ctx* ctx, const Spill& sp, HeavyArgs a) {
@@ -526,12 +550,14 @@ rt_status launch_heavy(rt_ctx* ctx, const Spill& sp, HeavyArgs a) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_heavy, kTraceThreads, smem) != cudaSuccess ||
         per_sm < 1)
         per_sm = 1;
-    k_trace_heavy<<<(uint32_t)per_sm * ctx->num_sms, kTraceThreads, smem, ctx->stream>>>(a);
+    launch_pdl(k_trace_heavy, (uint32_t)per_sm * ctx->num_sms, kTraceThreads, smem, ctx->stream, a);
     RT_CHECK_LAUNCH(ctx, "k_trace_heavy");
     return RT_OK;
 }
 
-__global__ void k_order_begin(TileOrder o) {
+__global__ void k_order_begin(TileOrder o, uint32_t* words, unsigned long long reset) {
+    grid_dep_wait();
+    zero_words(words, reset);
     __shared__ uint32_t s_w;
     if (threadIdx.x == 0) {
         const uint32_t w = *o.parity ^ 1u;
@@ -553,8 +579,8 @@ __global__ void k_order_begin(TileOrder o) {
 
 // Tile order of one trace kind (0 primary, 1 shading, 2 generic rays),
 // advanced to this call; enabled == false gives image order (cap 0: no list
-// is read or written).
-rt_status order_begin(rt_ctx* ctx, int kind, bool enabled, TileOrder* out) {
+// is read or written).  reset: the call's counters to zero (word_bit mask).
+rt_status order_begin(rt_ctx* ctx, int kind, bool enabled, TileOrder* out, uint64_t reset = 0) {
     TileOrder o;
     o.cap = enabled ? kOrderCap : 0u;
     o.parity = ctx->d_words + 40 + 4 * kind;
@@ -562,8 +588,11 @@ rt_status order_begin(rt_ctx* ctx, int kind, bool enabled, TileOrder* out) {
     o.lists = ctx->d_order + (size_t)kind * kOrderWords;
     o.bits = o.lists + 2 * (size_t)kOrderCap;
     if (enabled) {
-        k_order_begin<<<1, 256, 0, ctx->stream>>>(o);
+        launch_pdl(k_order_begin, 1, 256, 0, ctx->stream, o, ctx->d_words, (unsigned long long)reset);
         RT_CHECK_LAUNCH(ctx, "k_order_begin");
+    } else {
+        rt_status s = reset_words(ctx, reset);
+        if (s != RT_OK) return s;
     }
     *out = o;
     return RT_OK;
@@ -582,17 +611,18 @@ HeavyArgs heavy_args(rt_ctx* ctx, const rt_lbvh* l) {
 namespace {
 
 // sl (nullable): a frame's shading lists, filled by this pass as it goes
-// (counts zeroed by the caller); the statistics variant never fills them.
+// (their counts are zeroed with this call's counters); the statistics
+// variant never fills them.
 rt_status trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, rt_hit* d_hits, uint32_t* d_leaves,
                         uint32_t* d_stats, const char* who, const ShadeLists* sl = nullptr) {
     rt_status s = check_trace_args(ctx, l, cam, who);
     if (s != RT_OK) return s;
     if (!d_hits) return rt_fail(ctx, RT_ERR_INVALID, "%s: null output", who);
-    if ((s = reset_work(ctx, kWorkPrimary)) != RT_OK) return s;
     const Spill sp = spill_of(ctx, !d_stats && (uint64_t)cam->width * cam->height <= kHeavyIndexMask, 0);
-    if ((s = reset_spill(ctx, sp)) != RT_OK) return s;
+    uint64_t reset = word_bit(ctx, ctx->d_work + kWorkPrimary) | spill_reset_bits(ctx, sp);
+    if (sl && !d_stats) reset |= word_bit(ctx, sl->counts) | word_bit(ctx, sl->counts + 1);
     TileOrder ord;
-    if ((s = order_begin(ctx, 0, ctx->tile_order & 1u, &ord)) != RT_OK) return s;
+    if ((s = order_begin(ctx, 0, ctx->tile_order & 1u, &ord, reset)) != RT_OK) return s;
     const uint32_t tiles = pixel_tiles(cam);
     uint32_t* work = ctx->d_work + kWorkPrimary;
     ShadeLists none;
@@ -604,8 +634,9 @@ rt_status trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, rt_
             tree_ref(ctx, l), *cam, d_hits, d_leaves, d_stats, work, tiles, sp, ctx->d_spill, ord, none);
     } else {
         auto k = k_trace_primary<false>;
-        k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), *cam, d_hits, d_leaves, nullptr, work, tiles, sp, ctx->d_spill, ord, lists);
+        launch_pdl(k, persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream,
+                   tree_ref(ctx, l), *cam, d_hits, d_leaves, (uint32_t*)nullptr, work, tiles, sp, ctx->d_spill, ord,
+                   lists);
     }
     RT_CHECK_LAUNCH(ctx, "k_trace_primary");
     HeavyArgs a = heavy_args(ctx, l);
@@ -626,14 +657,13 @@ rt_status trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* ca
     if (s != RT_OK) return s;
     if (!light || !d_primary) return rt_fail(ctx, RT_ERR_INVALID, "%s: null argument", who);
     if (!l->src_tris) return rt_fail(ctx, RT_ERR_INVALID, "%s: no triangle soup bound", who);
-    if ((s = reset_work(ctx, kWorkSecondary)) != RT_OK) return s;
     const bool stats = d_shadow_stats || d_mirror_stats;
     const Spill sp = spill_of(ctx, !stats && (uint64_t)cam->width * cam->height <= kHeavyIndexMask, 1);
-    if ((s = reset_spill(ctx, sp)) != RT_OK) return s;
+    uint64_t reset = word_bit(ctx, ctx->d_work + kWorkSecondary) | spill_reset_bits(ctx, sp);
     const uint32_t tiles = pixel_tiles(cam);
     if (stats) {  // per-pixel counts in the oracle's order: the tile pass
         TileOrder ord;
-        if ((s = order_begin(ctx, 1, ctx->tile_order & 2u, &ord)) != RT_OK) return s;
+        if ((s = order_begin(ctx, 1, ctx->tile_order & 2u, &ord, reset)) != RT_OK) return s;
         uint32_t* work = ctx->d_work + kWorkSecondary;
         auto k = k_trace_secondary<true>;
         k<<<persistent_blocks(ctx, k, kTraceThreads, tiles), kTraceThreads, 0, ctx->stream>>>(
@@ -644,10 +674,11 @@ rt_status trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* ca
         const size_t px = (size_t)cam->width * cam->height;
         if ((s = ensure_shade_lists(ctx, const_cast<rt_lbvh*>(l), px)) != RT_OK) return s;
         uint32_t* counts = ctx->d_work + kShadeCounts;
-        if ((s = reset_work(ctx, kWorkShade)) != RT_OK) return s;
+        reset |= word_bit(ctx, ctx->d_work + kWorkShade);
+        if (!prebuilt) reset |= word_bit(ctx, counts) | word_bit(ctx, counts + 1);
+        if ((s = reset_words(ctx, reset)) != RT_OK) return s;
         const uint32_t cap = (uint32_t)l->s_pixels;
         if (!prebuilt) {
-            RT_CHECK_CUDA(ctx, cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), ctx->stream));
             const uint32_t sblocks = std::max(1u, std::min((tiles + 7) / 8, (uint32_t)ctx->num_sms * 8));
             k_shade_setup<<<sblocks, 256, 0, ctx->stream>>>(l->src_tris, *cam, light[0], light[1], light[2], d_primary,
                                                              d_vis, d_mirror, d_mirror_leaves, l->s_lists, cap, counts,
@@ -658,9 +689,10 @@ rt_status trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* ca
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_shade, kTraceThreads, 0) != cudaSuccess ||
             per_sm < 1)
             per_sm = 1;
-        k_trace_shade<<<(uint32_t)per_sm * ctx->num_sms, kTraceThreads, 0, ctx->stream>>>(
-            tree_ref(ctx, l), l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_prim_leaves, d_vis,
-            d_mirror, d_mirror_leaves, l->s_lists, cap, counts, ctx->d_work + kWorkShade, sp, ctx->d_spill);
+        launch_pdl(k_trace_shade, (uint32_t)per_sm * ctx->num_sms, kTraceThreads, 0, ctx->stream, tree_ref(ctx, l),
+                   l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_prim_leaves, d_vis, d_mirror,
+                   d_mirror_leaves, (const uint32_t*)l->s_lists, cap, (const uint32_t*)counts,
+                   ctx->d_work + kWorkShade, sp, ctx->d_spill);
         RT_CHECK_LAUNCH(ctx, "k_trace_shade");
     }
     HeavyArgs a = heavy_args(ctx, l);
@@ -683,12 +715,11 @@ rt_status trace_rays(rt_ctx* ctx, const rt_lbvh* l, const rt_ray* d_rays, uint32
     if (!l || !d_rays || !d_hits) return rt_fail(ctx, RT_ERR_INVALID, "%s: null argument", who);
     if (l->n == 0) return rt_fail(ctx, RT_ERR_INVALID, "%s: the LBVH has not been built", who);
     if (n == 0) return RT_OK;
-    rt_status s = reset_work(ctx, kWorkRays);
-    if (s != RT_OK) return s;
     const Spill sp = spill_of(ctx, !d_stats && n <= kHeavyIndexMask, 2);
-    if ((s = reset_spill(ctx, sp)) != RT_OK) return s;
+    const uint64_t reset = word_bit(ctx, ctx->d_work + kWorkRays) | spill_reset_bits(ctx, sp);
     TileOrder ord;
-    if ((s = order_begin(ctx, 2, ctx->tile_order & 4u, &ord)) != RT_OK) return s;
+    rt_status s = order_begin(ctx, 2, ctx->tile_order & 4u, &ord, reset);
+    if (s != RT_OK) return s;
     const uint32_t tiles = (n + 31) / 32;
     uint32_t* work = ctx->d_work + kWorkRays;
     if (d_stats) {
@@ -760,7 +791,6 @@ rt_status trace_frame(rt_ctx* ctx, rt_lbvh* l, const rt_camera* cam, const float
     // the primary pass (and its warp-per-ray pass) fills the shading lists
     ShadeLists sl{l->src_tris, light[0], light[1], light[2], d_vis, d_mirror, l->s_lists, (uint32_t)l->s_pixels,
                   ctx->d_work + kShadeCounts};
-    RT_CHECK_CUDA(ctx, cudaMemsetAsync(sl.counts, 0, 2 * sizeof(uint32_t), ctx->stream));
     rt_status s = trace_primary(ctx, l, cam, d_primary, leaves, nullptr, who, &sl);
     if (s == RT_OK)
         s = trace_shadow_mirror(ctx, l, cam, light, d_primary, leaves, d_vis, d_mirror, nullptr, nullptr, nullptr, who,
