@@ -100,7 +100,7 @@ struct rt_ctx {
     std::string last_error;
     uint32_t* d_err = nullptr;   // device error word (d_words[0])
     uint32_t* d_work = nullptr;  // work counters of the persistent kernels (d_words[16..])
-    uint32_t* d_spill_count = nullptr;  // heavy-ray list length (d_words[32])
+    uint32_t* d_spill_count = nullptr;  // heavy-ray list length (d_words[32]; shading rays: [33], claims [34])
     uint32_t* d_words = nullptr; // 64 device words
     uint32_t* d_spill = nullptr; // heavy-ray list, kSpillCap entries
     uint32_t* d_order = nullptr; // heavy-first tile order, kOrderKinds x kOrderWords (parity / counts: d_words[40..])

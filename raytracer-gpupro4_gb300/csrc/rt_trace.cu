@@ -504,10 +504,14 @@ namespace {
 // Heavy-ray hand-over of one trace call: the list is emptied before the
 // first pass (budget 0 or a counting pass: no hand-over), and the second pass
 // drains it.
+// The shading rays keep their own list length and claim counter, so a frame
+// zeroes both passes' counters in one launch before its primary pass.
 Spill spill_of(rt_ctx* ctx, bool enabled, int kind) {
     Spill sp;
     sp.budget = ctx->trace_budget[kind];
-    sp.count = (enabled && sp.budget) ? ctx->d_spill_count : nullptr;
+    const bool shade = kind == 1;
+    sp.count = (enabled && sp.budget) ? ctx->d_spill_count + (shade ? 1 : 0) : nullptr;
+    sp.work = shade ? ctx->d_spill_count + 2 : ctx->d_work + kWorkHeavy;
     sp.cap = kSpillCap;
     return sp;
 }
@@ -520,7 +524,13 @@ uint64_t word_bit(const rt_ctx* ctx, const uint32_t* p) { return 1ull << (uint32
 
 // The list length and the warp-per-ray pass's claim counter.
 uint64_t spill_reset_bits(const rt_ctx* ctx, const Spill& sp) {
-    return sp.count ? word_bit(ctx, ctx->d_spill_count) | word_bit(ctx, ctx->d_work + kWorkHeavy) : 0ull;
+    return sp.count ? word_bit(ctx, sp.count) | word_bit(ctx, sp.work) : 0ull;
+}
+
+// The counters of the compacted shading-ray pass.
+uint64_t shade_reset_bits(const rt_ctx* ctx, const Spill& sp) {
+    return word_bit(ctx, ctx->d_work + kWorkSecondary) | word_bit(ctx, ctx->d_work + kWorkShade) |
+           spill_reset_bits(ctx, sp);
 }
 
 __device__ __forceinline__ void zero_words(uint32_t* words, unsigned long long mask) {
@@ -542,9 +552,9 @@ rt_status reset_words(rt_ctx* ctx, uint64_t mask) {
 rt_status launch_heavy(rt_ctx* ctx, const Spill& sp, HeavyArgs a) {
     if (!sp.count) return RT_OK;
     a.list = ctx->d_spill;
-    a.count = ctx->d_spill_count;
+    a.count = sp.count;
     a.cap = kSpillCap;
-    a.work = ctx->d_work + kWorkHeavy;
+    a.work = sp.work;
     const size_t smem = wide_smem_bytes(a.wide_cap);
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_heavy, kTraceThreads, smem) != cudaSuccess ||
@@ -614,12 +624,13 @@ namespace {
 // (their counts are zeroed with this call's counters); the statistics
 // variant never fills them.
 rt_status trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, rt_hit* d_hits, uint32_t* d_leaves,
-                        uint32_t* d_stats, const char* who, const ShadeLists* sl = nullptr) {
+                        uint32_t* d_stats, const char* who, const ShadeLists* sl = nullptr,
+                        uint64_t extra_reset = 0) {
     rt_status s = check_trace_args(ctx, l, cam, who);
     if (s != RT_OK) return s;
     if (!d_hits) return rt_fail(ctx, RT_ERR_INVALID, "%s: null output", who);
     const Spill sp = spill_of(ctx, !d_stats && (uint64_t)cam->width * cam->height <= kHeavyIndexMask, 0);
-    uint64_t reset = word_bit(ctx, ctx->d_work + kWorkPrimary) | spill_reset_bits(ctx, sp);
+    uint64_t reset = word_bit(ctx, ctx->d_work + kWorkPrimary) | spill_reset_bits(ctx, sp) | extra_reset;
     if (sl && !d_stats) reset |= word_bit(ctx, sl->counts) | word_bit(ctx, sl->counts + 1);
     TileOrder ord;
     if ((s = order_begin(ctx, 0, ctx->tile_order & 1u, &ord, reset)) != RT_OK) return s;
@@ -648,7 +659,8 @@ rt_status trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, rt_
 }
 
 // prebuilt: the frame's primary pass has filled the shading lists (and the
-// results that need no ray), so the setup pass is skipped.
+// results that need no ray), so the setup pass is skipped, and the counters
+// of this pass were zeroed with the primary pass's (shade_reset_bits).
 rt_status trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, const float light[3],
                               const rt_hit* d_primary, const uint32_t* d_prim_leaves, uint8_t* d_vis,
                               rt_hit* d_mirror, uint32_t* d_mirror_leaves, uint32_t* d_shadow_stats,
@@ -674,9 +686,10 @@ rt_status trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* ca
         const size_t px = (size_t)cam->width * cam->height;
         if ((s = ensure_shade_lists(ctx, const_cast<rt_lbvh*>(l), px)) != RT_OK) return s;
         uint32_t* counts = ctx->d_work + kShadeCounts;
-        reset |= word_bit(ctx, ctx->d_work + kWorkShade);
-        if (!prebuilt) reset |= word_bit(ctx, counts) | word_bit(ctx, counts + 1);
-        if ((s = reset_words(ctx, reset)) != RT_OK) return s;
+        if (!prebuilt) {
+            reset = shade_reset_bits(ctx, sp) | word_bit(ctx, counts) | word_bit(ctx, counts + 1);
+            if ((s = reset_words(ctx, reset)) != RT_OK) return s;
+        }
         const uint32_t cap = (uint32_t)l->s_pixels;
         if (!prebuilt) {
             const uint32_t sblocks = std::max(1u, std::min((tiles + 7) / 8, (uint32_t)ctx->num_sms * 8));
@@ -791,7 +804,9 @@ rt_status trace_frame(rt_ctx* ctx, rt_lbvh* l, const rt_camera* cam, const float
     // the primary pass (and its warp-per-ray pass) fills the shading lists
     ShadeLists sl{l->src_tris, light[0], light[1], light[2], d_vis, d_mirror, l->s_lists, (uint32_t)l->s_pixels,
                   ctx->d_work + kShadeCounts};
-    rt_status s = trace_primary(ctx, l, cam, d_primary, leaves, nullptr, who, &sl);
+    // the shading pass's counters are zeroed with the primary pass's
+    const Spill ssp = spill_of(ctx, px <= kHeavyIndexMask, 1);
+    rt_status s = trace_primary(ctx, l, cam, d_primary, leaves, nullptr, who, &sl, shade_reset_bits(ctx, ssp));
     if (s == RT_OK)
         s = trace_shadow_mirror(ctx, l, cam, light, d_primary, leaves, d_vis, d_mirror, nullptr, nullptr, nullptr, who,
                                 true);

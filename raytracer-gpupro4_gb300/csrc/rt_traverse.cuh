@@ -444,6 +444,7 @@ struct Spill {
     uint32_t* count;
     uint32_t cap;
     uint32_t budget;
+    uint32_t* work;  // claim counter of the warp-per-ray pass (host side)
 };
 
 // Warp-cooperative traversal.  All 32 lanes of the warp call it together;
