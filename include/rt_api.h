@@ -98,6 +98,13 @@ rt_status rt_ctx_set_stream(rt_ctx* ctx, void* stream);
  * frame).  Path tracing never hands over. */
 rt_status rt_ctx_set_trace_budget(rt_ctx* ctx, uint32_t budget);
 rt_status rt_ctx_set_trace_budget_kind(rt_ctx* ctx, uint32_t kind, uint32_t budget);
+/* How the handed-over rays are traced, per trace kind in `kinds` (bit 0
+ * primary rays, bit 1 shadow / mirror rays, bit 2 rt_trace_rays): a set bit
+ * traces each with a whole block of 128 threads (suits a few hundred very
+ * long rays), a clear bit with a warp (suits thousands).  Same hits either
+ * way.  Default 2 (the shading rays a block per ray: the fastest on a
+ * 2.1 M-triangle frame). */
+rt_status rt_ctx_set_heavy_block(rt_ctx* ctx, uint32_t kinds);
 /* Heavy-first tile order: for each trace kind in `kinds` (bit 0 primary
  * rays, bit 1 shadow / mirror rays, bit 2 rt_trace_rays) a call first
  * traces the tiles that were the most expensive in the previous call of the

@@ -90,6 +90,13 @@ extern "C" rt_status rt_ctx_set_trace_budget_kind(rt_ctx* ctx, uint32_t kind, ui
     return RT_OK;
 }
 
+extern "C" rt_status rt_ctx_set_heavy_block(rt_ctx* ctx, uint32_t kinds) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (kinds > 7u) return rt_fail(ctx, RT_ERR_INVALID, "rt_ctx_set_heavy_block: kinds is a 3-bit mask");
+    ctx->heavy_team = kinds;
+    return RT_OK;
+}
+
 extern "C" rt_status rt_ctx_set_tile_order(rt_ctx* ctx, uint32_t kinds) {
     if (!ctx) return RT_ERR_INVALID;
     if (kinds > 7u) return rt_fail(ctx, RT_ERR_INVALID, "rt_ctx_set_tile_order: kinds is a 3-bit mask");

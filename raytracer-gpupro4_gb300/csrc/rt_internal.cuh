@@ -86,6 +86,7 @@ constexpr uint32_t kMaxTris = (1u << 29);
 // default budget of box + triangle tests a lane spends on one ray before it
 // hands the ray to the warp-per-ray kernel.
 constexpr uint32_t kSpillCap = 1u << 20;
+constexpr uint32_t kDefaultHeavyTeam = 2u;
 constexpr uint32_t kDefaultTraceBudget = 384;
 constexpr uint32_t kDefaultShadeBudget = 768;
 // Heavy-first tile order (TileOrder in rt_traverse.cuh): per trace kind two
@@ -106,6 +107,9 @@ struct rt_ctx {
     uint32_t* d_order = nullptr; // heavy-first tile order, kOrderKinds x kOrderWords (parity / counts: d_words[40..])
     // hand-over budget per trace kind (0 primary, 1 shading, 2 generic rays); 0: no hand-over
     uint32_t trace_budget[3] = {kDefaultTraceBudget, kDefaultShadeBudget, kDefaultTraceBudget};
+    // per trace kind (bit 0 primary, 1 shading, 2 generic rays): the handed-over
+    // rays are traced a block per ray (k_trace_heavy_team) instead of a warp
+    uint32_t heavy_team = kDefaultHeavyTeam;
     uint32_t tile_order = 1u;  // heavy-first tile order per kind: bit 0 primary, 1 shading, 2 generic rays
     int num_sms = 0;
 };

@@ -405,6 +405,7 @@ struct HeavyArgs {
     uint32_t* leaves;     // primary / generic-ray leaf output (nullable)
     uint32_t* mirror_leaves;
     uint32_t wide_cap;    // frontier-stack entries per warp (wide_stack_entries of the tree depth)
+    uint32_t team_cap;    // frontier-stack entries per block (team_stack_entries of the tree depth)
     ShadeLists sl;        // primary entries: set up their pixel's shading rays too (sl.lists != nullptr)
     const uint32_t* list;
     const uint32_t* count;
@@ -456,6 +457,62 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_heavy(HeavyArgs a) {
         }
     }
 }
+
+// k_trace_heavy with a block per ray (traverse_team): for the handed-over
+// shading rays, a few hundred grazing rays whose walks run for thousands of
+// tests, where a warp per ray leaves the GPU waiting on the longest few.
+__global__ void __launch_bounds__(kTeamThreads) k_trace_heavy_team(HeavyArgs a) {
+    grid_dep_wait();
+    __shared__ TeamShared ts;
+    __shared__ uint32_t s_e;
+    const uint32_t n = min(*a.count, a.cap);
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) s_e = atomicAdd(a.work, 1u);
+        __syncthreads();
+        const uint32_t e = s_e;
+        __syncthreads();
+        if (e >= n) break;
+        const uint32_t entry = __ldg(a.list + e);
+        const uint32_t kind = entry >> 30, idx = entry & kHeavyIndexMask;
+        if (kind == kHeavyPrimary) {
+            const uint32_t i = idx % a.cam.width, j = idx / a.cam.width;
+            const RayState r = make_ray(mk3(a.cam.eye[0], a.cam.eye[1], a.cam.eye[2]), primary_dir(a.cam, i, j),
+                                        1e16f, -1);
+            const Hit h = trace_team(r, a.tr, false, a.team_cap, ts);
+            if (tid == 0) {
+                store_hit(a.hits + idx, h);
+                if (a.leaves) a.leaves[idx] = 1u;  // the root: a valid restart node
+            }
+            if (a.sl.lists && tid < 32) {
+                const int4 ph = make_int4(h.id, __float_as_int(h.u), __float_as_int(h.v), __float_as_int(h.t));
+                shade_setup_pixel(a.sl, a.cam, ph, tid == 0, i, j, idx);
+            }
+        } else if (kind == kHeavyRay) {
+            const RayState r = load_ray(a.rays, idx, true);
+            const Hit h = trace_team(r, a.tr, a.any_hit != 0, a.team_cap, ts);
+            if (tid == 0) {
+                store_hit(a.hits + idx, h);
+                if (a.leaves) a.leaves[idx] = 1u;
+            }
+        } else {
+            const uint32_t i = idx % a.cam.width, j = idx / a.cam.width;
+            const int4 ph = __ldg(reinterpret_cast<const int4*>(a.prim + idx));
+            const ShadeRays sr = shade_rays(a.soup, a.cam, a.lx, a.ly, a.lz, ph, true, i, j, kind == kHeavyMirror);
+            if (kind == kHeavyShadow) {
+                const Hit h = trace_team(sr.shadow, a.tr, true, a.team_cap, ts);
+                if (tid == 0) a.vis[idx] = vis_code(sr.has, sr.cast, h.id >= 0);
+            } else {
+                const Hit h = trace_team(sr.mirror, a.tr, false, a.team_cap, ts);
+                if (tid == 0) {
+                    store_hit(a.mirror + idx, h);
+                    if (a.mirror_leaves) a.mirror_leaves[idx] = 1u;
+                }
+            }
+        }
+    }
+}
+
 
 uint32_t pixel_tiles(const rt_camera* cam) {
     return (uint32_t)(((cam->width + 7) / 8) * ((cam->height + 3) / 4));
@@ -549,12 +606,23 @@ rt_status reset_words(rt_ctx* ctx, uint64_t mask) {
     return RT_OK;
 }
 
-rt_status launch_heavy(rt_ctx* ctx, const Spill& sp, HeavyArgs a) {
+rt_status launch_heavy(rt_ctx* ctx, const Spill& sp, HeavyArgs a, int kind) {
     if (!sp.count) return RT_OK;
     a.list = ctx->d_spill;
     a.count = sp.count;
     a.cap = kSpillCap;
     a.work = sp.work;
+    if ((ctx->heavy_team >> kind) & 1u) {
+        const size_t smem = team_smem_bytes(a.team_cap);
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_heavy_team, kTeamThreads, smem) !=
+                cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+        launch_pdl(k_trace_heavy_team, (uint32_t)per_sm * ctx->num_sms, kTeamThreads, smem, ctx->stream, a);
+        RT_CHECK_LAUNCH(ctx, "k_trace_heavy_team");
+        return RT_OK;
+    }
     const size_t smem = wide_smem_bytes(a.wide_cap);
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_heavy, kTraceThreads, smem) != cudaSuccess ||
@@ -613,6 +681,7 @@ HeavyArgs heavy_args(rt_ctx* ctx, const rt_lbvh* l) {
     memset(&a, 0, sizeof(a));
     a.tr = tree_ref(ctx, l);
     a.wide_cap = wide_stack_entries(l->depth);
+    a.team_cap = team_stack_entries(l->depth);
     return a;
 }
 
@@ -655,7 +724,7 @@ rt_status trace_primary(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* cam, rt_
     a.hits = d_hits;
     a.leaves = d_leaves;
     a.sl = lists;
-    return launch_heavy(ctx, sp, a);
+    return launch_heavy(ctx, sp, a, 0);
 }
 
 // prebuilt: the frame's primary pass has filled the shading lists (and the
@@ -718,7 +787,7 @@ rt_status trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* ca
     a.vis = d_vis;
     a.mirror = d_mirror;
     a.mirror_leaves = d_mirror_leaves;
-    return launch_heavy(ctx, sp, a);
+    return launch_heavy(ctx, sp, a, 1);
 }
 
 rt_status trace_rays(rt_ctx* ctx, const rt_lbvh* l, const rt_ray* d_rays, uint32_t n, int any_hit,
@@ -750,7 +819,7 @@ rt_status trace_rays(rt_ctx* ctx, const rt_lbvh* l, const rt_ray* d_rays, uint32
     a.any_hit = any_hit;
     a.hits = d_hits;
     a.leaves = d_leaves;
-    return launch_heavy(ctx, sp, a);
+    return launch_heavy(ctx, sp, a, 2);
 }
 
 }  // namespace

@@ -765,6 +765,272 @@ __device__ __forceinline__ Hit traverse_wide(const RayState& r, const TreeRef& t
     return h;
 }
 
+// One ray traced by a whole block of kTeamThreads threads: traverse_wide's
+// frontier walk with the block as the team.  Each step pops up to
+// kTeamThreads nodes (the deepest), tests their children, and pushes /
+// queues them at offsets from a block-wide prefix sum; the queued leaves are
+// tested kTeamThreads (leaf, triangle) pairs at a time, the block minimum of
+// the (t, id) keys (a shared-memory atomicMin) becoming the shared bound.
+// The hit is traverse_wide's (the tie rule makes it order-free); a ray whose
+// frontier is wide (grazing rays with thousands of tests) finishes in a
+// quarter of the steps.  Every thread of the block calls it with the same
+// ray; it synchronises the block.  Stack bound as in traverse_wide with
+// kTeamThreads entries per level.
+constexpr int kTeamThreads = 128;
+constexpr int kTeamQueue = 4 * kTeamThreads;
+
+__host__ __device__ constexpr uint32_t team_stack_entries(uint32_t depth) {
+    return (depth + 2u) * (uint32_t)kTeamThreads;
+}
+
+// Dynamic shared memory of traverse_team with `cap` stack entries.
+__host__ __device__ constexpr size_t team_smem_bytes(uint32_t cap) {
+    return (size_t)cap * 8u + (size_t)kTeamQueue * 16u;
+}
+
+struct TeamShared {
+    unsigned long long best;
+    float bt, bu, bv;
+    uint32_t warp_sum[kTeamThreads / 32];
+    int tris_sum[kTeamThreads / 32];
+};
+
+// Inclusive block-wide prefix sum of v (all threads call); *total = the sum.
+__device__ __forceinline__ uint32_t team_scan(uint32_t v, TeamShared& ts, uint32_t* total) {
+    constexpr uint32_t kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, x, off);
+        if (lane >= off) x += y;
+    }
+    __syncthreads();
+    if (lane == 31) ts.warp_sum[w] = x;
+    __syncthreads();
+    uint32_t before = 0, all = 0;
+#pragma unroll
+    for (int q = 0; q < kTeamThreads / 32; ++q) {
+        const uint32_t t = ts.warp_sum[q];
+        if (q < w) before += t;
+        all += t;
+    }
+    *total = all;
+    return before + x;
+}
+
+template <bool EXACT>
+__device__ __forceinline__ Hit traverse_team(const RayState& r, const TreeRef& tr_, bool any_hit, uint32_t cap,
+                                             TeamShared& ts) {
+    constexpr uint32_t kFull = 0xffffffffu;
+    extern __shared__ uint4 wide_dyn[];
+    uint8_t* base8 = reinterpret_cast<uint8_t*>(wide_dyn);
+    const int tid = threadIdx.x, lane = tid & 31;
+    uint32_t* snode = reinterpret_cast<uint32_t*>(base8);
+    float* st0 = reinterpret_cast<float*>(base8 + (size_t)cap * 4u);
+    uint8_t* qbase = base8 + (size_t)cap * 8u;
+    int32_t* qpos = reinterpret_cast<int32_t*>(qbase);
+    int32_t* qcnt = qpos + kTeamQueue;
+    float* qt0 = reinterpret_cast<float*>(qcnt + kTeamQueue);
+    uint32_t* qincl = reinterpret_cast<uint32_t*>(qt0 + kTeamQueue);
+    const uint64_t init = hit_key(r.tmax, 0);
+    // uniform across the block (every thread keeps the same copy)
+    uint64_t best = init;
+    int size = 0, nq = 0, qtris = 0;
+    bool stop = false;
+    __syncthreads();  // the previous ray's readers of the shared state are done
+    if (tid == 0) {
+        ts.best = init;
+        ts.bt = r.tmax;
+        ts.bu = -1.0f;
+        ts.bv = -1.0f;
+    }
+    {
+        const NodeBox root = load_node(tr_.nodes, 1);
+        float t0;
+        const bool enter = r.tmax > 0.0f &&
+                           box_enter<EXACT>(r, root.a.x, root.a.y, root.a.z, root.a.w, root.b.x, root.b.y, r.tmax, &t0);
+        if (enter) {
+            if (__float_as_int(root.b.z) & 4) {
+                if (tid == 0) {
+                    qpos[0] = __float_as_int(root.b.w);
+                    qcnt[0] = __float_as_int(root.b.z) >> 3;
+                    qt0[0] = t0;
+                }
+                nq = 1;
+                qtris = __float_as_int(root.b.z) >> 3;
+            } else {
+                if (tid == 0) {
+                    snode[0] = child_pair(tr_, 1, root.b.w);
+                    st0[0] = t0;
+                }
+                size = 1;
+            }
+        }
+    }
+    __syncthreads();
+    while (!stop && (size > 0 || nq > 0)) {
+        if (nq > 0 && (size == 0 || qtris >= 2 * kTeamThreads || nq > kTeamQueue - 2 * kTeamThreads)) {
+            const float bound_t = key_t(best);
+            // drop leaves now behind the closest hit; prefix of the kept sizes
+            uint32_t run = 0;
+            for (int q0 = 0; q0 < nq; q0 += kTeamThreads) {
+                const int q = q0 + tid;
+                int c = 0;
+                if (q < nq) {
+                    c = qcnt[q];
+                    if (qt0[q] > bound_t || qpos[q] < 0 || c < 0 || (uint32_t)qpos[q] + (uint32_t)c > tr_.n) c = 0;
+                }
+                uint32_t chunk = 0;
+                const uint32_t incl = team_scan((uint32_t)c, ts, &chunk);
+                if (q < nq) qincl[q] = run + incl;
+                run += chunk;
+            }
+            __syncthreads();
+            const uint32_t total = run;
+            for (uint32_t base = 0; base < total; base += kTeamThreads) {
+                const uint32_t p = base + tid;
+                uint64_t key = ~0ull;
+                float kt = 0.0f, ku = 0.0f, kv = 0.0f;
+                if (p < total) {
+                    int lo = 0, hi = nq - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (qincl[mid] > p) hi = mid; else lo = mid + 1;
+                    }
+                    const uint32_t ex = lo > 0 ? qincl[lo - 1] : 0u;
+                    const float4* tp = tr_.tris + 3 * (size_t)(qpos[lo] + (int)(p - ex));
+                    const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                    const int id = __float_as_int(a.w);
+                    float u, v, t;
+                    if (id != r.exclude && tri_test(r, a, b, c, &u, &v, &t)) {
+                        const uint64_t k = hit_key(t, id);
+                        if (k < best) {
+                            key = k;
+                            kt = t;
+                            ku = u;
+                            kv = v;
+                        }
+                    }
+                }
+                const uint64_t wmin = warp_min_u64(key);
+                if (lane == 0 && wmin < best) atomicMin(&ts.best, (unsigned long long)wmin);
+                __syncthreads();
+                const uint64_t bmin = ts.best;
+                if (bmin < best && key == bmin) {  // the one triangle with this (t, id): same t, u, v
+                    ts.bt = kt;
+                    ts.bu = ku;
+                    ts.bv = kv;
+                }
+                best = bmin;
+                __syncthreads();
+                if (any_hit && best < init) break;
+            }
+            nq = 0;
+            qtris = 0;
+            if (any_hit && best < init) stop = true;
+            continue;
+        }
+        // pop up to kTeamThreads internal nodes from the top
+        const int k = min(kTeamThreads, size);
+        const float bound_t = key_t(best);
+        uint32_t nd = 0;
+        bool live = false;
+        if (tid < k) {
+            nd = snode[size - 1 - tid];
+            live = !(st0[size - 1 - tid] > bound_t);
+        }
+        size -= k;
+        __syncthreads();
+        bool push_l = false, push_r = false, leaf_l = false, leaf_r = false;
+        float tl = 0.0f, tr = 0.0f;
+        float4 l1 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = l1;
+        uint32_t c0 = 0;
+        if (live) {
+            c0 = nd;
+            if (c0 + 1 >= tr_.num_nodes) {
+                atomicOr(tr_.err, RT_DEVERR_BOUNDS);
+            } else {
+                const float4* p = reinterpret_cast<const float4*>(tr_.nodes + c0);
+                const float4 l0 = __ldg(p), r0 = __ldg(p + 2);
+                l1 = __ldg(p + 1);
+                r1 = __ldg(p + 3);
+                push_l = box_enter<EXACT>(r, l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, bound_t, &tl);
+                push_r = box_enter<EXACT>(r, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, bound_t, &tr);
+                leaf_l = push_l && (__float_as_int(l1.z) & 4);
+                leaf_r = push_r && (__float_as_int(r1.z) & 4);
+            }
+        }
+        const uint32_t ni = (uint32_t)((push_l && !leaf_l) + (push_r && !leaf_r));
+        const uint32_t nl = (uint32_t)(leaf_l + leaf_r);
+        // one scan for both counts (internal in the low half, leaves in the high)
+        uint32_t both = 0;
+        const uint32_t incl = team_scan(ni | (nl << 16), ts, &both);
+        const uint32_t excl = incl - (ni | (nl << 16));
+        const int itotal = (int)(both & 0xffffu), ltotal = (int)(both >> 16);
+        int lt_tris = (leaf_l ? (__float_as_int(l1.z) >> 3) : 0) + (leaf_r ? (__float_as_int(r1.z) >> 3) : 0);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) lt_tris += __shfl_xor_sync(kFull, lt_tris, off);
+        if (lane == 0) ts.tris_sum[threadIdx.x >> 5] = lt_tris;
+        if (size + itotal > (int)cap) {  // cannot happen within the tree's depth; stop rather than overflow
+            if (tid == 0) atomicOr(tr_.err, RT_DEVERR_BOUNDS);
+            stop = true;
+            __syncthreads();
+            break;
+        }
+        int io = size + (int)(excl & 0xffffu), lo_ = nq + (int)(excl >> 16);
+        if (push_l) {
+            if (leaf_l) {
+                qpos[lo_] = __float_as_int(l1.w);
+                qcnt[lo_] = __float_as_int(l1.z) >> 3;
+                qt0[lo_] = tl;
+                ++lo_;
+            } else {
+                snode[io] = child_pair(tr_, c0, l1.w);
+                st0[io] = tl;
+                ++io;
+            }
+        }
+        if (push_r) {
+            if (leaf_r) {
+                qpos[lo_] = __float_as_int(r1.w);
+                qcnt[lo_] = __float_as_int(r1.z) >> 3;
+                qt0[lo_] = tr;
+            } else {
+                snode[io] = child_pair(tr_, c0 | 1u, r1.w);
+                st0[io] = tr;
+            }
+        }
+        __syncthreads();
+        int tsum = 0;
+#pragma unroll
+        for (int q = 0; q < kTeamThreads / 32; ++q) tsum += ts.tris_sum[q];
+        size += itotal;
+        nq += ltotal;
+        qtris += tsum;
+    }
+    Hit h;
+    if (best < init) {
+        h.id = (int)(uint32_t)best;
+        h.t = ts.bt;
+        h.u = ts.bu;
+        h.v = ts.bv;
+    } else {
+        h.id = -1;
+        h.u = -1.0f;
+        h.v = -1.0f;
+        h.t = r.tmax;
+    }
+    __syncthreads();
+    return h;
+}
+
+__device__ __forceinline__ Hit trace_team(const RayState& r, const TreeRef& tr, bool any_hit, uint32_t cap,
+                                          TeamShared& ts) {
+    if (r.exact) return traverse_team<true>(r, tr, any_hit, cap, ts);
+    return traverse_team<false>(r, tr, any_hit, cap, ts);
+}
+
 // Warp-uniform dispatch between the fast and the NaN-exact box test.  Must be
 // called by all 32 lanes of the warp together (inactive lanes pass
 // active == false).  spill / slot: see Spill (nullptr: no budget).

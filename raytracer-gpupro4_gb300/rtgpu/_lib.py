@@ -27,7 +27,7 @@ assert NODE_DTYPE.itemsize == 32 and HIT_DTYPE.itemsize == 16 and RAY_DTYPE.item
 
 EXPORTED = [
     "rt_api_version", "rt_status_string", "rt_ctx_create", "rt_ctx_destroy", "rt_ctx_set_stream", "rt_ctx_sync",
-    "rt_ctx_set_trace_budget", "rt_ctx_set_trace_budget_kind", "rt_ctx_set_tile_order",
+    "rt_ctx_set_trace_budget", "rt_ctx_set_trace_budget_kind", "rt_ctx_set_heavy_block", "rt_ctx_set_tile_order",
     "rt_ctx_check", "rt_last_error", "rt_lbvh_create", "rt_lbvh_destroy", "rt_lbvh_build", "rt_lbvh_build_host",
     "rt_lbvh_import_host", "rt_lbvh_view_get", "rt_lbvh_compact_get", "rt_lbvh_world_bound", "rt_lbvh_download", "rt_trace_primary",
     "rt_trace_shadow_mirror", "rt_trace_rays", "rt_trace_primary_leaves", "rt_trace_shadow_mirror_from",
@@ -95,6 +95,7 @@ def lib() -> C.CDLL:
         "rt_ctx_sync": (i32, [vp]),
         "rt_ctx_set_trace_budget": (i32, [vp, u32]),
         "rt_ctx_set_trace_budget_kind": (i32, [vp, u32, u32]),
+        "rt_ctx_set_heavy_block": (i32, [vp, u32]),
         "rt_ctx_set_tile_order": (i32, [vp, u32]),
         "rt_ctx_check": (i32, [vp]),
         "rt_last_error": (C.c_char_p, [vp]),

@@ -83,6 +83,15 @@ class Context:
             L.check(L.lib().rt_ctx_set_trace_budget_kind(self.h, int(kind), int(budget)), self.h,
                     "rt_ctx_set_trace_budget_kind")
 
+    DEFAULT_HEAVY_BLOCK = 2
+
+    def set_heavy_block(self, kinds: int | None):
+        """Trace kinds (bit 0 primary, 1 shadow / mirror, 2 generic rays) whose
+        handed-over rays are traced a block per ray instead of a warp per
+        ray; None restores the default."""
+        k = self.DEFAULT_HEAVY_BLOCK if kinds is None else int(kinds)
+        L.check(L.lib().rt_ctx_set_heavy_block(self.h, k), self.h, "rt_ctx_set_heavy_block")
+
 
 class LBVH:
     """Device LBVH (heap layout, 1 << depth slots of 32 bytes)."""

@@ -46,10 +46,12 @@ def test_primary_leaves_and_shading_rays_from_leaves(gpu_ctx, oracle_mod, sphere
     assert oss[:, 0].sum() < rss[:, 0].sum() and oms[:, 0].sum() < rms[:, 0].sum()
 
 
+@pytest.mark.parametrize("block", [0, 2])
 @pytest.mark.parametrize("budget", [0, 24, 384])
-def test_production_shading_rays_from_leaves(gpu_ctx, oracle_mod, sphere, budget):
+def test_production_shading_rays_from_leaves(gpu_ctx, oracle_mod, sphere, budget, block):
     """The compacted production pass (k_shade_setup + k_trace_shade) with
-    and without the heavy-ray hand-over: vis and mirror hits equal the
+    and without the heavy-ray hand-over (its second pass a warp or, with
+    block, a block per ray): vis and mirror hits equal the
     oracle's restart walk; leaves too, except for rays the warp-per-ray pass
     traced, which report the root."""
     from rtgpu import scenes
@@ -59,12 +61,14 @@ def test_production_shading_rays_from_leaves(gpu_ctx, oracle_mod, sphere, budget
     light = scenes.TORUS_LIGHT
     rt = RayTracer(gpu_ctx)
     gpu_ctx.set_trace_budget(budget)
+    gpu_ctx.set_heavy_block(block)
     try:
         hits, leaves = rt.primary_leaves(lb, cam)
         vis, mir, ml = rt.shadow_mirror_from(lb, cam, light, hits, leaves)
         gpu_ctx.check()
     finally:
         gpu_ctx.set_trace_budget(None)
+        gpu_ctx.set_heavy_block(None)
     oh, ol = oracle_mod.trace_from(nodes, 18, ids, tris, oracle_mod.primary_rays(cam))
     ovis, omir, oml = oracle_mod.shadow_mirror_from(nodes, 18, ids, tris, cam, light, oh, ol)
     assert_hits_equal(hits_to_numpy(hits), oh, "primary")

@@ -195,23 +195,27 @@ def test_shared_traversal_generic_rays(gpu_ctx, oracle_mod, any_hit):
         assert_hits_equal(g, oh, "rays")
 
 
+@pytest.mark.parametrize("block", [0, 7])
 @pytest.mark.parametrize("budget", [1, 24, 0])
-def test_heavy_ray_handover_matches_oracle(gpu_ctx, oracle_mod, torus_scene, budget):
-    """Rays over the work budget are re-traced by the warp-per-ray pass; with
-    a budget of 1 nearly every ray is, with 0 none is: hits, visibility and
-    mirror hits equal the oracle's either way."""
+def test_heavy_ray_handover_matches_oracle(gpu_ctx, oracle_mod, torus_scene, budget, block):
+    """Rays over the work budget are re-traced by the second pass (a warp per
+    ray, or with `block` a block of 128 threads per ray); with a budget of 1
+    nearly every ray is, with 0 none is: hits, visibility and mirror hits
+    equal the oracle's either way."""
     from rtgpu import scenes
     from rtgpu.api import RayTracer, hits_to_numpy
     tris, lb, dt, nodes, ids = torus_scene
     rt = RayTracer(gpu_ctx)
     cam = scenes.look_at((2.2, 0.3, 0.4), (0.0, 0.0, 0.0), width=320, height=200)
     gpu_ctx.set_trace_budget(budget)
+    gpu_ctx.set_heavy_block(block)
     try:
         hits = rt.primary(lb, cam)
         vis, mirror = rt.shadow_mirror(lb, cam, scenes.TORUS_LIGHT, hits)
         gpu_ctx.check()
     finally:
         gpu_ctx.set_trace_budget(None)
+        gpu_ctx.set_heavy_block(None)
     oh = oracle_mod.trace(nodes, 20, ids, tris, oracle_mod.primary_rays(cam))
     ovis, omir = oracle_mod.shadow_mirror(nodes, 20, ids, tris, cam, scenes.TORUS_LIGHT, oh)
     assert_hits_equal(hits_to_numpy(hits), oh, "primary")
@@ -219,8 +223,9 @@ def test_heavy_ray_handover_matches_oracle(gpu_ctx, oracle_mod, torus_scene, bud
     assert_hits_equal(hits_to_numpy(mirror), omir, "mirror")
 
 
+@pytest.mark.parametrize("block", [0, 4])
 @pytest.mark.parametrize("any_hit", [False, True])
-def test_heavy_ray_handover_generic_rays(gpu_ctx, oracle_mod, any_hit):
+def test_heavy_ray_handover_generic_rays(gpu_ctx, oracle_mod, any_hit, block):
     from rtgpu import scenes
     from rtgpu.api import RayTracer, hits_to_numpy, rays_tensor
     tris = scenes.random_soup(30000, seed=71)
@@ -235,11 +240,13 @@ def test_heavy_ray_handover_generic_rays(gpu_ctx, oracle_mod, any_hit):
     excl = np.where(np.arange(n) % 2 == 0, src, -1).astype(np.int32)
     tmax = np.where(np.arange(n) % 3 == 0, 0.05, 1e16).astype(np.float32)
     gpu_ctx.set_trace_budget(2)
+    gpu_ctx.set_heavy_block(block)
     try:
         hits = RayTracer(gpu_ctx).rays(lb, rays_tensor(o, d, tmax, excl, "cuda"), any_hit=any_hit)
         gpu_ctx.check()
     finally:
         gpu_ctx.set_trace_budget(None)
+        gpu_ctx.set_heavy_block(None)
     oh = oracle_mod.trace(nodes, 16, ids, tris, oracle_mod.rays_array(o, d, tmax, excl), any_hit=any_hit)
     g = hits_to_numpy(hits)
     if any_hit:
