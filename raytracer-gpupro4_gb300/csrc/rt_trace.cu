@@ -614,6 +614,9 @@ rt_status launch_heavy(rt_ctx* ctx, const Spill& sp, HeavyArgs a, int kind) {
     a.work = sp.work;
     if ((ctx->heavy_team >> kind) & 1u) {
         const size_t smem = team_smem_bytes(a.team_cap);
+        if (smem > 48u * 1024u)
+            RT_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_trace_heavy_team, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)smem));
         int per_sm = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_heavy_team, kTeamThreads, smem) !=
                 cudaSuccess ||
