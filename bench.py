@@ -352,7 +352,8 @@ def run_ours(args, dist: Dist):
     # stage: (ms, algorithmic bytes, kernels of the stage's ncu traffic)
     groups = {"k_trace_primary (+ k_trace_heavy)": (prim_ms, bytes_primary,
                                                     ("k_trace_primary", "k_trace_heavy_primary")),
-              "k_trace_shade (+ k_trace_heavy)": (sec_ms, bytes_secondary, ("k_trace_shade", "k_trace_heavy_shade")),
+              "k_trace_shade (+ k_trace_heavy_team)": (sec_ms, bytes_secondary,
+                                                      ("k_trace_shade", "k_trace_heavy_team")),
               "build (10 kernels)": (build_ms, BUILD_BYTES_PER_TRI * n,
                                      ("k_bounds", "k_morton_hist") + ("k_onesweep",) * 4 + ("k_emit_leaves",
                                                                                          "k_emit_refit"))}
@@ -385,7 +386,7 @@ def run_ours(args, dist: Dist):
         "e2e": e2e,
         # per graph: 10 build kernels; k_order_begin (which also zeroes the frame's
         # counters), k_trace_primary (which also lists the shading rays),
-        # k_trace_heavy; k_trace_shade, k_trace_heavy
+        # k_trace_heavy; k_trace_shade, k_trace_heavy_team
         "gpu_launches": 15 * args.steps,
     }
     out["clocks"] = clk.summary()
