@@ -79,8 +79,10 @@ __device__ __forceinline__ void shade_setup_pixel(const ShadeLists& sl, const rt
     append_pixel(sl.mirror && valid && s.has, (uint32_t)p, sl.lists + sl.cap, sl.cap, sl.counts + 1);
 }
 
+// At most 72 registers (seven blocks per SM, no spills): a little faster
+// than the 80 the compiler picks unbounded; 64 spills and is slower.
 template <bool STATS>
-__global__ void __launch_bounds__(kTraceThreads) k_trace_primary(TreeRef tr, rt_camera cam,
+__global__ void __launch_bounds__(kTraceThreads, 7) k_trace_primary(TreeRef tr, rt_camera cam,
                                                                  rt_hit* __restrict__ hits,
                                                                  uint32_t* __restrict__ leaves,
                                                                  uint32_t* __restrict__ stats, uint32_t* work,
