@@ -1047,7 +1047,7 @@ void free_lbvh(rt_lbvh* l) {
     void* ptrs[] = {l->nodes,    l->keys,     l->ids,      l->keys_alt,  l->ids_alt, l->sorted_tris,
                     l->tris,     l->scene,    l->partials, l->counters,  l->hist,    l->lookback,
                     l->scan,     l->leaf_list, l->arrive,  l->f_primary, l->f_mirror, l->f_vis,
-                    l->s_lists,  l->cnodes,   l->inner,    l->inner_rank, l->w_buf};
+                    l->s_lists,  l->cnodes,   l->inner,    l->inner_rank, l->w_buf, l->s_rays};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete l;

@@ -148,8 +148,10 @@ struct rt_lbvh {
     rt_hit* f_mirror = nullptr;
     uint8_t* f_vis = nullptr;
     size_t f_pixels = 0;
-    // compacted shading-ray lists (shadow pixels, mirror pixels, primary leaves), 3 x s_pixels
+    // compacted shading-ray lists (shadow pixels, mirror pixels, primary leaves, then the start
+    // nodes of the listed rays, 2 x), 5 x s_pixels
     uint32_t* s_lists = nullptr;
+    float4* s_rays = nullptr;  // the listed rays, 2 x 2 x s_pixels float4 (ensure_shade_lists)
     size_t s_pixels = 0;
     // per-pixel state of the colour stage's bounce loop (rt_render_whitted)
     void* w_buf = nullptr;

@@ -35,21 +35,31 @@ __device__ __forceinline__ void spill_record(uint32_t* list, int slot, uint32_t 
     list[slot] = (kind << 30) | (uint32_t)index;
 }
 
+constexpr uint32_t kNoSlot = 0xffffffffu;
+
 // Warp-aggregated append of the lanes' pixels to a list (a warp's pixels in
-// lane order, so neighbouring rays stay neighbours).
-__device__ __forceinline__ void append_pixel(bool take, uint32_t p, uint32_t* list, uint32_t cap, uint32_t* count) {
+// lane order, so neighbouring rays stay neighbours).  Returns the lane's
+// slot, or kNoSlot.
+__device__ __forceinline__ uint32_t append_pixel(bool take, uint32_t p, uint32_t* list, uint32_t cap,
+                                                 uint32_t* count) {
     const uint32_t m = __ballot_sync(0xffffffffu, take);
-    if (!m) return;
+    if (!m) return kNoSlot;
     uint32_t base = 0;
     if ((threadIdx.x & 31) == 0) base = atomicAdd(count, (uint32_t)__popc(m));
     base = __shfl_sync(0xffffffffu, base, 0);
     const uint32_t k = base + __popc(m & ((1u << (threadIdx.x & 31)) - 1u));
-    if (take && k < cap) list[k] = p;
+    if (!take || k >= cap) return kNoSlot;
+    list[k] = p;
+    return k;
 }
 
 // The shading-ray lists of a frame (shadow pixels, then mirror pixels) and
 // the results that need no ray.  A frame's primary pass fills them as it
 // goes (lists != nullptr), so no separate pass re-reads the primary hits.
+// Beside each listed pixel its ray (two float4: origin and tmax, direction
+// and the excluded triangle) and the node its walk starts at, so the
+// tracing kernel neither re-reads the primary hit and the triangle nor
+// rebuilds the ray.
 struct ShadeLists {
     const float* soup;
     float lx, ly, lz;
@@ -58,15 +68,23 @@ struct ShadeLists {
     uint32_t* lists;
     uint32_t cap;
     uint32_t* counts;  // 2 words
+    float4* rays;      // 2 x cap rays (2 float4 each), by list slot
+    uint32_t* starts;  // 2 x cap start nodes, by list slot
 };
+
+__device__ __forceinline__ void put_ray(float4* q, const RayState& r) {
+    q[0] = make_float4(r.o.x, r.o.y, r.o.z, r.tmax);
+    q[1] = make_float4(r.d.x, r.d.y, r.d.z, __int_as_float(r.exclude));
+}
 
 // One pixel's shading-ray setup from its primary hit ph (all lanes call):
 // visibility 0 (no hit) or 1 (light behind the surface) and the mirror
 // miss record are written, the pixels that cast a shadow ray and those that
-// cast a mirror ray are appended to the two lists.
+// cast a mirror ray are appended to the two lists with their rays and
+// `start`, the restart node of the walks (the primary hit's leaf, or 1).
 __device__ __forceinline__ void shade_setup_pixel(const ShadeLists& sl, const rt_camera& cam, int4 ph, bool valid,
-                                                  uint32_t i, uint32_t j, size_t p) {
-    const ShadeRays s = shade_rays(sl.soup, cam, sl.lx, sl.ly, sl.lz, ph, valid, i, j, false);
+                                                  uint32_t i, uint32_t j, size_t p, uint32_t start) {
+    const ShadeRays s = shade_rays(sl.soup, cam, sl.lx, sl.ly, sl.lz, ph, valid, i, j, sl.mirror != nullptr);
     if (valid) {
         if (sl.vis && !(s.has && s.cast)) sl.vis[p] = vis_code(s.has, s.cast, false);
         if (sl.mirror && !s.has) {
@@ -75,8 +93,16 @@ __device__ __forceinline__ void shade_setup_pixel(const ShadeLists& sl, const rt
             store_hit(sl.mirror + p, mh);
         }
     }
-    append_pixel(sl.vis && valid && s.has && s.cast, (uint32_t)p, sl.lists, sl.cap, sl.counts);
-    append_pixel(sl.mirror && valid && s.has, (uint32_t)p, sl.lists + sl.cap, sl.cap, sl.counts + 1);
+    const uint32_t ks = append_pixel(sl.vis && valid && s.has && s.cast, (uint32_t)p, sl.lists, sl.cap, sl.counts);
+    const uint32_t km = append_pixel(sl.mirror && valid && s.has, (uint32_t)p, sl.lists + sl.cap, sl.cap, sl.counts + 1);
+    if (ks != kNoSlot) {
+        put_ray(sl.rays + 2 * (size_t)ks, s.shadow);
+        sl.starts[ks] = start;
+    }
+    if (km != kNoSlot) {
+        put_ray(sl.rays + 2 * ((size_t)sl.cap + km), s.mirror);
+        sl.starts[sl.cap + km] = start;
+    }
 }
 
 // At most 72 registers (seven blocks per SM, no spills): a little faster
@@ -116,7 +142,7 @@ __global__ void __launch_bounds__(kTraceThreads, 7) k_trace_primary(TreeRef tr, 
         }
         if (sl.lists) {  // uniform; a handed-over pixel is set up by the warp-per-ray pass
             const int4 ph = make_int4(h.id, __float_as_int(h.u), __float_as_int(h.v), __float_as_int(h.t));
-            shade_setup_pixel(sl, cam, ph, valid && slot < 0, i, j, p);
+            shade_setup_pixel(sl, cam, ph, valid && slot < 0, i, j, p, leaf);
         }
         record_tile_cost(ord, wbuf, tile, nb + nt);
     }
@@ -210,7 +236,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_secondary(
 __global__ void __launch_bounds__(256) k_shade_setup(const float* __restrict__ soup, rt_camera cam, float lx, float ly,
                                                      float lz, const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis,
                                                      rt_hit* __restrict__ mirror, uint32_t* __restrict__ mirror_leaves,
+                                                     const uint32_t* __restrict__ prim_leaves,
                                                      uint32_t* __restrict__ lists, uint32_t cap, uint32_t* counts,
+                                                     float4* __restrict__ rays, uint32_t* __restrict__ starts,
                                                      uint32_t num_tiles) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -221,8 +249,8 @@ __global__ void __launch_bounds__(256) k_shade_setup(const float* __restrict__ s
         const size_t p = (size_t)j * cam.width + i;
         int4 ph = make_int4(-1, 0, 0, 0);
         if (valid) ph = __ldg(reinterpret_cast<const int4*>(prim + p));
-        const ShadeLists sl{soup, lx, ly, lz, vis, mirror, lists, cap, counts};
-        shade_setup_pixel(sl, cam, ph, valid, i, j, p);
+        const ShadeLists sl{soup, lx, ly, lz, vis, mirror, lists, cap, counts, rays, starts};
+        shade_setup_pixel(sl, cam, ph, valid, i, j, p, shade_start(prim_leaves, ph, valid, p));
         if (valid && mirror_leaves && ph.x < 0) mirror_leaves[p] = 1u;
     }
 }
@@ -242,7 +270,8 @@ __global__ void __launch_bounds__(kTraceThreads, 7) k_trace_shade(
     TreeRef tr, const float* __restrict__ soup, rt_camera cam, float lx, float ly, float lz,
     const rt_hit* __restrict__ prim, const uint32_t* __restrict__ prim_leaves, uint8_t* __restrict__ vis,
     rt_hit* __restrict__ mirror, uint32_t* __restrict__ mirror_leaves, const uint32_t* __restrict__ lists,
-    uint32_t cap, const uint32_t* counts, uint32_t* work, Spill spill, uint32_t* __restrict__ list) {
+    uint32_t cap, const uint32_t* counts, const float4* __restrict__ rays, const uint32_t* __restrict__ starts,
+    uint32_t* work, Spill spill, uint32_t* __restrict__ list) {
     grid_dep_wait();
     constexpr uint32_t kFull = 0xffffffffu;
     const uint32_t ns = min(counts[0], cap), nm = min(counts[1], cap), total = ns + nm;
@@ -276,12 +305,11 @@ __global__ void __launch_bounds__(kTraceThreads, 7) k_trace_shade(
             uint32_t start = 1u;
             if (take) {
                 shadow = k < ns;
-                p = __ldg(lists + (shadow ? k : cap + (k - ns)));
-                const uint32_t i = p % cam.width, j = p / cam.width;
-                const int4 ph = __ldg(reinterpret_cast<const int4*>(prim + p));
-                const ShadeRays s = shade_rays(soup, cam, lx, ly, lz, ph, true, i, j, !shadow);
-                r = shadow ? s.shadow : s.mirror;
-                start = shade_start(prim_leaves, ph, true, p);
+                const uint32_t q = shadow ? k : cap + (k - ns);  // list slot: pixel, ray, start node
+                p = __ldg(lists + q);
+                const float4 ra = __ldg(rays + 2 * (size_t)q), rb = __ldg(rays + 2 * (size_t)q + 1);
+                r = make_ray(mk3(ra.x, ra.y, ra.z), mk3(rb.x, rb.y, rb.z), ra.w, __float_as_int(rb.w));
+                start = __ldg(starts + q);
                 b.key = hit_key(r.tmax, 0);
                 b.id = -1;
                 b.u = b.v = -1.0f;
@@ -433,7 +461,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_heavy(HeavyArgs a) {
             }
             if (a.sl.lists) {
                 const int4 ph = make_int4(h.id, __float_as_int(h.u), __float_as_int(h.v), __float_as_int(h.t));
-                shade_setup_pixel(a.sl, a.cam, ph, lane == 0, i, j, idx);
+                shade_setup_pixel(a.sl, a.cam, ph, lane == 0, i, j, idx, 1u);
             }
         } else if (kind == kHeavyRay) {
             const RayState r = load_ray(a.rays, idx, true);
@@ -488,7 +516,7 @@ __global__ void __launch_bounds__(kTeamThreads) k_trace_heavy_team(HeavyArgs a) 
             }
             if (a.sl.lists && tid < 32) {
                 const int4 ph = make_int4(h.id, __float_as_int(h.u), __float_as_int(h.v), __float_as_int(h.t));
-                shade_setup_pixel(a.sl, a.cam, ph, tid == 0, i, j, idx);
+                shade_setup_pixel(a.sl, a.cam, ph, tid == 0, i, j, idx, 1u);
             }
         } else if (kind == kHeavyRay) {
             const RayState r = load_ray(a.rays, idx, true);
@@ -539,10 +567,14 @@ rt_status ensure_shade_lists(rt_ctx* ctx, rt_lbvh* l, size_t px) {
                        l->s_pixels, px);
     RT_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (l->s_lists) cudaFree(l->s_lists);
+    if (l->s_rays) cudaFree(l->s_rays);
     l->s_lists = nullptr;
+    l->s_rays = nullptr;
     l->s_pixels = 0;
-    // shadow-ray pixels, mirror-ray pixels, primary leaves of a frame
-    RT_CHECK_CUDA(ctx, cudaMalloc((void**)&l->s_lists, 3 * sizeof(uint32_t) * px));
+    // shadow-ray pixels, mirror-ray pixels, primary leaves of a frame, start
+    // nodes of the listed rays (2 x px); the listed rays (2 x px x 32 bytes)
+    RT_CHECK_CUDA(ctx, cudaMalloc((void**)&l->s_lists, 5 * sizeof(uint32_t) * px));
+    RT_CHECK_CUDA(ctx, cudaMalloc((void**)&l->s_rays, 4 * sizeof(float4) * px));
     l->s_pixels = px;
     return RT_OK;
 }
@@ -768,7 +800,9 @@ rt_status trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* ca
         if (!prebuilt) {
             const uint32_t sblocks = std::max(1u, std::min((tiles + 7) / 8, (uint32_t)ctx->num_sms * 8));
             k_shade_setup<<<sblocks, 256, 0, ctx->stream>>>(l->src_tris, *cam, light[0], light[1], light[2], d_primary,
-                                                             d_vis, d_mirror, d_mirror_leaves, l->s_lists, cap, counts,
+                                                             d_vis, d_mirror, d_mirror_leaves, d_prim_leaves,
+                                                             l->s_lists, cap, counts, l->s_rays,
+                                                             l->s_lists + 3 * l->s_pixels,
                                                              tiles);
             RT_CHECK_LAUNCH(ctx, "k_shade_setup");
         }
@@ -779,6 +813,7 @@ rt_status trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* ca
         launch_pdl(k_trace_shade, (uint32_t)per_sm * ctx->num_sms, kTraceThreads, 0, ctx->stream, tree_ref(ctx, l),
                    l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_prim_leaves, d_vis, d_mirror,
                    d_mirror_leaves, (const uint32_t*)l->s_lists, cap, (const uint32_t*)counts,
+                   (const float4*)l->s_rays, (const uint32_t*)(l->s_lists + 3 * l->s_pixels),
                    ctx->d_work + kWorkShade, sp, ctx->d_spill);
         RT_CHECK_LAUNCH(ctx, "k_trace_shade");
     }
@@ -876,8 +911,9 @@ rt_status trace_frame(rt_ctx* ctx, rt_lbvh* l, const rt_camera* cam, const float
     if (!leaves) return trace_primary(ctx, l, cam, d_primary, nullptr, nullptr, who);
     if (!l->src_tris) return rt_fail(ctx, RT_ERR_INVALID, "%s: no triangle soup bound", who);
     // the primary pass (and its warp-per-ray pass) fills the shading lists
-    ShadeLists sl{l->src_tris, light[0], light[1], light[2], d_vis, d_mirror, l->s_lists, (uint32_t)l->s_pixels,
-                  ctx->d_work + kShadeCounts};
+    ShadeLists sl{l->src_tris, light[0], light[1], light[2], d_vis,     d_mirror,
+                  l->s_lists, (uint32_t)l->s_pixels, ctx->d_work + kShadeCounts, l->s_rays,
+                  l->s_lists + 3 * l->s_pixels};
     // the shading pass's counters are zeroed with the primary pass's
     const Spill ssp = spill_of(ctx, px <= kHeavyIndexMask, 1);
     rt_status s = trace_primary(ctx, l, cam, d_primary, leaves, nullptr, who, &sl, shade_reset_bits(ctx, ssp));

@@ -123,3 +123,16 @@ def test_errors(gpu_ctx):
         gpu_ctx.check()
     assert e.value.status == L.RT_ERR_NONFINITE
     gpu_ctx.check()  # the flag was cleared
+
+
+def test_context_setter_errors(gpu_ctx):
+    """The context's tuning setters refuse out-of-range arguments and leave
+    the previous setting in place."""
+    from rtgpu import _lib as L
+    for call in (lambda: gpu_ctx.set_trace_budget(10, kind=3), lambda: gpu_ctx.set_heavy_block(8)):
+        with pytest.raises(L.RtError) as e:
+            call()
+        assert e.value.status == L.RT_ERR_INVALID
+    assert L.lib().rt_ctx_set_tile_order(gpu_ctx.h, 8) == L.RT_ERR_INVALID
+    gpu_ctx.set_heavy_block(None)
+    gpu_ctx.set_trace_budget(None)
