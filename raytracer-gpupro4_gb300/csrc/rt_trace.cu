@@ -229,10 +229,10 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_secondary(
 // primary hit: visibility 0 and the mirror miss record; light behind the
 // surface: visibility 1) and appends the pixels that cast a shadow ray and
 // those that cast a mirror ray to two lists, a warp's pixels in order, so
-// neighbouring rays stay neighbours.  k_trace_shade then traces the lists
-// 32 rays per warp with every lane busy (the tile pass leaves the lanes of
-// sky pixels and of pixels without a cast ray idle), rebuilding each ray from
-// its pixel exactly as the tile pass does.
+// neighbouring rays stay neighbours, each with the ray the tile pass would
+// cast and its start node.  k_trace_shade then traces the lists 32 rays per
+// warp with every lane busy (the tile pass leaves the lanes of sky pixels and
+// of pixels without a cast ray idle).
 __global__ void __launch_bounds__(256) k_shade_setup(const float* __restrict__ soup, rt_camera cam, float lx, float ly,
                                                      float lz, const rt_hit* __restrict__ prim, uint8_t* __restrict__ vis,
                                                      rt_hit* __restrict__ mirror, uint32_t* __restrict__ mirror_leaves,
