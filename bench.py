@@ -600,7 +600,9 @@ def run_batch(args, dist: Dist):
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": ncu_traffic(dom),
                      "algorithmic_bytes_per_launch": int(byts), "avg_launch_ms": round(float(ms), 4)},
         "e2e": e2e,
-        "gpu_launches": 13 * args.steps,  # 12 build kernels + k_batch_trace per graph
+        # per graph: 12 build kernels, k_reset_words, k_batch_trace (primary rays, listing the
+        # shadow rays), k_trace_shade (the shadow rays)
+        "gpu_launches": 15 * args.steps,
     }
     out["clocks"] = clk.summary()
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:

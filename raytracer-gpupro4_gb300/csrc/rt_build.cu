@@ -1650,7 +1650,7 @@ extern "C" rt_status rt_batch_destroy(rt_batch* b) {
 void free_batch(rt_batch* b) {
     void* ptrs[] = {b->tri_off, b->node_off, b->chunks, b->nodes, b->keys, b->ids, b->keys_alt, b->ids_alt,
                     b->ids_local, b->sorted_tris, b->sbounds, b->counters, b->hist, b->lookback, b->scan,
-                    b->leaf_list, b->arrive, b->cams, b->lights};
+                    b->leaf_list, b->arrive, b->cams, b->lights, b->s_lists, b->s_rays};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete b;

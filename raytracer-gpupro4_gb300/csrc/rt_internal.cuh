@@ -197,6 +197,12 @@ struct rt_batch {
     rt_camera* cams = nullptr;      // S, device
     float* lights = nullptr;        // 3 S, device
     uint32_t width = 0, height = 0;
+    // the shadow rays of a batched trace, listed by the primary pass (batch
+    // pixel s * width * height + p, ray, start node) for the lane-refill
+    // pass; s_cap = 0: no list (the primary pass traces them itself)
+    uint32_t* s_lists = nullptr;    // s_cap pixels, then s_cap start nodes
+    float4* s_rays = nullptr;       // 2 s_cap
+    uint32_t s_cap = 0;
     rt_batch_tuning tuning = {128u, 0u, 1u, 0u};
 };
 

@@ -266,13 +266,25 @@ __global__ void __launch_bounds__(256) k_shade_setup(const float* __restrict__ s
 // lanes, or without the register cap, is slower.
 constexpr int kRefillLanes = 16;
 
+// The scenes of a batch as seen by k_trace_shade (nodes == nullptr: one tree):
+// a listed pixel g belongs to scene g / px, whose heap is at nodes + (s <<
+// depth) and whose triangles are [tri_off[s], tri_off[s + 1]) of the batch's
+// sorted-triangle array.
+struct BatchTrees {
+    const rt_node* nodes;
+    const uint32_t* tri_off;
+    uint32_t depth, px;
+};
+
+template <bool BATCH>
 __global__ void __launch_bounds__(kTraceThreads, 7) k_trace_shade(
-    TreeRef tr, const float* __restrict__ soup, rt_camera cam, float lx, float ly, float lz,
+    TreeRef tr0, const float* __restrict__ soup, rt_camera cam, float lx, float ly, float lz,
     const rt_hit* __restrict__ prim, const uint32_t* __restrict__ prim_leaves, uint8_t* __restrict__ vis,
     rt_hit* __restrict__ mirror, uint32_t* __restrict__ mirror_leaves, const uint32_t* __restrict__ lists,
     uint32_t cap, const uint32_t* counts, const float4* __restrict__ rays, const uint32_t* __restrict__ starts,
-    uint32_t* work, Spill spill, uint32_t* __restrict__ list) {
+    uint32_t* work, Spill spill, uint32_t* __restrict__ list, BatchTrees bt) {
     grid_dep_wait();
+    TreeRef tr = tr0;  // per lane: a batch's lanes may walk different scenes
     constexpr uint32_t kFull = 0xffffffffu;
     const uint32_t ns = min(counts[0], cap), nm = min(counts[1], cap), total = ns + nm;
     const int lane = threadIdx.x & 31;
@@ -307,6 +319,12 @@ __global__ void __launch_bounds__(kTraceThreads, 7) k_trace_shade(
                 shadow = k < ns;
                 const uint32_t q = shadow ? k : cap + (k - ns);  // list slot: pixel, ray, start node
                 p = __ldg(lists + q);
+                if (BATCH) {
+                    const uint32_t sc = p / bt.px;
+                    tr.nodes = bt.nodes + ((size_t)sc << bt.depth);
+                    tr.tri_base = __ldg(bt.tri_off + sc);
+                    tr.n = __ldg(bt.tri_off + sc + 1);
+                }
                 const float4 ra = __ldg(rays + 2 * (size_t)q), rb = __ldg(rays + 2 * (size_t)q + 1);
                 r = make_ray(mk3(ra.x, ra.y, ra.z), mk3(rb.x, rb.y, rb.z), ra.w, __float_as_int(rb.w));
                 start = __ldg(starts + q);
@@ -582,6 +600,7 @@ rt_status ensure_shade_lists(rt_ctx* ctx, rt_lbvh* l, size_t px) {
 TreeRef tree_ref(const rt_ctx* ctx, const rt_lbvh* l) {
     TreeRef t;
     t.compact = l->compact_valid;
+    t.tri_base = 0;
     t.nodes = t.compact ? l->cnodes : l->nodes;
     t.num_nodes = t.compact ? l->ccap : l->num_nodes;
     t.tris = l->sorted_tris;
@@ -807,14 +826,15 @@ rt_status trace_shadow_mirror(rt_ctx* ctx, const rt_lbvh* l, const rt_camera* ca
             RT_CHECK_LAUNCH(ctx, "k_shade_setup");
         }
         int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_shade, kTraceThreads, 0) != cudaSuccess ||
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_shade<false>, kTraceThreads, 0) !=
+                cudaSuccess ||
             per_sm < 1)
             per_sm = 1;
-        launch_pdl(k_trace_shade, (uint32_t)per_sm * ctx->num_sms, kTraceThreads, 0, ctx->stream, tree_ref(ctx, l),
+        launch_pdl(k_trace_shade<false>, (uint32_t)per_sm * ctx->num_sms, kTraceThreads, 0, ctx->stream, tree_ref(ctx, l),
                    l->src_tris, *cam, light[0], light[1], light[2], d_primary, d_prim_leaves, d_vis, d_mirror,
                    d_mirror_leaves, (const uint32_t*)l->s_lists, cap, (const uint32_t*)counts,
-                   (const float4*)l->s_rays, (const uint32_t*)(l->s_lists + 3 * l->s_pixels),
-                   ctx->d_work + kWorkShade, sp, ctx->d_spill);
+                   (const float4*)l->s_rays, (const uint32_t*)(l->s_lists + 3 * l->s_pixels), ctx->d_work + kWorkShade,
+                   sp, ctx->d_spill, BatchTrees{nullptr, nullptr, 0u, 0u});
         RT_CHECK_LAUNCH(ctx, "k_trace_shade");
     }
     HeavyArgs a = heavy_args(ctx, l);
@@ -1134,6 +1154,7 @@ extern "C" rt_status rt_trace_frame_shader_order(rt_ctx* ctx, const rt_lbvh* l, 
     uint32_t* leaves = l->s_lists + 2 * l->s_pixels;
     TreeRef tr;  // the reference's walk runs over the heap
     tr.compact = false;
+    tr.tri_base = 0;
     tr.nodes = l->nodes;
     tr.num_nodes = l->num_nodes;
     tr.tris = l->sorted_tris;
@@ -1158,8 +1179,11 @@ extern "C" rt_status rt_trace_frame_shader_order(rt_ctx* ctx, const rt_lbvh* l, 
 // Batched trace: primary + shadow rays of every pixel of every scene of an
 // rt_batch.  A work item is one 8 x 4 tile of one scene; warps take `grab`
 // consecutive items per increment of one work counter, so the scenes with
-// the costliest rays never hold the grid back.  The primary hit stays in
-// registers for the shadow ray of the same pixel.
+// the costliest rays never hold the grid back.  The primary pass lists the
+// pixels that cast a shadow ray (with the ray and its start node, the
+// primary leaf) and the lane-refill kernel traces them, lanes of one warp
+// walking different scenes: in the tile pass only one lane in seven had a
+// shadow ray to trace.  Without a list the tile pass traces them itself.
 namespace {
 
 struct BatchTraceArgs {
@@ -1175,7 +1199,21 @@ struct BatchTraceArgs {
     uint32_t S, depth, width, height, tiles_per_scene, grab, order;
 };
 
-__global__ void __launch_bounds__(256) k_batch_trace(BatchTraceArgs a, uint32_t* work) {
+// The shadow-ray list of a batched trace.  (A separate kernel argument:
+// with these fields inside BatchTraceArgs the compiler gives k_batch_trace
+// 78 registers instead of 64, and its primary rays run 20 % slower.)
+struct BatchListArgs {
+    uint32_t* lists;
+    uint32_t cap;
+    uint32_t* counts;
+    float4* rays;
+    uint32_t* starts;
+};
+
+// LIST: the shadow rays are listed (a.lists set), else traced here (a.vis
+// set) or not cast (a.vis null).
+template <bool LIST>
+__device__ __forceinline__ void batch_trace_body(const BatchTraceArgs& a, const BatchListArgs& la, uint32_t* work) {
     const uint32_t total = a.S * a.tiles_per_scene;
     const uint32_t lane = threadIdx.x & 31;
     const size_t px = (size_t)a.width * a.height;
@@ -1191,6 +1229,7 @@ __global__ void __launch_bounds__(256) k_batch_trace(BatchTraceArgs a, uint32_t*
             const uint32_t toff = __ldg(a.tri_off + s);
             TreeRef tr;
             tr.compact = false;
+            tr.tri_base = 0;
             tr.nodes = a.nodes + ((size_t)s << a.depth);
             tr.tris = a.sorted_tris + 3 * (size_t)toff;
             tr.num_nodes = 1u << a.depth;
@@ -1206,7 +1245,13 @@ __global__ void __launch_bounds__(256) k_batch_trace(BatchTraceArgs a, uint32_t*
             const Hit h = trace_ray<false>(r, valid, tr, false, &nb, &nt, nullptr, nullptr, 1u, &leaf);
             const size_t p = (size_t)j * a.width + i;
             if (valid) store_hit(a.hits + s * px + p, h);
-            if (a.vis) {  // uniform across the grid; the shadow ray restarts at the primary leaf
+            if (LIST) {  // the shadow ray (restarting at the primary leaf) goes to the list
+                const int4 ph = make_int4(h.id, __float_as_int(h.u), __float_as_int(h.v), __float_as_int(h.t));
+                const ShadeLists sl{a.soup + 9 * (size_t)toff, __ldg(a.lights + 3 * s), __ldg(a.lights + 3 * s + 1),
+                                    __ldg(a.lights + 3 * s + 2), a.vis, nullptr, la.lists, la.cap, la.counts,
+                                    la.rays, la.starts};
+                shade_setup_pixel(sl, cam, ph, valid, i, j, s * px + p, h.id >= 0 ? leaf : 1u);
+            } else if (a.vis) {  // uniform across the grid; the shadow ray restarts at the primary leaf
                 const int4 ph = make_int4(h.id, __float_as_int(h.u), __float_as_int(h.v), __float_as_int(h.t));
                 secondary_pixel<false>(tr, a.soup + 9 * (size_t)toff, cam, __ldg(a.lights + 3 * s),
                                        __ldg(a.lights + 3 * s + 1), __ldg(a.lights + 3 * s + 2), ph,
@@ -1215,6 +1260,17 @@ __global__ void __launch_bounds__(256) k_batch_trace(BatchTraceArgs a, uint32_t*
             }
         }
     }
+}
+
+__global__ void __launch_bounds__(256) k_batch_trace(BatchTraceArgs a, uint32_t* work) {
+    grid_dep_wait();
+    const BatchListArgs none = {nullptr, 0u, nullptr, nullptr, nullptr};
+    batch_trace_body<false>(a, none, work);
+}
+
+__global__ void __launch_bounds__(256) k_batch_list(BatchTraceArgs a, BatchListArgs la, uint32_t* work) {
+    grid_dep_wait();
+    batch_trace_body<true>(a, la, work);
 }
 
 }  // namespace
@@ -1232,6 +1288,22 @@ extern "C" rt_status rt_batch_set_views(rt_ctx* ctx, rt_batch* b, const rt_camer
     RT_CHECK_CUDA(ctx, cudaMemcpyAsync(b->cams, h_cams, sizeof(rt_camera) * b->S, cudaMemcpyHostToDevice, ctx->stream));
     RT_CHECK_CUDA(ctx, cudaMemcpyAsync(b->lights, h_lights, sizeof(float) * 3 * b->S, cudaMemcpyHostToDevice,
                                        ctx->stream));
+    // the shadow-ray list: one entry per pixel of the batch at most
+    const uint64_t cap = (uint64_t)w * h * b->S;
+    if (cap > b->s_cap && cap <= (1ull << 31)) {
+        if (b->graph_refs > 0)
+            return rt_fail(ctx, RT_ERR_CAPACITY,
+                           "rt_batch_set_views: the shadow-ray list cannot grow while a captured frame uses it");
+        RT_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (b->s_lists) cudaFree(b->s_lists);
+        if (b->s_rays) cudaFree(b->s_rays);
+        b->s_lists = nullptr;
+        b->s_rays = nullptr;
+        b->s_cap = 0;
+        RT_CHECK_CUDA(ctx, cudaMalloc((void**)&b->s_lists, 2 * sizeof(uint32_t) * cap));
+        RT_CHECK_CUDA(ctx, cudaMalloc((void**)&b->s_rays, 2 * sizeof(float4) * cap));
+        b->s_cap = (uint32_t)cap;
+    }
     b->width = w;
     b->height = h;
     return RT_OK;
@@ -1260,7 +1332,13 @@ extern "C" rt_status rt_batch_trace(rt_ctx* ctx, const rt_batch* b, rt_hit* d_hi
     if (!b || !d_hits) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_trace: null argument");
     if (!b->built) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_trace: the batch has not been built");
     if (b->width == 0) return rt_fail(ctx, RT_ERR_INVALID, "rt_batch_trace: no views set (rt_batch_set_views)");
-    rt_status s = reset_work(ctx, kWorkBatch);
+    const uint64_t cap = (uint64_t)b->width * b->height * b->S;
+    const bool listed = d_vis && b->s_cap >= cap && cap > 0;
+    uint32_t* counts = ctx->d_work + kShadeCounts;
+    uint64_t reset = word_bit(ctx, ctx->d_work + kWorkBatch);
+    if (listed)
+        reset |= word_bit(ctx, ctx->d_work + kWorkShade) | word_bit(ctx, counts) | word_bit(ctx, counts + 1);
+    rt_status s = reset_words(ctx, reset);
     if (s != RT_OK) return s;
     BatchTraceArgs a;
     a.nodes = b->nodes;
@@ -1279,15 +1357,45 @@ extern "C" rt_status rt_batch_trace(rt_ctx* ctx, const rt_batch* b, rt_hit* d_hi
     a.tiles_per_scene = ((b->width + 7) / 8) * ((b->height + 3) / 4);
     a.grab = b->tuning.grab;
     a.order = b->tuning.order;
+    const BatchListArgs la = {b->s_lists, (uint32_t)cap, counts, b->s_rays, b->s_lists + cap};
     const int threads = (int)b->tuning.threads;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_trace, threads, 0) != cudaSuccess || per_sm < 1)
-        per_sm = 1;
+    const cudaError_t oe = listed ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_list, threads, 0)
+                                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_trace, threads, 0);
+    if (oe != cudaSuccess || per_sm < 1) per_sm = 1;
     if (b->tuning.blocks_per_sm) per_sm = std::min(per_sm, (int)b->tuning.blocks_per_sm);
     const uint64_t items = (uint64_t)a.S * a.tiles_per_scene;
     const uint64_t need = (items * 32 + threads - 1) / threads;
     const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)per_sm * ctx->num_sms, need));
-    k_batch_trace<<<blocks, threads, 0, ctx->stream>>>(a, ctx->d_work + kWorkBatch);
+    if (listed)
+        launch_pdl(k_batch_list, blocks, threads, 0, ctx->stream, a, la, ctx->d_work + kWorkBatch);
+    else
+        launch_pdl(k_batch_trace, blocks, threads, 0, ctx->stream, a, ctx->d_work + kWorkBatch);
     RT_CHECK_LAUNCH(ctx, "k_batch_trace");
+    if (!listed) return RT_OK;
+    TreeRef tr;  // the batch's whole sorted-triangle array; nodes, tri_base and n set per lane
+    tr.compact = false;
+    tr.tri_base = 0;
+    tr.nodes = b->nodes;
+    tr.tris = b->sorted_tris;
+    tr.num_nodes = 1u << b->depth;
+    tr.n = 0;
+    tr.err = ctx->d_err;
+    Spill none;
+    memset(&none, 0, sizeof(none));
+    int shade_per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&shade_per_sm, k_trace_shade<true>, kTraceThreads, 0) !=
+            cudaSuccess ||
+        shade_per_sm < 1)
+        shade_per_sm = 1;
+    rt_camera cam0;
+    memset(&cam0, 0, sizeof(cam0));
+    launch_pdl(k_trace_shade<true>, (uint32_t)shade_per_sm * ctx->num_sms, kTraceThreads, 0, ctx->stream, tr,
+               (const float*)nullptr, cam0, 0.0f, 0.0f, 0.0f, (const rt_hit*)nullptr, (const uint32_t*)nullptr, d_vis,
+               (rt_hit*)nullptr, (uint32_t*)nullptr, (const uint32_t*)b->s_lists, (uint32_t)cap,
+               (const uint32_t*)counts, (const float4*)b->s_rays, (const uint32_t*)(b->s_lists + cap),
+               ctx->d_work + kWorkShade, none, (uint32_t*)nullptr,
+               BatchTrees{b->nodes, b->tri_off, b->depth, b->width * b->height});
+    RT_CHECK_LAUNCH(ctx, "k_trace_shade");
     return RT_OK;
 }

@@ -37,6 +37,11 @@ struct TreeRef {
     // compact layout: the children of an internal node are the pair at
     // slots PrimPos, PrimPos + 1 (even), not at heap slots 2i, 2i + 1
     bool compact;
+    // added to every leaf's PrimPos by the per-lane walk: one scene of a
+    // batch read through the batch's whole sorted-triangle array (its
+    // triangles are [tri_base, n)); 0 otherwise, and 0 for the warp- and
+    // block-per-ray walks
+    uint32_t tri_base;
 };
 
 // First slot of the children pair of internal node `node` whose record's
@@ -178,10 +183,11 @@ __device__ __forceinline__ bool leaf_phase(const TreeRef& tr_, const RayState& r
     if (have) {
         cnt = __float_as_int(cur.b.z) >> 3;
         pos = __float_as_int(cur.b.w);
-        if (pos < 0 || cnt < 0 || (uint32_t)pos + (uint32_t)cnt > tr_.n) {
+        if (pos < 0 || cnt < 0 || (uint32_t)pos + tr_.tri_base + (uint32_t)cnt > tr_.n) {
             atomicOr(tr_.err, RT_DEVERR_BOUNDS);
             cnt = 0;
         }
+        pos += (int)tr_.tri_base;
     }
     ntri += (uint32_t)cnt;
     bool improved = false;

@@ -412,6 +412,7 @@ extern "C" rt_status rt_render_whitted(rt_ctx* ctx, const rt_lbvh* l, const rt_c
     // the walks restart at heap nodes: use the heap even when a compact layout exists
     TreeRef tr;
     tr.compact = false;
+    tr.tri_base = 0;
     tr.nodes = l->nodes;
     tr.num_nodes = l->num_nodes;
     tr.tris = l->sorted_tris;
