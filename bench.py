@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--frames", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-components", action="store_true",
+                    help="frame workload: skip the batched / path-traced / adjoint component runs")
     return ap.parse_args()
 
 
@@ -158,18 +160,32 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def _ncu_summary() -> dict:
+    p = ROOT / "profiles" / "ncu_traffic.json"
+    try:
+        return json.loads(p.read_text())
+    except (ValueError, OSError):
+        return {}
+
+
 def ncu_traffic(*kernels: str):
     """Per-launch DRAM traffic (read + write bytes) of a stage's kernels, summed,
     from the committed ncu summary; None when one of them was not captured."""
-    p = ROOT / "profiles" / "ncu_traffic.json"
-    if not p.exists():
-        return None
-    try:
-        d = json.loads(p.read_text())
-    except (ValueError, OSError):
-        return None
+    d = _ncu_summary().get("dram_bytes", {})
     vals = [d.get(k) for k in kernels]
     return None if any(v is None for v in vals) else int(sum(vals))
+
+
+def ncu_cache_fractions(kernel: str):
+    """L1 / L2 throughput of a kernel (percent of peak) from the committed ncu
+    summary: the trace kernels are L1/L2-latency-bound, so these are their
+    real utilisation figures beside the HBM-roofline fraction."""
+    d = _ncu_summary()
+    l1, l2 = d.get("l1_pct", {}).get(kernel), d.get("l2_pct", {}).get(kernel)
+    if l1 is None and l2 is None:
+        return None
+    return {"kernel": kernel, "l1_throughput_pct": l1, "l2_throughput_pct": l2,
+            "active_lanes_of_32": d.get("active_lanes", {}).get(kernel)}
 
 
 # ---------------------------------------------------------------------------
@@ -235,6 +251,15 @@ def run_ours(args, dist: Dist):
     bytes_primary = 32 * pst[0] + 40 * pst[1] + 32 * n_prim
     bytes_secondary = 32 * (sst[0] + mst[0]) + 40 * (sst[1] + mst[1]) + 32 * (n_shadow + n_mirror)
     rays_per_frame = n_prim + n_shadow + n_mirror
+    # the same figure on this project's own walk (split-axis child order, any-hit
+    # shadow rays, shading rays restarted at the primary leaf): its counting
+    # variants' box and triangle tests per ray
+    ohits, oleaves, opst = rt.primary_leaves(lb, cam, stats=True)
+    _, _, _, osst, omst = rt.shadow_mirror_from(lb, cam, light, ohits, oleaves, stats=True)
+    ctx.check()
+    opst, osst, omst = (x.to(torch.int64).sum(0).tolist() for x in (opst, osst, omst))
+    own_primary = 32 * opst[0] + 40 * opst[1] + 32 * n_prim
+    own_secondary = 32 * (osst[0] + omst[0]) + 40 * (osst[1] + omst[1]) + 32 * (n_shadow + n_mirror)
 
     stream = torch.cuda.current_stream(dev)
 
@@ -361,20 +386,36 @@ def run_ours(args, dist: Dist):
     ms, byts, kern = groups[dom]
     achieved = byts / (ms / 1e3) / 1e9
     frame_bytes = BUILD_BYTES_PER_TRI * n + bytes_primary + bytes_secondary
+    own_frame_bytes = BUILD_BYTES_PER_TRI * n + own_primary + own_secondary
     frame_ms = float(step_ms.mean())
+
+    def frac(b, t_ms):
+        return round(b / (t_ms / 1e3) / 1e9 / peak, 4)
+
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                 "traffic": ncu_traffic(*kern), "algorithmic_bytes_per_launch": int(byts),
                 "avg_launch_ms": round(float(ms), 4),
+                "bytes_defined_on": "node visits and triangle tests of the reference's own walk (LBVH_IntersectP order)",
+                "cache": ncu_cache_fractions(kern[0]),
                 "frame": {"algorithmic_bytes": int(frame_bytes), "ms": round(frame_ms, 4),
                           "achieved": round(frame_bytes / (frame_ms / 1e3) / 1e9, 1),
-                          "frac": round(frame_bytes / (frame_ms / 1e3) / 1e9 / peak, 4)}}
+                          "frac": frac(frame_bytes, frame_ms)},
+                # the same fractions with the trace bytes of this project's own walk
+                "own_walk": {"frame_algorithmic_bytes": int(own_frame_bytes), "frame_frac": frac(own_frame_bytes, frame_ms),
+                             "primary_frac": frac(own_primary, prim_ms), "shading_frac": frac(own_secondary, sec_ms)},
+                "stages": {"build": {"ms": round(float(build_ms), 4), "frac": frac(BUILD_BYTES_PER_TRI * n, build_ms),
+                                     "traffic": ncu_traffic(*groups["build (10 kernels)"][2])},
+                           "primary": {"ms": round(float(prim_ms), 4), "frac": frac(bytes_primary, prim_ms),
+                                       "cache": ncu_cache_fractions("k_trace_primary")},
+                           "shading": {"ms": round(float(sec_ms), 4), "frac": frac(bytes_secondary, sec_ms),
+                                       "cache": ncu_cache_fractions("k_trace_shade")}}}
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mtri/s", "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(float(step_ms.mean()), 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-        "config": {"workload": name, "triangles": n, "pixels": npx, "depth": args.depth,
-                   "l2": "flushed between steps (256 MiB write outside the per-step events)",
+        "config": frame_config(name, n, npx, args.depth),
+        "timing": {"l2": "flushed between steps (256 MiB write outside the per-step events)",
                    "parallelism": "replicas" if dist.world > 1 else "single GPU"},
         "components": {"graph_frame_ms": round(float(step_ms.mean()), 4), "stream_frame_ms": round(stream_frame_ms, 4),
                        "build_ms": round(float(build_ms), 4), "build_mtri_s": round(n / build_ms / 1e3, 2),
@@ -394,7 +435,28 @@ def run_ours(args, dist: Dist):
         out["cpu_baseline"] = cpu_frame_baseline(frames[0], cam, light, args.depth, n)
     lb.close()
     ctx.close()
+    del dfr, host, graphs
+    if args.workload == "frame" and not args.no_components and dist.world == 1:
+        # the other forms, each on its own workload, timed the same way
+        # (CUDA events on the launching stream, L2 flushed between steps)
+        comps = out["components"]
+        for key, fn in (("batched", lambda: run_batch(args, dist)), ("pt", lambda: run_pt(args, dist)),
+                        ("adjoint", lambda: run_pt(args, dist, adjoint=True))):
+            torch.cuda.empty_cache()
+            comps[key] = component_summary(fn())
+            out["gpu_launches"] += comps[key].get("gpu_launches", 0)
     return out
+
+
+def frame_config(name, n, npx, depth):
+    return {"workload": name, "triangles": n, "pixels": npx, "depth": depth}
+
+
+def component_summary(r: dict) -> dict:
+    """One form's bench line, nested under the headline's components."""
+    keep = ("value", "unit", "ms_per_step", "steps", "warmup", "config", "components", "roofline", "e2e",
+            "cpu_baseline", "clocks", "gpu_launches")
+    return {k: r[k] for k in keep if k in r}
 
 
 # ---------------------------------------------------------------------------
@@ -578,7 +640,7 @@ def run_batch(args, dist: Dist):
         frame.close()
 
     peak, peak_kind = measured_peaks()
-    groups = {"k_batch_trace": (trace_ms, trace_bytes), "batched build (9 kernels)": (build_ms, BUILD_BYTES_PER_TRI * total)}
+    groups = {"k_batch_trace": (trace_ms, trace_bytes), "batched build (12 kernels)": (build_ms, BUILD_BYTES_PER_TRI * total)}
     dom = max(groups, key=lambda g: groups[g][0])
     ms, byts = groups[dom]
     achieved = byts / (ms / 1e3) / 1e9
@@ -586,8 +648,8 @@ def run_batch(args, dist: Dist):
         "metric": METRIC, "value": round(value, 3), "unit": "Mtri/s", "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(float(step_ms.mean()), 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded random soups)",
-        "config": {"workload": name, "scenes": S, "triangles": total, "pixels_per_scene": npx, "depth": args.depth,
-                   "l2": "flushed between steps (256 MiB write outside the per-step events); inputs 346 MB > L2",
+        "config": batch_config(name, S, total, npx, args.depth),
+        "timing": {"l2": "flushed between steps (256 MiB write outside the per-step events); inputs 416 MB > L2",
                    "parallelism": "replicas" if dist.world > 1 else "single GPU"},
         "components": {"graph_frame_ms": round(float(step_ms.mean()), 4), "build_ms": round(float(build_ms), 4),
                        "trace_ms": round(float(trace_ms), 4), "build_mtri_s": round(total / build_ms / 1e3, 1),
@@ -606,11 +668,16 @@ def run_batch(args, dist: Dist):
     }
     out["clocks"] = clk.summary()
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_batch_baseline(soup, off, cams, lights, args.depth)
+        out["cpu_baseline"] = cpu_batch_baseline(soup, off, cams, lights, args.depth,
+                                                 budget_s=8.0 if args.workload == "frame" else 15.0)
     b.close()
     lb.close()
     ctx.close()
     return out
+
+
+def batch_config(name, scenes_n, total, npx, depth):
+    return {"workload": name, "scenes": scenes_n, "triangles": total, "pixels_per_scene": npx, "depth": depth}
 
 
 def cpu_batch_baseline(soup, off, cams, lights, depth, budget_s: float = 15.0):
@@ -710,7 +777,7 @@ def run_reference(args, dist: Dist):
     return {"metric": METRIC, "value": round(value, 4), "unit": "Mtri/s", "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": {"workload": name, "triangles": n, "pixels": cam.width * cam.height, "depth": args.depth},
+            "config": frame_config(name, n, cam.width * cam.height, args.depth),
             "impl": "reference",
             "cpu_baseline": {"value": round(value, 4), "unit": "Mtri/s", "cores": nth, "kind": kind,
                              "sample": "every step one full frame: LBVH build on 1 thread, primary/shadow/mirror "
@@ -760,7 +827,7 @@ def run_reference_batch(args, dist: Dist, O):
     return {"metric": METRIC, "value": round(value, 4), "unit": "Mtri/s", "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded random soups)",
-            "config": {"workload": name, "scenes": len(sizes), "triangles": int(sizes.sum()), "depth": args.depth},
+            "config": batch_config(name, len(sizes), int(sizes.sum()), args.batch_res * args.batch_res, args.depth),
             "impl": "reference",
             "cpu_baseline": {"value": round(value, 4), "unit": "Mtri/s", "cores": nth, "kind": kind,
                              "sample": f"every step {per_step} scenes of the batch (rotating): LBVH build on 1 thread, "
@@ -773,7 +840,7 @@ def run_pt(args, dist: Dist, adjoint: bool = False):
     4 bounces), or with adjoint=True the differentiable workload (same scene at
     512x512, 8 spp, 3 bounces: forward render + L2 image loss + adjoint
     gradients w.r.t. every albedo and the emitter radiance).  A step = LBVH
-    rebuild + render (+ backward)."""
+    rebuild + render (+ loss and backward)."""
     import torch
     from rtgpu import scenes
     from rtgpu.api import LBVH, Context, RayTracer
@@ -798,41 +865,44 @@ def run_pt(args, dist: Dist, adjoint: bool = False):
     le = torch.tensor([10.0, 10.0, 10.0], device=dev)
     img = torch.empty((W * H, 4), dtype=torch.float32, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    lb.Build(tris)
+    # walk counts of one render (this project's walk): the algorithmic bytes
+    _, cnt = rt.pathtrace_counted(lb, alb, em, cam, spp, bounces, 999)
     target = None
     if adjoint:
         rng = np.random.Generator(np.random.PCG64(7))
         talb = np.clip(sc.albedo + rng.uniform(-0.1, 0.1, sc.albedo.shape), 0, 1).astype(np.float32)
-        lb.Build(tris)
         with torch.no_grad():
             target = render(torch.from_numpy(talb).to(dev), le, mask, rt, lb, cam, spp, bounces, 12345)
     stream = torch.cuda.current_stream(dev)
-    fwd_ev, bwd_ev = [], []
 
     def step(k, evs=None):
         seed = 1000 + k
         if evs:
             evs[0].record(stream)
         lb.Build(tris)
+        if evs:
+            evs[1].record(stream)
         if adjoint:
             a = alb.clone().requires_grad_(True)
             lp = le.clone().requires_grad_(True)
             out = render(a, lp, mask, rt, lb, cam, spp, bounces, seed)
             if evs:
-                evs[1].record(stream)
+                evs[2].record(stream)
             loss = ((out[:, :3] - target[:, :3]) ** 2).mean()
             loss.backward()
         else:
             rt.pathtrace(lb, alb, em, cam, spp, bounces, seed, out=img)
             if evs:
-                evs[1].record(stream)
+                evs[2].record(stream)
         if evs:
-            evs[2].record(stream)
+            evs[3].record(stream)
 
     for k in range(args.warmup):
         flush.zero_()
         step(k)
     ctx.check()
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
     dist.barrier()
     torch.cuda.synchronize()
     with Clocks(dist.local) as clk:
@@ -842,44 +912,82 @@ def run_pt(args, dist: Dist, adjoint: bool = False):
         torch.cuda.synchronize()
     dist.barrier()
     ctx.check()
-    per = np.array([[e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])] for e in evs])  # ms: build+forward, backward
+    per = np.array([[e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2]), e[2].elapsed_time(e[3])] for e in evs])
+    build_ms, fwd_ms, bwd_ms = (float(x) for x in per.mean(0))
     step_ms = per.sum(1)
     value = replica_rate(dist, W * H * spp * args.steps, float(step_ms.sum()) / 1e3) / 1e6
     name = (f"GI box {n} tris, {W}x{H}, {spp} spp, {bounces} bounces" +
             (", forward + L2 loss + adjoint (albedo x3, emitter radiance)" if adjoint else ""))
+    # algorithmic bytes: per traced segment 32 per box test + 40 per triangle
+    # test + 32 (ray in, hit out); 12 B albedo per hit; 16 B accumulator per
+    # pixel-sample.  The adjoint kernel replays the same walk and adds a 12 B
+    # gradient atomic per hit and the 16 B dL/dI read per pixel.
+    trace_bytes = 32 * cnt["box_tests"] + 40 * cnt["tri_tests"] + 32 * cnt["segments"]
+    fwd_bytes = trace_bytes + 12 * cnt["hits"] + 16 * W * H * spp
+    bwd_bytes = trace_bytes + 24 * cnt["hits"] + 16 * W * H
+    peak, peak_kind = measured_peaks()
+    kern, k_ms, k_bytes = (("k_pathtrace_adjoint", bwd_ms, bwd_bytes) if adjoint else ("k_pathtrace", fwd_ms, fwd_bytes))
+    achieved = k_bytes / (k_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": kern, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": ncu_traffic(kern),
+                "algorithmic_bytes_per_launch": int(k_bytes), "avg_launch_ms": round(k_ms, 4),
+                "bytes_defined_on": "box / triangle tests of this project's walk (rt_pathtrace_counted)",
+                "cache": ncu_cache_fractions(kern),
+                "walk": {k: int(v) for k, v in cnt.items()}}
+    if adjoint:
+        step_bytes = BUILD_BYTES_PER_TRI * n + fwd_bytes + bwd_bytes
+        roofline["step"] = {"algorithmic_bytes": int(step_bytes), "ms": round(float(step_ms.mean()), 4),
+                            "frac": round(step_bytes / (float(step_ms.mean()) / 1e3) / 1e9 / peak, 4)}
+    segs_per_s = cnt["segments"] / (fwd_ms / 1e3) / 1e6
     out = {"metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": dist.world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(float(step_ms.mean()), 4),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded procedural scene)",
            "config": {"workload": name, "triangles": n, "pixels": W * H, "spp": spp, "bounces": bounces,
-                      "depth": args.depth, "l2": "flushed between steps (256 MiB write outside the events)"},
-           "components": {"build_plus_forward_ms": round(float(per[:, 0].mean()), 4),
-                          "segments_per_step_upper_bound": W * H * spp * (bounces + 1)},
-           "clocks": clk.summary(), "gpu_launches": (10 + 1 + (1 if adjoint else 0)) * args.steps}
+                      "depth": args.depth},
+           "timing": {"l2": "flushed between steps (256 MiB write outside the events)"},
+           "components": {"build_ms": round(build_ms, 4), "forward_ms": round(fwd_ms, 4),
+                          "forward_msegments_s": round(segs_per_s, 1)},
+           "roofline": roofline,
+           "clocks": clk.summary(),
+           # per step: 10 build kernels + the render (+ the adjoint kernel)
+           "gpu_launches": (10 + 1 + (1 if adjoint else 0)) * args.steps}
     if adjoint:
-        out["components"]["backward_ms"] = round(float(per[:, 1].mean()), 4)
-        out["components"]["backward_over_forward"] = round(float(per[:, 1].mean() / per[:, 0].mean()), 3)
+        out["components"]["backward_ms"] = round(bwd_ms, 4)
+        out["components"]["backward_over_forward"] = round(bwd_ms / fwd_ms, 3)
+        out["components"]["adjoint_vs_plain"] = {
+            "forward_only_msamples_s": round(W * H * spp / ((build_ms + fwd_ms) / 1e3) / 1e6, 3),
+            "forward_plus_adjoint_msamples_s": round(value, 3)}
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_pt_baseline(sc, cam, spp, bounces, args.depth)
+        out["cpu_baseline"] = cpu_pt_baseline(sc, cam, spp, bounces, args.depth, adjoint=adjoint)
     lb.close()
     ctx.close()
     return out
 
 
-def cpu_pt_baseline(sc, cam, spp, bounces, depth):
-    """The oracle's path tracer on a 128x128 crop of the image, all host cores."""
+def cpu_pt_baseline(sc, cam, spp, bounces, depth, adjoint=False):
+    """The oracle's path tracer (and with adjoint=True its FP64 adjoint) on a
+    128x128 crop of the same image (same pixels and sample streams), all host
+    cores, after the oracle's LBVH build of the scene."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as O
-    from rtgpu import scenes
     O.build_oracle()
     nth = O.nthreads_default()
     nodes, ids, _, _ = O.lbvh_build(sc.tris, depth)
-    crop = scenes.look_at(cam.eye[:], (0.5, 0.5, 1.0), vfov_deg=60.0 * 128 / cam.height, width=128, height=128)
+    win = ((cam.width - 128) // 2, (cam.height - 128) // 2, 128, 128)
     t0 = time.perf_counter()
-    O.pathtrace(nodes, depth, ids, sc.tris, sc.albedo, sc.emission, crop, spp, bounces, 1000, nthreads=nth)
+    img = O.pathtrace(nodes, depth, ids, sc.tris, sc.albedo, sc.emission, cam, spp, bounces, 1000, nthreads=nth,
+                      window=win)
+    if adjoint:
+        g = np.zeros_like(img)
+        g[:, :3] = 1.0 / (cam.width * cam.height * 3)
+        O.pathtrace_adjoint(nodes, depth, ids, sc.tris, sc.albedo, sc.emission, cam, spp, bounces, 1000, g,
+                            nthreads=nth, window=win)
     dt = time.perf_counter() - t0
+    what = "forward + FP64 adjoint" if adjoint else "forward"
     return {"value": round(128 * 128 * spp / dt / 1e6, 4), "unit": "Msamples/s", "cores": nth, "kind": "port",
-            "sample": f"128x128 crop, {spp} spp, {bounces} bounces, {dt:.2f}s on {nth} threads", "cpu": _cpu_name()}
+            "sample": f"128x128 crop, {spp} spp, {bounces} bounces, {what}, {dt:.2f}s on {nth} threads",
+            "cpu": _cpu_name()}
 
 
 def main():

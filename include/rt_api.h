@@ -143,27 +143,60 @@ rt_status rt_lbvh_import_host(rt_ctx* ctx, rt_lbvh* lbvh, const rt_node* h_nodes
                               const float* h_tris, uint32_t n);
 
 /* Allocation-free rebuild.  No counterpart in the reference: it exists for
- * callers that may not allocate device memory when they rebuild -- a host
- * capturing its frame into a CUDA graph, an engine whose allocator owns all
- * device memory, a real-time loop that cannot absorb an allocation's
- * implicit synchronisation.  The caller passes the device soup (n x 9
- * floats) and every output: d_nodes (1 << depth rt_node), d_ids and d_keys
- * (n each), d_sorted_tris (n x 12 floats, the layout of rt_lbvh_view).  The
- * results equal rt_lbvh_build's.  All scratch lives in one fixed device
- * array of 5,577,088 bytes that every GPU loading this library holds until the
- * process exits; n above RT_NOALLOC_MAX_TRIS or depth above
- * RT_NOALLOC_MAX_DEPTH returns RT_ERR_CAPACITY.  The first call on a device
- * looks up that array's device address (cudaGetSymbolAddress), so make it
- * before any stream capture.  Every call reuses the same array and clears
- * what must start at zero; calls that overlap on the GPU race on it and
- * must be serialised by the caller.  ctx may be NULL; if given, it receives
- * the error message (rt_last_error).  Asynchronous on `stream`; calls no
- * allocating routine. */
+ * callers that cannot call cudaMalloc when they rebuild -- an engine whose
+ * own allocator owns all device memory (a caching pool that has reserved
+ * the free memory, or a budgeted heap that must account for every byte),
+ * or a real-time loop that cannot absorb the implicit device-wide
+ * synchronisation of cudaMalloc / cudaFree.  The caller passes the device
+ * soup (n x 9 floats) and every output: d_nodes (1 << depth rt_node), d_ids
+ * and d_keys (n each), d_sorted_tris (n x 12 floats, the layout of
+ * rt_lbvh_view).  The results equal rt_lbvh_build's.  All scratch lives in
+ * one fixed device array of 5,577,088 bytes that every GPU loading this
+ * library holds until the process exits; n above RT_NOALLOC_MAX_TRIS or
+ * depth above RT_NOALLOC_MAX_DEPTH returns RT_ERR_CAPACITY.  flags may hold
+ * RT_BUILD_CLEAR_UNREACHED only (the compact layout needs allocated
+ * buffers: RT_ERR_INVALID).  The first call on a device looks up that
+ * array's device address (cudaGetSymbolAddress, once per device, with the
+ * device current), so make it before any stream capture.  `stream` must
+ * belong to the current device.  Every call reuses the same array and
+ * clears what must start at zero; calls that overlap on the GPU race on it
+ * and must be serialised by the caller.  ctx may be NULL.  If given, it
+ * must be bound to the current device; it receives the error message
+ * (rt_last_error) and the kernels' device-side errors (a non-finite soup,
+ * a look-back wait that gave up), which rt_ctx_check reports.  With
+ * ctx == NULL device-side errors are not reported.  Asynchronous on
+ * `stream`; calls no allocating routine. */
 #define RT_NOALLOC_MAX_TRIS 262144u
 #define RT_NOALLOC_MAX_DEPTH 20u
 rt_status rt_lbvh_build_noalloc(rt_ctx* ctx, void* stream, const float* d_tris, uint32_t n, uint32_t depth,
                                 uint32_t flags, rt_node* d_nodes, uint32_t* d_ids, uint32_t* d_keys,
                                 float* d_sorted_tris);
+
+/* ---- sort stage ------------------------------------------------------ */
+/* Stable LSD radix sort of n (key, value) pairs by the full 32-bit key, in
+ * place: four 8-bit passes (one digit histogram kernel, then per pass
+ * warp-ballot ranks, a bounded decoupled look-back over 4,096-key tiles and
+ * a shared-memory-staged scatter).  Equal keys keep their input order.
+ * Replaces the sort stage of the GPU build, BitonicSort::GPUSort
+ * (RayTracerCS/BitonicSort.cpp:56-117, 45 dispatches over a fixed 512 x 512
+ * array) and RadixSort::Sort (RayTracerCS/RadixSort.cpp:46-74), without
+ * their fixed size.  d_scratch: device memory of at least
+ * rt_radix_sort_scratch_bytes(n) bytes, 16-byte aligned (the caller owns
+ * it; the call allocates nothing).  Asynchronous on the context stream;
+ * a look-back wait that gives up is reported by rt_ctx_check
+ * (RT_ERR_TIMEOUT). */
+size_t rt_radix_sort_scratch_bytes(uint32_t n);
+rt_status rt_radix_sort(rt_ctx* ctx, uint32_t* d_keys, uint32_t* d_values, uint32_t n, void* d_scratch,
+                        size_t scratch_bytes);
+/* Test hook of the bounded look-back wait (no counterpart in the
+ * reference): runs the first radix pass of rt_radix_sort with its first
+ * tile never started, so the second tile's look-back can never complete;
+ * that wait gives up after spin_limit polls, records RT_ERR_TIMEOUT for
+ * rt_ctx_check and returns.  Every access stays inside the buffers; d_keys
+ * and d_values are left untouched (the pass writes into the scratch).
+ * n must exceed 4,096 (two tiles). */
+rt_status rt_radix_sort_stall_test(rt_ctx* ctx, const uint32_t* d_keys, const uint32_t* d_values, uint32_t n,
+                                   void* d_scratch, size_t scratch_bytes, uint32_t spin_limit);
 
 /* Device views (GetPtrToElements / GetOrderedElementsIds, LBVH.h:109-113). */
 typedef struct rt_lbvh_view {
@@ -425,16 +458,35 @@ typedef struct rt_pt_params {
     uint32_t bounces;   /* segments traced per path = bounces + 1 (RayTracerCS.cpp:289) */
     uint64_t seed;
     float sky[3];       /* radiance of a miss; the reference adds white (1,1,1) */
-    uint32_t reserved;
+    uint32_t first_sample;  /* n0: samples already averaged into d_image (0 = start afresh) */
 } rt_pt_params;
 /* d_albedo, d_emission: n x 3 floats indexed by triangle id.
- * d_image: width*height float4 (rgb, 1), progressive mean over spp. */
+ * d_image: width*height float4 (rgb, 1), the progressive mean over samples
+ * n0 .. n0 + spp - 1 blended into the mean of samples 0 .. n0 - 1 that
+ * d_image holds on entry: per sample n the image is scaled by n / (n + 1)
+ * and the sample added with weight 1 / (n + 1), the factors of
+ * cbGlobalIllumination::Update (ConstantBuffers.h:102-109) applied in
+ * CSPrimaryRays.hlsl:62-63.  n0 plays the reference's frame counter
+ * (RayTracerCS.cpp:306), and n0 = 0 its reset on camera motion
+ * (RayTracerCS.cpp:246-250); d_image is not read when n0 = 0.  Sample n of
+ * a pixel has its own PCG32 stream, so two calls of k samples with n0 = 0
+ * and n0 = k give the image of one call of 2k samples, bit for bit. */
 rt_status rt_pathtrace(rt_ctx* ctx, const rt_lbvh* lbvh, const float* d_albedo, const float* d_emission,
                        const rt_camera* cam, const rt_pt_params* p, float* d_image);
+/* rt_pathtrace that also adds its walk counts to d_counts (device, 4 x
+ * uint64, not cleared by the call): segments traced, box tests, triangle
+ * tests, segments that hit a triangle.  Same image; the counting makes it
+ * slower, so it serves measurement (the path tracer's algorithmic bytes are
+ * defined on these counts), not rendering. */
+rt_status rt_pathtrace_counted(rt_ctx* ctx, const rt_lbvh* lbvh, const float* d_albedo, const float* d_emission,
+                               const rt_camera* cam, const rt_pt_params* p, float* d_image,
+                               unsigned long long* d_counts);
 /* Adjoint of rt_pathtrace by path replay: given dL/dImage (width*height
  * float4), accumulates dL/dalbedo (n x 3) and dL/dLe (3 floats: the shared
  * radiance of every emitting triangle) into the output buffers (not
- * cleared by the call). */
+ * cleared by the call).  With n0 = first_sample > 0 it differentiates the
+ * samples n0 .. n0 + spp - 1 of that call (each with its weight in the
+ * final mean); the n0 samples already in the image are constants. */
 rt_status rt_pathtrace_adjoint(rt_ctx* ctx, const rt_lbvh* lbvh, const float* d_albedo, const float* d_emission,
                                const rt_camera* cam, const rt_pt_params* p, const float* d_dimage,
                                float* d_dalbedo, float* d_demission);

@@ -32,7 +32,14 @@ class OrCamera(C.Structure):
 
 
 class OrPtParams(C.Structure):
-    _fields_ = [("spp", C.c_uint32), ("bounces", C.c_uint32), ("seed", C.c_uint64), ("sky", C.c_float * 3)]
+    _fields_ = [("spp", C.c_uint32), ("bounces", C.c_uint32), ("seed", C.c_uint64), ("sky", C.c_float * 3),
+                ("first_sample", C.c_uint32), ("x0", C.c_uint32), ("y0", C.c_uint32), ("win_w", C.c_uint32),
+                ("win_h", C.c_uint32)]
+
+
+def _pt_params(spp, bounces, seed, sky, first_sample, window):
+    x0, y0, w, h = window if window is not None else (0, 0, 0, 0)
+    return OrPtParams(spp, bounces, seed, (C.c_float * 3)(*sky), first_sample, x0, y0, w, h)
 
 
 class OrShadeParams(C.Structure):
@@ -46,15 +53,14 @@ def build_oracle() -> Path:
 
 
 def build_reference() -> Path | None:
-    """Compiles the reference CPU code when its sources are present."""
-    ref = Path(os.environ.get("RT_REFERENCE_DIR", "/root/reference"))
-    if not (ref / "AccelerationStructures" / "LBVH" / "LBVH.cpp").exists():
-        return None
+    """Compiles the reference CPU code when its sources are present.  The
+    recipe (ref/build_ref.sh) locates the checkout (RT_REFERENCE_DIR) and
+    builds nothing where it is absent; None is returned then."""
     srcs = [HERE / "ref" / "ref_shim.cpp", HERE / "ref" / "build_ref.sh"]
     if REF_LIB.exists() and all(s.stat().st_mtime <= REF_LIB.stat().st_mtime for s in srcs):
         return REF_LIB
     subprocess.run(["bash", str(HERE / "ref" / "build_ref.sh")], check=True, capture_output=True)
-    return REF_LIB
+    return REF_LIB if REF_LIB.exists() else None
 
 
 def _ptr(a: np.ndarray):
@@ -313,10 +319,16 @@ def bvh_shadow_mirror(nodes, ids, tris, cam, light, prim, nthreads=None, stats=F
     return (vis, mirror, ss, ms) if stats else (vis, mirror)
 
 
-def pathtrace(nodes, depth, ids, tris, albedo, emission, cam, spp, bounces, seed, sky=(1.0, 1.0, 1.0), nthreads=None):
+def pathtrace(nodes, depth, ids, tris, albedo, emission, cam, spp, bounces, seed, sky=(1.0, 1.0, 1.0), nthreads=None,
+              first_sample=0, window=None, image=None):
+    """CPU rendering of samples first_sample .. first_sample + spp - 1.
+    window = (x0, y0, w, h) renders that crop of the cam.width x cam.height
+    image (w*h x 4 floats, row-major); image (same shape) holds the mean of
+    the first_sample earlier samples when first_sample > 0."""
     oc = to_or_camera(cam)
-    p = OrPtParams(spp, bounces, seed, (C.c_float * 3)(*sky))
-    img = np.zeros((cam.height * cam.width, 4), np.float32)
+    p = _pt_params(spp, bounces, seed, sky, first_sample, window)
+    npx = window[2] * window[3] if window is not None else cam.height * cam.width
+    img = np.zeros((npx, 4), np.float32) if image is None else np.array(image, np.float32, copy=True).reshape(npx, 4)
     olib().or_pathtrace(_ptr(nodes), depth, _ptr(ids), _ptr(np.ascontiguousarray(tris, np.float32)),
                         _ptr(np.ascontiguousarray(albedo, np.float32)), _ptr(np.ascontiguousarray(emission, np.float32)),
                         C.byref(oc), C.byref(p), _ptr(img), nthreads or nthreads_default())
@@ -324,9 +336,11 @@ def pathtrace(nodes, depth, ids, tris, albedo, emission, cam, spp, bounces, seed
 
 
 def pathtrace_adjoint(nodes, depth, ids, tris, albedo, emission, cam, spp, bounces, seed, d_image,
-                      sky=(1.0, 1.0, 1.0), nthreads=None):
+                      sky=(1.0, 1.0, 1.0), nthreads=None, first_sample=0, window=None):
+    """FP64 adjoint; with window = (x0, y0, w, h), d_image holds that crop's
+    w*h pixels and the pixels outside it contribute nothing."""
     oc = to_or_camera(cam)
-    p = OrPtParams(spp, bounces, seed, (C.c_float * 3)(*sky))
+    p = _pt_params(spp, bounces, seed, sky, first_sample, window)
     da = np.zeros((len(tris), 3), np.float64)
     de = np.zeros(3, np.float64)
     olib().or_pathtrace_adjoint(_ptr(nodes), depth, _ptr(ids), _ptr(np.ascontiguousarray(tris, np.float32)),

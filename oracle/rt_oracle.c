@@ -633,17 +633,32 @@ static int trace_path(const or_node* nodes, const uint32_t* ids, const float* tr
  * cbGlobalIllumination::Update (ConstantBuffers.h:102-109):
  *   acc *= n/(n+1)  (CSPrimaryRays.hlsl:63), then per segment
  *   acc += (1/(n+1) * beta) * Le,  beta *= albedo; a miss adds the sky. */
+/* The window of the image a call covers (the whole image when win_w = 0). */
+static void pt_window(const or_camera* cam, const or_pt_params* p, uint32_t* x0, uint32_t* y0, uint32_t* w,
+                      uint32_t* h) {
+    if (p->win_w == 0) {
+        *x0 = 0; *y0 = 0; *w = cam->width; *h = cam->height;
+    } else {
+        *x0 = p->x0; *y0 = p->y0; *w = p->win_w; *h = p->win_h;
+    }
+}
+
 void or_pathtrace(const or_node* nodes, uint32_t depth, const uint32_t* ids, const float* tris,
                   const float* albedo, const float* emission, const or_camera* cam,
                   const or_pt_params* p, float* image, int nthreads) {
     (void)depth;
-    const long npx = (long)cam->width * cam->height;
+    uint32_t wx0, wy0, ww, wh;
+    pt_window(cam, p, &wx0, &wy0, &ww, &wh);
+    const long npx = (long)ww * wh;
+    const uint32_t n0 = p->first_sample;
     if (nthreads <= 0) nthreads = 1;
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
     for (long px = 0; px < npx; ++px) {
-        uint32_t i = (uint32_t)(px % cam->width), j = (uint32_t)(px / cam->width);
+        uint32_t i = wx0 + (uint32_t)(px % ww), j = wy0 + (uint32_t)(px / ww);
         float acc[3] = {0.0f, 0.0f, 0.0f};
-        for (uint32_t n = 0; n < p->spp; ++n) {
+        if (n0 > 0) /* continue the progressive mean of samples 0 .. n0-1 */
+            for (int c = 0; c < 3; ++c) acc[c] = image[4 * px + c];
+        for (uint32_t n = n0; n < n0 + p->spp; ++n) {
             float fant = (float)n / (float)(n + 1);
             float fact = 1.0f / (float)(n + 1);
             for (int c = 0; c < 3; ++c) acc[c] *= fant;
@@ -677,14 +692,19 @@ void or_pathtrace_adjoint(const or_node* nodes, uint32_t depth, const uint32_t* 
                           const or_camera* cam, const or_pt_params* p, const float* d_image,
                           double* d_albedo, double* d_emission_scale, int nthreads) {
     (void)depth;
-    const long npx = (long)cam->width * cam->height;
+    uint32_t wx0, wy0, ww, wh;
+    pt_window(cam, p, &wx0, &wy0, &ww, &wh);
+    const long npx = (long)ww * wh;
     if (nthreads <= 0) nthreads = 1;
+    /* weight of sample n0 + k in the progressive mean after the call */
     double wsample[64];
+    const uint32_t n0 = p->first_sample;
     uint32_t spp = p->spp < 64 ? p->spp : 64;
-    for (uint32_t n = 0; n < spp; ++n) {
+    for (uint32_t k = 0; k < spp; ++k) {
+        uint32_t n = n0 + k;
         double w = (double)(1.0f / (float)(n + 1));
-        for (uint32_t m = n + 1; m < spp; ++m) w *= (double)((float)m / (float)(m + 1));
-        wsample[n] = w;
+        for (uint32_t m = n + 1; m < n0 + spp; ++m) w *= (double)((float)m / (float)(m + 1));
+        wsample[k] = w;
     }
     double dle[3] = {0.0, 0.0, 0.0};
 #pragma omp parallel num_threads(nthreads)
@@ -692,11 +712,12 @@ void or_pathtrace_adjoint(const or_node* nodes, uint32_t depth, const uint32_t* 
         double dle_local[3] = {0.0, 0.0, 0.0};
 #pragma omp for schedule(dynamic, 16)
         for (long px = 0; px < npx; ++px) {
-            uint32_t i = (uint32_t)(px % cam->width), j = (uint32_t)(px / cam->width);
+            uint32_t i = wx0 + (uint32_t)(px % ww), j = wy0 + (uint32_t)(px / ww);
             const float* g = d_image + 4 * px;
-            for (uint32_t n = 0; n < spp; ++n) {
+            for (uint32_t k = 0; k < spp; ++k) {
+                const uint32_t n = k;  /* wsample index; the stream is sample n0 + k */
                 int seg[OR_MAX_SEG], missed;
-                int ns = trace_path(nodes, ids, tris, cam, i, j, n, p, seg, &missed);
+                int ns = trace_path(nodes, ids, tris, cam, i, j, n0 + k, p, seg, &missed);
                 double beta[OR_MAX_SEG + 1][3];
                 beta[0][0] = beta[0][1] = beta[0][2] = 1.0;
                 for (int s = 0; s < ns; ++s)

@@ -111,6 +111,11 @@ typedef struct or_pt_params {
     uint32_t bounces;   /* segments traced = bounces + 1 */
     uint64_t seed;
     float sky[3];       /* radiance added on a miss (reference: white, i.e. 1) */
+    uint32_t first_sample;  /* n0: samples 0 .. n0-1 are already in image (ConstantBuffers.h:102-109) */
+    /* pixel window [x0, x0 + win_w) x [y0, y0 + win_h) of the cam->width x
+     * cam->height image (win_w = 0: the whole image); image / d_image hold
+     * the window's pixels only, row-major */
+    uint32_t x0, y0, win_w, win_h;
 } or_pt_params;
 void or_pathtrace(const or_node* nodes, uint32_t depth, const uint32_t* ids, const float* tris,
                   const float* albedo /* n x 3 */, const float* emission /* n x 3 */,

@@ -32,6 +32,8 @@
 // follows from two scans and its own code: depth = popcount(mask), index =
 // 1 followed by the code's bits at the mask positions, high to low.
 #include <algorithm>
+#include <atomic>
+#include <mutex>
 
 #include "rt_internal.cuh"
 
@@ -335,7 +337,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
                                                            const uint32_t* __restrict__ hist, uint32_t* lookback,
                                                            uint32_t* tile_counter, uint32_t* err,
                                                            const uint32_t* __restrict__ scene_off = nullptr,
-                                                           uint32_t S = 0) {
+                                                           uint32_t S = 0, uint32_t spin_limit = kSpinLimit) {
     grid_dep_wait();
     __shared__ uint32_t s_keys[kSortTile];
     __shared__ uint32_t s_ids[kSortTile];
@@ -420,7 +422,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
                 used = q + 1;
                 if (f == kFlagInc) done = true;
             }
-            if (!done && used == 0 && ++spins > kSpinLimit) {
+            if (!done && used == 0 && ++spins > spin_limit) {
                 atomicOr(err, RT_DEVERR_TIMEOUT);
                 break;
             }
@@ -782,9 +784,10 @@ __device__ __forceinline__ void leaf_boxes(int64_t gpos, int cnt, const float4* 
         }
         float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
         if (p < total) {
-            lo[0] = fminf(a.x, fminf(b.x, c.x)); hi[0] = fmaxf(a.x, fmaxf(b.x, c.x));
-            lo[1] = fminf(a.y, fminf(b.y, c.y)); hi[1] = fmaxf(a.y, fmaxf(b.y, c.y));
-            lo[2] = fminf(a.z, fminf(b.z, c.z)); hi[2] = fmaxf(a.z, fmaxf(b.z, c.z));
+            // gMinVertices / gMaxVertices (LBVH.cpp:505-509): min(V0, min(V1, V2))
+            lo[0] = smin(a.x, smin(b.x, c.x)); hi[0] = smax(a.x, smax(b.x, c.x));
+            lo[1] = smin(a.y, smin(b.y, c.y)); hi[1] = smax(a.y, smax(b.y, c.y));
+            lo[2] = smin(a.z, smin(b.z, c.z)); hi[2] = smax(a.z, smax(b.z, c.z));
         }
         // segmented min / max (lanes of one owner are contiguous); afterwards
         // the first lane of each owner's run holds the run's box
@@ -796,9 +799,9 @@ __device__ __forceinline__ void leaf_boxes(int64_t gpos, int cnt, const float4* 
             for (int c = 0; c < 3; ++c) {
                 const float l2 = __shfl_down_sync(kFull, lo[c], off);
                 const float h2 = __shfl_down_sync(kFull, hi[c], off);
-                if (take) {
-                    lo[c] = fminf(lo[c], l2);
-                    hi[c] = fmaxf(hi[c], h2);
+                if (take) {  // lane + off holds later triangles of the same leaf
+                    lo[c] = smin(lo[c], l2);
+                    hi[c] = smax(hi[c], h2);
                 }
             }
         }
@@ -808,9 +811,9 @@ __device__ __forceinline__ void leaf_boxes(int64_t gpos, int cnt, const float4* 
         for (int c = 0; c < 3; ++c) {
             const float l2 = __shfl_sync(kFull, lo[c], head);
             const float h2 = __shfl_sync(kFull, hi[c], head);
-            if (mine) {
-                mn[c] = fminf(mn[c], l2);
-                mx[c] = fmaxf(mx[c], h2);
+            if (mine) {  // earlier batches first, as the leaf loop of LBVH.cpp:202-206 runs
+                mn[c] = smin(mn[c], l2);
+                mx[c] = smax(mx[c], h2);
             }
         }
     }
@@ -863,7 +866,13 @@ __device__ __forceinline__ void refit_walk(uint32_t h, int32_t pos, int32_t end,
             break;
         }
         const int d = hb(__ldg(keys + rpos - 1) ^ __ldg(keys + rpos));
-        for (int q = 0; q < 3; ++q) { nd.min[q] = fminf(nd.min[q], smn[q]); nd.max[q] = fmaxf(nd.max[q], smx[q]); }
+        // minBox / maxBox(left, right) (LBVH.cpp:312-313): the left child's
+        // bound is kept on a tie, which decides the sign of a zero bound
+        if (h & 1u) {
+            for (int q = 0; q < 3; ++q) { nd.min[q] = smin(smn[q], nd.min[q]); nd.max[q] = smax(smx[q], nd.max[q]); }
+        } else {
+            for (int q = 0; q < 3; ++q) { nd.min[q] = smin(nd.min[q], smn[q]); nd.max[q] = smax(nd.max[q], smx[q]); }
+        }
         nd.prim_count = (pcount << 3) | ((30 - d) % 3);
         nd.prim_pos = lpos;
         h >>= 1;
@@ -1071,7 +1080,7 @@ static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint
     for (int p = 0; p < kSortPasses; ++p) {
         launch_pdl(k_onesweep<false>, sort_tiles, kSortThreads, 0, st, (const uint32_t*)kin, (const uint32_t*)iin,
                    kout, iout, n, p, (const uint32_t*)l->hist, l->lookback + (size_t)p * 256 * sort_tiles,
-                   l->counters + 1 + p, ctx->d_err, (const uint32_t*)nullptr, 0u);
+                   l->counters + 1 + p, ctx->d_err, (const uint32_t*)nullptr, 0u, kSpinLimit);
         RT_CHECK_LAUNCH(ctx, "k_onesweep");
         std::swap(kin, kout);
         std::swap(iin, iout);
@@ -1187,16 +1196,17 @@ extern "C" rt_status rt_lbvh_download(rt_ctx* ctx, const rt_lbvh* l, rt_node* h_
 // ===========================================================================
 // Allocation-free LBVH build.
 //
-// Some callers cannot call cudaMalloc at the moment they need a rebuild: a
-// host that is capturing its frame into a CUDA graph (an allocation inside
-// stream capture is an error), an engine whose device memory is owned by
-// its own allocator and must not be touched behind its back, or a real-time
-// loop that cannot afford the implicit synchronisation of an allocation.
-// rt_lbvh_build_noalloc serves them: the caller passes the soup and every
-// output buffer, and all of the build's scratch (sort ping-pong buffers,
-// digit histograms, look-back words, tile scans, leaf list, refit arrival
-// words) lives in the fixed array below, which the CUDA module reserves on
-// every GPU that loads this library and keeps until the process exits.
+// Some callers cannot call cudaMalloc at the moment they need a rebuild: an
+// engine whose device memory is owned by its own allocator (a caching pool
+// that has already reserved the free memory, or a budgeted heap that must
+// account for every byte) and must not be touched behind its back, or a
+// real-time loop that cannot afford the implicit device-wide
+// synchronisation of an allocation.  rt_lbvh_build_noalloc serves them: the
+// caller passes the soup and every output buffer, and all of the build's
+// scratch (sort ping-pong buffers, digit histograms, look-back words, tile
+// scans, leaf list, refit arrival words) lives in the fixed array below,
+// which the CUDA module reserves on every GPU that loads this library and
+// keeps until the process exits.
 //
 // Limits: at most RT_NOALLOC_MAX_TRIS triangles (the 512 x 512 = 262,144
 // primitives the reference's own GPU rebuild handles, BitonicSort.cpp:20-27)
@@ -1221,19 +1231,51 @@ constexpr size_t kNaLeaves = kNaScan + 4 * (size_t)kNoAllocEmitTiles;           
 constexpr size_t kNaKeysAlt = kNaLeaves + RT_NOALLOC_MAX_TRIS;
 constexpr size_t kNaIdsAlt = kNaKeysAlt + RT_NOALLOC_MAX_TRIS;
 constexpr size_t kNaArrive = kNaIdsAlt + RT_NOALLOC_MAX_TRIS;                       // 1 << (depth - 1)
-constexpr size_t kNaErr = kNaArrive + ((size_t)1 << (RT_NOALLOC_MAX_DEPTH - 1));
+constexpr size_t kNaErr = kNaArrive + ((size_t)1 << (RT_NOALLOC_MAX_DEPTH - 1));   // error word (ctx == NULL)
 constexpr size_t kNaWords = kNaErr + 64;
+static_assert(kNaWords * sizeof(uint32_t) == 5577088, "the documented size of the fixed scratch");
 
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kNaWords];
 
-// Device address of g_noalloc_scratch and the SM count, per device; filled
-// on the first call on that device.
+// Device address of g_noalloc_scratch and the SM count, per device.  The
+// first call on a device fills them under g_noalloc_mutex, with that device
+// current, and publishes `scratch` last (release); later calls read it
+// without the lock (acquire), so a non-null address always comes with its
+// SM count.
 struct NoAllocDevice {
-    uint32_t* scratch = nullptr;
+    std::atomic<uint32_t*> scratch{nullptr};
     int num_sms = 0;
 };
 constexpr int kNoAllocMaxDevices = 64;
 NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
+std::mutex g_noalloc_mutex;
+
+rt_status noalloc_setup(rt_ctx* ctx, int dev, NoAllocDevice& D, uint32_t** out) {
+    uint32_t* S = D.scratch.load(std::memory_order_acquire);
+    if (S) {
+        *out = S;
+        return RT_OK;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    S = D.scratch.load(std::memory_order_acquire);
+    if (!S) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_build_noalloc: cudaGetSymbolAddress failed: %s",
+                           cudaGetErrorString(e));
+        int sms = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess || sms < 1)
+            return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_build_noalloc: cudaDeviceGetAttribute failed: %s",
+                           cudaGetErrorString(e));
+        D.num_sms = sms;
+        S = static_cast<uint32_t*>(p);
+        D.scratch.store(S, std::memory_order_release);
+    }
+    *out = S;
+    return RT_OK;
+}
 
 }  // namespace
 
@@ -1243,6 +1285,10 @@ extern "C" rt_status rt_lbvh_build_noalloc(rt_ctx* ctx, void* stream, const floa
     if (!d_tris || !d_nodes || !d_ids || !d_keys || !d_sorted_tris)
         return rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_build_noalloc: null buffer");
     if (n == 0 || depth == 0) return rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_build_noalloc: n and depth must be > 0");
+    if (flags & ~RT_BUILD_CLEAR_UNREACHED)
+        return rt_fail(ctx, RT_ERR_INVALID,
+                       "rt_lbvh_build_noalloc: flags 0x%x: only RT_BUILD_CLEAR_UNREACHED is supported "
+                       "(the compact layout needs allocated buffers)", flags);
     if (n > RT_NOALLOC_MAX_TRIS || depth > RT_NOALLOC_MAX_DEPTH)
         return rt_fail(ctx, RT_ERR_CAPACITY,
                        "rt_lbvh_build_noalloc: n=%u depth=%u exceeds the fixed scratch (at most %u triangles, depth %u)",
@@ -1251,20 +1297,13 @@ extern "C" rt_status rt_lbvh_build_noalloc(rt_ctx* ctx, void* stream, const floa
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
         return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_build_noalloc: no usable current device");
+    if (ctx && ctx->device != dev)
+        return rt_fail(ctx, RT_ERR_INVALID, "rt_lbvh_build_noalloc: ctx is bound to device %d, the current device is %d",
+                       ctx->device, dev);
     NoAllocDevice& D = g_noalloc_dev[dev];
-    if (!D.scratch) {  // set-up, once per device, with that device current
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess)
-            return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_build_noalloc: cudaGetSymbolAddress failed: %s",
-                           cudaGetErrorString(e));
-        e = cudaDeviceGetAttribute(&D.num_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess)
-            return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_build_noalloc: cudaDeviceGetAttribute failed: %s",
-                           cudaGetErrorString(e));
-        D.scratch = static_cast<uint32_t*>(p);
-    }
-    uint32_t* S = D.scratch;
+    uint32_t* S = nullptr;
+    rt_status rs = noalloc_setup(ctx, dev, D, &S);
+    if (rs != RT_OK) return rs;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     SceneInfo* scene = reinterpret_cast<SceneInfo*>(S + kNaScene);
     uint32_t* counters = S + kNaCounters;
@@ -1276,13 +1315,16 @@ extern "C" rt_status rt_lbvh_build_noalloc(rt_ctx* ctx, void* stream, const floa
     uint32_t* keys_alt = S + kNaKeysAlt;
     uint32_t* ids_alt = S + kNaIdsAlt;
     uint32_t* arrive = S + kNaArrive;
-    uint32_t* err = S + kNaErr;
+    // device-side errors go to the context's error word (read and cleared by
+    // rt_ctx_check); without a context to a word of the array, cleared below
+    uint32_t* err = ctx ? ctx->d_err : S + kNaErr;
     const uint32_t num_nodes = 1u << depth;
     // what must start at zero: the bounds ticket, the refit epoch (k_bounds
-    // advances it to 1) and the refit arrival words; the other counters,
-    // histograms and look-back words are reset by k_bounds
+    // advances it to 1), the refit arrival words and the array's error word;
+    // the other counters, histograms and look-back words are reset by k_bounds
     e = cudaMemsetAsync(counters, 0, 8 * sizeof(uint32_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(arrive, 0, sizeof(uint32_t) * std::max(1u, num_nodes >> 1), st);
+    if (e == cudaSuccess && !ctx) e = cudaMemsetAsync(S + kNaErr, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess)
         return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_build_noalloc: cudaMemsetAsync failed: %s", cudaGetErrorString(e));
     const uint32_t sort_tiles = ceil_div(n, kSortTile);
@@ -1311,6 +1353,110 @@ extern "C" rt_status rt_lbvh_build_noalloc(rt_ctx* ctx, void* stream, const floa
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_build_noalloc: launch failed: %s", cudaGetErrorString(e));
+    return RT_OK;
+}
+
+// ===========================================================================
+// The sort stage on its own (rt_radix_sort): the four onesweep passes of the
+// build over caller-given (key, value) pairs with caller-owned scratch.
+// Scratch words: [0, 16) tile tickets (pass p at 1 + p), [16, 1040) the
+// four digit histograms, then the look-back words (4 x 256 per tile), then
+// the ping-pong keys and values (n each, 16-byte aligned).
+namespace {
+
+constexpr size_t kRsHist = 16;
+constexpr size_t kRsLookback = kRsHist + 4 * 256;
+
+size_t rs_tiles(uint32_t n) { return ((size_t)n + kSortTile - 1) / kSortTile; }
+size_t rs_alt_offset(uint32_t n) { return kRsLookback + (size_t)kSortPasses * 256 * rs_tiles(n); }
+size_t rs_words(uint32_t n) { return rs_alt_offset(n) + 2 * (((size_t)n + 3) & ~(size_t)3); }
+
+// Digit histograms of the four passes (block-local shared-memory atomics,
+// one global add per bin and block).
+__global__ void __launch_bounds__(512) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* hist) {
+    __shared__ uint32_t s_hist[4 * 256];
+    for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) s_hist[i] = 0u;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = __ldg(keys + i);
+#pragma unroll
+        for (int p = 0; p < kSortPasses; ++p) atomicAdd(&s_hist[p * 256 + ((k >> (8 * p)) & 0xffu)], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x)
+        if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
+}
+
+__global__ void k_set_word(uint32_t* p, uint32_t v) { *p = v; }
+
+rt_status rs_prepare(rt_ctx* ctx, const uint32_t* d_keys, const uint32_t* d_values, uint32_t n, void* d_scratch,
+                     size_t scratch_bytes, const char* who, uint32_t** S) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (!d_keys || !d_values || !d_scratch) return rt_fail(ctx, RT_ERR_INVALID, "%s: null buffer", who);
+    if ((reinterpret_cast<uintptr_t>(d_scratch) & 15u) != 0)
+        return rt_fail(ctx, RT_ERR_INVALID, "%s: the scratch must be 16-byte aligned", who);
+    if (n > kMaxTris) return rt_fail(ctx, RT_ERR_INVALID, "%s: n=%u exceeds %u", who, n, kMaxTris);
+    if (scratch_bytes < rs_words(n) * sizeof(uint32_t))
+        return rt_fail(ctx, RT_ERR_CAPACITY, "%s: scratch of %zu bytes, %zu needed", who, scratch_bytes,
+                       rs_words(n) * sizeof(uint32_t));
+    *S = static_cast<uint32_t*>(d_scratch);
+    // tile tickets, histograms and look-back words start at zero
+    RT_CHECK_CUDA(ctx, cudaMemsetAsync(*S, 0, sizeof(uint32_t) * rs_alt_offset(n), ctx->stream));
+    const uint32_t hb_blocks = std::max(1u, std::min(ceil_div(n, 512), (uint32_t)ctx->num_sms * 4));
+    k_sort_hist<<<hb_blocks, 512, 0, ctx->stream>>>(d_keys, n, *S + kRsHist);
+    RT_CHECK_LAUNCH(ctx, "k_sort_hist");
+    return RT_OK;
+}
+
+}  // namespace
+
+extern "C" size_t rt_radix_sort_scratch_bytes(uint32_t n) { return rs_words(n) * sizeof(uint32_t); }
+
+extern "C" rt_status rt_radix_sort(rt_ctx* ctx, uint32_t* d_keys, uint32_t* d_values, uint32_t n, void* d_scratch,
+                                   size_t scratch_bytes) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (n == 0) return RT_OK;
+    uint32_t* S = nullptr;
+    rt_status s = rs_prepare(ctx, d_keys, d_values, n, d_scratch, scratch_bytes, "rt_radix_sort", &S);
+    if (s != RT_OK) return s;
+    const uint32_t tiles = (uint32_t)rs_tiles(n);
+    uint32_t* kalt = S + rs_alt_offset(n);
+    uint32_t* valt = kalt + (((size_t)n + 3) & ~(size_t)3);
+    uint32_t *kin = d_keys, *iin = d_values, *kout = kalt, *iout = valt;
+    for (int p = 0; p < kSortPasses; ++p) {
+        k_onesweep<false><<<tiles, kSortThreads, 0, ctx->stream>>>(kin, iin, kout, iout, n, p, S + kRsHist,
+                                                                   S + kRsLookback + (size_t)p * 256 * tiles,
+                                                                   S + 1 + p, ctx->d_err);
+        RT_CHECK_LAUNCH(ctx, "k_onesweep");
+        std::swap(kin, kout);
+        std::swap(iin, iout);
+    }
+    return RT_OK;  // four passes: the sorted pairs are back in d_keys / d_values
+}
+
+extern "C" rt_status rt_radix_sort_stall_test(rt_ctx* ctx, const uint32_t* d_keys, const uint32_t* d_values,
+                                              uint32_t n, void* d_scratch, size_t scratch_bytes,
+                                              uint32_t spin_limit) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (n <= (uint32_t)kSortTile)
+        return rt_fail(ctx, RT_ERR_INVALID, "rt_radix_sort_stall_test: n must exceed %d (two tiles)", kSortTile);
+    if (spin_limit == 0) return rt_fail(ctx, RT_ERR_INVALID, "rt_radix_sort_stall_test: spin_limit must be > 0");
+    uint32_t* S = nullptr;
+    rt_status s = rs_prepare(ctx, d_keys, d_values, n, d_scratch, scratch_bytes, "rt_radix_sort_stall_test", &S);
+    if (s != RT_OK) return s;
+    const uint32_t tiles = (uint32_t)rs_tiles(n);
+    uint32_t* kalt = S + rs_alt_offset(n);
+    uint32_t* valt = kalt + (((size_t)n + 3) & ~(size_t)3);
+    // the pass's tile tickets start at 1: tiles 1 .. tiles-1 run and tile 0
+    // never publishes its digit counts, so tile 1's look-back gives up after
+    // spin_limit polls (a later tile that passed tile 1's aggregate before
+    // tile 1 gave up waits on tile 0 too and gives up the same way)
+    k_set_word<<<1, 1, 0, ctx->stream>>>(S + 1, 1u);
+    RT_CHECK_LAUNCH(ctx, "k_set_word");
+    k_onesweep<false><<<tiles - 1, kSortThreads, 0, ctx->stream>>>(d_keys, d_values, kalt, valt, n, 0, S + kRsHist,
+                                                                   S + kRsLookback, S + 1, ctx->d_err, nullptr, 0u,
+                                                                   spin_limit);
+    RT_CHECK_LAUNCH(ctx, "k_onesweep");
     return RT_OK;
 }
 

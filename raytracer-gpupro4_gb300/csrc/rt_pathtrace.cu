@@ -90,15 +90,23 @@ struct PathParams {
     uint32_t spp, bounces;
     uint64_t seed;
     float sky[3];
+    uint32_t n0;  // first sample index (samples 0 .. n0-1 are already in the image)
+};
+
+// Walk counts of the counting variant (rt_pathtrace_counted), per lane.
+struct PathCounts {
+    uint32_t segments = 0, boxes = 0, tris = 0, hits = 0;
 };
 
 // Traces one path; returns the number of hit segments and their triangle
 // ids.  Called by all lanes of the warp together (valid == false for lanes
 // past the image edge): every segment is one warp-wide traversal in which
-// lanes whose path already ended only help.
+// lanes whose path already ended only help.  STATS adds each traced
+// segment's box and triangle tests to *cnt.
+template <bool STATS = false>
 __device__ __forceinline__ int trace_path(const TreeRef& tr, const float* __restrict__ soup, const PathParams& P,
                                           bool valid, uint32_t i, uint32_t j, uint32_t sample, int* seg,
-                                          bool* missed) {
+                                          bool* missed, PathCounts* cnt = nullptr) {
     Pcg32 g;
     pt_seed(g, P.seed, (uint64_t)j * P.cam.width + i, sample);
     const float inv = fdiv(1.0f, (float)P.cam.height);
@@ -114,8 +122,14 @@ __device__ __forceinline__ int trace_path(const TreeRef& tr, const float* __rest
     bool alive = valid;
     for (uint32_t s = 0; s <= P.bounces && s < (uint32_t)kMaxSeg; ++s) {
         const RayState r = make_ray(o, d, 1e16f, exclude);
-        uint32_t nb, nt;
-        const Hit h = trace_ray<false>(r, alive, tr, false, &nb, &nt);
+        uint32_t nb = 0, nt = 0;
+        const Hit h = trace_ray<STATS>(r, alive, tr, false, &nb, &nt);
+        if (STATS && alive) {
+            cnt->segments += 1;
+            cnt->boxes += nb;
+            cnt->tris += nt;
+            cnt->hits += (h.id >= 0) ? 1u : 0u;
+        }
         if (alive) {
             if (h.id < 0) {
                 *missed = true;
@@ -136,38 +150,56 @@ __device__ __forceinline__ int trace_path(const TreeRef& tr, const float* __rest
     return ns;
 }
 
+template <bool STATS>
 __device__ __forceinline__ void path_pixel(const TreeRef& tr, const float* __restrict__ soup,
                                            const float* __restrict__ albedo, const float* __restrict__ emission,
                                            const PathParams& P, float4* __restrict__ image, bool valid, uint32_t i,
-                                           uint32_t j);
+                                           uint32_t j, PathCounts* cnt);
 
 // At most 72 registers (seven blocks per SM): 1 % faster than the 80 the
-// compiler picks unbounded; 79 or 88 are slower.
+// compiler picks unbounded; 79 or 88 are slower.  STATS: the counting
+// variant, which also sums the walk counts into counts[4] (64-bit).
+template <bool STATS>
 __global__ void __launch_bounds__(kPtThreads, 7) k_pathtrace(TreeRef tr, const float* __restrict__ soup,
                                                           const float* __restrict__ albedo,
                                                           const float* __restrict__ emission, PathParams P,
                                                           float4* __restrict__ image, uint32_t* work,
-                                                          uint32_t num_tiles) {
+                                                          uint32_t num_tiles, unsigned long long* counts) {
+    PathCounts cnt;
     for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
         uint32_t i, j;
         const bool valid = tile_pixel(tile, threadIdx.x & 31, P.cam.width, P.cam.height, &i, &j);
         if (!valid) i = j = 0;
-        path_pixel(tr, soup, albedo, emission, P, image, valid, i, j);
+        path_pixel<STATS>(tr, soup, albedo, emission, P, image, valid, i, j, &cnt);
+    }
+    if (STATS) {
+        unsigned long long v[4] = {cnt.segments, cnt.boxes, cnt.tris, cnt.hits};
+        for (int q = 0; q < 4; ++q) {
+            for (int off = 16; off > 0; off >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], off);
+            if ((threadIdx.x & 31) == 0 && v[q]) atomicAdd(counts + q, v[q]);
+        }
     }
 }
 
+template <bool STATS>
 __device__ __forceinline__ void path_pixel(const TreeRef& tr, const float* __restrict__ soup,
                                            const float* __restrict__ albedo, const float* __restrict__ emission,
                                            const PathParams& P, float4* __restrict__ image, bool valid, uint32_t i,
-                                           uint32_t j) {
+                                           uint32_t j, PathCounts* cnt) {
     float acc[3] = {0.0f, 0.0f, 0.0f};
-    for (uint32_t n = 0; n < P.spp; ++n) {
+    if (P.n0 > 0 && valid) {  // continue the progressive mean the image holds
+        const float4 prev = image[(size_t)j * P.cam.width + i];
+        acc[0] = prev.x;
+        acc[1] = prev.y;
+        acc[2] = prev.z;
+    }
+    for (uint32_t n = P.n0; n < P.n0 + P.spp; ++n) {
         const float fant = fdiv((float)n, (float)(n + 1));
         const float fact = fdiv(1.0f, (float)(n + 1));
         for (int c = 0; c < 3; ++c) acc[c] = fmul(acc[c], fant);
         int seg[kMaxSeg];
         bool missed;
-        const int ns = trace_path(tr, soup, P, valid, i, j, n, seg, &missed);
+        const int ns = trace_path<STATS>(tr, soup, P, valid, i, j, n, seg, &missed, cnt);
         float beta[3] = {1.0f, 1.0f, 1.0f};
         for (int s = 0; s < ns; ++s) {
             const float* le = emission + 3 * (size_t)seg[s];
@@ -195,10 +227,10 @@ __global__ void __launch_bounds__(kPtThreads) k_pathtrace_adjoint(
         if (!valid) i = j = 0;
         const float4 g4 = valid ? __ldg(dimage + (size_t)j * P.cam.width + i) : make_float4(0.f, 0.f, 0.f, 0.f);
         const float gimg[3] = {g4.x, g4.y, g4.z};
-        for (uint32_t n = 0; n < P.spp; ++n) {
-            // weight of sample n in the progressive mean
+        for (uint32_t n = P.n0; n < P.n0 + P.spp; ++n) {
+            // weight of sample n in the progressive mean after the call
             float w = 1.0f / (float)(n + 1);
-            for (uint32_t m = n + 1; m < P.spp; ++m) w *= (float)m / (float)(m + 1);
+            for (uint32_t m = n + 1; m < P.n0 + P.spp; ++m) w *= (float)m / (float)(m + 1);
             int seg[kMaxSeg];
             bool missed;
             const int ns = trace_path(tr, soup, P, valid, i, j, n, seg, &missed);
@@ -241,10 +273,13 @@ rt_status pt_args(rt_ctx* ctx, const rt_lbvh* l, const float* a, const float* e,
     if (cam->width == 0 || cam->height == 0) return rt_fail(ctx, RT_ERR_INVALID, "%s: empty image", who);
     if (p->spp == 0 || p->bounces + 1 > (uint32_t)kMaxSeg)
         return rt_fail(ctx, RT_ERR_INVALID, "%s: spp must be > 0 and bounces < %d", who, kMaxSeg);
+    if ((uint64_t)p->first_sample + p->spp > 65535u)  // the per-pixel streams are seeded with pixel * 65536 + sample
+        return rt_fail(ctx, RT_ERR_INVALID, "%s: first_sample + spp must stay below 65536", who);
     out->cam = *cam;
     out->spp = p->spp;
     out->bounces = p->bounces;
     out->seed = p->seed;
+    out->n0 = p->first_sample;
     for (int c = 0; c < 3; ++c) out->sky[c] = p->sky[c];
     return RT_OK;
 }
@@ -257,19 +292,40 @@ uint32_t px_tiles(const rt_camera* cam) {
 
 TreeRef tree_ref(const rt_ctx* ctx, const rt_lbvh* l);
 
-extern "C" rt_status rt_pathtrace(rt_ctx* ctx, const rt_lbvh* l, const float* d_albedo, const float* d_emission,
-                                  const rt_camera* cam, const rt_pt_params* p, float* d_image) {
+static rt_status launch_pathtrace(rt_ctx* ctx, const rt_lbvh* l, const float* d_albedo, const float* d_emission,
+                                  const rt_camera* cam, const rt_pt_params* p, float* d_image,
+                                  unsigned long long* d_counts, const char* who) {
     PathParams P;
-    rt_status s = pt_args(ctx, l, d_albedo, d_emission, cam, p, &P, "rt_pathtrace");
+    rt_status s = pt_args(ctx, l, d_albedo, d_emission, cam, p, &P, who);
     if (s != RT_OK) return s;
-    if (!d_image) return rt_fail(ctx, RT_ERR_INVALID, "rt_pathtrace: null image");
+    if (!d_image) return rt_fail(ctx, RT_ERR_INVALID, "%s: null image", who);
     if ((s = reset_work(ctx, kWorkPath)) != RT_OK) return s;
     const uint32_t tiles = px_tiles(cam);
-    k_pathtrace<<<persistent_blocks(ctx, k_pathtrace, kPtThreads, tiles), kPtThreads, 0, ctx->stream>>>(
-        tree_ref(ctx, l), l->src_tris, d_albedo, d_emission, P, reinterpret_cast<float4*>(d_image),
-        ctx->d_work + kWorkPath, tiles);
+    if (d_counts) {
+        k_pathtrace<true><<<persistent_blocks(ctx, k_pathtrace<true>, kPtThreads, tiles), kPtThreads, 0,
+                            ctx->stream>>>(tree_ref(ctx, l), l->src_tris, d_albedo, d_emission, P,
+                                           reinterpret_cast<float4*>(d_image), ctx->d_work + kWorkPath, tiles,
+                                           d_counts);
+    } else {
+        k_pathtrace<false><<<persistent_blocks(ctx, k_pathtrace<false>, kPtThreads, tiles), kPtThreads, 0,
+                             ctx->stream>>>(tree_ref(ctx, l), l->src_tris, d_albedo, d_emission, P,
+                                            reinterpret_cast<float4*>(d_image), ctx->d_work + kWorkPath, tiles,
+                                            nullptr);
+    }
     RT_CHECK_LAUNCH(ctx, "k_pathtrace");
     return RT_OK;
+}
+
+extern "C" rt_status rt_pathtrace(rt_ctx* ctx, const rt_lbvh* l, const float* d_albedo, const float* d_emission,
+                                  const rt_camera* cam, const rt_pt_params* p, float* d_image) {
+    return launch_pathtrace(ctx, l, d_albedo, d_emission, cam, p, d_image, nullptr, "rt_pathtrace");
+}
+
+extern "C" rt_status rt_pathtrace_counted(rt_ctx* ctx, const rt_lbvh* l, const float* d_albedo,
+                                          const float* d_emission, const rt_camera* cam, const rt_pt_params* p,
+                                          float* d_image, unsigned long long* d_counts) {
+    if (!d_counts) return ctx ? rt_fail(ctx, RT_ERR_INVALID, "rt_pathtrace_counted: null counts") : RT_ERR_INVALID;
+    return launch_pathtrace(ctx, l, d_albedo, d_emission, cam, p, d_image, d_counts, "rt_pathtrace_counted");
 }
 
 extern "C" rt_status rt_pathtrace_adjoint(rt_ctx* ctx, const rt_lbvh* l, const float* d_albedo,

@@ -32,8 +32,9 @@ EXPORTED = [
     "rt_lbvh_import_host", "rt_lbvh_view_get", "rt_lbvh_compact_get", "rt_lbvh_world_bound", "rt_lbvh_download", "rt_trace_primary",
     "rt_trace_shadow_mirror", "rt_trace_rays", "rt_trace_primary_leaves", "rt_trace_shadow_mirror_from",
     "rt_trace_rays_from", "rt_trace_frame_shader_order", "rt_render_whitted", "rt_bvh_create", "rt_bvh_destroy", "rt_bvh_import_host",
-    "rt_bvh_trace_primary", "rt_bvh_trace_shadow_mirror", "rt_bvh_trace_rays", "rt_render_frame_host", "rt_render_frame_host_async", "rt_pathtrace", "rt_pathtrace_adjoint",
-    "rt_lbvh_build_noalloc", "rt_frame_capture_host", "rt_frame_capture", "rt_frame_launch", "rt_frame_node_count", "rt_frame_destroy",
+    "rt_bvh_trace_primary", "rt_bvh_trace_shadow_mirror", "rt_bvh_trace_rays", "rt_render_frame_host", "rt_render_frame_host_async", "rt_pathtrace", "rt_pathtrace_counted", "rt_pathtrace_adjoint",
+    "rt_lbvh_build_noalloc", "rt_radix_sort_scratch_bytes", "rt_radix_sort", "rt_radix_sort_stall_test",
+    "rt_frame_capture_host", "rt_frame_capture", "rt_frame_launch", "rt_frame_node_count", "rt_frame_destroy",
     "rt_batch_create", "rt_batch_destroy", "rt_batch_scene_count", "rt_batch_build", "rt_batch_view_get",
     "rt_batch_download", "rt_batch_set_views", "rt_batch_trace", "rt_batch_set_tuning", "rt_batch_get_tuning", "rt_batch_frame_capture",
 ]
@@ -72,7 +73,7 @@ assert C.sizeof(Material) == 56 and C.sizeof(ShadeParams) == 36
 
 class PtParams(C.Structure):
     _fields_ = [("spp", C.c_uint32), ("bounces", C.c_uint32), ("seed", C.c_uint64), ("sky", C.c_float * 3),
-                ("reserved", C.c_uint32)]
+                ("first_sample", C.c_uint32)]
 
 
 _lib = None
@@ -125,8 +126,12 @@ def lib() -> C.CDLL:
         "rt_render_frame_host": (i32, [vp, vp, vp, u32, C.POINTER(Camera), fp, vp, vp, vp]),
         "rt_render_frame_host_async": (i32, [vp, vp, vp, u32, C.POINTER(Camera), fp, vp, vp, vp]),
         "rt_pathtrace": (i32, [vp, vp, vp, vp, C.POINTER(Camera), C.POINTER(PtParams), vp]),
+        "rt_pathtrace_counted": (i32, [vp, vp, vp, vp, C.POINTER(Camera), C.POINTER(PtParams), vp, vp]),
         "rt_pathtrace_adjoint": (i32, [vp, vp, vp, vp, C.POINTER(Camera), C.POINTER(PtParams), vp, vp, vp]),
         "rt_lbvh_build_noalloc": (i32, [vp, vp, vp, u32, u32, u32, vp, vp, vp, vp]),
+        "rt_radix_sort_scratch_bytes": (C.c_size_t, [u32]),
+        "rt_radix_sort": (i32, [vp, vp, vp, u32, vp, C.c_size_t]),
+        "rt_radix_sort_stall_test": (i32, [vp, vp, vp, u32, vp, C.c_size_t, u32]),
         "rt_frame_capture": (i32, [vp, vp, vp, u32, u32, C.POINTER(Camera), fp, vp, vp, vp, C.POINTER(vp)]),
         "rt_frame_capture_host": (i32, [vp, vp, vp, u32, u32, C.POINTER(Camera), fp, vp, vp, vp, C.POINTER(vp)]),
         "rt_frame_launch": (i32, [vp, vp]),

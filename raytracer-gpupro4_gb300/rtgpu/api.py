@@ -227,6 +227,40 @@ class StructureConstruction:
         return self.lbvh.Build(tris)
 
 
+class RadixSort:
+    """The build's sort stage on its own (rt_radix_sort): a stable sort of
+    (key, value) uint32 pairs by key, in place, in place of the reference's
+    BitonicSort::GPUSort / RadixSort::Sort (BitonicSort.cpp:56-117,
+    RadixSort.cpp:46-74).  The scratch is a device tensor kept between calls
+    and grown when a larger n arrives."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self._scratch = None
+
+    def scratch(self, n: int) -> torch.Tensor:
+        need = int(L.lib().rt_radix_sort_scratch_bytes(n))
+        if self._scratch is None or self._scratch.numel() * 4 < need:
+            self._scratch = torch.empty((need + 3) // 4, dtype=torch.int32, device=self.ctx.torch_device)
+        return self._scratch
+
+    def Sort(self, keys: torch.Tensor, values: torch.Tensor) -> None:
+        assert keys.dtype in (torch.int32, torch.uint32) and values.dtype in (torch.int32, torch.uint32)
+        assert keys.numel() == values.numel()
+        n = keys.numel()
+        sc = self.scratch(n)
+        L.check(L.lib().rt_radix_sort(self.ctx.h, _dev_ptr(keys), _dev_ptr(values), n, _dev_ptr(sc), sc.numel() * 4),
+                self.ctx.h, "rt_radix_sort")
+
+    def stall_test(self, keys: torch.Tensor, values: torch.Tensor, spin_limit: int) -> int:
+        """Runs rt_radix_sort_stall_test; returns its status (the look-back
+        timeout itself is reported by Context.check)."""
+        n = keys.numel()
+        sc = self.scratch(n)
+        return L.lib().rt_radix_sort_stall_test(self.ctx.h, _dev_ptr(keys), _dev_ptr(values), n, _dev_ptr(sc),
+                                                sc.numel() * 4, spin_limit)
+
+
 def hits_to_numpy(t: torch.Tensor) -> np.ndarray:
     return t.cpu().numpy().view(L.HIT_DTYPE).reshape(-1)
 
@@ -388,19 +422,37 @@ class RayTracer:
                    _host_ptr(vis), _host_ptr(mirror)), self.ctx.h, "rt_render_frame_host")
 
     def pathtrace(self, lbvh: LBVH, albedo: torch.Tensor, emission: torch.Tensor, cam: L.Camera, spp: int,
-                  bounces: int, seed: int, sky=(1.0, 1.0, 1.0), out: torch.Tensor | None = None) -> torch.Tensor:
+                  bounces: int, seed: int, sky=(1.0, 1.0, 1.0), out: torch.Tensor | None = None,
+                  first_sample: int = 0) -> torch.Tensor:
+        """Samples first_sample .. first_sample + spp - 1 of every pixel; with
+        first_sample > 0, `out` holds the mean of the earlier samples and the
+        new ones are blended into it (progressive accumulation)."""
+        if first_sample > 0 and out is None:
+            raise ValueError("first_sample > 0 continues an image: pass it as out")
         img = out if out is not None else torch.empty((cam.height * cam.width, 4), dtype=torch.float32,
                                                       device=self.ctx.torch_device)
-        p = L.PtParams(spp, bounces, seed, (C.c_float * 3)(*sky), 0)
+        p = L.PtParams(spp, bounces, seed, (C.c_float * 3)(*sky), first_sample)
         L.check(L.lib().rt_pathtrace(self.ctx.h, lbvh.h, _dev_ptr(albedo), _dev_ptr(emission), C.byref(cam),
                                      C.byref(p), _dev_ptr(img)), self.ctx.h, "rt_pathtrace")
         return img
 
+    def pathtrace_counted(self, lbvh: LBVH, albedo: torch.Tensor, emission: torch.Tensor, cam: L.Camera, spp: int,
+                          bounces: int, seed: int, sky=(1.0, 1.0, 1.0)):
+        """rt_pathtrace_counted: (image, {segments, box_tests, tri_tests, hits})."""
+        img = torch.empty((cam.height * cam.width, 4), dtype=torch.float32, device=self.ctx.torch_device)
+        cnt = torch.zeros(4, dtype=torch.int64, device=self.ctx.torch_device)
+        p = L.PtParams(spp, bounces, seed, (C.c_float * 3)(*sky), 0)
+        L.check(L.lib().rt_pathtrace_counted(self.ctx.h, lbvh.h, _dev_ptr(albedo), _dev_ptr(emission), C.byref(cam),
+                                             C.byref(p), _dev_ptr(img), _dev_ptr(cnt)), self.ctx.h,
+                "rt_pathtrace_counted")
+        c = cnt.cpu().tolist()
+        return img, {"segments": c[0], "box_tests": c[1], "tri_tests": c[2], "hits": c[3]}
+
     def pathtrace_adjoint(self, lbvh: LBVH, albedo: torch.Tensor, emission: torch.Tensor, cam: L.Camera, spp: int,
-                          bounces: int, seed: int, d_image: torch.Tensor, sky=(1.0, 1.0, 1.0)):
+                          bounces: int, seed: int, d_image: torch.Tensor, sky=(1.0, 1.0, 1.0), first_sample: int = 0):
         d_alb = torch.zeros_like(albedo)
         d_le = torch.zeros(3, dtype=torch.float32, device=self.ctx.torch_device)
-        p = L.PtParams(spp, bounces, seed, (C.c_float * 3)(*sky), 0)
+        p = L.PtParams(spp, bounces, seed, (C.c_float * 3)(*sky), first_sample)
         L.check(L.lib().rt_pathtrace_adjoint(self.ctx.h, lbvh.h, _dev_ptr(albedo), _dev_ptr(emission), C.byref(cam),
                                              C.byref(p), _dev_ptr(d_image.contiguous()), _dev_ptr(d_alb),
                                              _dev_ptr(d_le)), self.ctx.h, "rt_pathtrace_adjoint")

@@ -3,7 +3,7 @@ code (AccelerationStructures/LBVH/LBVH.cpp: LBVH::Build, LBVH::IntersectP),
 compiled from the reference checkout by oracle/ref/build_ref.sh.
 
 Run from the repository root where the reference checkout is present:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 Each case stores its input soup, the reference's reachable nodes (index +
 record; unreached heap slots are uninitialised in the reference), its
 ordered ids, world bound, and its closest hits (id, t) for a ray set.
@@ -38,6 +38,22 @@ def cases():
     three = scenes.random_soup(1, seed=15)
     yield "three_equal", np.ascontiguousarray(np.repeat(three, 3, axis=0)), 10, scenes.look_at((0.5, 0.5, -1.5), (0.5, 0.5, 0.5), width=16, height=16)
     yield "depth1_root_leaf", scenes.random_soup(64, seed=16), 1, scenes.look_at((0.5, 0.5, -1.5), (0.5, 0.5, 0.5), width=16, height=16)
+    yield "signed_zero", signed_zero_soup(2000, seed=17), 12, scenes.look_at((0.3, 0.4, -2.5), (0.0, 0.0, 0.0), width=48, height=48)
+
+
+def signed_zero_soup(n, seed):
+    """Triangles on either side of the coordinate planes with many vertex
+    coordinates exactly +0.0 or -0.0: box bounds of 0 are ties between the
+    two zeros, whose sign only the order of the reference's min / max
+    (std::min / std::max keep their first argument on a tie) decides."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t = np.abs(scenes.random_soup(n, seed)).reshape(n, 3, 3)
+    side = rng.choice(np.array([-1.0, 1.0], np.float32), size=(n, 1, 3))
+    t = t * side
+    zero = rng.random((n, 3, 3)) < 0.3
+    sign = rng.choice(np.array([-0.0, 0.0], np.float32), size=(n, 3, 3))
+    t = np.where(zero, sign, t).astype(np.float32)
+    return np.ascontiguousarray(t.reshape(n, 9))
 
 
 def centroid_rays(tris, count=256, seed=5):
@@ -55,7 +71,10 @@ def main():
     O.build_oracle()
     if O.build_reference() is None:
         raise SystemExit("reference checkout not found; set RT_REFERENCE_DIR")
+    only = set(sys.argv[1:])  # optional case names: regenerate only those
     for name, tris, depth, cam in cases():
+        if only and name not in only:
+            continue
         tris = np.ascontiguousarray(tris, np.float32)
         ref = O.RefStructure(tris, "lbvh", depth)
         nodes = ref.nodes()

@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 from test_gpu_trace import assert_hits_equal
+from bitcmp import same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -29,7 +30,7 @@ def check_trees(gpu_ctx, oracle_mod, b, soups, depth, scenes_to_check=None):
         assert np.array_equal(keys, okeys), f"scene {s}: codes"
         assert np.array_equal(ids, oids), f"scene {s}: permutation"
         r = np.nonzero(reached)[0]
-        assert np.array_equal(nodes[r], onodes[r]), f"scene {s}: nodes"
+        assert same_bits(nodes[r], onodes[r]), f"scene {s}: nodes"
 
 
 def test_batch_build_mixed_sizes(gpu_ctx, oracle_mod):

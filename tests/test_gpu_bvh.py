@@ -9,6 +9,7 @@ import pytest
 import tri_np
 from test_gpu_trace import assert_hits_equal
 from test_oracle_bvh import bvh_cases, load_bvh
+from bitcmp import same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -36,7 +37,7 @@ def test_bvh_rays_fixture(gpu_ctx, oracle_mod, case, any_hit):
     else:
         assert_hits_equal(gh, oh, case)
         tri_np.assert_matches_reference(gh["id"], gh["t"], g["hit_id"], g["hit_t"], r, g["tris"])
-        assert np.array_equal(gh["t"], g["hit_t"])
+        assert same_bits(gh["t"], g["hit_t"])
     assert np.array_equal(st.cpu().numpy().astype(np.uint32), ost)
     b.close()
 

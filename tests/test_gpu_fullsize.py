@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 from test_gpu_trace import assert_hits_equal
+from bitcmp import same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -39,7 +40,7 @@ def test_full_frame_build_and_trace(gpu_ctx, oracle_mod, frames):
         onodes, oids, okeys, reached = oracle_mod.lbvh_build(tris, 20)
         assert np.array_equal(keys, okeys) and np.array_equal(ids, oids)
         r = np.nonzero(reached)[0]
-        assert np.array_equal(nodes[r], onodes[r])
+        assert same_bits(nodes[r], onodes[r])
         oh = oracle_mod.trace(onodes, 20, oids, tris, oracle_mod.primary_rays(cam))
         ovis, omir = oracle_mod.shadow_mirror(onodes, 20, oids, tris, cam, light, oh)
         assert_hits_equal(hits_to_numpy(hits), oh, "primary")

@@ -3,6 +3,7 @@ replays to the same bits as the direct calls, frame after frame (the refit's
 arrival epoch lives in device memory, so replays stay correct)."""
 import numpy as np
 import pytest
+from bitcmp import same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -37,10 +38,10 @@ def test_graph_frames_equal_direct_calls(gpu_ctx):
             gpu_ctx.check()
             d_nodes, d_ids, d_keys = lb_d.download(True, True, True)
             assert np.array_equal(g_keys, d_keys) and np.array_equal(g_ids, d_ids)
-            assert np.array_equal(g_nodes, d_nodes), f"replay {rep} frame {k}: nodes differ"
-            assert np.array_equal(gp, hits_to_numpy(dp))
+            assert same_bits(g_nodes, d_nodes), f"replay {rep} frame {k}: nodes differ"
+            assert same_bits(gp, hits_to_numpy(dp))
             assert np.array_equal(gv, dv.cpu().numpy())
-            assert np.array_equal(gm, hits_to_numpy(dm))
+            assert same_bits(gm, hits_to_numpy(dm))
     for g in graphs:
         g.close()
 

@@ -8,6 +8,7 @@ Adjoint: against the oracle's FP64 adjoint and central finite differences
 """
 import numpy as np
 import pytest
+from bitcmp import same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -39,7 +40,7 @@ def test_pathtrace_matches_cpu(gpu_ctx, oracle_mod, gi_small):
     ref = oracle_mod.pathtrace(nodes, depth, ids, sc.tris, sc.albedo, sc.emission, cam, 3, 4, 1234)
     rmse = np.sqrt(np.mean((img[:, :3].astype(np.float64) - ref[:, :3]) ** 2, axis=0))
     assert np.all(rmse <= 1e-4), rmse
-    assert np.array_equal(img, ref)
+    assert same_bits(img, ref)
     assert img[:, :3].mean() > 0.0
 
 
@@ -90,3 +91,60 @@ def test_adjoint_matches_fp64_and_fd(gpu_ctx, oracle_mod, gi_small):
         a_m = sc.albedo.copy(); a_m.ravel()[k] -= h
         fd = (loss_at(a_p) - loss_at(a_m)) / (2 * h)
         assert abs(fd - ref_alb.ravel()[k]) <= 2e-2 * abs(ref_alb.ravel()[k]) + 1e-9, (k, fd, ref_alb.ravel()[k])
+
+
+def test_progressive_accumulation_across_calls(gpu_ctx, oracle_mod, gi_small):
+    """rt_pt_params.first_sample = n0 continues the progressive mean the image
+    holds (the reference's frame counter, RayTracerCS.cpp:306, with the
+    factors of ConstantBuffers.h:102-109): 2 spp from n0 = 0 then 2 spp from
+    n0 = 2 equal one call of 4 spp bit for bit, and the oracle's
+    continuation; n0 = 0 starts afresh (the reset on camera motion)."""
+    import torch
+    from rtgpu import scenes
+    from rtgpu.api import RayTracer
+    sc, lb, dt, nodes, ids, depth = gi_small
+    cam = scenes.gi_camera(64, 48)
+    alb = torch.from_numpy(sc.albedo).cuda()
+    em = torch.from_numpy(sc.emission).cuda()
+    rt = RayTracer(gpu_ctx)
+    full = rt.pathtrace(lb, alb, em, cam, spp=4, bounces=3, seed=77).cpu().numpy()
+    img = torch.full((cam.width * cam.height, 4), 123.0, device="cuda")  # not read at n0 = 0
+    rt.pathtrace(lb, alb, em, cam, spp=2, bounces=3, seed=77, out=img)
+    half = img.cpu().numpy()
+    rt.pathtrace(lb, alb, em, cam, spp=2, bounces=3, seed=77, out=img, first_sample=2)
+    gpu_ctx.check()
+    assert same_bits(img.cpu().numpy(), full)
+    o_half = oracle_mod.pathtrace(nodes, depth, ids, sc.tris, sc.albedo, sc.emission, cam, 2, 3, 77)
+    assert same_bits(o_half, half)
+    o_cont = oracle_mod.pathtrace(nodes, depth, ids, sc.tris, sc.albedo, sc.emission, cam, 2, 3, 77,
+                                  first_sample=2, image=o_half)
+    assert same_bits(o_cont, full)
+    # frames of one sample each, as the reference renders (n0 = frame count)
+    rt.pathtrace(lb, alb, em, cam, spp=1, bounces=3, seed=77, out=img)
+    for n0 in (1, 2, 3):
+        rt.pathtrace(lb, alb, em, cam, spp=1, bounces=3, seed=77, out=img, first_sample=n0)
+    gpu_ctx.check()
+    assert same_bits(img.cpu().numpy(), full)
+
+
+def test_progressive_adjoint_differentiates_the_new_samples(gpu_ctx, oracle_mod, gi_small):
+    """The adjoint of a call with n0 > 0 weights each new sample by its
+    weight in the final mean; the FP64 oracle with the same n0 agrees."""
+    import torch
+    from rtgpu import scenes
+    from rtgpu.api import RayTracer
+    sc, lb, dt, nodes, ids, depth = gi_small
+    cam = scenes.gi_camera(40, 32)
+    rt = RayTracer(gpu_ctx)
+    alb = torch.from_numpy(sc.albedo).cuda()
+    em = torch.from_numpy(sc.emission).cuda()
+    rng = np.random.default_rng(3)
+    g = rng.normal(size=(cam.width * cam.height, 4)).astype(np.float32)
+    g[:, 3] = 0.0
+    d_alb, d_le = rt.pathtrace_adjoint(lb, alb, em, cam, 3, 2, 55, torch.from_numpy(g).cuda(), first_sample=2)
+    gpu_ctx.check()
+    ref_alb, ref_le = oracle_mod.pathtrace_adjoint(nodes, depth, ids, sc.tris, sc.albedo, sc.emission, cam, 3, 2, 55,
+                                                   g, first_sample=2)
+    scale = np.abs(ref_alb).max()
+    assert scale > 0
+    assert np.abs(d_alb.cpu().numpy().astype(np.float64) - ref_alb).max() <= 1e-4 * scale

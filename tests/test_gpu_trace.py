@@ -7,6 +7,7 @@ import pytest
 
 from conftest import camera_from_array, golden_cases, load_golden
 import tri_np
+from bitcmp import same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -26,8 +27,8 @@ def assert_hits_equal(gpu, ref, what):
     hit = ref["id"] >= 0
     t_rel = np.abs(gpu["t"][hit] - ref["t"][hit]) / np.maximum(np.abs(ref["t"][hit]), 1e-30)
     assert t_rel.max(initial=0.0) <= 1e-6, what
-    # the kernels evaluate the reference's operation order without contraction: exact
-    assert np.array_equal(gpu["t"], ref["t"]) and np.array_equal(gpu["u"], ref["u"]) and np.array_equal(gpu["v"], ref["v"])
+    # the kernels evaluate the reference's operation order without contraction: equal bits
+    assert same_bits(gpu["t"], ref["t"]) and same_bits(gpu["u"], ref["u"]) and same_bits(gpu["v"], ref["v"]), what
 
 
 @pytest.fixture(scope="module")
