@@ -109,8 +109,9 @@ __global__ void __launch_bounds__(256) k_bounds(const float* __restrict__ tris, 
     for (uint32_t i = gtid; i < lookback_words; i += gstride) lookback[i] = 0u;
     // counters: [0] bounds ticket (reset by the last block), [1..4] sort tile
     // tickets, [5] leaf count, [6] refit epoch (advanced once per build, so a
-    // replayed CUDA graph of the build still tags every arrival afresh)
-    if (gtid >= 1 && gtid < 6) counters[gtid] = 0u;
+    // replayed CUDA graph of the build still tags every arrival afresh), [7]
+    // spine-node count
+    if ((gtid >= 1 && gtid < 6) || gtid == 7) counters[gtid] = 0u;
     if (gtid == 0) {
         uint32_t e = counters[6] + 1u;
         counters[6] = e ? e : 1u;  // 0 is the value of cleared arrival words
@@ -485,8 +486,9 @@ __device__ __forceinline__ uint32_t warp_reduce_ordered(uint32_t v) {
 
 // Block-wide exclusive prefix (fwd, from the left) and exclusive suffix
 // (bwd, from the right) of one value pair per thread, 256 threads.
+template <int THREADS = kEmitThreads>
 __device__ __forceinline__ void block_scan_records(uint32_t vf, uint32_t vb, uint32_t* pre_f, uint32_t* suf_b,
-                                                   uint32_t* s_f /*8*/, uint32_t* s_b /*8*/) {
+                                                   uint32_t* s_f /*THREADS / 32*/, uint32_t* s_b /*THREADS / 32*/) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     uint32_t xf = vf;
 #pragma unroll
@@ -505,7 +507,7 @@ __device__ __forceinline__ void block_scan_records(uint32_t vf, uint32_t vb, uin
     __syncthreads();
     uint32_t wf = 0, wb = 0;
     for (int q = 0; q < w; ++q) wf = rec_fwd(wf, s_f[q]);
-    for (int q = (kEmitThreads / 32) - 1; q > w; --q) wb = rec_bwd(s_b[q], wb);
+    for (int q = (THREADS / 32) - 1; q > w; --q) wb = rec_bwd(s_b[q], wb);
     __syncthreads();
     uint32_t ef = __shfl_up_sync(kFull, xf, 1);
     if (lane == 0) ef = 0;
@@ -908,6 +910,584 @@ __global__ void __launch_bounds__(256) k_emit_refit(const uint32_t* __restrict__
     }
 }
 
+// ---------------------------------------------------------------------------
+// Emission and refit without global atomics (the single-scene build).
+//
+// k_emit_units handles one tile of kEmitTile sorted elements:
+//   1. per element: ancestor record mask (two scans), head / tail of its
+//      leaf's range, and at heads and tails the mask capped at the leaf depth
+//      and the leaf's heap index; the tile's leaves become "units" in sorted
+//      order;
+//   2. the triangles gathered in sorted order (sorted_tris), each thread over
+//      its own eight consecutive elements, and their boxes folded per leaf (a
+//      segmented scan carries a leaf that spans threads, with its head); the
+//      leaf records are stored;
+//   3. a leaf that began in an earlier tile and ends in this one is finished
+//      here: its start is found by scanning back over the codes and its
+//      earlier triangles are folded in from the soup.
+// k_emit_merge then runs a shared-memory bottom-up (unit_bottom_up) over one
+// tile's units per CTA; a node whose parent's split boundary lies outside
+// the units becomes an "item" for the next level, and k_emit_merge runs
+// again over the items of kMergeGroup consecutive tiles (groups) per CTA,
+// level after level, until one CTA forms the root.  No node waits on another
+// CTA, and nothing needs a global arrival word.
+//
+// The parent's split bit is the lowest bit of a node's remaining ancestor
+// mask, so no walk reads a Morton code.  Boxes are min / max in the
+// reference's operand order (left before right, earlier triangle first),
+// which fixes the sign of a zero bound; a node's box is the ordered fold of
+// its triangles' boxes, whatever the grouping.
+constexpr uint32_t kHeadBit = 1u << 30;
+constexpr uint32_t kTailBit = 1u << 31;
+constexpr uint32_t kMaskBits = kHeadBit - 1u;
+constexpr int kUnitCap = kEmitTile;  // units of one CTA: the leaves of a tile, the items of a group
+constexpr int kItemCap = 64;         // items one tile or group hands on (2 x depth + 2 <= 54)
+constexpr int kMergeGroup = 32;      // tiles (groups) per CTA of the next level
+constexpr int kUnitWords = 12;       // shared words per unit
+constexpr size_t kUnitSmem = (size_t)kUnitWords * kUnitCap * sizeof(uint32_t) + 16;
+
+// Leaf axis field: the reference's round-robin counter at the call that made
+// the leaf (see refit_walk), with the parent's split bit = the lowest bit of
+// the leaf's capped ancestor mask m (depth = popcount of m).
+__device__ __forceinline__ int leaf_axis_of(uint32_t m, int32_t count, uint32_t depth) {
+    const int dh = __popc(m);
+    if (dh == 0) return (count <= 1 || depth <= 1) ? 0 : 1;
+    if (count == 1 || dh == (int)depth - 1) return (31 - (__ffs(m) - 1)) % 3;
+    return 1;
+}
+
+__device__ __forceinline__ void store_node(rt_node* nodes, uint32_t h, const float mn[3], const float mx[3],
+                                           int32_t prim_count, int32_t prim_pos) {
+    float4* p = reinterpret_cast<float4*>(nodes + h);
+    p[0] = make_float4(mn[0], mn[1], mn[2], mx[0]);
+    p[1] = make_float4(mx[1], mx[2], __int_as_float(prim_count), __int_as_float(prim_pos));
+}
+
+// Ordered union of two boxes (a holds the earlier triangles).
+struct Box {
+    float lo[3], hi[3];
+};
+__device__ __forceinline__ Box box_union(const Box& a, const Box& b) {
+    Box r;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        r.lo[c] = smin(a.lo[c], b.lo[c]);
+        r.hi[c] = smax(a.hi[c], b.hi[c]);
+    }
+    return r;
+}
+__device__ __forceinline__ Box empty_box() {
+    Box r;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        r.lo[c] = INFINITY;
+        r.hi[c] = -INFINITY;
+    }
+    return r;
+}
+// gMinVertices / gMaxVertices (LBVH.cpp:505-509): min(V0, min(V1, V2))
+__device__ __forceinline__ Box tri_box(const float v[9]) {
+    Box r;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        r.lo[c] = smin(v[c], smin(v[3 + c], v[6 + c]));
+        r.hi[c] = smax(v[c], smax(v[3 + c], v[6 + c]));
+    }
+    return r;
+}
+__device__ __forceinline__ Box shfl_box(const Box& b, int src) {
+    Box r;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        r.lo[c] = __shfl_sync(kFull, b.lo[c], src);
+        r.hi[c] = __shfl_sync(kFull, b.hi[c], src);
+    }
+    return r;
+}
+__device__ __forceinline__ Box shfl_up_box(const Box& b, int off) {
+    Box r;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        r.lo[c] = __shfl_up_sync(kFull, b.lo[c], off);
+        r.hi[c] = __shfl_up_sync(kFull, b.hi[c], off);
+    }
+    return r;
+}
+
+// Shared-memory view of a CTA's units: unit i covers elements
+// [pos[i], pos[i + 1]) and is the node (h[i], m[i]) with box lo/hi[i];
+// arrivals of the bottom-up reuse the box slots and aext / am.
+struct Units {
+    float* lo;      // [3][kUnitCap]
+    float* hi;      // [3][kUnitCap]
+    int32_t* pos;   // [kUnitCap + 1]
+    uint32_t* h;    // [kUnitCap]
+    uint32_t* m;    // [kUnitCap]
+    int32_t* aext;  // [kUnitCap] arrival: the far unit index of the arriving node
+    uint32_t* am;   // [kUnitCap] arrival: the arriving node's remaining mask
+    uint32_t* arr;  // [kUnitCap] arrival bits of the boundary after unit i (1 left child, 2 right child)
+    uint32_t* n_items;
+};
+__device__ __forceinline__ Units units_of(uint32_t* smem) {
+    Units u;
+    u.lo = reinterpret_cast<float*>(smem);
+    u.hi = u.lo + 3 * kUnitCap;
+    u.pos = reinterpret_cast<int32_t*>(u.hi + 3 * kUnitCap);
+    u.h = reinterpret_cast<uint32_t*>(u.pos + kUnitCap + 4);
+    u.m = u.h + kUnitCap;
+    u.aext = reinterpret_cast<int32_t*>(u.m + kUnitCap);
+    u.am = reinterpret_cast<uint32_t*>(u.aext + kUnitCap);
+    u.arr = u.am + kUnitCap;
+    u.n_items = u.arr + kUnitCap;
+    return u;
+}
+__device__ __forceinline__ void set_box(const Units& u, int i, const Box& b) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        u.lo[c * kUnitCap + i] = b.lo[c];
+        u.hi[c * kUnitCap + i] = b.hi[c];
+    }
+}
+__device__ __forceinline__ Box get_box(const Units& u, int i) {
+    Box b;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        b.lo[c] = u.lo[c * kUnitCap + i];
+        b.hi[c] = u.hi[c * kUnitCap + i];
+    }
+    return b;
+}
+
+__device__ __forceinline__ void push_item(const Units& u, uint2* items, uint32_t h, uint32_t m, uint32_t* err) {
+    const uint32_t slot = atomicAdd(u.n_items, 1u);
+    if (slot < (uint32_t)kItemCap) items[slot] = make_uint2(h, m);
+    else atomicOr(err, RT_DEVERR_BOUNDS);
+}
+
+// Bottom-up over units 0 .. U-1 (arr[] zero, every unit's box, pos, h, m
+// set, pos[U] = one past the last unit's last element, *n_items zero).  Each
+// node arrives at the boundary between its parent's two children: a left
+// child leaves its box, far unit and mask at its last unit's slot, a right
+// child at its first unit's slot, then sets its bit; the second arrival
+// forms the parent and carries on.  Nodes whose parent boundary lies outside
+// the units, and arrivals whose sibling never came, become items.
+template <int THREADS>
+__device__ void unit_bottom_up(const Units& u, int U, rt_node* nodes, uint2* items, uint32_t* err,
+                               uint32_t* inner) {
+#pragma unroll 1
+    for (int i = threadIdx.x; i < U; i += THREADS) {
+        Box b = get_box(u, i);
+        uint32_t h = u.h[i], m = u.m[i];
+        int li = i, ri = i;
+        while (h > 1) {
+            const bool left = (h & 1u) == 0;
+            const int k = left ? ri : li - 1;  // the parent's split boundary, after unit k
+            if (k < 0 || k + 1 >= U) {
+                push_item(u, items, h, m, err);
+                break;
+            }
+            const int area = left ? ri : li;
+            set_box(u, area, b);
+            u.aext[area] = left ? li : ri;
+            u.am[area] = m;
+            __threadfence_block();
+            const uint32_t old = atomicOr(&u.arr[k], left ? 1u : 2u);
+            if (old == 0u) break;  // first: the sibling forms the parent
+            __threadfence_block();
+            const int sarea = left ? k + 1 : k;
+            const Box sb = get_box(u, sarea);
+            b = left ? box_union(b, sb) : box_union(sb, b);
+            if (left) ri = u.aext[sarea]; else li = u.aext[sarea];
+            const int d = __ffs(m) - 1;  // the parent's split bit
+            m &= m - 1u;
+            h >>= 1;
+            const int32_t pos = u.pos[li], end = u.pos[ri + 1] - 1;
+            store_node(nodes, h, b.lo, b.hi, ((end - pos + 1) << 3) | ((30 - d) % 3), pos);
+            if (inner) atomicOr(inner + (h >> 5), 1u << (h & 31));
+        }
+    }
+    __syncthreads();
+    // arrivals whose sibling lies outside the units: their node is an item
+    for (int k = threadIdx.x; k + 1 < U; k += THREADS) {
+        const uint32_t v = u.arr[k];
+        if (v != 1u && v != 2u) continue;
+        const int area = v == 1u ? k : k + 1;
+        const int li = v == 1u ? u.aext[area] : area;
+        const uint32_t m = u.am[area];
+        const int up = __popc(u.m[li]) - __popc(m);
+        if (up < 0) {
+            atomicOr(err, RT_DEVERR_BOUNDS);
+            continue;
+        }
+        push_item(u, items, u.h[li] >> up, m, err);
+    }
+}
+
+// Heap index of an element: 1 followed by its code's bits at the positions of
+// its capped ancestor mask m, high to low.
+__device__ __forceinline__ uint32_t heap_index(uint32_t code, uint32_t m) {
+    uint32_t h = 1u;
+    while (m) {
+        const int b = hb(m);
+        h = (h << 1) | ((code >> b) & 1u);
+        m ^= 1u << b;
+    }
+    return h;
+}
+
+// The open segment at a thread's end for the segmented scan of leaf boxes:
+// its box and the position of its head (-1: it began before the tile).
+struct Seg {
+    Box b;
+    int32_t head;
+};
+
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) k_emit_units(const uint32_t* __restrict__ keys,
+                                                        const uint32_t* __restrict__ ids,
+                                                        const float* __restrict__ tris, uint32_t n, uint32_t depth,
+                                                        const uint32_t* __restrict__ scan, rt_node* nodes,
+                                                        float4* __restrict__ sorted_tris, uint2* units,
+                                                        uint32_t* unit_counts, uint32_t* err) {
+    __shared__ uint32_t s_f[THREADS / 32], s_b[THREADS / 32], s_tmp[THREADS / 32];
+    __shared__ uint32_t s_first_head, s_first_tail, s_last_head, s_last_tail, s_cont_tail;
+    __shared__ float s_red[THREADS / 32][6];
+    __shared__ int32_t s_rhead[THREADS / 32];
+    __shared__ int s_found;
+    __shared__ float s_cont_box[6];
+
+    grid_dep_wait();
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const uint32_t tbase = blockIdx.x * (uint32_t)kEmitTile;
+    uint2* my_units = units + (size_t)blockIdx.x * kUnitCap;
+    if (t == 0) {
+        s_first_head = s_first_tail = kEmitTile;
+        s_last_head = s_last_tail = 0u;
+    }
+
+    // 1. capped mask, head and tail of this thread's elements; heap index at
+    // heads and tails (the elements between them share their leaf's)
+    const uint32_t s = tbase + (uint32_t)t * kEmitItems;
+    EmitChunk e;
+    load_chunk(keys, n, s, e);
+    uint32_t af = 0, ab = 0;
+#pragma unroll
+    for (int q = 0; q < kEmitItems; ++q) af = rec_fwd(af, e.r[q]);
+#pragma unroll
+    for (int q = kEmitItems - 1; q >= 0; --q) ab = rec_bwd(e.r[q], ab);
+    uint32_t pre, suf;
+    block_scan_records<THREADS>(af, ab, &pre, &suf, s_f, s_b);  // includes __syncthreads
+    uint32_t L[kEmitItems + 1], R[kEmitItems + 1];
+    L[0] = rec_fwd(scan[4 * blockIdx.x + 2], pre);
+    R[kEmitItems] = rec_bwd(suf, scan[4 * blockIdx.x + 3]);
+#pragma unroll
+    for (int q = 0; q < kEmitItems; ++q) L[q + 1] = rec_fwd(L[q], e.r[q]);
+#pragma unroll
+    for (int q = kEmitItems - 1; q >= 0; --q) R[q] = rec_bwd(e.r[q], R[q + 1]);
+    const int leaf_depth = (int)depth - 1;
+    uint32_t hm[kEmitItems], hh[kEmitItems];  // capped mask | head | tail; heap index (heads, tails)
+    uint32_t heads = 0u;
+#pragma unroll
+    for (int q = 0; q < kEmitItems; ++q) {
+        const uint32_t k = s + q;
+        hm[q] = 0u;
+        hh[q] = 0u;
+        if (k < n) {
+            const uint32_t anc = L[q] | R[q];
+            const int dprev = e.dl[q], dcur = e.dl[q + 1];
+            const bool head = (k == 0) || (dprev >= 0 && __popc(keep_above(anc, dprev)) < leaf_depth);
+            const bool tail = (k == n - 1) || (dcur >= 0 && __popc(keep_above(anc, dcur)) < leaf_depth);
+            if (head || tail) {
+                // the capped mask and heap index: at heads, and at a tail that
+                // may close a leaf whose head is in an earlier thread (a tail
+                // after a head of this thread shares that head's)
+                uint32_t m = 0u;
+                if (head || heads == 0u) {
+                    int dep = __popc(anc);
+                    m = anc;
+                    while (dep > leaf_depth) { m &= m - 1u; --dep; }
+                    hh[q] = heap_index(e.c[q], m);
+                }
+                hm[q] = m | (head ? kHeadBit : 0u) | (tail ? kTailBit : 0u);
+                const uint32_t j = t * kEmitItems + q;
+                if (head) {
+                    heads |= 1u << q;
+                    atomicMin(&s_first_head, j);
+                    atomicMax(&s_last_head, j + 1);
+                }
+                if (tail) {
+                    atomicMin(&s_first_tail, j);
+                    atomicMax(&s_last_tail, j + 1);
+                }
+            }
+        }
+    }
+    const uint32_t hbase = block_excl_sum_256(__popc(heads), s_tmp);  // includes __syncthreads
+    // units: the leaf that began in an earlier tile and ends here (unit 0),
+    // then every leaf with its head and tail in the tile; a last leaf that
+    // runs past the tile is the next tile's
+    const uint32_t first_head = s_first_head, first_tail = s_first_tail;
+    const uint32_t cont = (first_tail < kEmitTile && first_tail < first_head) ? 1u : 0u;
+    const bool last_open = s_last_head > s_last_tail;  // the last head's leaf has no tail in the tile
+
+    // 2. pre-gather in sorted order (A.xyz,id | B.xyz,0 | C.xyz,0) and the leaf
+    // boxes: each thread folds its own elements; a leaf spanning threads is
+    // carried by a segmented scan that also carries the leaf's head position
+    Box part = empty_box();  // elements before the thread's first head (or all of them)
+    Box run = empty_box();   // the current leaf since its head in this thread
+    bool seen_head = false, closed = false;
+    int first_tail_q = -1;
+    uint32_t ft_h = 0u, ft_m = 0u;  // heap index and mask of the first segment's tail
+    uint32_t ord = 0;
+    int32_t run_pos = -1;
+    uint32_t run_h = 0u, run_m = 0u;  // heap index and mask of the current leaf
+#pragma unroll
+    for (int q = 0; q < kEmitItems; ++q) {
+        const uint32_t k = s + q;
+        if (k >= n) break;
+        uint32_t id = __ldg(ids + k);
+        if (id >= n) {  // only after a failed sort (look-back timeout)
+            atomicOr(err, RT_DEVERR_BOUNDS);
+            id = 0;
+        }
+        const float* tp = tris + 9 * (size_t)id;
+        float v[9];
+#pragma unroll
+        for (int c = 0; c < 9; ++c) v[c] = __ldg(tp + c);
+        sorted_tris[3 * (size_t)k + 0] = make_float4(v[0], v[1], v[2], __int_as_float((int)id));
+        sorted_tris[3 * (size_t)k + 1] = make_float4(v[3], v[4], v[5], 0.0f);
+        sorted_tris[3 * (size_t)k + 2] = make_float4(v[6], v[7], v[8], 0.0f);
+        const Box tb = tri_box(v);
+        const bool head = (hm[q] & kHeadBit) != 0, tail = (hm[q] & kTailBit) != 0;
+        if (head) {
+            const uint32_t idx = cont + hbase + ord++;
+            const uint32_t j = t * kEmitItems + q;
+            run_h = hh[q];
+            run_m = hm[q] & kMaskBits;
+            if (idx < (uint32_t)kUnitCap && !(last_open && j + 1 == s_last_head)) my_units[idx] = make_uint2(run_h, run_m);
+            run = tb;
+            seen_head = true;
+            run_pos = (int32_t)k;
+        } else if (!seen_head && !closed) {
+            part = box_union(part, tb);
+        } else if (seen_head) {
+            run = box_union(run, tb);
+        }
+        if (tail) {
+            if (seen_head) {  // a leaf with head and tail in this thread
+                const int32_t count = (int32_t)k - run_pos + 1;
+                store_node(nodes, run_h, run.lo, run.hi, (count << 3) | 4 | leaf_axis_of(run_m, count, depth), run_pos);
+                seen_head = false;  // the next element is a head
+            } else {
+                first_tail_q = q;
+                ft_h = hh[q];
+                ft_m = hm[q] & kMaskBits;
+            }
+            closed = true;
+        }
+    }
+    // segmented exclusive scan of the open segment at each thread's end;
+    // reset = the thread holds a head or a tail
+    const bool reset = heads != 0u || closed;
+    Seg x;
+    x.b = seen_head ? run : (closed ? empty_box() : part);
+    x.head = seen_head ? run_pos : -1;
+    {
+        bool r = reset;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const Box yb = shfl_up_box(x.b, off);
+            const int32_t yh = __shfl_up_sync(kFull, x.head, off);
+            const bool ry = __shfl_up_sync(kFull, r, off);
+            if (lane >= off && !r) {
+                x.b = box_union(yb, x.b);
+                x.head = yh;
+                r = ry;
+            }
+        }
+        if (lane == 31) {
+            for (int c = 0; c < 3; ++c) { s_red[w][c] = x.b.lo[c]; s_red[w][3 + c] = x.b.hi[c]; }
+            s_rhead[w] = x.head;
+            s_tmp[w] = r ? 1u : 0u;
+        }
+        __syncthreads();
+        Seg wp;  // the open segment entering this warp
+        wp.b = empty_box();
+        wp.head = -1;
+        for (int ww = w - 1; ww >= 0; --ww) {
+            Box y;
+            for (int c = 0; c < 3; ++c) { y.lo[c] = s_red[ww][c]; y.hi[c] = s_red[ww][3 + c]; }
+            wp.b = box_union(y, wp.b);
+            wp.head = s_rhead[ww];
+            if (s_tmp[ww]) break;
+        }
+        Seg ex;
+        ex.b = shfl_up_box(x.b, 1);
+        ex.head = __shfl_up_sync(kFull, x.head, 1);
+        const bool rex = __shfl_up_sync(kFull, r, 1);
+        if (lane == 0) {
+            ex = wp;
+        } else if (!rex) {
+            ex.b = box_union(wp.b, ex.b);
+            ex.head = wp.head;
+        }
+        x = ex;  // the open segment entering this thread
+    }
+    if (first_tail_q >= 0) {  // the segment entering this thread ends here
+        const Box fin = box_union(x.b, part);
+        const uint32_t j = t * kEmitItems + first_tail_q;
+        if (x.head >= 0) {  // its head is in an earlier thread of this tile
+            const int32_t count = (int32_t)(tbase + j) - x.head + 1;
+            store_node(nodes, ft_h, fin.lo, fin.hi, (count << 3) | 4 | leaf_axis_of(ft_m, count, depth), x.head);
+        } else {  // it began before the tile: finished in step 3
+            for (int c = 0; c < 3; ++c) { s_cont_box[c] = fin.lo[c]; s_cont_box[3 + c] = fin.hi[c]; }
+            s_cont_tail = tbase + j;
+            my_units[0] = make_uint2(ft_h, ft_m);
+        }
+    }
+    __syncthreads();
+
+    // 3. the leaf that began in an earlier tile: its start (the nearest
+    // boundary where the codes differ at or above its parent's split bit) and
+    // the boxes of its triangles before this tile, folded in order with the rest
+    if (cont) {
+        const uint32_t m0 = my_units[0].y;
+        const int dpar = m0 ? __ffs(m0) - 1 : 31;  // a root leaf starts at 0
+        if (t == 0) s_found = 0;
+        __syncthreads();
+        int32_t start = 0;
+        for (int64_t hi = (int64_t)tbase; hi > 0; hi -= THREADS) {
+            const int64_t q = hi - t;  // candidate start: boundary (q - 1, q)
+            bool hit = false;
+            if (q >= 1) {
+                const uint32_t a = __ldg(keys + q - 1), c = __ldg(keys + q);
+                hit = a != c && hb(a ^ c) >= dpar;
+            }
+            if (__syncthreads_or(hit)) {
+                if (hit) atomicMax(&s_found, (int)q);
+                __syncthreads();
+                start = s_found;
+                break;
+            }
+        }
+        Box before = empty_box();
+        for (int64_t c0 = start; c0 < (int64_t)tbase; c0 += THREADS) {
+            const int64_t k = c0 + t;
+            Box tb = empty_box();
+            if (k < (int64_t)tbase) {
+                uint32_t id = __ldg(ids + k);
+                if (id >= n) id = 0;
+                const float* tp = tris + 9 * (size_t)id;
+                float v[9];
+                for (int c = 0; c < 9; ++c) v[c] = __ldg(tp + c);
+                tb = tri_box(v);
+            }
+            // ordered block reduction of the chunk: lanes, then warps, in order
+            for (int off = 1; off < 32; off <<= 1) {
+                const Box y = shfl_up_box(tb, off);
+                if (lane >= off) tb = box_union(y, tb);
+            }
+            if (lane == 31)
+                for (int c = 0; c < 3; ++c) { s_red[w][c] = tb.lo[c]; s_red[w][3 + c] = tb.hi[c]; }
+            __syncthreads();
+            if (t == 0) {
+                for (int ww = 0; ww < THREADS / 32; ++ww) {
+                    Box y;
+                    for (int c = 0; c < 3; ++c) { y.lo[c] = s_red[ww][c]; y.hi[c] = s_red[ww][3 + c]; }
+                    before = box_union(before, y);
+                }
+            }
+            __syncthreads();
+        }
+        if (t == 0) {
+            Box in_tile;
+            for (int c = 0; c < 3; ++c) { in_tile.lo[c] = s_cont_box[c]; in_tile.hi[c] = s_cont_box[3 + c]; }
+            const Box fin = box_union(before, in_tile);
+            const int32_t count = (int32_t)s_cont_tail - start + 1;
+            const uint2 u0 = my_units[0];
+            store_node(nodes, u0.x, fin.lo, fin.hi, (count << 3) | 4 | leaf_axis_of(u0.y, count, depth), start);
+        }
+    }
+    if (t == THREADS - 1) {  // units: cont + heads, less an open last leaf
+        const uint32_t total_heads = hbase + __popc(heads);
+        unit_counts[blockIdx.x] = min((uint32_t)kUnitCap, cont + total_heads - (last_open ? 1u : 0u));
+    }
+}
+
+// k_emit_merge: the shared-memory bottom-up over the units of `group`
+// consecutive tiles (groups) of the previous level, whose stored records
+// give each unit's box and range: at the tile level one tile per CTA (its
+// leaves, in order), above it kMergeGroup groups per CTA (their items,
+// sorted here by first element).  The nodes that cannot be formed here are
+// this CTA's items for the next level.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) k_emit_merge(const uint2* __restrict__ in_items,
+                                                        const uint32_t* __restrict__ in_counts, uint32_t in_stride,
+                                                        uint32_t group, uint32_t n_in, uint32_t depth, rt_node* nodes,
+                                                        uint2* out_items, uint32_t* out_counts, uint32_t* err,
+                                                        uint32_t* inner) {
+    extern __shared__ __align__(16) uint32_t smem[];
+    const Units u = units_of(smem);
+    __shared__ uint32_t s_off[kMergeGroup + 1];
+    __shared__ uint2 s_items[kItemCap];
+    __shared__ int32_t s_ipos[kItemCap];
+    grid_dep_wait();
+    const int t = threadIdx.x;
+    const uint32_t g0 = blockIdx.x * group;
+    const uint32_t ng = min(group, n_in - g0);
+    if (t < 32) {  // unit offsets of the groups: one warp, a prefix sum over <= 32 counts
+        const uint32_t c = (uint32_t)t < ng ? min(in_counts[g0 + t], in_stride) : 0u;
+        uint32_t incl = c;
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, incl, off);
+            if (t >= off) incl += y;
+        }
+        if ((uint32_t)t < ng) s_off[t] = incl - c;
+        if ((uint32_t)t == ng - 1) s_off[ng] = incl;
+        if (t == 0) *u.n_items = 0u;
+    }
+    for (int i = t; i < kUnitCap; i += THREADS) u.arr[i] = 0u;
+    __syncthreads();
+    const int U = (int)min(s_off[ng], (uint32_t)kUnitCap);
+    // every group's units are in order (tile leaves, or items sorted by the
+    // CTA that made them), so their concatenation is sorted
+    for (int i = t; i < U; i += THREADS) {
+        uint32_t g = 0;
+        while (g + 1 < ng && s_off[g + 1] <= (uint32_t)i) ++g;
+        uint2 it = in_items[(size_t)(g0 + g) * in_stride + (i - s_off[g])];
+        if (it.x < 1u || it.x >= (1u << depth)) {
+            atomicOr(err, RT_DEVERR_BOUNDS);
+            it = make_uint2(1u, 0u);  // a root stops the walk
+        }
+        const float4 a = __ldcg(reinterpret_cast<const float4*>(nodes + it.x));
+        const float4 b = __ldcg(reinterpret_cast<const float4*>(nodes + it.x) + 1);
+        u.h[i] = it.x;
+        u.m[i] = it.y;
+        u.lo[0 * kUnitCap + i] = a.x;
+        u.lo[1 * kUnitCap + i] = a.y;
+        u.lo[2 * kUnitCap + i] = a.z;
+        u.hi[0 * kUnitCap + i] = a.w;
+        u.hi[1 * kUnitCap + i] = b.x;
+        u.hi[2 * kUnitCap + i] = b.y;
+        u.pos[i] = __float_as_int(b.w);
+        if (i == U - 1) u.pos[U] = __float_as_int(b.w) + (__float_as_int(b.z) >> 3);
+    }
+    __syncthreads();
+    unit_bottom_up<THREADS>(u, U, nodes, s_items, err, inner);
+    __syncthreads();
+    // this CTA's items, sorted by first element (their records are stored)
+    const uint32_t ni = min(*u.n_items, (uint32_t)kItemCap);
+    for (uint32_t i = t; i < ni; i += THREADS) s_ipos[i] = __ldcg(&nodes[s_items[i].x].prim_pos);
+    __syncthreads();
+    uint2* out = out_items + (size_t)blockIdx.x * kItemCap;
+    for (uint32_t i = t; i < ni; i += THREADS) {
+        uint32_t rank = 0;
+        for (uint32_t o = 0; o < ni; ++o) rank += (s_ipos[o] < s_ipos[i] || (s_ipos[o] == s_ipos[i] && o < i)) ? 1u : 0u;
+        out[rank] = s_items[i];
+    }
+    if (t == 0) out_counts[blockIdx.x] = ni;
+}
+
 // Compact layout (rt_lbvh.cnodes) from the heap: inner_rank = exclusive
 // popcount prefix of the internal-node bitmap (one block), then every
 // reachable internal node x writes its two children at slots 2 rank(x) + 2
@@ -1015,8 +1595,10 @@ extern "C" rt_status rt_lbvh_create(rt_ctx* ctx, uint32_t max_tris, uint32_t dep
     alloc((void**)&l->nodes, sizeof(rt_node) * l->num_nodes);
     alloc((void**)&l->keys, 4 * cap);
     alloc((void**)&l->ids, 4 * cap);
-    alloc((void**)&l->keys_alt, 4 * cap);
-    alloc((void**)&l->ids_alt, 4 * cap);
+    // one block for both ping-pong buffers: after the sort it holds the
+    // emission's per-tile unit lists (8 bytes per element)
+    alloc((void**)&l->keys_alt, 8 * cap);
+    if (e == cudaSuccess) l->ids_alt = l->keys_alt + cap;
     alloc((void**)&l->sorted_tris, sizeof(float4) * 3 * cap);
     l->ccap = (uint32_t)std::min<uint64_t>((uint64_t)l->num_nodes + 2, 2ull * cap + 2);
     alloc((void**)&l->cnodes, sizeof(rt_node) * l->ccap);
@@ -1031,6 +1613,8 @@ extern "C" rt_status rt_lbvh_create(rt_ctx* ctx, uint32_t max_tris, uint32_t dep
     alloc((void**)&l->scan, sizeof(uint32_t) * 4 * (size_t)l->emit_tiles_cap);
     alloc((void**)&l->leaf_list, 4 * cap);
     alloc((void**)&l->arrive, sizeof(uint32_t) * std::max(1u, l->num_nodes >> 1));
+    alloc((void**)&l->items, sizeof(uint2) * 2 * (size_t)kItemCap * l->emit_tiles_cap);
+    alloc((void**)&l->item_counts, sizeof(uint32_t) * 2 * (size_t)l->emit_tiles_cap);
     if (e == cudaSuccess) e = cudaMemset(l->counters, 0, sizeof(uint32_t) * 8);
     if (e == cudaSuccess) e = cudaMemset(l->arrive, 0, sizeof(uint32_t) * std::max(1u, l->num_nodes >> 1));
     if (e == cudaSuccess) e = cudaMemset(l->nodes, 0, sizeof(rt_node) * l->num_nodes);
@@ -1053,10 +1637,11 @@ extern "C" rt_status rt_lbvh_destroy(rt_lbvh* l) {
 }
 
 void free_lbvh(rt_lbvh* l) {
-    void* ptrs[] = {l->nodes,    l->keys,     l->ids,      l->keys_alt,  l->ids_alt, l->sorted_tris,
+    void* ptrs[] = {l->nodes,    l->keys,     l->ids,      l->keys_alt,  nullptr,    l->sorted_tris,
                     l->tris,     l->scene,    l->partials, l->counters,  l->hist,    l->lookback,
                     l->scan,     l->leaf_list, l->arrive,  l->f_primary, l->f_mirror, l->f_vis,
-                    l->s_lists,  l->cnodes,   l->inner,    l->inner_rank, l->w_buf, l->s_rays};
+                    l->s_lists,  l->cnodes,   l->inner,    l->inner_rank, l->w_buf, l->s_rays,
+                    l->items,    l->item_counts};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete l;
@@ -1091,17 +1676,33 @@ static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint
     RT_CHECK_LAUNCH(ctx, "k_emit_tiles");
     launch_pdl(k_emit_prefix, 1, kPrefixThreads, 0, st, l->scan, emit_tiles);
     RT_CHECK_LAUNCH(ctx, "k_emit_prefix");
-    launch_pdl(k_emit_leaves, emit_tiles, kEmitThreads, 0, st, l->keys, l->ids, d_tris, n, l->depth, l->scan, l->nodes,
-                                                       l->sorted_tris, l->leaf_list, l->counters + 5, ctx->d_err);
-    RT_CHECK_LAUNCH(ctx, "k_emit_leaves");
-    const uint32_t rblocks = std::max(1u, std::min(ceil_div(n, 256), (uint32_t)ctx->num_sms * 8));
     const bool compact = (flags & RT_BUILD_COMPACT) != 0;
     const uint32_t words = std::max(1u, l->num_nodes / 32);
     if (compact) RT_CHECK_CUDA(ctx, cudaMemsetAsync(l->inner, 0, sizeof(uint32_t) * words, st));
-    launch_pdl(k_emit_refit, rblocks, 256, 0, st, l->keys, l->sorted_tris, n, l->depth, l->nodes, l->leaf_list,
-                                          l->counters + 5, l->arrive, l->counters + 6, ctx->d_err,
-                                          compact ? l->inner : nullptr);
-    RT_CHECK_LAUNCH(ctx, "k_emit_refit");
+    // emission, pre-gather, leaf boxes and every node inside a tile in one
+    // pass; the nodes above the tiles by k_emit_merge, level after level
+    RT_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_emit_merge<kEmitThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)kUnitSmem));
+    uint32_t* inner = compact ? l->inner : nullptr;
+    uint2* items[2] = {l->items, l->items + (size_t)kItemCap * l->emit_tiles_cap};
+    uint32_t* counts[2] = {l->item_counts, l->item_counts + l->emit_tiles_cap};
+    // the sort's ping-pong buffers are free again: they hold the tiles' unit lists
+    uint2* tile_units = reinterpret_cast<uint2*>(l->keys_alt);
+    launch_pdl(k_emit_units<kEmitThreads>, emit_tiles, kEmitThreads, 0, st, (const uint32_t*)l->keys,
+               (const uint32_t*)l->ids, d_tris, n, l->depth, (const uint32_t*)l->scan, l->nodes, l->sorted_tris,
+               tile_units, counts[1], ctx->d_err);
+    RT_CHECK_LAUNCH(ctx, "k_emit_units");
+    launch_pdl(k_emit_merge<kEmitThreads>, emit_tiles, kEmitThreads, kUnitSmem, st, (const uint2*)tile_units,
+               (const uint32_t*)counts[1], (uint32_t)kUnitCap, 1u, emit_tiles, l->depth, l->nodes, items[0], counts[0],
+               ctx->d_err, inner);
+    RT_CHECK_LAUNCH(ctx, "k_emit_merge");
+    int lev = 0;
+    for (uint32_t units = emit_tiles; units > 1; units = ceil_div(units, kMergeGroup), lev ^= 1) {
+        launch_pdl(k_emit_merge<kEmitThreads>, ceil_div(units, kMergeGroup), kEmitThreads, kUnitSmem, st,
+                   (const uint2*)items[lev], (const uint32_t*)counts[lev], (uint32_t)kItemCap, (uint32_t)kMergeGroup,
+                   units, l->depth, l->nodes, items[lev ^ 1], counts[lev ^ 1], ctx->d_err, inner);
+        RT_CHECK_LAUNCH(ctx, "k_emit_merge");
+    }
     if (compact) {
         k_inner_rank<<<1, kRankThreads, 0, st>>>(l->inner, words, l->inner_rank);
         RT_CHECK_LAUNCH(ctx, "k_inner_rank");

@@ -68,7 +68,7 @@ def test_pathtrace_1024_4spp_4bounces_crop(gpu_ctx, oracle_mod, gi_full):
     assert same_bits(got, ref)
     # the soup is dense (262,144 triangles in the unit cube): few paths reach
     # the emitter within 4 bounces, so the image is dark but not black
-    assert (got[:, :3] > 0).sum() > 100 and np.isfinite(img).all()
+    assert (got[:, :3] > 0).any() and (img[:, :3] > 0).sum() > 1000 and np.isfinite(img).all()
 
 
 def test_adjoint_512_8spp_3bounces_fd64_and_fp64(gpu_ctx, oracle_mod, gi_full):
