@@ -460,7 +460,9 @@ typedef struct rt_pt_params {
     float sky[3];       /* radiance of a miss; the reference adds white (1,1,1) */
     uint32_t first_sample;  /* n0: samples already averaged into d_image (0 = start afresh) */
 } rt_pt_params;
-/* d_albedo, d_emission: n x 3 floats indexed by triangle id.
+/* Every bounce's walk starts at the leaf that held the previous hit (the
+ * iRoot of CSIntersections.hlsl:32); the camera segment at the root.
+ * d_albedo, d_emission: n x 3 floats indexed by triangle id.
  * d_image: width*height float4 (rgb, 1), the progressive mean over samples
  * n0 .. n0 + spp - 1 blended into the mean of samples 0 .. n0 - 1 that
  * d_image holds on entry: per sample n the image is scaled by n / (n + 1)

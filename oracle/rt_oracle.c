@@ -611,10 +611,15 @@ static int trace_path(const or_node* nodes, const uint32_t* ids, const float* tr
     pt_camera_ray(cam, i, j, &g, r);
     int nseg = 0;
     *missed = 0;
+    /* each bounce walks from the leaf of the previous hit, the iRoot of the
+     * reference's intersection stage (CSIntersections.hlsl:32) */
+    uint32_t start = 1u;
     for (uint32_t s = 0; s <= p->bounces && s < OR_MAX_SEG; ++s) {
         or_hit h;
-        trace_one(nodes, ids, tris, r, &h, NULL, 0);
+        uint32_t leaf = 1u;
+        trace_one_from(nodes, ids, tris, r, &h, NULL, 0, start, &leaf);
         if (h.id < 0) { *missed = 1; break; }
+        start = leaf;
         seg_id[nseg++] = h.id;
         if (s == p->bounces) break;
         const float* t = tris + 9 * (size_t)h.id;

@@ -2,10 +2,12 @@
 //
 // Forward: the GI branch of the reference (CSPrimaryRays.hlsl:23-34,63 and
 // CSComputeColorGI.hlsl:19-238 with the progressive factors of
-// cbGlobalIllumination, ConstantBuffers.h:85-110), one thread per pixel with
-// the whole bounce loop in registers instead of a 48-byte ray / 24-byte hit
-// round trip through global memory per segment.  Per segment: closest hit;
-// on a hit acc += (1/(n+1) * beta) * Le, beta *= albedo, new direction
+// cbGlobalIllumination, ConstantBuffers.h:85-110), one lane per pixel with
+// its path state in registers (path regeneration, below) instead of a
+// 48-byte ray / 24-byte hit round trip through global memory per segment.
+// Per segment: closest hit, the walk started at the previous hit's leaf
+// (CSIntersections.hlsl:32); on a hit acc += (1/(n+1) * beta) * Le,
+// beta *= albedo, new direction
 // cosine-distributed about the facing geometric normal; on a miss
 // acc += (1/(n+1) * beta) * sky.  Sampling uses one PCG32 stream per
 // (pixel, sample) and Malley's method, so every operation is an IEEE
@@ -98,79 +100,154 @@ struct PathCounts {
     uint32_t segments = 0, boxes = 0, tris = 0, hits = 0;
 };
 
-// Traces one path; returns the number of hit segments and their triangle
-// ids.  Called by all lanes of the warp together (valid == false for lanes
-// past the image edge): every segment is one warp-wide traversal in which
-// lanes whose path already ended only help.  STATS adds each traced
-// segment's box and triangle tests to *cnt.
-template <bool STATS = false>
-__device__ __forceinline__ int trace_path(const TreeRef& tr, const float* __restrict__ soup, const PathParams& P,
-                                          bool valid, uint32_t i, uint32_t j, uint32_t sample, int* seg,
-                                          bool* missed, PathCounts* cnt = nullptr) {
+// Path regeneration.  A warp's lanes each hold one pixel and trace its
+// samples one segment at a time; every segment of every lane is one
+// warp-wide traversal (trace_ray), whatever bounce each lane is at.  A lane
+// whose sample ends begins the pixel's next sample, and a lane whose pixel
+// is done takes the next pixel from the work counter as soon as
+// kPtRefillLanes lanes of its warp are idle (the last pixels of the image
+// leave lanes idle).  The pixels are handed out in 8 x 4 tiles, lanes of
+// one grab taking consecutive pixels.  A pixel's samples stay on one lane
+// and in order, so its progressive mean is the same sequence of fp32
+// operations as a sample-by-sample loop.
+constexpr int kPtRefillLanes = 16;
+
+struct PathLane {
+    bool live = false;           // holds a pixel
+    uint32_t i = 0, j = 0;       // the pixel
+    uint32_t n = 0;              // the sample being traced
+    uint32_t s = 0;              // its segment
     Pcg32 g;
-    pt_seed(g, P.seed, (uint64_t)j * P.cam.width + i, sample);
-    const float inv = fdiv(1.0f, (float)P.cam.height);
-    const float jx = fsub(fmul(2.0f, g.uniform()), 1.0f);
-    const float jy = fsub(fmul(2.0f, g.uniform()), 1.0f);
-    const float x = fmul(fadd((float)(2 * (int)i + 1 - (int)P.cam.width), jx), inv);
-    const float y = -fmul(fadd((float)(2 * (int)j + 1 - (int)P.cam.height), jy), inv);
-    f3 d = camera_dir(P.cam, x, y);
-    f3 o = mk3(P.cam.eye[0], P.cam.eye[1], P.cam.eye[2]);
+    f3 o, d;
     int exclude = -1;
-    int ns = 0;
-    *missed = false;
-    bool alive = valid;
-    for (uint32_t s = 0; s <= P.bounces && s < (uint32_t)kMaxSeg; ++s) {
-        const RayState r = make_ray(o, d, 1e16f, exclude);
-        uint32_t nb = 0, nt = 0;
-        const Hit h = trace_ray<STATS>(r, alive, tr, false, &nb, &nt);
-        if (STATS && alive) {
-            cnt->segments += 1;
-            cnt->boxes += nb;
-            cnt->tris += nt;
-            cnt->hits += (h.id >= 0) ? 1u : 0u;
-        }
-        if (alive) {
-            if (h.id < 0) {
-                *missed = true;
-                alive = false;
-            } else {
-                seg[ns++] = h.id;
-                if (s == P.bounces) {
-                    alive = false;
-                } else {
-                    const f3 N = facing_normal(soup, h.id, d);
-                    o = mk3(fadd(o.x, fmul(h.t, d.x)), fadd(o.y, fmul(h.t, d.y)), fadd(o.z, fmul(h.t, d.z)));
-                    d = cosine_dir(g, N);
-                    exclude = h.id;
-                }
-            }
-        }
-    }
-    return ns;
+    uint32_t start = 1u;         // restart node of the segment's walk
+    float fact = 0.0f;           // 1 / (n + 1)
+    float beta[3];
+};
+
+// Sample n of the lane's pixel: its stream and camera ray (the GI branch of
+// CSPrimaryRays.hlsl:23-34 with a sub-pixel jitter).
+__device__ __forceinline__ void begin_sample(PathLane& L, const PathParams& P) {
+    pt_seed(L.g, P.seed, (uint64_t)L.j * P.cam.width + L.i, L.n);
+    const float inv = fdiv(1.0f, (float)P.cam.height);
+    const float jx = fsub(fmul(2.0f, L.g.uniform()), 1.0f);
+    const float jy = fsub(fmul(2.0f, L.g.uniform()), 1.0f);
+    const float x = fmul(fadd((float)(2 * (int)L.i + 1 - (int)P.cam.width), jx), inv);
+    const float y = -fmul(fadd((float)(2 * (int)L.j + 1 - (int)P.cam.height), jy), inv);
+    L.d = camera_dir(P.cam, x, y);
+    L.o = mk3(P.cam.eye[0], P.cam.eye[1], P.cam.eye[2]);
+    L.exclude = -1;
+    L.start = 1u;
+    L.s = 0;
+    L.beta[0] = L.beta[1] = L.beta[2] = 1.0f;
 }
 
-template <bool STATS>
-__device__ __forceinline__ void path_pixel(const TreeRef& tr, const float* __restrict__ soup,
-                                           const float* __restrict__ albedo, const float* __restrict__ emission,
-                                           const PathParams& P, float4* __restrict__ image, bool valid, uint32_t i,
-                                           uint32_t j, PathCounts* cnt);
+// Next ray of a path that hit triangle `id` at t (not its last segment):
+// origin at the hit, a cosine-distributed direction about the facing
+// normal, the walk restarted at the hit's leaf.
+__device__ __forceinline__ void bounce(PathLane& L, const float* __restrict__ soup, int id, float t, uint32_t leaf) {
+    const f3 N = facing_normal(soup, id, L.d);
+    L.o = mk3(fadd(L.o.x, fmul(t, L.d.x)), fadd(L.o.y, fmul(t, L.d.y)), fadd(L.o.z, fmul(t, L.d.z)));
+    L.d = cosine_dir(L.g, N);
+    L.exclude = id;
+    L.start = leaf;
+    ++L.s;
+}
 
-// At most 72 registers (seven blocks per SM): 1 % faster than the 80 the
-// compiler picks unbounded; 79 or 88 are slower.  STATS: the counting
-// variant, which also sums the walk counts into counts[4] (64-bit).
+// Warp-aggregated grab of pixels for the idle lanes (all lanes call).
+// Returns true for a lane that took a pixel inside the image.
+__device__ __forceinline__ bool grab_pixel(PathLane& L, const PathParams& P, uint32_t* work, uint32_t total,
+                                           bool& drained) {
+    constexpr uint32_t kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t idle = __ballot_sync(kFull, !L.live);
+    if (drained || !(idle == kFull || __popc(idle) >= kPtRefillLanes)) return false;
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(work, (uint32_t)__popc(idle));
+    base = __shfl_sync(kFull, base, 0);
+    if (base + (uint32_t)__popc(idle) >= total) drained = true;
+    const uint32_t k = base + __popc(idle & ((1u << lane) - 1u));
+    if (L.live || k >= total) return false;
+    uint32_t i, j;
+    if (!tile_pixel(k >> 5, k & 31u, P.cam.width, P.cam.height, &i, &j)) return false;
+    L.i = i;
+    L.j = j;
+    L.n = P.n0;
+    L.live = true;
+    return true;
+}
+
+// At most 72 registers (seven blocks per SM).  Per segment: closest hit; on
+// a hit acc += (1/(n+1) * beta) * Le, beta *= albedo; on a miss
+// acc += (1/(n+1) * beta) * sky.  STATS: the counting variant, which also
+// sums the walk counts into counts[4] (64-bit).
 template <bool STATS>
 __global__ void __launch_bounds__(kPtThreads, 7) k_pathtrace(TreeRef tr, const float* __restrict__ soup,
                                                           const float* __restrict__ albedo,
                                                           const float* __restrict__ emission, PathParams P,
                                                           float4* __restrict__ image, uint32_t* work,
                                                           uint32_t num_tiles, unsigned long long* counts) {
+    constexpr uint32_t kFull = 0xffffffffu;
+    const uint32_t total = num_tiles * 32u;
     PathCounts cnt;
-    for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
-        uint32_t i, j;
-        const bool valid = tile_pixel(tile, threadIdx.x & 31, P.cam.width, P.cam.height, &i, &j);
-        if (!valid) i = j = 0;
-        path_pixel<STATS>(tr, soup, albedo, emission, P, image, valid, i, j, &cnt);
+    PathLane L;
+    L.o = mk3(0.f, 0.f, 0.f);
+    L.d = mk3(0.f, 0.f, 1.f);
+    float acc[3] = {0.0f, 0.0f, 0.0f};
+    bool drained = false;
+    for (;;) {
+        if (grab_pixel(L, P, work, total, drained)) {
+            acc[0] = acc[1] = acc[2] = 0.0f;
+            if (P.n0 > 0) {  // continue the progressive mean the image holds
+                const float4 prev = image[(size_t)L.j * P.cam.width + L.i];
+                acc[0] = prev.x;
+                acc[1] = prev.y;
+                acc[2] = prev.z;
+            }
+            const float fant = fdiv((float)L.n, (float)(L.n + 1));
+            L.fact = fdiv(1.0f, (float)(L.n + 1));
+            for (int c = 0; c < 3; ++c) acc[c] = fmul(acc[c], fant);
+            begin_sample(L, P);
+        }
+        if (!__any_sync(kFull, L.live)) {
+            if (drained) break;
+            continue;
+        }
+        const RayState r = make_ray(L.o, L.d, 1e16f, L.exclude);
+        uint32_t nb = 0, nt = 0, leaf = 1u;
+        const Hit h = trace_ray<STATS>(r, L.live, tr, false, &nb, &nt, nullptr, nullptr, L.start, &leaf);
+        if (!L.live) continue;
+        if (STATS) {
+            cnt.segments += 1;
+            cnt.boxes += nb;
+            cnt.tris += nt;
+            cnt.hits += (h.id >= 0) ? 1u : 0u;
+        }
+        bool ended;
+        if (h.id < 0) {
+            for (int c = 0; c < 3; ++c) acc[c] = fadd(acc[c], fmul(fmul(L.fact, L.beta[c]), P.sky[c]));
+            ended = true;
+        } else {
+            const float* le = emission + 3 * (size_t)h.id;
+            const float* al = albedo + 3 * (size_t)h.id;
+            for (int c = 0; c < 3; ++c) {
+                acc[c] = fadd(acc[c], fmul(fmul(L.fact, L.beta[c]), __ldg(le + c)));
+                L.beta[c] = fmul(L.beta[c], __ldg(al + c));
+            }
+            ended = L.s == P.bounces;
+            if (!ended) bounce(L, soup, h.id, h.t, leaf);
+        }
+        if (ended) {
+            if (++L.n == P.n0 + P.spp) {
+                image[(size_t)L.j * P.cam.width + L.i] = make_float4(acc[0], acc[1], acc[2], 1.0f);
+                L.live = false;
+            } else {
+                const float fant = fdiv((float)L.n, (float)(L.n + 1));
+                L.fact = fdiv(1.0f, (float)(L.n + 1));
+                for (int c = 0; c < 3; ++c) acc[c] = fmul(acc[c], fant);
+                begin_sample(L, P);
+            }
+        }
     }
     if (STATS) {
         unsigned long long v[4] = {cnt.segments, cnt.boxes, cnt.tris, cnt.hits};
@@ -181,81 +258,76 @@ __global__ void __launch_bounds__(kPtThreads, 7) k_pathtrace(TreeRef tr, const f
     }
 }
 
-template <bool STATS>
-__device__ __forceinline__ void path_pixel(const TreeRef& tr, const float* __restrict__ soup,
-                                           const float* __restrict__ albedo, const float* __restrict__ emission,
-                                           const PathParams& P, float4* __restrict__ image, bool valid, uint32_t i,
-                                           uint32_t j, PathCounts* cnt) {
-    float acc[3] = {0.0f, 0.0f, 0.0f};
-    if (P.n0 > 0 && valid) {  // continue the progressive mean the image holds
-        const float4 prev = image[(size_t)j * P.cam.width + i];
-        acc[0] = prev.x;
-        acc[1] = prev.y;
-        acc[2] = prev.z;
-    }
-    for (uint32_t n = P.n0; n < P.n0 + P.spp; ++n) {
-        const float fant = fdiv((float)n, (float)(n + 1));
-        const float fact = fdiv(1.0f, (float)(n + 1));
-        for (int c = 0; c < 3; ++c) acc[c] = fmul(acc[c], fant);
-        int seg[kMaxSeg];
-        bool missed;
-        const int ns = trace_path<STATS>(tr, soup, P, valid, i, j, n, seg, &missed, cnt);
-        float beta[3] = {1.0f, 1.0f, 1.0f};
-        for (int s = 0; s < ns; ++s) {
-            const float* le = emission + 3 * (size_t)seg[s];
-            const float* al = albedo + 3 * (size_t)seg[s];
-            for (int c = 0; c < 3; ++c) {
-                acc[c] = fadd(acc[c], fmul(fmul(fact, beta[c]), __ldg(le + c)));
-                beta[c] = fmul(beta[c], __ldg(al + c));
-            }
-        }
-        if (missed)
-            for (int c = 0; c < 3; ++c) acc[c] = fadd(acc[c], fmul(fmul(fact, beta[c]), P.sky[c]));
-    }
-    if (valid) image[(size_t)j * P.cam.width + i] = make_float4(acc[0], acc[1], acc[2], 1.0f);
-}
-
+// Adjoint by path replay: the same paths as k_pathtrace (same streams, same
+// walks); a lane records the triangles its sample hits, and when the sample
+// ends runs the backward recurrence G_j = E_{j+1} + a_{j+1} G_{j+1} over
+// them with the sample's weight in the final mean.
 __global__ void __launch_bounds__(kPtThreads) k_pathtrace_adjoint(
     TreeRef tr, const float* __restrict__ soup,
     const float* __restrict__ albedo, const float* __restrict__ emission, PathParams P,
     const float4* __restrict__ dimage, float* __restrict__ dalbedo, float* __restrict__ demission, uint32_t* work,
     uint32_t num_tiles) {
+    constexpr uint32_t kFull = 0xffffffffu;
+    const uint32_t total = num_tiles * 32u;
+    PathLane L;
+    L.o = mk3(0.f, 0.f, 0.f);
+    L.d = mk3(0.f, 0.f, 1.f);
     float dle[3] = {0.0f, 0.0f, 0.0f};
-    for (uint32_t tile = next_tile(work); tile < num_tiles; tile = next_tile(work)) {
-        uint32_t i, j;
-        const bool valid = tile_pixel(tile, threadIdx.x & 31, P.cam.width, P.cam.height, &i, &j);
-        if (!valid) i = j = 0;
-        const float4 g4 = valid ? __ldg(dimage + (size_t)j * P.cam.width + i) : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float gimg[3] = {g4.x, g4.y, g4.z};
-        for (uint32_t n = P.n0; n < P.n0 + P.spp; ++n) {
-            // weight of sample n in the progressive mean after the call
-            float w = 1.0f / (float)(n + 1);
-            for (uint32_t m = n + 1; m < P.n0 + P.spp; ++m) w *= (float)m / (float)(m + 1);
-            int seg[kMaxSeg];
-            bool missed;
-            const int ns = trace_path(tr, soup, P, valid, i, j, n, seg, &missed);
-            float beta[kMaxSeg][3];
-            beta[0][0] = beta[0][1] = beta[0][2] = 1.0f;
-            for (int s = 0; s + 1 < ns; ++s)
-                for (int c = 0; c < 3; ++c) beta[s + 1][c] = beta[s][c] * __ldg(albedo + 3 * (size_t)seg[s] + c);
-            float G[3] = {0.0f, 0.0f, 0.0f};
-            if (missed)
-                for (int c = 0; c < 3; ++c) G[c] = P.sky[c];
-            for (int s = ns - 1; s >= 0; --s) {
-                const float* al = albedo + 3 * (size_t)seg[s];
-                const float* le = emission + 3 * (size_t)seg[s];
-                const float l0 = __ldg(le), l1 = __ldg(le + 1), l2 = __ldg(le + 2);
-                const bool emitter = (l0 != 0.0f) || (l1 != 0.0f) || (l2 != 0.0f);
-                const float lev[3] = {l0, l1, l2};
-                for (int c = 0; c < 3; ++c) {
-                    const float gw = gimg[c] * w;
-                    const float da = gw * beta[s][c] * G[c];
-                    if (da != 0.0f) atomicAdd(dalbedo + 3 * (size_t)seg[s] + c, da);
-                    if (emitter) dle[c] += gw * beta[s][c];
-                    G[c] = lev[c] + __ldg(al + c) * G[c];
-                }
+    float gimg[3] = {0.0f, 0.0f, 0.0f};
+    int seg[kMaxSeg];
+    int ns = 0;
+    bool drained = false;
+    for (;;) {
+        if (grab_pixel(L, P, work, total, drained)) {
+            const float4 g4 = __ldg(dimage + (size_t)L.j * P.cam.width + L.i);
+            gimg[0] = g4.x;
+            gimg[1] = g4.y;
+            gimg[2] = g4.z;
+            ns = 0;
+            begin_sample(L, P);
+        }
+        if (!__any_sync(kFull, L.live)) {
+            if (drained) break;
+            continue;
+        }
+        const RayState r = make_ray(L.o, L.d, 1e16f, L.exclude);
+        uint32_t nb = 0, nt = 0, leaf = 1u;
+        const Hit h = trace_ray<false>(r, L.live, tr, false, &nb, &nt, nullptr, nullptr, L.start, &leaf);
+        if (!L.live) continue;
+        const bool missed = h.id < 0;
+        if (!missed) seg[ns++] = h.id;
+        const bool ended = missed || L.s == P.bounces;
+        if (!ended) {
+            bounce(L, soup, h.id, h.t, leaf);
+            continue;
+        }
+        // weight of sample n in the progressive mean after the call
+        float w = 1.0f / (float)(L.n + 1);
+        for (uint32_t m = L.n + 1; m < P.n0 + P.spp; ++m) w *= (float)m / (float)(m + 1);
+        float beta[kMaxSeg][3];
+        beta[0][0] = beta[0][1] = beta[0][2] = 1.0f;
+        for (int q = 0; q + 1 < ns; ++q)
+            for (int c = 0; c < 3; ++c) beta[q + 1][c] = beta[q][c] * __ldg(albedo + 3 * (size_t)seg[q] + c);
+        float G[3] = {0.0f, 0.0f, 0.0f};
+        if (missed)
+            for (int c = 0; c < 3; ++c) G[c] = P.sky[c];
+        for (int q = ns - 1; q >= 0; --q) {
+            const float* al = albedo + 3 * (size_t)seg[q];
+            const float* le = emission + 3 * (size_t)seg[q];
+            const float l0 = __ldg(le), l1 = __ldg(le + 1), l2 = __ldg(le + 2);
+            const bool emitter = (l0 != 0.0f) || (l1 != 0.0f) || (l2 != 0.0f);
+            const float lev[3] = {l0, l1, l2};
+            for (int c = 0; c < 3; ++c) {
+                const float gw = gimg[c] * w;
+                const float da = gw * beta[q][c] * G[c];
+                if (da != 0.0f) atomicAdd(dalbedo + 3 * (size_t)seg[q] + c, da);
+                if (emitter) dle[c] += gw * beta[q][c];
+                G[c] = lev[c] + __ldg(al + c) * G[c];
             }
         }
+        ns = 0;
+        if (++L.n == P.n0 + P.spp) L.live = false;
+        else begin_sample(L, P);
     }
     // emitter gradient: warp reduction, one atomic per warp and channel
     for (int c = 0; c < 3; ++c) {
