@@ -375,13 +375,14 @@ def run_ours(args, dist: Dist):
 
     peak, peak_kind = measured_peaks()
     # stage: (ms, algorithmic bytes, kernels of the stage's ncu traffic)
-    groups = {"k_trace_primary (+ k_trace_heavy)": (prim_ms, bytes_primary,
-                                                    ("k_trace_primary", "k_trace_heavy_primary")),
+    nb = build_launches(n)
+    build_label = f"build ({nb} kernels)"
+    groups = {"k_trace_primary (+ k_trace_heavy)": (prim_ms, bytes_primary, ("k_trace_primary", "k_trace_heavy")),
               "k_trace_shade (+ k_trace_heavy_team)": (sec_ms, bytes_secondary,
                                                       ("k_trace_shade", "k_trace_heavy_team")),
-              "build (10 kernels)": (build_ms, BUILD_BYTES_PER_TRI * n,
-                                     ("k_bounds", "k_morton_hist") + ("k_onesweep",) * 4 + ("k_emit_leaves",
-                                                                                         "k_emit_refit"))}
+              build_label: (build_ms, BUILD_BYTES_PER_TRI * n,
+                            ("k_bounds", "k_morton_hist") + ("k_onesweep",) * 4 +
+                            ("k_emit_tiles", "k_emit_prefix", "k_emit_units") + ("k_emit_merge",) * (nb - 9))}
     dom = max(groups, key=lambda g: groups[g][0])
     ms, byts, kern = groups[dom]
     achieved = byts / (ms / 1e3) / 1e9
@@ -405,7 +406,7 @@ def run_ours(args, dist: Dist):
                 "own_walk": {"frame_algorithmic_bytes": int(own_frame_bytes), "frame_frac": frac(own_frame_bytes, frame_ms),
                              "primary_frac": frac(own_primary, prim_ms), "shading_frac": frac(own_secondary, sec_ms)},
                 "stages": {"build": {"ms": round(float(build_ms), 4), "frac": frac(BUILD_BYTES_PER_TRI * n, build_ms),
-                                     "traffic": ncu_traffic(*groups["build (10 kernels)"][2])},
+                                     "traffic": ncu_traffic(*groups[build_label][2])},
                            "primary": {"ms": round(float(prim_ms), 4), "frac": frac(bytes_primary, prim_ms),
                                        "cache": ncu_cache_fractions("k_trace_primary")},
                            "shading": {"ms": round(float(sec_ms), 4), "frac": frac(bytes_secondary, sec_ms),
@@ -425,10 +426,10 @@ def run_ours(args, dist: Dist):
                        "wall_s": round(wall, 3)},
         "roofline": roofline,
         "e2e": e2e,
-        # per graph: 10 build kernels; k_order_begin (which also zeroes the frame's
-        # counters), k_trace_primary (which also lists the shading rays),
-        # k_trace_heavy; k_trace_shade, k_trace_heavy_team
-        "gpu_launches": 15 * args.steps,
+        # per graph: the build's kernels; k_order_begin (which also zeroes the
+        # frame's counters), k_trace_primary (which also lists the shading
+        # rays), k_trace_heavy; k_trace_shade, k_trace_heavy_team
+        "gpu_launches": (nb + 5) * args.steps,
     }
     out["clocks"] = clk.summary()
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
@@ -446,6 +447,18 @@ def run_ours(args, dist: Dist):
             comps[key] = component_summary(fn())
             out["gpu_launches"] += comps[key].get("gpu_launches", 0)
     return out
+
+
+def build_launches(n: int) -> int:
+    """Kernels of one rt_lbvh_build: k_bounds, k_morton_hist, four radix
+    passes, k_emit_tiles, k_emit_prefix, k_emit_units, then k_emit_merge at
+    the tile level and once per level of 32 tiles (groups) up to the root."""
+    tiles = max(1, -(-n // 2048))
+    merges = 1
+    while tiles > 1:
+        tiles = -(-tiles // 32)
+        merges += 1
+    return 9 + merges
 
 
 def frame_config(name, n, npx, depth):
@@ -951,7 +964,7 @@ def run_pt(args, dist: Dist, adjoint: bool = False):
            "roofline": roofline,
            "clocks": clk.summary(),
            # per step: 10 build kernels + the render (+ the adjoint kernel)
-           "gpu_launches": (10 + 1 + (1 if adjoint else 0)) * args.steps}
+           "gpu_launches": (build_launches(n) + 1 + (1 if adjoint else 0)) * args.steps}
     if adjoint:
         out["components"]["backward_ms"] = round(bwd_ms, 4)
         out["components"]["backward_over_forward"] = round(bwd_ms / fwd_ms, 3)
