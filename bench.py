@@ -382,7 +382,7 @@ def run_ours(args, dist: Dist):
                                                       ("k_trace_shade", "k_trace_heavy_team")),
               build_label: (build_ms, BUILD_BYTES_PER_TRI * n,
                             ("k_bounds", "k_morton_hist") + ("k_onesweep",) * 4 +
-                            ("k_emit_tiles", "k_emit_prefix", "k_emit_units") + ("k_emit_merge",) * (nb - 9))}
+                            ("k_emit_tiles", "k_emit_prefix", "k_emit_units", "k_emit_chunks", "k_emit_merge"))}
     dom = max(groups, key=lambda g: groups[g][0])
     ms, byts, kern = groups[dom]
     achieved = byts / (ms / 1e3) / 1e9
@@ -451,14 +451,9 @@ def run_ours(args, dist: Dist):
 
 def build_launches(n: int) -> int:
     """Kernels of one rt_lbvh_build: k_bounds, k_morton_hist, four radix
-    passes, k_emit_tiles, k_emit_prefix, k_emit_units, then k_emit_merge at
-    the tile level and once per level of 32 tiles (groups) up to the root."""
-    tiles = max(1, -(-n // 2048))
-    merges = 1
-    while tiles > 1:
-        tiles = -(-tiles // 32)
-        merges += 1
-    return 9 + merges
+    passes, k_emit_tiles, k_emit_prefix, k_emit_units, k_emit_chunks (the
+    tile level of the merge), k_emit_merge (every level above it)."""
+    return 11
 
 
 def frame_config(name, n, npx, depth):

@@ -941,10 +941,13 @@ constexpr uint32_t kHeadBit = 1u << 30;
 constexpr uint32_t kTailBit = 1u << 31;
 constexpr uint32_t kMaskBits = kHeadBit - 1u;
 constexpr int kUnitCap = kEmitTile;  // units of one CTA: the leaves of a tile, the items of a group
+constexpr int kChunkUnits = 512;     // units of one CTA of the tile level (a tile's leaves in chunks)
+constexpr int kTileChunks = kUnitCap / kChunkUnits;
 constexpr int kItemCap = 64;         // items one tile or group hands on (2 x depth + 2 <= 54)
 constexpr int kMergeGroup = 32;      // tiles (groups) per CTA of the next level
 constexpr int kUnitWords = 12;       // shared words per unit
 constexpr size_t kUnitSmem = (size_t)kUnitWords * kUnitCap * sizeof(uint32_t) + 16;
+constexpr size_t kChunkSmem = (size_t)kUnitWords * kChunkUnits * sizeof(uint32_t) + 16;
 
 // Leaf axis field: the reference's round-robin counter at the call that made
 // the leaf (see refit_walk), with the parent's split bit = the lowest bit of
@@ -1014,46 +1017,48 @@ __device__ __forceinline__ Box shfl_up_box(const Box& b, int off) {
     return r;
 }
 
-// Shared-memory view of a CTA's units: unit i covers elements
+// Shared-memory view of a CTA's units (capacity cap): unit i covers elements
 // [pos[i], pos[i + 1]) and is the node (h[i], m[i]) with box lo/hi[i];
 // arrivals of the bottom-up reuse the box slots and aext / am.
 struct Units {
-    float* lo;      // [3][kUnitCap]
-    float* hi;      // [3][kUnitCap]
-    int32_t* pos;   // [kUnitCap + 1]
-    uint32_t* h;    // [kUnitCap]
-    uint32_t* m;    // [kUnitCap]
-    int32_t* aext;  // [kUnitCap] arrival: the far unit index of the arriving node
-    uint32_t* am;   // [kUnitCap] arrival: the arriving node's remaining mask
-    uint32_t* arr;  // [kUnitCap] arrival bits of the boundary after unit i (1 left child, 2 right child)
+    int cap;
+    float* lo;      // [3][cap]
+    float* hi;      // [3][cap]
+    int32_t* pos;   // [cap + 1]
+    uint32_t* h;    // [cap]
+    uint32_t* m;    // [cap]
+    int32_t* aext;  // [cap] arrival: the far unit index of the arriving node
+    uint32_t* am;   // [cap] arrival: the arriving node's remaining mask
+    uint32_t* arr;  // [cap] arrival bits of the boundary after unit i (1 left child, 2 right child)
     uint32_t* n_items;
 };
-__device__ __forceinline__ Units units_of(uint32_t* smem) {
+__device__ __forceinline__ Units units_of(uint32_t* smem, int cap) {
     Units u;
+    u.cap = cap;
     u.lo = reinterpret_cast<float*>(smem);
-    u.hi = u.lo + 3 * kUnitCap;
-    u.pos = reinterpret_cast<int32_t*>(u.hi + 3 * kUnitCap);
-    u.h = reinterpret_cast<uint32_t*>(u.pos + kUnitCap + 4);
-    u.m = u.h + kUnitCap;
-    u.aext = reinterpret_cast<int32_t*>(u.m + kUnitCap);
-    u.am = reinterpret_cast<uint32_t*>(u.aext + kUnitCap);
-    u.arr = u.am + kUnitCap;
-    u.n_items = u.arr + kUnitCap;
+    u.hi = u.lo + 3 * cap;
+    u.pos = reinterpret_cast<int32_t*>(u.hi + 3 * cap);
+    u.h = reinterpret_cast<uint32_t*>(u.pos + cap + 4);
+    u.m = u.h + cap;
+    u.aext = reinterpret_cast<int32_t*>(u.m + cap);
+    u.am = reinterpret_cast<uint32_t*>(u.aext + cap);
+    u.arr = u.am + cap;
+    u.n_items = u.arr + cap;
     return u;
 }
 __device__ __forceinline__ void set_box(const Units& u, int i, const Box& b) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        u.lo[c * kUnitCap + i] = b.lo[c];
-        u.hi[c * kUnitCap + i] = b.hi[c];
+        u.lo[c * u.cap + i] = b.lo[c];
+        u.hi[c * u.cap + i] = b.hi[c];
     }
 }
 __device__ __forceinline__ Box get_box(const Units& u, int i) {
     Box b;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        b.lo[c] = u.lo[c * kUnitCap + i];
-        b.hi[c] = u.hi[c * kUnitCap + i];
+        b.lo[c] = u.lo[c * u.cap + i];
+        b.hi[c] = u.hi[c * u.cap + i];
     }
     return b;
 }
@@ -1414,29 +1419,22 @@ __global__ void __launch_bounds__(THREADS) k_emit_units(const uint32_t* __restri
     }
 }
 
-// k_emit_merge: the shared-memory bottom-up over the units of `group`
-// consecutive tiles (groups) of the previous level, whose stored records
-// give each unit's box and range: at the tile level one tile per CTA (its
-// leaves, in order), above it kMergeGroup groups per CTA (their items,
-// sorted here by first element).  The nodes that cannot be formed here are
-// this CTA's items for the next level.
+// merge_group: the shared-memory bottom-up over the units of `ng` consecutive
+// tiles (groups) of a level, whose stored records give each unit's box and
+// range: at the tile level one tile (its leaves, in order), above it up to
+// kMergeGroup groups (their items, each group's sorted by first element).
+// The nodes that cannot be formed here are written to `out` sorted by first
+// element, their number to *out_count.
 template <int THREADS>
-__global__ void __launch_bounds__(THREADS) k_emit_merge(const uint2* __restrict__ in_items,
-                                                        const uint32_t* __restrict__ in_counts, uint32_t in_stride,
-                                                        uint32_t group, uint32_t n_in, uint32_t depth, rt_node* nodes,
-                                                        uint2* out_items, uint32_t* out_counts, uint32_t* err,
-                                                        uint32_t* inner) {
-    extern __shared__ __align__(16) uint32_t smem[];
-    const Units u = units_of(smem);
-    __shared__ uint32_t s_off[kMergeGroup + 1];
-    __shared__ uint2 s_items[kItemCap];
-    __shared__ int32_t s_ipos[kItemCap];
-    grid_dep_wait();
+__device__ void merge_group(const Units& u, const uint2* in_items, const uint32_t* in_counts, int fixed_count,
+                            uint32_t in_stride, uint32_t ng, uint32_t depth, rt_node* nodes, uint2* out,
+                            uint32_t* out_count, uint32_t* err, uint32_t* inner, uint32_t* s_off, uint2* s_items,
+                            int32_t* s_ipos) {
     const int t = threadIdx.x;
-    const uint32_t g0 = blockIdx.x * group;
-    const uint32_t ng = min(group, n_in - g0);
     if (t < 32) {  // unit offsets of the groups: one warp, a prefix sum over <= 32 counts
-        const uint32_t c = (uint32_t)t < ng ? min(in_counts[g0 + t], in_stride) : 0u;
+        const uint32_t c = (uint32_t)t < ng ? min(fixed_count >= 0 ? (uint32_t)fixed_count : __ldcg(in_counts + t),
+                                                  in_stride)
+                                            : 0u;
         uint32_t incl = c;
         for (int off = 1; off < 32; off <<= 1) {
             const uint32_t y = __shfl_up_sync(kFull, incl, off);
@@ -1446,15 +1444,15 @@ __global__ void __launch_bounds__(THREADS) k_emit_merge(const uint2* __restrict_
         if ((uint32_t)t == ng - 1) s_off[ng] = incl;
         if (t == 0) *u.n_items = 0u;
     }
-    for (int i = t; i < kUnitCap; i += THREADS) u.arr[i] = 0u;
+    for (int i = t; i < u.cap; i += THREADS) u.arr[i] = 0u;
     __syncthreads();
-    const int U = (int)min(s_off[ng], (uint32_t)kUnitCap);
+    const int U = (int)min(s_off[ng], (uint32_t)u.cap);
     // every group's units are in order (tile leaves, or items sorted by the
     // CTA that made them), so their concatenation is sorted
     for (int i = t; i < U; i += THREADS) {
         uint32_t g = 0;
         while (g + 1 < ng && s_off[g + 1] <= (uint32_t)i) ++g;
-        uint2 it = in_items[(size_t)(g0 + g) * in_stride + (i - s_off[g])];
+        uint2 it = __ldcg(in_items + (size_t)g * in_stride + (i - s_off[g]));
         if (it.x < 1u || it.x >= (1u << depth)) {
             atomicOr(err, RT_DEVERR_BOUNDS);
             it = make_uint2(1u, 0u);  // a root stops the walk
@@ -1463,29 +1461,111 @@ __global__ void __launch_bounds__(THREADS) k_emit_merge(const uint2* __restrict_
         const float4 b = __ldcg(reinterpret_cast<const float4*>(nodes + it.x) + 1);
         u.h[i] = it.x;
         u.m[i] = it.y;
-        u.lo[0 * kUnitCap + i] = a.x;
-        u.lo[1 * kUnitCap + i] = a.y;
-        u.lo[2 * kUnitCap + i] = a.z;
-        u.hi[0 * kUnitCap + i] = a.w;
-        u.hi[1 * kUnitCap + i] = b.x;
-        u.hi[2 * kUnitCap + i] = b.y;
+        u.lo[0 * u.cap + i] = a.x;
+        u.lo[1 * u.cap + i] = a.y;
+        u.lo[2 * u.cap + i] = a.z;
+        u.hi[0 * u.cap + i] = a.w;
+        u.hi[1 * u.cap + i] = b.x;
+        u.hi[2 * u.cap + i] = b.y;
         u.pos[i] = __float_as_int(b.w);
         if (i == U - 1) u.pos[U] = __float_as_int(b.w) + (__float_as_int(b.z) >> 3);
     }
     __syncthreads();
     unit_bottom_up<THREADS>(u, U, nodes, s_items, err, inner);
     __syncthreads();
-    // this CTA's items, sorted by first element (their records are stored)
+    // the items, sorted by first element (their records are stored)
     const uint32_t ni = min(*u.n_items, (uint32_t)kItemCap);
     for (uint32_t i = t; i < ni; i += THREADS) s_ipos[i] = __ldcg(&nodes[s_items[i].x].prim_pos);
     __syncthreads();
-    uint2* out = out_items + (size_t)blockIdx.x * kItemCap;
     for (uint32_t i = t; i < ni; i += THREADS) {
         uint32_t rank = 0;
         for (uint32_t o = 0; o < ni; ++o) rank += (s_ipos[o] < s_ipos[i] || (s_ipos[o] == s_ipos[i] && o < i)) ? 1u : 0u;
         out[rank] = s_items[i];
     }
-    if (t == 0) out_counts[blockIdx.x] = ni;
+    if (t == 0) *out_count = ni;
+}
+
+// k_emit_chunks: the tile level.  A tile's leaves are merged in chunks of
+// kChunkUnits consecutive leaves, one CTA per chunk (kTileChunks chunk slots
+// per tile, most of them empty for tiles with big leaves), so that the
+// shared-memory units of eight CTAs fit an SM.  Chunk slot c's items go to
+// items + c * kItemCap, their number to counts[c].
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) k_emit_chunks(const uint2* __restrict__ tile_units,
+                                                         const uint32_t* __restrict__ tile_counts, uint32_t depth,
+                                                         rt_node* nodes, uint2* items, uint32_t* counts, uint32_t* err,
+                                                         uint32_t* inner) {
+    extern __shared__ __align__(16) uint32_t smem[];
+    const Units u = units_of(smem, kChunkUnits);
+    __shared__ uint32_t s_off[kMergeGroup + 1];
+    __shared__ uint2 s_items[kItemCap];
+    __shared__ int32_t s_ipos[kItemCap];
+    grid_dep_wait();
+    const uint32_t c = blockIdx.x, tile = c / kTileChunks, chunk = c % kTileChunks;
+    const uint32_t tc = min(__ldcg(tile_counts + tile), (uint32_t)kUnitCap);
+    const int cnt = (int)min((uint32_t)kChunkUnits, tc > chunk * kChunkUnits ? tc - chunk * kChunkUnits : 0u);
+    if (cnt == 0) {
+        if (threadIdx.x == 0) counts[c] = 0u;
+        return;
+    }
+    merge_group<THREADS>(u, tile_units + (size_t)tile * kUnitCap + (size_t)chunk * kChunkUnits, nullptr, cnt,
+                         (uint32_t)kChunkUnits, 1u, depth, nodes, items + (size_t)c * kItemCap, counts + c, err, inner,
+                         s_off, s_items, s_ipos);
+}
+
+// k_emit_merge: the levels above.  One CTA per kMergeGroup consecutive units
+// of the level below (chunk slots, then groups) merges their items; then,
+// level by level, the last CTA to finish among kMergeGroup consecutive groups
+// merges their items (a ticket per group, taken after the CTA's items are
+// stored and fenced; the last taker resets it for the next build), until one
+// group covers the whole tree and forms the root.  No CTA waits on another.
+// The first level's items are at out_items + g * kItemCap (counts at
+// out_counts + g), each next level's after the previous one's.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) k_emit_merge(const uint2* __restrict__ in_items,
+                                                        const uint32_t* __restrict__ in_counts, uint32_t n_in,
+                                                        uint32_t depth, rt_node* nodes, uint2* out_items,
+                                                        uint32_t* out_counts, uint32_t* tickets, uint32_t* err,
+                                                        uint32_t* inner) {
+    extern __shared__ __align__(16) uint32_t smem[];
+    const Units u = units_of(smem, kUnitCap);
+    __shared__ uint32_t s_off[kMergeGroup + 1];
+    __shared__ uint2 s_items[kItemCap];
+    __shared__ int32_t s_ipos[kItemCap];
+    __shared__ int s_last;
+    grid_dep_wait();
+    const int t = threadIdx.x;
+    uint32_t g = blockIdx.x;
+    uint32_t n_lev = (n_in + kMergeGroup - 1) / kMergeGroup;
+    merge_group<THREADS>(u, in_items + (size_t)g * kMergeGroup * kItemCap, in_counts + (size_t)g * kMergeGroup, -1,
+                         (uint32_t)kItemCap, min((uint32_t)kMergeGroup, n_in - g * kMergeGroup), depth, nodes,
+                         out_items + (size_t)g * kItemCap, out_counts + g, err, inner, s_off, s_items, s_ipos);
+    size_t ioff = 0, coff = 0, toff = 0;
+    while (n_lev > 1) {
+        const uint32_t parent = g / kMergeGroup;
+        const uint32_t gs = min((uint32_t)kMergeGroup, n_lev - parent * kMergeGroup);
+        const uint32_t n_next = (n_lev + kMergeGroup - 1) / kMergeGroup;
+        __threadfence();  // this CTA's items, count and records before its ticket
+        __syncthreads();
+        if (t == 0) {
+            const uint32_t k = atomicAdd(tickets + toff + parent, 1u);
+            s_last = (k + 1 == gs) ? 1 : 0;
+            if (s_last) tickets[toff + parent] = 0u;
+        }
+        __syncthreads();
+        if (!s_last) return;
+        __threadfence();  // the other CTAs' items and records after their tickets
+        const size_t pioff = ioff + (size_t)parent * kMergeGroup * kItemCap;
+        const size_t pcoff = coff + (size_t)parent * kMergeGroup;
+        ioff += (size_t)n_lev * kItemCap;
+        coff += n_lev;
+        merge_group<THREADS>(u, out_items + pioff, out_counts + pcoff, -1, (uint32_t)kItemCap, gs, depth, nodes,
+                             out_items + ioff + (size_t)parent * kItemCap, out_counts + coff + parent, err, inner,
+                             s_off, s_items, s_ipos);
+        toff += n_next;
+        g = parent;
+        n_lev = n_next;
+    }
 }
 
 // Compact layout (rt_lbvh.cnodes) from the heap: inner_rank = exclusive
@@ -1613,11 +1693,15 @@ extern "C" rt_status rt_lbvh_create(rt_ctx* ctx, uint32_t max_tris, uint32_t dep
     alloc((void**)&l->scan, sizeof(uint32_t) * 4 * (size_t)l->emit_tiles_cap);
     alloc((void**)&l->leaf_list, 4 * cap);
     alloc((void**)&l->arrive, sizeof(uint32_t) * std::max(1u, l->num_nodes >> 1));
-    alloc((void**)&l->items, sizeof(uint2) * 2 * (size_t)kItemCap * l->emit_tiles_cap);
-    alloc((void**)&l->item_counts, sizeof(uint32_t) * 2 * (size_t)l->emit_tiles_cap);
+    // items and item counts of every merge level (chunk slots = 4 x tiles, then
+    // the groups above: < 6 x tiles in all), the tiles' unit counts (tiles),
+    // the merge tickets (tiles, zero between builds)
+    alloc((void**)&l->items, sizeof(uint2) * 6 * (size_t)kItemCap * l->emit_tiles_cap);
+    alloc((void**)&l->item_counts, sizeof(uint32_t) * 8 * (size_t)l->emit_tiles_cap);
     if (e == cudaSuccess) e = cudaMemset(l->counters, 0, sizeof(uint32_t) * 8);
     if (e == cudaSuccess) e = cudaMemset(l->arrive, 0, sizeof(uint32_t) * std::max(1u, l->num_nodes >> 1));
     if (e == cudaSuccess) e = cudaMemset(l->nodes, 0, sizeof(rt_node) * l->num_nodes);
+    if (e == cudaSuccess) e = cudaMemset(l->item_counts, 0, sizeof(uint32_t) * 8 * (size_t)l->emit_tiles_cap);
     if (e != cudaSuccess) {
         rt_lbvh_destroy(l);
         return rt_fail(ctx, RT_ERR_CUDA, "rt_lbvh_create: allocation failed: %s", cudaGetErrorString(e));
@@ -1684,25 +1768,23 @@ static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint
     RT_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_emit_merge<kEmitThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)kUnitSmem));
     uint32_t* inner = compact ? l->inner : nullptr;
-    uint2* items[2] = {l->items, l->items + (size_t)kItemCap * l->emit_tiles_cap};
-    uint32_t* counts[2] = {l->item_counts, l->item_counts + l->emit_tiles_cap};
     // the sort's ping-pong buffers are free again: they hold the tiles' unit lists
     uint2* tile_units = reinterpret_cast<uint2*>(l->keys_alt);
+    const size_t cap = l->emit_tiles_cap;
+    uint32_t* tile_counts = l->item_counts + 6 * cap;
     launch_pdl(k_emit_units<kEmitThreads>, emit_tiles, kEmitThreads, 0, st, (const uint32_t*)l->keys,
                (const uint32_t*)l->ids, d_tris, n, l->depth, (const uint32_t*)l->scan, l->nodes, l->sorted_tris,
-               tile_units, counts[1], ctx->d_err);
+               tile_units, tile_counts, ctx->d_err);
     RT_CHECK_LAUNCH(ctx, "k_emit_units");
-    launch_pdl(k_emit_merge<kEmitThreads>, emit_tiles, kEmitThreads, kUnitSmem, st, (const uint2*)tile_units,
-               (const uint32_t*)counts[1], (uint32_t)kUnitCap, 1u, emit_tiles, l->depth, l->nodes, items[0], counts[0],
-               ctx->d_err, inner);
+    const uint32_t chunks = emit_tiles * kTileChunks;
+    launch_pdl(k_emit_chunks<kEmitThreads>, chunks, kEmitThreads, kChunkSmem, st, (const uint2*)tile_units,
+               (const uint32_t*)tile_counts, l->depth, l->nodes, l->items, l->item_counts, ctx->d_err, inner);
+    RT_CHECK_LAUNCH(ctx, "k_emit_chunks");
+    launch_pdl(k_emit_merge<kEmitThreads>, ceil_div(chunks, kMergeGroup), kEmitThreads, kUnitSmem, st,
+               (const uint2*)l->items, (const uint32_t*)l->item_counts, chunks, l->depth, l->nodes,
+               l->items + (size_t)chunks * kItemCap, l->item_counts + chunks, l->item_counts + 7 * cap, ctx->d_err,
+               inner);
     RT_CHECK_LAUNCH(ctx, "k_emit_merge");
-    int lev = 0;
-    for (uint32_t units = emit_tiles; units > 1; units = ceil_div(units, kMergeGroup), lev ^= 1) {
-        launch_pdl(k_emit_merge<kEmitThreads>, ceil_div(units, kMergeGroup), kEmitThreads, kUnitSmem, st,
-                   (const uint2*)items[lev], (const uint32_t*)counts[lev], (uint32_t)kItemCap, (uint32_t)kMergeGroup,
-                   units, l->depth, l->nodes, items[lev ^ 1], counts[lev ^ 1], ctx->d_err, inner);
-        RT_CHECK_LAUNCH(ctx, "k_emit_merge");
-    }
     if (compact) {
         k_inner_rank<<<1, kRankThreads, 0, st>>>(l->inner, words, l->inner_rank);
         RT_CHECK_LAUNCH(ctx, "k_inner_rank");

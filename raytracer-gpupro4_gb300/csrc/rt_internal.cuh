@@ -142,8 +142,8 @@ struct rt_lbvh {
     uint32_t* scan = nullptr;        // emission tiles x 4 (fwd agg, bwd agg, fwd prefix, bwd suffix)
     uint32_t* leaf_list = nullptr;   // cap
     uint32_t* arrive = nullptr;      // 1 << (depth-1) refit arrival words (epoch-tagged)
-    uint2* items = nullptr;          // emission items (heap index, mask): 2 x emit tiles x 64, ping-pong per level
-    uint32_t* item_counts = nullptr; // 2 x emit tiles
+    uint2* items = nullptr;          // emission items (heap index, mask) of every merge level: 6 x emit tiles x 64
+    uint32_t* item_counts = nullptr; // 8 x emit tiles: item counts of every level (6x), tile unit counts, merge tickets
     uint32_t sort_tiles_cap = 0, emit_tiles_cap = 0, bounds_blocks = 0;
     // frame buffers for rt_render_frame_host (grown on demand)
     rt_hit* f_primary = nullptr;
