@@ -918,10 +918,13 @@ __global__ void __launch_bounds__(256) k_emit_refit(const uint32_t* __restrict__
 //      leaf's range, and at heads and tails the mask capped at the leaf depth
 //      and the leaf's heap index; the tile's leaves become "units" in sorted
 //      order;
-//   2. the triangles gathered in sorted order (sorted_tris), each thread over
-//      its own eight consecutive elements, and their boxes folded per leaf (a
-//      segmented scan carries a leaf that spans threads, with its head); the
-//      leaf records are stored;
+//   0. the triangles gathered in sorted order (sorted_tris), striped so that
+//      a warp takes 32 consecutive elements at a time: they leave through a
+//      per-warp staging buffer as 512-byte runs, and their boxes go to
+//      shared memory;
+//   2. the boxes folded per leaf, each thread over its own eight consecutive
+//      elements (a segmented scan carries a leaf that spans threads, with its
+//      head); the leaf records are stored;
 //   3. a leaf that began in an earlier tile and ends in this one is finished
 //      here: its start is found by scanning back over the codes and its
 //      earlier triangles are folded in from the soup.
@@ -948,6 +951,37 @@ constexpr int kMergeGroup = 32;      // tiles (groups) per CTA of the next level
 constexpr int kUnitWords = 12;       // shared words per unit
 constexpr size_t kUnitSmem = (size_t)kUnitWords * kUnitCap * sizeof(uint32_t) + 16;
 constexpr size_t kChunkSmem = (size_t)kUnitWords * kChunkUnits * sizeof(uint32_t) + 16;
+// k_emit_units: the tile's triangle boxes, six planes of kBoxStride floats
+// (element e at e + e / 32, so that a warp reading eight consecutive
+// elements per lane hits 32 different banks), then one staging buffer of
+// 32 triangles (96 float4) per warp
+constexpr int kBoxStride = kEmitTile + kEmitTile / 32;
+constexpr int kGatherBatch = 4;  // triangles a thread has in flight in the gather
+constexpr size_t kEmitUnitsSmem = 6 * kBoxStride * sizeof(float) + (kEmitThreads / 32) * 96 * sizeof(float4);
+static_assert((6 * kBoxStride) % 4 == 0, "staging buffer must start 16-byte aligned");
+static_assert(kEmitItems % kGatherBatch == 0, "gather batches must tile a thread's elements");
+
+// Triangle `id` of a soup of n triangles (9 floats each): three 16-byte
+// loads of the 12 floats starting at float 9 id - (id mod 4), which is 16-byte
+// aligned when the soup is (9 id = id mod 4, mod 4), then a shift by id mod 4.
+// The last triangles, whose 12 floats would run past the soup, and an
+// unaligned soup take scalar loads.
+__device__ __forceinline__ void load_tri(const float* __restrict__ tris, uint32_t id, uint32_t n, bool aligned,
+                                         float v[9]) {
+    const uint32_t r = id & 3u;
+    const size_t f0 = 9 * (size_t)id - r;
+    if (aligned && f0 + 12 <= 9 * (size_t)n) {
+        const float4* p = reinterpret_cast<const float4*>(tris + f0);
+        const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+        const float w[12] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
+#pragma unroll
+        for (int k = 0; k < 9; ++k) v[k] = r == 0 ? w[k] : r == 1 ? w[k + 1] : r == 2 ? w[k + 2] : w[k + 3];
+    } else {
+        const float* tp = tris + 9 * (size_t)id;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) v[k] = __ldg(tp + k);
+    }
+}
 
 // Leaf axis field: the reference's round-robin counter at the call that made
 // the leaf (see refit_walk), with the parent's split bit = the lowest bit of
@@ -995,15 +1029,6 @@ __device__ __forceinline__ Box tri_box(const float v[9]) {
     for (int c = 0; c < 3; ++c) {
         r.lo[c] = smin(v[c], smin(v[3 + c], v[6 + c]));
         r.hi[c] = smax(v[c], smax(v[3 + c], v[6 + c]));
-    }
-    return r;
-}
-__device__ __forceinline__ Box shfl_box(const Box& b, int src) {
-    Box r;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        r.lo[c] = __shfl_sync(kFull, b.lo[c], src);
-        r.hi[c] = __shfl_sync(kFull, b.hi[c], src);
     }
     return r;
 }
@@ -1128,15 +1153,25 @@ __device__ void unit_bottom_up(const Units& u, int U, rt_node* nodes, uint2* ite
     }
 }
 
-// Heap index of an element: 1 followed by its code's bits at the positions of
-// its capped ancestor mask m, high to low.
-__device__ __forceinline__ uint32_t heap_index(uint32_t code, uint32_t m) {
-    uint32_t h = 1u;
-    while (m) {
-        const int b = hb(m);
-        h = (h << 1) | ((code >> b) & 1u);
-        m ^= 1u << b;
+// The capped mask and heap index of an element with ancestor mask anc: the
+// highest `cap` bits of anc (its ancestors down to the leaf depth), and 1
+// followed by the code's bits at those positions, high to low.  Taken a run
+// of consecutive mask bits at a time rather than bit by bit (a balanced
+// region's mask is one run).
+__device__ __forceinline__ uint32_t heap_index_capped(uint32_t code, uint32_t anc, int cap, uint32_t* m_out) {
+    uint32_t h = 1u, m = 0u;
+    int left = cap;
+    while (anc != 0u && left > 0) {
+        const int top = hb(anc);
+        const int len = min(__clz(~(anc << (31 - top))), left);  // the run from top down, at most `left` bits
+        const int lo = top - len + 1;
+        const uint32_t ones = (len >= 32) ? ~0u : ((1u << len) - 1u);
+        h = (h << len) | ((code >> lo) & ones);
+        m |= ones << lo;
+        anc &= ~(ones << lo);
+        left -= len;
     }
+    *m_out = m;
     return h;
 }
 
@@ -1160,6 +1195,9 @@ __global__ void __launch_bounds__(THREADS) k_emit_units(const uint32_t* __restri
     __shared__ int32_t s_rhead[THREADS / 32];
     __shared__ int s_found;
     __shared__ float s_cont_box[6];
+    static_assert(THREADS == kEmitThreads, "the shared-memory layout is sized for kEmitThreads");
+    extern __shared__ float4 emit_smem[];
+    float* s_box = reinterpret_cast<float*>(emit_smem);  // [6][kBoxStride]: lo xyz, hi xyz
 
     grid_dep_wait();
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -1168,6 +1206,55 @@ __global__ void __launch_bounds__(THREADS) k_emit_units(const uint32_t* __restri
     if (t == 0) {
         s_first_head = s_first_tail = kEmitTile;
         s_last_head = s_last_tail = 0u;
+    }
+
+    // 0. pre-gather in sorted order (A.xyz,id | B.xyz,0 | C.xyz,0): element
+    // tbase + b * THREADS + t, a batch of loads in flight per thread; the
+    // warp's 32 triangles are staged and stored as three 512-byte runs
+    {
+        float4* stage = emit_smem + (6 * kBoxStride) / 4 + w * 96;
+        const bool soup_aligned = (reinterpret_cast<uintptr_t>(tris) & 15u) == 0;
+#pragma unroll 1
+        for (int g = 0; g < kEmitItems; g += kGatherBatch) {
+            uint32_t idv[kGatherBatch];
+            float v[kGatherBatch][9];
+#pragma unroll
+            for (int b = 0; b < kGatherBatch; ++b) {
+                const uint32_t k = tbase + (uint32_t)((g + b) * THREADS + t);
+                uint32_t id = k < n ? __ldg(ids + k) : 0u;
+                if (id >= n) {  // only after a failed sort (look-back timeout)
+                    atomicOr(err, RT_DEVERR_BOUNDS);
+                    id = 0;
+                }
+                idv[b] = id;
+            }
+#pragma unroll
+            for (int b = 0; b < kGatherBatch; ++b) load_tri(tris, idv[b], n, soup_aligned, v[b]);
+#pragma unroll
+            for (int b = 0; b < kGatherBatch; ++b) {
+                const uint32_t e0 = (uint32_t)((g + b) * THREADS + w * 32);  // the warp's first element
+                const uint32_t el = e0 + lane;
+                const Box tb = tri_box(v[b]);
+                const uint32_t pb = el + (el >> 5);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    s_box[c * kBoxStride + pb] = tb.lo[c];
+                    s_box[(3 + c) * kBoxStride + pb] = tb.hi[c];
+                }
+                stage[3 * lane + 0] = make_float4(v[b][0], v[b][1], v[b][2], __int_as_float((int)idv[b]));
+                stage[3 * lane + 1] = make_float4(v[b][3], v[b][4], v[b][5], 0.0f);
+                stage[3 * lane + 2] = make_float4(v[b][6], v[b][7], v[b][8], 0.0f);
+                __syncwarp();
+                const uint32_t kw = tbase + e0;
+                const uint32_t live = kw < n ? min(32u, n - kw) : 0u;  // the run's elements inside the soup
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    const uint32_t f = (uint32_t)(lane + 32 * j);
+                    if (f < 3 * live) sorted_tris[3 * (size_t)kw + f] = stage[f];
+                }
+                __syncwarp();
+            }
+        }
     }
 
     // 1. capped mask, head and tail of this thread's elements; heap index at
@@ -1207,12 +1294,7 @@ __global__ void __launch_bounds__(THREADS) k_emit_units(const uint32_t* __restri
                 // may close a leaf whose head is in an earlier thread (a tail
                 // after a head of this thread shares that head's)
                 uint32_t m = 0u;
-                if (head || heads == 0u) {
-                    int dep = __popc(anc);
-                    m = anc;
-                    while (dep > leaf_depth) { m &= m - 1u; --dep; }
-                    hh[q] = heap_index(e.c[q], m);
-                }
+                if (head || heads == 0u) hh[q] = heap_index_capped(e.c[q], anc, leaf_depth, &m);
                 hm[q] = m | (head ? kHeadBit : 0u) | (tail ? kTailBit : 0u);
                 const uint32_t j = t * kEmitItems + q;
                 if (head) {
@@ -1235,8 +1317,8 @@ __global__ void __launch_bounds__(THREADS) k_emit_units(const uint32_t* __restri
     const uint32_t cont = (first_tail < kEmitTile && first_tail < first_head) ? 1u : 0u;
     const bool last_open = s_last_head > s_last_tail;  // the last head's leaf has no tail in the tile
 
-    // 2. pre-gather in sorted order (A.xyz,id | B.xyz,0 | C.xyz,0) and the leaf
-    // boxes: each thread folds its own elements; a leaf spanning threads is
+    // 2. the leaf boxes: each thread folds its own elements' boxes (gathered
+    // in step 0, ordered by the scans' barriers); a leaf spanning threads is
     // carried by a segmented scan that also carries the leaf's head position
     Box part = empty_box();  // elements before the thread's first head (or all of them)
     Box run = empty_box();   // the current leaf since its head in this thread
@@ -1250,19 +1332,13 @@ __global__ void __launch_bounds__(THREADS) k_emit_units(const uint32_t* __restri
     for (int q = 0; q < kEmitItems; ++q) {
         const uint32_t k = s + q;
         if (k >= n) break;
-        uint32_t id = __ldg(ids + k);
-        if (id >= n) {  // only after a failed sort (look-back timeout)
-            atomicOr(err, RT_DEVERR_BOUNDS);
-            id = 0;
-        }
-        const float* tp = tris + 9 * (size_t)id;
-        float v[9];
+        const uint32_t el = (uint32_t)t * kEmitItems + q, pb = el + (el >> 5);
+        Box tb;
 #pragma unroll
-        for (int c = 0; c < 9; ++c) v[c] = __ldg(tp + c);
-        sorted_tris[3 * (size_t)k + 0] = make_float4(v[0], v[1], v[2], __int_as_float((int)id));
-        sorted_tris[3 * (size_t)k + 1] = make_float4(v[3], v[4], v[5], 0.0f);
-        sorted_tris[3 * (size_t)k + 2] = make_float4(v[6], v[7], v[8], 0.0f);
-        const Box tb = tri_box(v);
+        for (int c = 0; c < 3; ++c) {
+            tb.lo[c] = s_box[c * kBoxStride + pb];
+            tb.hi[c] = s_box[(3 + c) * kBoxStride + pb];
+        }
         const bool head = (hm[q] & kHeadBit) != 0, tail = (hm[q] & kTailBit) != 0;
         if (head) {
             const uint32_t idx = cont + hbase + ord++;
@@ -1767,12 +1843,14 @@ static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint
     // pass; the nodes above the tiles by k_emit_merge, level after level
     RT_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_emit_merge<kEmitThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)kUnitSmem));
+    RT_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_emit_units<kEmitThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)kEmitUnitsSmem));
     uint32_t* inner = compact ? l->inner : nullptr;
     // the sort's ping-pong buffers are free again: they hold the tiles' unit lists
     uint2* tile_units = reinterpret_cast<uint2*>(l->keys_alt);
     const size_t cap = l->emit_tiles_cap;
     uint32_t* tile_counts = l->item_counts + 6 * cap;
-    launch_pdl(k_emit_units<kEmitThreads>, emit_tiles, kEmitThreads, 0, st, (const uint32_t*)l->keys,
+    launch_pdl(k_emit_units<kEmitThreads>, emit_tiles, kEmitThreads, kEmitUnitsSmem, st, (const uint32_t*)l->keys,
                (const uint32_t*)l->ids, d_tris, n, l->depth, (const uint32_t*)l->scan, l->nodes, l->sorted_tris,
                tile_units, tile_counts, ctx->d_err);
     RT_CHECK_LAUNCH(ctx, "k_emit_units");
