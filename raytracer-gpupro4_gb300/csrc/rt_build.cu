@@ -301,6 +301,8 @@ constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagInc = 2u << 30;
 constexpr uint32_t kFlagMask = 3u << 30;
 constexpr uint32_t kValMask = (1u << 30) - 1u;
+constexpr int kLookWidth = 4;  // predecessor words a look-back step reads at once
+constexpr unsigned kLookSleepNs = 100;  // back-off before polling an unpublished word again
 
 // k_onesweep: one LSD pass over 8 bits.  Each CTA takes the next tile ticket
 // (so every tile it waits on belongs to a CTA that is already running),
@@ -401,21 +403,26 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
     // decoupled look-back (bounded)
     uint32_t* my = lookback + (size_t)tile * 256 + t;
     st_relaxed(my, (tile == 0 ? kFlagInc : kFlagAgg) | count);
-    // Look-back over the predecessors' words for this digit, four at a time
-    // (the four loads are in flight together): add aggregates until an
-    // inclusive prefix; a word not yet published is polled again (bounded).
+    // Look-back over the predecessors' words for this digit, kLookWidth at a
+    // time (the loads are in flight together): add aggregates until an
+    // inclusive prefix; a word not yet published is polled again (bounded),
+    // after a short sleep, so that the polls of waiting warps do not take
+    // issue slots from the warps of the same SM that are still ranking.
+    // (Reading 8 or 16 words a step was slower: the extra polls cost more
+    // than the shorter chain of inclusive prefixes saved.)
     uint32_t excl = 0;
     if (tile > 0) {
         int p = (int)tile - 1;
         uint32_t spins = 0;
         bool done = false;
         while (!done && p >= 0) {
-            uint32_t v[4];
+            uint32_t v[kLookWidth];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) v[q] = (p - q >= 0) ? ld_relaxed(lookback + (size_t)(p - q) * 256 + t) : 0u;
+            for (int q = 0; q < kLookWidth; ++q)
+                v[q] = (p - q >= 0) ? ld_relaxed(lookback + (size_t)(p - q) * 256 + t) : 0u;
             int used = 0;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < kLookWidth; ++q) {
                 if (done || used < q || p - q < 0) continue;
                 const uint32_t f = v[q] & kFlagMask;
                 if (f == 0u) continue;  // not published yet: poll again from here
@@ -423,9 +430,12 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
                 used = q + 1;
                 if (f == kFlagInc) done = true;
             }
-            if (!done && used == 0 && ++spins > spin_limit) {
-                atomicOr(err, RT_DEVERR_TIMEOUT);
-                break;
+            if (!done && used == 0) {
+                if (++spins > spin_limit) {
+                    atomicOr(err, RT_DEVERR_TIMEOUT);
+                    break;
+                }
+                __nanosleep(kLookSleepNs);
             }
             p -= used;
         }

@@ -251,8 +251,10 @@ inline void launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem,
     } while (0)
 
 // Bounded spin used by every device-side wait (look-back): after this many
-// polls the waiter records RT_DEVERR_TIMEOUT and stops waiting.
-constexpr uint32_t kSpinLimit = 1u << 22;
+// polls the waiter records RT_DEVERR_TIMEOUT and stops waiting.  A poll that
+// finds nothing new sleeps ~100 ns first, so a wait gives up within about a
+// second (2^20 polls x (sleep + an L2 round trip)).
+constexpr uint32_t kSpinLimit = 1u << 20;
 
 // Grid of a persistent kernel: as many blocks as fit on every SM at once,
 // capped by the number of 32-item tiles.
