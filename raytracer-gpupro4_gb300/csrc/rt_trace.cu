@@ -265,6 +265,12 @@ __global__ void __launch_bounds__(256) k_shade_setup(const float* __restrict__ s
 // faster than 32 rays per warp taken at once; refilling at 8, 24 or 32 idle
 // lanes, or without the register cap, is slower.
 constexpr int kRefillLanes = 16;
+// A lane expands at most kShadeSteps internal nodes per round before the
+// warp's leaf phase, so that lanes holding a leaf do not wait out one lane's
+// long descent (shading rays start on the surface, where descents vary
+// most).  4 was the fastest of 1-16 at 2.1 M triangles / 1080p (7 % over an
+// unbounded descent); the primary walk is fastest unbounded.
+constexpr int kShadeSteps = 4;
 
 // The scenes of a batch as seen by k_trace_shade (nodes == nullptr: one tree):
 // a listed pixel g belongs to scene g / px, whose heap is at nodes + (s <<
@@ -350,15 +356,19 @@ __global__ void __launch_bounds__(kTraceThreads, 7) k_trace_shade(
             if (drained) break;
             continue;
         }
-        // one round of the walk: descend to a leaf, test the held leaves together, pop
+        // one round of the walk: descend (at most kShadeSteps nodes) towards a
+        // leaf, test the held leaves together, pop
         const bool ex = __any_sync(kFull, have && r.exact);
+        bool leaf = false;
         if (have) {
-            have = ex ? descend<true, false>(tr, r, b.t, node, cur, stack_node, stack_t0, sp, 0u, nbox)
-                      : descend<false, false>(tr, r, b.t, node, cur, stack_node, stack_t0, sp, 0u, nbox);
+            have = ex ? descend<true, false, true>(tr, r, b.t, node, cur, stack_node, stack_t0, sp, 0u, nbox,
+                                                   kShadeSteps, &leaf)
+                      : descend<false, false, true>(tr, r, b.t, node, cur, stack_node, stack_t0, sp, 0u, nbox,
+                                                    kShadeSteps, &leaf);
         }
         __syncwarp();
-        leaf_phase<false>(tr, r, have, cur, node, bound, b, ntri);
-        if (have) {
+        if (__any_sync(kFull, have && leaf)) leaf_phase<false>(tr, r, have && leaf, cur, node, bound, b, ntri);
+        if (have && leaf) {
             if (shadow && b.id >= 0) {
                 have = false;  // any hit
             } else {

@@ -320,12 +320,19 @@ __device__ __forceinline__ bool leaf_phase(const TreeRef& tr_, const RayState& r
 // child is re-checked, LBVH.cpp:992).  The stack is a ring of kStackSize
 // entries holding [base, sp); a depth-first walk never holds more than the
 // tree depth.  Returns false when the lane has nothing left.
-template <bool EXACT, bool STATS>
+//
+// CAPPED: at most max_steps internal nodes are expanded in this call; a lane
+// that runs out keeps its place (returns true with *at_leaf false) and goes
+// on at the next call.  The walk, and so every test, is the same.
+template <bool EXACT, bool STATS, bool CAPPED = false>
 __device__ __forceinline__ bool descend(const TreeRef& tr_, const RayState& r, float bt, uint32_t& node, NodeBox& cur,
                                         uint32_t* stack_node, float* stack_t0, uint32_t& sp, uint32_t base,
-                                        uint32_t& nbox) {
+                                        uint32_t& nbox, int max_steps = 0, bool* at_leaf = nullptr) {
     const rt_node* __restrict__ nodes = tr_.nodes;
+    int steps = 0;
+    if (CAPPED) *at_leaf = false;
     while (!(__float_as_int(cur.b.z) & 4)) {
+        if (CAPPED && steps++ >= max_steps) return true;
         const int pc = __float_as_int(cur.b.z);
         const uint32_t c0 = child_pair(tr_, node, cur.b.w);
         if (c0 + 1 >= tr_.num_nodes) {
@@ -376,6 +383,7 @@ __device__ __forceinline__ bool descend(const TreeRef& tr_, const RayState& r, f
             cur = load_node(nodes, node);
         }
     }
+    if (CAPPED) *at_leaf = true;
     return true;
 }
 
