@@ -260,16 +260,16 @@ __global__ void __launch_bounds__(256) k_shade_setup(const float* __restrict__ s
 // (the newcomers take consecutive entries, so they stay neighbours), instead
 // of idling until the warp's slowest ray is done (dynamic ray fetch, Aila
 // and Laine 2009).  Each ray's walk and result are those of a whole-warp
-// trace_ray: the same start, the same descent, the same leaf phase.  At 2.1 M
-// triangles / 1080p this, with at most 73 registers (7 blocks per SM), is 1 %
-// faster than 32 rays per warp taken at once; refilling at 8, 24 or 32 idle
-// lanes, or without the register cap, is slower.
-constexpr int kRefillLanes = 16;
+// trace_ray: the same start, the same descent, the same leaf phase.
+//
 // A lane expands at most kShadeSteps internal nodes per round before the
 // warp's leaf phase, so that lanes holding a leaf do not wait out one lane's
 // long descent (shading rays start on the surface, where descents vary
-// most).  4 was the fastest of 1-16 at 2.1 M triangles / 1080p (7 % over an
-// unbounded descent); the primary walk is fastest unbounded.
+// most).  At 2.1 M triangles / 1080p, with at most 72 registers (7 blocks per
+// SM), 4 steps and a refill at 24 idle lanes were the fastest pair of those
+// tried (steps 1-16, refill at 8-32 idle lanes): 9 % faster than an unbounded
+// descent with a refill at 16.  The primary walk is fastest unbounded.
+constexpr int kRefillLanes = 24;
 constexpr int kShadeSteps = 4;
 
 // The scenes of a batch as seen by k_trace_shade (nodes == nullptr: one tree):
