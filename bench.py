@@ -211,7 +211,7 @@ def run_ours(args, dist: Dist):
     import torch
     from rtgpu import _lib as L
     from rtgpu import build as B
-    from rtgpu.api import LBVH, Context, Frame, RayTracer
+    from rtgpu.api import LBVH, Context, Frame, Pipe, RayTracer
 
     B.build_cuda()
     torch.cuda.set_device(dist.local)
@@ -321,57 +321,45 @@ def run_ours(args, dist: Dist):
         g.close()
 
     # e2e: the public C ABI with host buffers, copies inside the timed region.
-    # Two contexts on two streams take alternate frames, each frame one launch
-    # of a graph captured by rt_frame_capture_host (pinned soup upload,
-    # rebuild, trace, read-back of hits / visibility / mirror hits into pinned
-    # host buffers), so one frame's copies overlap the other frame's kernels;
-    # every frame's upload and read-back is inside the timed region.
+    # rt_pipe_* keeps two frames in flight: frame k's pinned soup upload and
+    # frame k-1's read-back (hits / visibility / mirror hits into pinned host
+    # buffers) run on two copy streams while the frames' captured rebuild +
+    # trace graphs run one after another on the context stream; every
+    # frame's upload and read-back is inside the timed region.
     e2e = None
     if not args.no_e2e:
-        lanes = []
-        for q in range(2):
-            st_q = torch.cuda.Stream(dev)
-            ctx_q = Context(dist.local, stream=st_q)
-            lb_q = LBVH(ctx_q, n, args.depth)
-            hp_t = torch.empty((npx, 4), dtype=torch.int32).pin_memory()
-            hm_t = torch.empty((npx, 4), dtype=torch.int32).pin_memory()
-            hv_t = torch.empty(npx, dtype=torch.uint8).pin_memory()
-            fr_q = [Frame(ctx_q, lb_q, host[k], cam, light, hp_t, hv_t, hm_t, host=True) for k in range(len(frames))]
-            lanes.append((ctx_q, lb_q, fr_q, hp_t, hv_t, hm_t))
+        pipe = Pipe(ctx, lb, n, cam, light)
+        outs = [(torch.empty((npx, 4), dtype=torch.int32).pin_memory(), torch.empty(npx, dtype=torch.uint8).pin_memory(),
+                 torch.empty((npx, 4), dtype=torch.int32).pin_memory()) for _ in range(2)]
 
-        def e2e_frame(k):
-            ctx_q, _, fr_q = lanes[k % 2][:3]
-            ctx_q.sync()  # this lane's previous frame is done with its host buffers
-            fr_q[k % len(frames)].launch()
+        def e2e_frame(k):  # tickets are issued in submission order, from 0
+            if k >= 2:
+                pipe.wait(k - 2)  # frame k-2 is done with the host buffers frame k reuses
+            pipe.submit(host[k % len(frames)], *outs[k % 2])
 
         for k in range(args.warmup):
             e2e_frame(k)
-        for q in range(2):
-            lanes[q][0].sync()
+        pipe.wait(args.warmup - 1)
         dist.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for k in range(args.steps):
             e2e_frame(args.warmup + k)
-        for q in range(2):
-            lanes[q][0].sync()
+        last_k = args.warmup + args.steps - 1
+        pipe.wait(last_k - 1)
+        pipe.wait(last_k)
         te = dist.max(time.perf_counter() - t0)
-        for q in range(2):
-            lanes[q][0].check()
+        ctx.check()
         # the last frame read back equals the last graph frame (same soup)
-        last = lanes[(args.warmup + args.steps - 1) % 2][3]
-        e2e_ok = bool(np.array_equal(last.numpy(), hits.cpu().numpy()))
+        e2e_ok = bool(np.array_equal(outs[last_k % 2][0].numpy(), hits.cpu().numpy()))
         e2e = {"value": round(frames_done * n / te / 1e6, 3), "unit": "Mtri/s",
                "h2d_bytes_per_step": int(n * 36), "d2h_bytes_per_step": int(npx * (16 + 1 + 16)),
                "ms_per_step": round(te / args.steps * 1e3, 3),
-               "call": "rt_frame_capture_host graphs on two contexts / streams, alternate frames "
-                       "(pinned host soup in, hits / visibility / mirror hits out)",
+               "call": "rt_pipe_submit / rt_pipe_wait: two frames in flight, copies on two copy streams, "
+                       "frame graphs in order on the context stream (pinned host soup in, hits / visibility / "
+                       "mirror hits out)",
                "matches_device_path": e2e_ok}
-        for q in range(2):
-            for f in lanes[q][2]:
-                f.close()
-            lanes[q][1].close()
-            lanes[q][0].close()
+        pipe.close()
 
     peak, peak_kind = measured_peaks()
     # stage: (ms, algorithmic bytes, kernels of the stage's ncu traffic)

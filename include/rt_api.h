@@ -395,6 +395,33 @@ rt_status rt_frame_capture_host(rt_ctx* ctx, rt_lbvh* lbvh, const float* h_tris,
                                 const rt_camera* cam, const float light[3], rt_hit* h_primary, uint8_t* h_vis,
                                 rt_hit* h_mirror, rt_frame** out);
 
+/* ---- double-buffered host frames ------------------------------------- */
+/* The dynamic per-frame path with host buffers, pipelined (replaces the
+ * vertex-buffer update + RayTracerCS::Render loop of a dynamic model,
+ * RayTracerCS.cpp:241-311, which the D3D immediate context serialises).
+ * rt_pipe_create captures two frames (rt_frame_capture) over two device soup
+ * slots and two sets of device result buffers.  rt_pipe_submit queues frame
+ * k in slot k mod 2: the upload of the pinned host soup on a private copy
+ * stream, the captured rebuild + trace on the context stream (frames run
+ * their kernels one after another), the read-back into the pinned host
+ * buffers on a second private copy stream.  So frame k's upload and frame
+ * k-1's read-back run while frame k-1's or k's kernels do, and no two
+ * frames' kernels share the GPU.  The host soup of frame k may be rewritten
+ * once rt_pipe_wait(k) has returned; its host results are complete then.
+ * Waiting on a ticket whose slot a later frame has reused waits for that
+ * later frame.  want_vis / want_mirror select the shading outputs (0: the
+ * frame traces primary rays only and h_vis / h_mirror must be NULL).  Host
+ * buffers must be page-locked (RT_ERR_INVALID otherwise).  Device-side
+ * errors are reported by rt_ctx_check (it waits for the context stream).
+ * The pipe holds a reference on lbvh, as a captured frame does. */
+typedef struct rt_pipe rt_pipe;
+rt_status rt_pipe_create(rt_ctx* ctx, rt_lbvh* lbvh, uint32_t n, uint32_t flags, const rt_camera* cam,
+                         const float light[3], int want_vis, int want_mirror, rt_pipe** out);
+rt_status rt_pipe_submit(rt_pipe* pipe, const float* h_tris, rt_hit* h_primary, uint8_t* h_vis, rt_hit* h_mirror,
+                         uint64_t* ticket);
+rt_status rt_pipe_wait(rt_pipe* pipe, uint64_t ticket);
+rt_status rt_pipe_destroy(rt_pipe* pipe);
+
 /* ---- batched scenes ------------------------------------------------- */
 /* Up to 256 independent scenes rebuilt and traced together: one pass of the
  * build kernels over the concatenated soups and one persistent trace kernel

@@ -1288,7 +1288,7 @@ __global__ void __launch_bounds__(THREADS) k_emit_units(const uint32_t* __restri
     for (int q = kEmitItems - 1; q >= 0; --q) R[q] = rec_bwd(e.r[q], R[q + 1]);
     const int leaf_depth = (int)depth - 1;
     uint32_t hm[kEmitItems], hh[kEmitItems];  // capped mask | head | tail; heap index (heads, tails)
-    uint32_t heads = 0u;
+    uint32_t heads = 0u, tails = 0u;
 #pragma unroll
     for (int q = 0; q < kEmitItems; ++q) {
         const uint32_t k = s + q;
@@ -1306,17 +1306,22 @@ __global__ void __launch_bounds__(THREADS) k_emit_units(const uint32_t* __restri
                 uint32_t m = 0u;
                 if (head || heads == 0u) hh[q] = heap_index_capped(e.c[q], anc, leaf_depth, &m);
                 hm[q] = m | (head ? kHeadBit : 0u) | (tail ? kTailBit : 0u);
-                const uint32_t j = t * kEmitItems + q;
-                if (head) {
-                    heads |= 1u << q;
-                    atomicMin(&s_first_head, j);
-                    atomicMax(&s_last_head, j + 1);
-                }
-                if (tail) {
-                    atomicMin(&s_first_tail, j);
-                    atomicMax(&s_last_tail, j + 1);
-                }
+                if (head) heads |= 1u << q;
+                if (tail) tails |= 1u << q;
             }
+        }
+    }
+    {  // the tile's first / last head and tail: warp reductions, one shared atomic per warp
+        const uint32_t j0 = (uint32_t)t * kEmitItems;
+        const uint32_t fh = __reduce_min_sync(kFull, heads ? j0 + __ffs(heads) - 1 : (uint32_t)kEmitTile);
+        const uint32_t lh = __reduce_max_sync(kFull, heads ? j0 + (32 - __clz(heads)) : 0u);
+        const uint32_t ft = __reduce_min_sync(kFull, tails ? j0 + __ffs(tails) - 1 : (uint32_t)kEmitTile);
+        const uint32_t lt = __reduce_max_sync(kFull, tails ? j0 + (32 - __clz(tails)) : 0u);
+        if (lane == 0) {
+            atomicMin(&s_first_head, fh);
+            atomicMax(&s_last_head, lh);
+            atomicMin(&s_first_tail, ft);
+            atomicMax(&s_last_tail, lt);
         }
     }
     const uint32_t hbase = block_excl_sum_256(__popc(heads), s_tmp);  // includes __syncthreads

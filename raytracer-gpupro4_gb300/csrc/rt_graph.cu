@@ -187,3 +187,140 @@ extern "C" rt_status rt_frame_destroy(rt_frame* f) {
     delete f;
     return RT_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Double-buffered host frames (rt_pipe_*).  Frame k uses slot s = k mod 2:
+//   upload stream:  wait for the kernels of frame k-2 (they read soup[s]),
+//                   copy the host soup into soup[s]                  -> ev_in[s]
+//   context stream: wait ev_in[s] and the read-back of frame k-2 (it reads
+//                   the results of slot s), the captured frame of slot s -> ev_comp[s]
+//   read-back stream: wait ev_comp[s], copy the results to the host  -> ev_out[s]
+// The kernels of consecutive frames are ordered by the context stream, so
+// only copies overlap kernels.
+struct rt_pipe {
+    rt_ctx* ctx = nullptr;
+    rt_lbvh* lbvh = nullptr;
+    uint32_t n = 0;
+    size_t px = 0;
+    bool vis = false, mirror = false;
+    float* soup[2] = {nullptr, nullptr};
+    rt_hit* prim[2] = {nullptr, nullptr};
+    uint8_t* vbuf[2] = {nullptr, nullptr};
+    rt_hit* mbuf[2] = {nullptr, nullptr};
+    rt_frame* frame[2] = {nullptr, nullptr};
+    cudaStream_t up = nullptr, down = nullptr;
+    cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_comp[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
+    uint64_t next = 0;
+};
+
+static void free_pipe(rt_pipe* p) {
+    for (int s = 0; s < 2; ++s) {
+        if (p->frame[s]) rt_frame_destroy(p->frame[s]);
+        for (void* q : {(void*)p->soup[s], (void*)p->prim[s], (void*)p->vbuf[s], (void*)p->mbuf[s]})
+            if (q) cudaFree(q);
+        for (cudaEvent_t e : {p->ev_in[s], p->ev_comp[s], p->ev_out[s]})
+            if (e) cudaEventDestroy(e);
+    }
+    if (p->up) cudaStreamDestroy(p->up);
+    if (p->down) cudaStreamDestroy(p->down);
+    delete p;
+}
+
+extern "C" rt_status rt_pipe_create(rt_ctx* ctx, rt_lbvh* l, uint32_t n, uint32_t flags, const rt_camera* cam,
+                                    const float light[3], int want_vis, int want_mirror, rt_pipe** out) {
+    if (!ctx) return RT_ERR_INVALID;
+    if (!l || !cam || !light || !out) return rt_fail(ctx, RT_ERR_INVALID, "rt_pipe_create: null argument");
+    *out = nullptr;
+    if (n == 0 || n > l->cap) return rt_fail(ctx, RT_ERR_CAPACITY, "rt_pipe_create: n=%u (capacity %u)", n, l->cap);
+    const size_t px = (size_t)cam->width * cam->height;
+    if (px == 0 || px > (1ull << 31)) return rt_fail(ctx, RT_ERR_INVALID, "rt_pipe_create: bad image size");
+    RT_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+    rt_pipe* p = new rt_pipe();
+    p->ctx = ctx;
+    p->n = n;
+    p->px = px;
+    p->vis = want_vis != 0;
+    p->mirror = want_mirror != 0;
+    cudaError_t e = cudaSuccess;
+    auto ok = [&](cudaError_t r) {
+        if (e == cudaSuccess) e = r;
+        return e == cudaSuccess;
+    };
+    for (int s = 0; s < 2; ++s) {
+        ok(cudaMalloc((void**)&p->soup[s], sizeof(float) * 9 * (size_t)n));
+        ok(cudaMalloc((void**)&p->prim[s], sizeof(rt_hit) * px));
+        if (p->vis) ok(cudaMalloc((void**)&p->vbuf[s], px));
+        if (p->mirror) ok(cudaMalloc((void**)&p->mbuf[s], sizeof(rt_hit) * px));
+        ok(cudaEventCreateWithFlags(&p->ev_in[s], cudaEventDisableTiming));
+        ok(cudaEventCreateWithFlags(&p->ev_comp[s], cudaEventDisableTiming));
+        ok(cudaEventCreateWithFlags(&p->ev_out[s], cudaEventDisableTiming));
+    }
+    ok(cudaStreamCreateWithFlags(&p->up, cudaStreamNonBlocking));
+    ok(cudaStreamCreateWithFlags(&p->down, cudaStreamNonBlocking));
+    // the captured frames read an uninitialised soup only if submitted
+    // without an upload, which rt_pipe_submit never does
+    if (e != cudaSuccess) {
+        free_pipe(p);
+        return rt_fail(ctx, RT_ERR_CUDA, "rt_pipe_create: %s", cudaGetErrorString(e));
+    }
+    for (int s = 0; s < 2; ++s) {
+        const rt_status cs = rt_frame_capture(ctx, l, p->soup[s], n, flags, cam, light, p->prim[s], p->vbuf[s],
+                                              p->mbuf[s], &p->frame[s]);
+        if (cs != RT_OK) {
+            free_pipe(p);
+            return cs;
+        }
+    }
+    p->lbvh = l;
+    *out = p;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_pipe_submit(rt_pipe* p, const float* h_tris, rt_hit* h_primary, uint8_t* h_vis,
+                                    rt_hit* h_mirror, uint64_t* ticket) {
+    if (!p) return RT_ERR_INVALID;
+    rt_ctx* ctx = p->ctx;
+    if (!h_tris) return rt_fail(ctx, RT_ERR_INVALID, "rt_pipe_submit: null soup");
+    if ((h_vis && !p->vis) || (h_mirror && !p->mirror))
+        return rt_fail(ctx, RT_ERR_INVALID, "rt_pipe_submit: the pipe was created without that output");
+    const void* host[] = {h_tris, h_primary, h_vis, h_mirror};
+    for (const void* h : host)
+        if (h && !pinned(h)) return rt_fail(ctx, RT_ERR_INVALID, "rt_pipe_submit: host buffers must be page-locked");
+    const uint64_t k = p->next;
+    const int s = (int)(k & 1u);
+    cudaStream_t cs = ctx->stream;
+    if (k >= 2) RT_CHECK_CUDA(ctx, cudaStreamWaitEvent(p->up, p->ev_comp[s], 0));
+    RT_CHECK_CUDA(ctx, cudaMemcpyAsync(p->soup[s], h_tris, sizeof(float) * 9 * (size_t)p->n, cudaMemcpyHostToDevice, p->up));
+    RT_CHECK_CUDA(ctx, cudaEventRecord(p->ev_in[s], p->up));
+    RT_CHECK_CUDA(ctx, cudaStreamWaitEvent(cs, p->ev_in[s], 0));
+    if (k >= 2) RT_CHECK_CUDA(ctx, cudaStreamWaitEvent(cs, p->ev_out[s], 0));
+    RT_CHECK_CUDA(ctx, cudaGraphLaunch(p->frame[s]->exec, cs));
+    RT_CHECK_CUDA(ctx, cudaEventRecord(p->ev_comp[s], cs));
+    RT_CHECK_CUDA(ctx, cudaStreamWaitEvent(p->down, p->ev_comp[s], 0));
+    if (h_primary)
+        RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_primary, p->prim[s], sizeof(rt_hit) * p->px, cudaMemcpyDeviceToHost, p->down));
+    if (h_vis) RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_vis, p->vbuf[s], p->px, cudaMemcpyDeviceToHost, p->down));
+    if (h_mirror)
+        RT_CHECK_CUDA(ctx, cudaMemcpyAsync(h_mirror, p->mbuf[s], sizeof(rt_hit) * p->px, cudaMemcpyDeviceToHost, p->down));
+    RT_CHECK_CUDA(ctx, cudaEventRecord(p->ev_out[s], p->down));
+    p->next = k + 1;
+    if (ticket) *ticket = k;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_pipe_wait(rt_pipe* p, uint64_t ticket) {
+    if (!p) return RT_ERR_INVALID;
+    if (ticket >= p->next) return rt_fail(p->ctx, RT_ERR_INVALID, "rt_pipe_wait: frame %llu was not submitted",
+                                          (unsigned long long)ticket);
+    RT_CHECK_CUDA(p->ctx, cudaEventSynchronize(p->ev_out[ticket & 1u]));
+    return RT_OK;
+}
+
+extern "C" rt_status rt_pipe_destroy(rt_pipe* p) {
+    if (!p) return RT_OK;
+    cudaStreamSynchronize(p->up);
+    cudaStreamSynchronize(p->ctx->stream);
+    cudaStreamSynchronize(p->down);
+    free_pipe(p);
+    return RT_OK;
+}

@@ -35,6 +35,7 @@ EXPORTED = [
     "rt_bvh_trace_primary", "rt_bvh_trace_shadow_mirror", "rt_bvh_trace_rays", "rt_render_frame_host", "rt_render_frame_host_async", "rt_pathtrace", "rt_pathtrace_counted", "rt_pathtrace_adjoint",
     "rt_lbvh_build_noalloc", "rt_radix_sort_scratch_bytes", "rt_radix_sort", "rt_radix_sort_stall_test",
     "rt_frame_capture_host", "rt_frame_capture", "rt_frame_launch", "rt_frame_node_count", "rt_frame_destroy",
+    "rt_pipe_create", "rt_pipe_submit", "rt_pipe_wait", "rt_pipe_destroy",
     "rt_batch_create", "rt_batch_destroy", "rt_batch_scene_count", "rt_batch_build", "rt_batch_view_get",
     "rt_batch_download", "rt_batch_set_views", "rt_batch_trace", "rt_batch_set_tuning", "rt_batch_get_tuning", "rt_batch_frame_capture",
 ]
@@ -137,6 +138,10 @@ def lib() -> C.CDLL:
         "rt_frame_launch": (i32, [vp, vp]),
         "rt_frame_node_count": (u32, [vp]),
         "rt_frame_destroy": (i32, [vp]),
+        "rt_pipe_create": (i32, [vp, vp, u32, u32, C.POINTER(Camera), fp, i32, i32, C.POINTER(vp)]),
+        "rt_pipe_submit": (i32, [vp, vp, vp, vp, vp, C.POINTER(C.c_uint64)]),
+        "rt_pipe_wait": (i32, [vp, C.c_uint64]),
+        "rt_pipe_destroy": (i32, [vp]),
         "rt_batch_create": (i32, [vp, u32, vp, u32, C.POINTER(vp)]),
         "rt_batch_destroy": (i32, [vp]),
         "rt_batch_scene_count": (u32, [vp]),

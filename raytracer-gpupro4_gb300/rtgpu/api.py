@@ -504,6 +504,54 @@ class Frame:
             pass
 
 
+class Pipe:
+    """Double-buffered host frames (rt_pipe_*): submit() queues the upload of
+    a pinned host soup, the captured rebuild + trace and the read-back into
+    pinned host tensors; frames' kernels run one after another on the
+    context stream while their copies overlap them.  wait(ticket) returns
+    once that frame's host results are complete."""
+
+    def __init__(self, ctx: Context, lbvh: LBVH, n: int, cam: L.Camera, light, vis: bool = True,
+                 mirror: bool = True, flags: int = 0):
+        self.ctx = ctx
+        self.lbvh = lbvh
+        h = C.c_void_p()
+        lf = (C.c_float * 3)(*light)
+        L.check(L.lib().rt_pipe_create(ctx.h, lbvh.h, n, flags, C.byref(cam), lf, int(vis), int(mirror), C.byref(h)),
+                ctx.h, "rt_pipe_create")
+        self.h = h
+        self._keep = {}
+        lbvh.n = n
+
+    def submit(self, tris: torch.Tensor, primary: torch.Tensor | None, vis: torch.Tensor | None = None,
+               mirror: torch.Tensor | None = None) -> int:
+        def ptr(t):
+            if t is None:
+                return None
+            assert t.is_contiguous() and not t.is_cuda  # rt_pipe_submit checks that they are page-locked
+            return C.c_void_p(t.data_ptr())
+
+        ticket = C.c_uint64()
+        L.check(L.lib().rt_pipe_submit(self.h, ptr(tris), ptr(primary), ptr(vis), ptr(mirror), C.byref(ticket)),
+                self.ctx.h, "rt_pipe_submit")
+        self._keep[ticket.value & 1] = (tris, primary, vis, mirror)
+        return ticket.value
+
+    def wait(self, ticket: int):
+        L.check(L.lib().rt_pipe_wait(self.h, ticket), self.ctx.h, "rt_pipe_wait")
+
+    def close(self):
+        if self.h:
+            L.lib().rt_pipe_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Batch:
     """Many scenes rebuilt and traced together (rt_batch_*): one pass of the
     build kernels over the concatenated soups, one persistent trace kernel

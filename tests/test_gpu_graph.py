@@ -116,3 +116,64 @@ def test_frame_holds_its_structure(gpu_ctx):
     gpu_ctx.check()
     assert torch.equal(prim, ref[0]) and torch.equal(vis, ref[1]) and torch.equal(mir, ref[2])
     f.close()  # frees the LBVH
+
+
+def test_pipe_frames_equal_device_frames(gpu_ctx):
+    """rt_pipe_*: frames submitted back to back (two in flight, host result
+    buffers alternating) read back the same bits as a device frame graph of
+    each soup; a frame's results are complete once its ticket is waited on;
+    pageable buffers, outputs the pipe was created without and unsubmitted
+    tickets are refused."""
+    import torch
+    from rtgpu import scenes
+    from rtgpu._lib import RtError
+    from rtgpu.api import LBVH, Frame, Pipe
+    s = scenes.icosphere(freq=40)
+    soups = [torch.from_numpy(s.frame(k)).pin_memory() for k in range(3)]
+    cam = scenes.sphere_camera(320, 180)
+    light = scenes.TORUS_LIGHT
+    n, npx = soups[0].shape[0], cam.width * cam.height
+    ref = []
+    lb_d = LBVH(gpu_ctx, n, 16)
+    dp = torch.empty((npx, 4), dtype=torch.int32, device="cuda")
+    dv = torch.empty(npx, dtype=torch.uint8, device="cuda")
+    dm = torch.empty((npx, 4), dtype=torch.int32, device="cuda")
+    for k in range(3):
+        fd = Frame(gpu_ctx, lb_d, soups[k].cuda(), cam, light, dp, dv, dm)
+        fd.launch()
+        gpu_ctx.check()
+        ref.append((dp.cpu(), dv.cpu(), dm.cpu()))
+        fd.close()
+    lb = LBVH(gpu_ctx, n, 16)
+    pipe = Pipe(gpu_ctx, lb, n, cam, light)
+    outs = [(torch.empty((npx, 4), dtype=torch.int32).pin_memory(), torch.empty(npx, dtype=torch.uint8).pin_memory(),
+             torch.empty((npx, 4), dtype=torch.int32).pin_memory()) for _ in range(2)]
+    order = [0, 1, 2, 2, 0, 1, 1]  # soup of each submitted frame
+    for k, f in enumerate(order):
+        if k >= 2:
+            pipe.wait(k - 2)
+            hp, hv, hm = outs[k % 2]
+            r = ref[order[k - 2]]
+            assert torch.equal(hp, r[0]) and torch.equal(hv, r[1]) and torch.equal(hm, r[2]), f"frame {k - 2}"
+            for t in outs[k % 2]:
+                t.fill_(0x55)
+        assert pipe.submit(soups[f], *outs[k % 2]) == k
+    for k in (len(order) - 2, len(order) - 1):
+        pipe.wait(k)
+        r = ref[order[k]]
+        hp, hv, hm = outs[k % 2]
+        assert torch.equal(hp, r[0]) and torch.equal(hv, r[1]) and torch.equal(hm, r[2]), f"frame {k}"
+    gpu_ctx.check()
+    with pytest.raises(RtError):
+        pipe.wait(len(order))  # not submitted
+    with pytest.raises(RtError):
+        pipe.submit(soups[0].clone(), *outs[0])  # pageable soup
+    pipe.close()
+    prim_only = Pipe(gpu_ctx, lb, n, cam, light, vis=False, mirror=False)
+    with pytest.raises(RtError):
+        prim_only.submit(soups[0], *outs[0])  # visibility / mirror outputs the pipe does not have
+    t = prim_only.submit(soups[1], outs[1][0])
+    prim_only.wait(t)
+    assert torch.equal(outs[1][0], ref[1][0])
+    prim_only.close()
+    gpu_ctx.check()
