@@ -332,7 +332,22 @@ __device__ __forceinline__ uint32_t sort_digit(uint32_t key, uint32_t id, int sh
     return SCENE ? scene_of(s_off, S, id) : ((key >> shift) & 0xffu);
 }
 
-template <bool SCENE>
+// Grouped look-back (GROUPED = true, the single-scene build): the tiles form
+// groups of kLookGroup consecutive tickets.  A tile publishes its digit
+// counts, sums those of the earlier tiles of its group (one round of
+// parallel loads), and the group's last tile publishes the group's
+// aggregate, then, once it knows the prefix of all earlier groups, the
+// group's inclusive prefix.  A tile's global offset is that group prefix,
+// found by the usual look-back over the group words, plus its sum inside
+// the group.  The chain of dependent L2 round trips runs over 17 group words
+// instead of 513 tile words at 2.1 M keys.  Every wait is on a lower ticket,
+// so no tile waits on one that may not have started.  The group words
+// follow the tile words in `lookback` (256 per group).
+constexpr uint32_t kLookGroup = 32;
+
+__host__ __device__ constexpr uint32_t look_groups(uint32_t tiles) { return (tiles + kLookGroup - 1) / kLookGroup; }
+
+template <bool SCENE, bool GROUPED = false>
 __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __restrict__ keys_in,
                                                            const uint32_t* __restrict__ ids_in,
                                                            uint32_t* __restrict__ keys_out,
@@ -400,6 +415,68 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
     }
     const uint32_t count = run;
 
+    uint32_t excl = 0;
+    if (GROUPED) {
+        uint32_t* gwords = lookback + (size_t)gridDim.x * 256;
+        const uint32_t G = tile / kLookGroup, g0 = G * kLookGroup;
+        const bool group_last = (tile - g0 == kLookGroup - 1) || (tile + 1 == gridDim.x);
+        st_relaxed(lookback + (size_t)tile * 256 + t, kFlagAgg | count);
+        // sum of the earlier tiles of the group (published right after their
+        // ranking; each word polled until it is)
+        uint32_t pre = 0, spins = 0;
+        for (uint32_t j0 = g0; j0 < tile; j0 += 8) {
+            uint32_t v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v[q] = (j0 + q < tile) ? ld_relaxed(lookback + (size_t)(j0 + q) * 256 + t) : kFlagAgg;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                while ((v[q] & kFlagMask) == 0u) {
+                    if (++spins > spin_limit) {
+                        atomicOr(err, RT_DEVERR_TIMEOUT);
+                        v[q] = kFlagAgg;
+                        break;
+                    }
+                    __nanosleep(kLookSleepNs);
+                    v[q] = ld_relaxed(lookback + (size_t)(j0 + q) * 256 + t);
+                }
+                pre += v[q] & kValMask;
+            }
+        }
+        uint32_t* gw = gwords + (size_t)G * 256 + t;
+        if (group_last) st_relaxed(gw, (G == 0 ? kFlagInc : kFlagAgg) | (pre + count));
+        // prefix of the earlier groups: look-back over the group words
+        uint32_t gex = 0;
+        if (G > 0) {
+            int p = (int)G - 1;
+            bool done = false;
+            while (!done && p >= 0) {
+                uint32_t v[kLookWidth];
+#pragma unroll
+                for (int q = 0; q < kLookWidth; ++q)
+                    v[q] = (p - q >= 0) ? ld_relaxed(gwords + (size_t)(p - q) * 256 + t) : 0u;
+                int used = 0;
+#pragma unroll
+                for (int q = 0; q < kLookWidth; ++q) {
+                    if (done || used < q || p - q < 0) continue;
+                    const uint32_t f = v[q] & kFlagMask;
+                    if (f == 0u) continue;  // not published yet: poll again from here
+                    gex += v[q] & kValMask;
+                    used = q + 1;
+                    if (f == kFlagInc) done = true;
+                }
+                if (!done && used == 0) {
+                    if (++spins > spin_limit) {
+                        atomicOr(err, RT_DEVERR_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(kLookSleepNs);
+                }
+                p -= used;
+            }
+            if (group_last) st_relaxed(gw, kFlagInc | (gex + pre + count));
+        }
+        excl = gex + pre;
+    } else {
     // decoupled look-back (bounded)
     uint32_t* my = lookback + (size_t)tile * 256 + t;
     st_relaxed(my, (tile == 0 ? kFlagInc : kFlagAgg) | count);
@@ -410,7 +487,6 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
     // issue slots from the warps of the same SM that are still ranking.
     // (Reading 8 or 16 words a step was slower: the extra polls cost more
     // than the shorter chain of inclusive prefixes saved.)
-    uint32_t excl = 0;
     if (tile > 0) {
         int p = (int)tile - 1;
         uint32_t spins = 0;
@@ -440,6 +516,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
             p -= used;
         }
         st_relaxed(my, kFlagInc | (excl + count));
+    }
     }
 
     const uint32_t lstart = block_excl_sum_256(count, s_tmp);
@@ -1780,7 +1857,9 @@ extern "C" rt_status rt_lbvh_create(rt_ctx* ctx, uint32_t max_tris, uint32_t dep
     alloc((void**)&l->partials, sizeof(float) * 8 * l->bounds_blocks);
     alloc((void**)&l->counters, sizeof(uint32_t) * 8);
     alloc((void**)&l->hist, sizeof(uint32_t) * 4 * 256);
-    alloc((void**)&l->lookback, sizeof(uint32_t) * kSortPasses * 256 * (size_t)l->sort_tiles_cap);
+    // per radix pass: 256 look-back words per tile, then 256 per tile group
+    alloc((void**)&l->lookback,
+          sizeof(uint32_t) * kSortPasses * 256 * ((size_t)l->sort_tiles_cap + look_groups(l->sort_tiles_cap)));
     alloc((void**)&l->scan, sizeof(uint32_t) * 4 * (size_t)l->emit_tiles_cap);
     alloc((void**)&l->leaf_list, 4 * cap);
     alloc((void**)&l->arrive, sizeof(uint32_t) * std::max(1u, l->num_nodes >> 1));
@@ -1828,7 +1907,8 @@ static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint
     l->src_tris = d_tris;
     const uint32_t sort_tiles = ceil_div(n, kSortTile);
     const uint32_t emit_tiles = ceil_div(n, kEmitTile);
-    const uint32_t lb_words = kSortPasses * 256 * sort_tiles;
+    const uint32_t lb_pass = 256 * (sort_tiles + look_groups(sort_tiles));  // tile words, group words
+    const uint32_t lb_words = kSortPasses * lb_pass;
     const uint32_t bblocks = std::max(1u, std::min(ceil_div(3ull * n, 256), l->bounds_blocks));
     launch_pdl(k_bounds, bblocks, 256, 0, st, d_tris, n, l->scene, l->partials, l->counters, l->hist, l->lookback,
                                       lb_words, l->nodes, l->num_nodes, (flags & RT_BUILD_CLEAR_UNREACHED) ? 1 : 0);
@@ -1838,8 +1918,8 @@ static rt_status launch_build(rt_ctx* ctx, rt_lbvh* l, const float* d_tris, uint
     RT_CHECK_LAUNCH(ctx, "k_morton_hist");
     uint32_t *kin = l->keys, *iin = l->ids, *kout = l->keys_alt, *iout = l->ids_alt;
     for (int p = 0; p < kSortPasses; ++p) {
-        launch_pdl(k_onesweep<false>, sort_tiles, kSortThreads, 0, st, (const uint32_t*)kin, (const uint32_t*)iin,
-                   kout, iout, n, p, (const uint32_t*)l->hist, l->lookback + (size_t)p * 256 * sort_tiles,
+        launch_pdl(k_onesweep<false, true>, sort_tiles, kSortThreads, 0, st, (const uint32_t*)kin, (const uint32_t*)iin,
+                   kout, iout, n, p, (const uint32_t*)l->hist, l->lookback + (size_t)p * lb_pass,
                    l->counters + 1 + p, ctx->d_err, (const uint32_t*)nullptr, 0u, kSpinLimit);
         RT_CHECK_LAUNCH(ctx, "k_onesweep");
         std::swap(kin, kout);
