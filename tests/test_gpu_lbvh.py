@@ -74,6 +74,17 @@ def test_build_large(gpu_ctx, oracle_mod, n, depth):
     assert_same_tree(oracle_mod, tris, depth, nodes, ids, keys)
 
 
+# Radix-pass tile groups of the single-scene build (4,096 keys a tile, 32
+# tiles a group): one group, a full group plus one ragged tile, and several
+# groups whose last one is partial; codes, permutation and tree bit-exact.
+@pytest.mark.parametrize("n", [32 * 4096 - 1, 32 * 4096 + 1, 65 * 4096 + 17, 97 * 4096])
+def test_build_sort_tile_groups(gpu_ctx, oracle_mod, n):
+    from rtgpu import scenes
+    tris = scenes.random_soup(n, seed=n)
+    lb, nodes, ids, keys = gpu_build(gpu_ctx, tris, 18)
+    assert_same_tree(oracle_mod, tris, 18, nodes, ids, keys)
+
+
 def test_build_host_input_and_rebuild(gpu_ctx, oracle_mod):
     """Host soup path, then rebuilds of the same object with other inputs
     (epoch-tagged refit words, reused scratch)."""
