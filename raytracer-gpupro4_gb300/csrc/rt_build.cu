@@ -5,20 +5,27 @@
 // (RayTracerCS/StructureConstruction.cpp:86-131: LBVH_PreBuild, bitonic sort,
 // one LBVH_Build dispatch per level, one LBVH_BuildAABB dispatch per level).
 //
-// Launch sequence (all on the context stream, no host synchronisation):
+// Launch sequence of rt_lbvh_build (all on the context stream, no host
+// synchronisation, programmatic dependent launch between kernels):
 //   k_bounds        scene AABB (last-block reduction) + scratch reset
 //   k_morton_hist   per-triangle centroid and 30-bit Morton code
 //                   (LBVH.cpp:512, 520-553) + the four 8-bit digit histograms
 //   k_onesweep x4   stable LSD radix sort of (code, id): warp-ballot digit
-//                   ranks, decoupled look-back over tiles, shared-memory
-//                   staged scatter.  Result = qsort(cmpMorton) order
-//                   (LBVH.cpp:21-38).
+//                   ranks, grouped decoupled look-back over tiles,
+//                   shared-memory staged scatter.  Result = qsort(cmpMorton)
+//                   order (LBVH.cpp:21-38).
 //   k_emit_tiles    per-tile aggregates of the boundary "record masks"
-//   k_emit_prefix   tile prefixes (one warp)
-//   k_emit_leaves   heap index of every element's leaf, leaf ranges, and the
-//                   triangle pre-gather in sorted order
-//   k_emit_refit    leaf boxes, then an atomic bottom-up walk that writes
-//                   every internal node (parent = h/2, sibling = h^1)
+//   k_emit_prefix   tile prefixes (one block)
+//   k_emit_units    per tile: each leaf's heap index and range, the triangle
+//                   pre-gather in sorted order, the leaf records (boxes by a
+//                   segmented scan) and the tile's leaves as ordered units
+//   k_emit_chunks   shared-memory bottom-up over each tile's units
+//   k_emit_merge    the same over groups of 32 chunks / groups, level after
+//                   level to the root, in one launch
+// The allocation-free build (rt_lbvh_build_noalloc) and the batched build
+// keep the one-level look-back and k_emit_leaves + k_emit_refit (leaf
+// boxes, then an atomic bottom-up walk with epoch-tagged arrival words that
+// writes every internal node: parent = h/2, sibling = h^1).
 //
 // Tree = the reference's: LBVH::build_recursive (LBVH.cpp:190-314) splits a
 // sorted range at its highest differing Morton bit, keeps equal-code runs as
