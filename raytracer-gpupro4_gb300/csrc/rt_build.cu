@@ -23,9 +23,10 @@
 //   k_emit_merge    the same over groups of 32 chunks / groups, level after
 //                   level to the root, in one launch
 // The allocation-free build (rt_lbvh_build_noalloc) and the batched build
-// keep the one-level look-back and k_emit_leaves + k_emit_refit (leaf
-// boxes, then an atomic bottom-up walk with epoch-tagged arrival words that
-// writes every internal node: parent = h/2, sibling = h^1).
+// keep the one-level look-back and the first emission form, k_emit_leaves +
+// k_emit_refit (kb_emit_leaves + kb_emit_refit for a batch): leaf boxes,
+// then an atomic bottom-up walk with epoch-tagged arrival words that writes
+// every internal node (parent = h/2, sibling = h^1).
 //
 // Tree = the reference's: LBVH::build_recursive (LBVH.cpp:190-314) splits a
 // sorted range at its highest differing Morton bit, keeps equal-code runs as
