@@ -2779,12 +2779,13 @@ extern "C" rt_status rt_batch_build(rt_ctx* ctx, rt_batch* b, const float* d_tri
                                                         b->sorted_tris, b->ids_local, b->leaf_list, b->counters + 5,
                                                         ctx->d_err);
     RT_CHECK_LAUNCH(ctx, "kb_emit_leaves");
-    // one thread per leaf at most (no persistent cap): a warp's time is its
-    // longest climb, and fresh warps then take the SM slots of finished ones
-    // instead of each thread walking ~40 leaves in turn (256 random-soup
-    // scenes, 11.5 M triangles: 3.89 -> 3.31 ms a batched build)
-    const uint32_t rblocks = std::max(1u, ceil_div(n, 256));
-    kb_emit_refit<<<rblocks, 256, 0, st>>>(kin, b->sorted_tris, b->tri_off, b->depth, b->nodes, b->leaf_list,
+    // one thread per leaf at most (no persistent cap), in blocks of two warps:
+    // a warp's time is its longest climb, and fresh warps then take the SM
+    // slots of finished ones instead of each thread walking ~40 leaves in
+    // turn (256 random-soup scenes, 11.5 M triangles: 3.89 -> 3.31 ms a
+    // batched build with 256-thread blocks, 3.15 ms with 64)
+    const uint32_t rblocks = std::max(1u, ceil_div(n, 64));
+    kb_emit_refit<<<rblocks, 64, 0, st>>>(kin, b->sorted_tris, b->tri_off, b->depth, b->nodes, b->leaf_list,
                                            b->counters + 5, n, b->arrive, b->counters + 6, ctx->d_err);
     RT_CHECK_LAUNCH(ctx, "kb_emit_refit");
     b->src_tris = d_tris;
