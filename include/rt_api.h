@@ -175,8 +175,9 @@ rt_status rt_lbvh_build_noalloc(rt_ctx* ctx, void* stream, const float* d_tris, 
 /* ---- sort stage ------------------------------------------------------ */
 /* Stable LSD radix sort of n (key, value) pairs by the full 32-bit key, in
  * place: four 8-bit passes (one digit histogram kernel, then per pass
- * warp-ballot ranks, a bounded decoupled look-back over 4,096-key tiles and
- * a shared-memory-staged scatter).  Equal keys keep their input order.
+ * warp-ballot ranks, a bounded decoupled look-back over 4,096-key tiles
+ * taken in groups of 32 tiles, as the build's sort does, and a
+ * shared-memory-staged scatter).  Equal keys keep their input order.
  * Replaces the sort stage of the GPU build, BitonicSort::GPUSort
  * (RayTracerCS/BitonicSort.cpp:56-117, 45 dispatches over a fixed 512 x 512
  * array) and RadixSort::Sort (RayTracerCS/RadixSort.cpp:46-74), without
@@ -190,9 +191,9 @@ rt_status rt_radix_sort(rt_ctx* ctx, uint32_t* d_keys, uint32_t* d_values, uint3
                         size_t scratch_bytes);
 /* Test hook of the bounded look-back wait (no counterpart in the
  * reference): runs the first radix pass of rt_radix_sort with its first
- * tile never started, so the second tile's look-back can never complete;
- * that wait gives up after spin_limit polls, records RT_ERR_TIMEOUT for
- * rt_ctx_check and returns.  Every access stays inside the buffers; d_keys
+ * tile never started, so the waits of the other tiles of its group for its
+ * digit counts can never complete; each gives up after spin_limit polls,
+ * records RT_ERR_TIMEOUT for rt_ctx_check and goes on, and the pass returns.  Every access stays inside the buffers; d_keys
  * and d_values are left untouched (the pass writes into the scratch).
  * n must exceed 4,096 (two tiles). */
 rt_status rt_radix_sort_stall_test(rt_ctx* ctx, const uint32_t* d_keys, const uint32_t* d_values, uint32_t n,

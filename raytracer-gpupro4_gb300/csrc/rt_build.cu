@@ -425,9 +425,10 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_onesweep(const uint32_t* __
 
     uint32_t excl = 0;
     if (GROUPED) {
-        uint32_t* gwords = lookback + (size_t)gridDim.x * 256;
+        const uint32_t T = (n + kSortTile - 1) / kSortTile;  // the pass's tiles (the grid may start later)
+        uint32_t* gwords = lookback + (size_t)T * 256;
         const uint32_t G = tile / kLookGroup, g0 = G * kLookGroup;
-        const bool group_last = (tile - g0 == kLookGroup - 1) || (tile + 1 == gridDim.x);
+        const bool group_last = (tile - g0 == kLookGroup - 1) || (tile + 1 == T);
         st_relaxed(lookback + (size_t)tile * 256 + t, kFlagAgg | count);
         // sum of the earlier tiles of the group (published right after their
         // ranking; each word polled until it is)
@@ -2224,15 +2225,17 @@ extern "C" rt_status rt_lbvh_build_noalloc(rt_ctx* ctx, void* stream, const floa
 // The sort stage on its own (rt_radix_sort): the four onesweep passes of the
 // build over caller-given (key, value) pairs with caller-owned scratch.
 // Scratch words: [0, 16) tile tickets (pass p at 1 + p), [16, 1040) the
-// four digit histograms, then the look-back words (4 x 256 per tile), then
-// the ping-pong keys and values (n each, 16-byte aligned).
+// four digit histograms, then the look-back words (per pass 256 per tile and
+// 256 per group of tiles: the build's grouped look-back), then the ping-pong
+// keys and values (n each, 16-byte aligned).
 namespace {
 
 constexpr size_t kRsHist = 16;
 constexpr size_t kRsLookback = kRsHist + 4 * 256;
 
 size_t rs_tiles(uint32_t n) { return ((size_t)n + kSortTile - 1) / kSortTile; }
-size_t rs_alt_offset(uint32_t n) { return kRsLookback + (size_t)kSortPasses * 256 * rs_tiles(n); }
+size_t rs_pass_words(uint32_t n) { return 256 * (rs_tiles(n) + look_groups((uint32_t)rs_tiles(n))); }
+size_t rs_alt_offset(uint32_t n) { return kRsLookback + (size_t)kSortPasses * rs_pass_words(n); }
 size_t rs_words(uint32_t n) { return rs_alt_offset(n) + 2 * (((size_t)n + 3) & ~(size_t)3); }
 
 // Digit histograms of the four passes (block-local shared-memory atomics,
@@ -2288,9 +2291,9 @@ extern "C" rt_status rt_radix_sort(rt_ctx* ctx, uint32_t* d_keys, uint32_t* d_va
     uint32_t* valt = kalt + (((size_t)n + 3) & ~(size_t)3);
     uint32_t *kin = d_keys, *iin = d_values, *kout = kalt, *iout = valt;
     for (int p = 0; p < kSortPasses; ++p) {
-        k_onesweep<false><<<tiles, kSortThreads, 0, ctx->stream>>>(kin, iin, kout, iout, n, p, S + kRsHist,
-                                                                   S + kRsLookback + (size_t)p * 256 * tiles,
-                                                                   S + 1 + p, ctx->d_err);
+        k_onesweep<false, true><<<tiles, kSortThreads, 0, ctx->stream>>>(kin, iin, kout, iout, n, p, S + kRsHist,
+                                                                         S + kRsLookback + (size_t)p * rs_pass_words(n),
+                                                                         S + 1 + p, ctx->d_err);
         RT_CHECK_LAUNCH(ctx, "k_onesweep");
         std::swap(kin, kout);
         std::swap(iin, iout);
@@ -2312,14 +2315,15 @@ extern "C" rt_status rt_radix_sort_stall_test(rt_ctx* ctx, const uint32_t* d_key
     uint32_t* kalt = S + rs_alt_offset(n);
     uint32_t* valt = kalt + (((size_t)n + 3) & ~(size_t)3);
     // the pass's tile tickets start at 1: tiles 1 .. tiles-1 run and tile 0
-    // never publishes its digit counts, so tile 1's look-back gives up after
-    // spin_limit polls (a later tile that passed tile 1's aggregate before
-    // tile 1 gave up waits on tile 0 too and gives up the same way)
+    // never publishes its digit counts, so the other tiles of its group give
+    // up waiting for them after spin_limit polls (the grouped look-back of
+    // rt_radix_sort and the build; the group's last tile then publishes a
+    // group prefix, and later groups finish)
     k_set_word<<<1, 1, 0, ctx->stream>>>(S + 1, 1u);
     RT_CHECK_LAUNCH(ctx, "k_set_word");
-    k_onesweep<false><<<tiles - 1, kSortThreads, 0, ctx->stream>>>(d_keys, d_values, kalt, valt, n, 0, S + kRsHist,
-                                                                   S + kRsLookback, S + 1, ctx->d_err, nullptr, 0u,
-                                                                   spin_limit);
+    k_onesweep<false, true><<<tiles - 1, kSortThreads, 0, ctx->stream>>>(d_keys, d_values, kalt, valt, n, 0,
+                                                                         S + kRsHist, S + kRsLookback, S + 1,
+                                                                         ctx->d_err, nullptr, 0u, spin_limit);
     RT_CHECK_LAUNCH(ctx, "k_onesweep");
     return RT_OK;
 }

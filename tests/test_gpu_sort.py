@@ -36,7 +36,7 @@ def test_reference_reverse_pattern_kat(gpu_ctx):
     assert np.array_equal(v, ((1023 - p // 256) + 1024 * (p % 256)).astype(np.uint32))
 
 
-@pytest.mark.parametrize("n", [1, 2, 4095, 4096, 4097, 100_003, 2_099_520])
+@pytest.mark.parametrize("n", [1, 2, 4095, 4096, 4097, 100_003, 32 * 4096 + 1, 33 * 4096, 2_099_520])
 def test_random_keys_match_stable_cpu_sort(gpu_ctx, n):
     rng = np.random.default_rng(n)
     keys = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
@@ -74,12 +74,12 @@ def test_scratch_too_small_is_rejected(gpu_ctx):
 
 
 def test_lookback_wait_runs_out_and_the_next_build_is_correct(gpu_ctx, oracle_mod):
-    """The look-back of a radix pass waits on its predecessor tile's
-    published prefix.  The stall hook never starts the first tile, so the
-    wait of the second can never end: it must give up after the given
-    number of polls, report RT_ERR_TIMEOUT through rt_ctx_check, leave the
-    inputs untouched, and leave the context usable (a full build after it
-    equals the oracle)."""
+    """The look-back of a radix pass waits for the digit counts of the
+    earlier tiles of its group.  The stall hook never starts the first tile,
+    so the waits of the other tiles of its group can never end: they must
+    give up after the given number of polls, report RT_ERR_TIMEOUT through
+    rt_ctx_check, leave the inputs untouched, and leave the context usable
+    (a full build after it equals the oracle)."""
     import torch
     from rtgpu import _lib as L
     from rtgpu import scenes
