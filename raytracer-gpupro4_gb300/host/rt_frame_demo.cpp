@@ -11,7 +11,9 @@
 // LoadFile + Model::Scale; n is then the model's triangle count);
 // camera.f32: eye, right, up, fwd (3 floats each), tan(fovy/2).  Writes
 // <out_prefix>.primary / .vis / .mirror (raw rt_hit / uint8 arrays of the
-// last frame) and prints one JSON summary line.
+// last frame), the same frames streamed from pinned host memory through
+// FramePipeline to <out_prefix>.pipe.primary / .pipe.vis / .pipe.mirror, and
+// prints one JSON summary line.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -112,6 +114,33 @@ int main(int argc, char** argv) {
         write_raw(out + ".primary", prim);
         write_raw(out + ".vis", vis);
         write_raw(out + ".mirror", mir);
+        // the same frames with host data, pipelined (rt_pipe_*: two frames
+        // in flight, host result buffers alternating); the last frame's
+        // results go to <out_prefix>.pipe.primary / .pipe.vis / .pipe.mirror
+        {
+            const size_t px = (size_t)cam.width * cam.height;
+            rtgb::FramePipeline pipe(ctx, n, cam, light, depth);
+            rtgb::PinnedBuffer hsoup(sizeof(float) * 9 * (size_t)n);
+            std::memcpy(hsoup.data(), soup.data(), sizeof(float) * 9 * (size_t)n);
+            rtgb::PinnedBuffer hp[2] = {rtgb::PinnedBuffer(sizeof(rt_hit) * px), rtgb::PinnedBuffer(sizeof(rt_hit) * px)};
+            rtgb::PinnedBuffer hv[2] = {rtgb::PinnedBuffer(px), rtgb::PinnedBuffer(px)};
+            rtgb::PinnedBuffer hm[2] = {rtgb::PinnedBuffer(sizeof(rt_hit) * px), rtgb::PinnedBuffer(sizeof(rt_hit) * px)};
+            uint64_t last = 0;
+            for (int f = 0; f < frames; ++f) {
+                if (f >= 2) pipe.Wait((uint64_t)(f - 2));
+                last = pipe.Submit(static_cast<const float*>(hsoup.data()), static_cast<rt_hit*>(hp[f & 1].data()),
+                                   static_cast<uint8_t*>(hv[f & 1].data()), static_cast<rt_hit*>(hm[f & 1].data()));
+            }
+            pipe.Wait(last);
+            ctx.Check();
+            const int q = (int)(last & 1u);
+            const rt_hit* pp = static_cast<const rt_hit*>(hp[q].data());
+            const uint8_t* pv = static_cast<const uint8_t*>(hv[q].data());
+            const rt_hit* pm = static_cast<const rt_hit*>(hm[q].data());
+            write_raw(out + ".pipe.primary", std::vector<rt_hit>(pp, pp + px));
+            write_raw(out + ".pipe.vis", std::vector<uint8_t>(pv, pv + px));
+            write_raw(out + ".pipe.mirror", std::vector<rt_hit>(pm, pm + px));
+        }
         size_t hits = 0, lit = 0;
         for (auto& h : prim) hits += h.id >= 0;
         for (auto v : vis) lit += v == 3;

@@ -263,4 +263,50 @@ std::vector<rt_hit> RayTracerCS::DownloadMirror() const {
     return h;
 }
 
+// ---------------------------------------------------------------------------
+PinnedBuffer::PinnedBuffer(size_t bytes) {
+    cuda_check(cudaHostAlloc(&p_, bytes, cudaHostAllocDefault), "cudaHostAlloc");
+    bytes_ = bytes;
+}
+PinnedBuffer::~PinnedBuffer() {
+    if (p_) cudaFreeHost(p_);
+}
+PinnedBuffer::PinnedBuffer(PinnedBuffer&& o) noexcept : p_(o.p_), bytes_(o.bytes_) {
+    o.p_ = nullptr;
+    o.bytes_ = 0;
+}
+PinnedBuffer& PinnedBuffer::operator=(PinnedBuffer&& o) noexcept {
+    if (this != &o) {
+        if (p_) cudaFreeHost(p_);
+        p_ = o.p_;
+        bytes_ = o.bytes_;
+        o.p_ = nullptr;
+        o.bytes_ = 0;
+    }
+    return *this;
+}
+
+// ---------------------------------------------------------------------------
+FramePipeline::FramePipeline(Context& ctx, unsigned int numPrimitives, const rt_camera& camera, const float light[3],
+                             unsigned int lbvhDepth, bool visibility, bool mirror)
+    : m_ctx(ctx) {
+    check(rt_lbvh_create(ctx.get(), numPrimitives, lbvhDepth, &m_lbvh), ctx.get(), "rt_lbvh_create");
+    const rt_status s = rt_pipe_create(ctx.get(), m_lbvh, numPrimitives, 0, &camera, light, visibility ? 1 : 0,
+                                       mirror ? 1 : 0, &m_pipe);
+    if (s != RT_OK) {
+        rt_lbvh_destroy(m_lbvh);
+        check(s, ctx.get(), "rt_pipe_create");
+    }
+}
+FramePipeline::~FramePipeline() {
+    rt_pipe_destroy(m_pipe);
+    rt_lbvh_destroy(m_lbvh);  // freed with the pipe's last captured frame
+}
+uint64_t FramePipeline::Submit(const float* h_soup, rt_hit* h_primary, uint8_t* h_vis, rt_hit* h_mirror) {
+    uint64_t ticket = 0;
+    check(rt_pipe_submit(m_pipe, h_soup, h_primary, h_vis, h_mirror, &ticket), m_ctx.get(), "rt_pipe_submit");
+    return ticket;
+}
+void FramePipeline::Wait(uint64_t ticket) { check(rt_pipe_wait(m_pipe, ticket), m_ctx.get(), "rt_pipe_wait"); }
+
 }  // namespace rtgb

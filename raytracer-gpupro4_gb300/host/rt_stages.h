@@ -230,4 +230,46 @@ class RayTracerCS {
     unsigned int m_NumMuestras = 0;
 };
 
+// Page-locked host buffer (cudaHostAlloc): what rt_pipe_submit copies from
+// and into.
+class PinnedBuffer {
+   public:
+    PinnedBuffer() = default;
+    explicit PinnedBuffer(size_t bytes);
+    ~PinnedBuffer();
+    PinnedBuffer(PinnedBuffer&& o) noexcept;
+    PinnedBuffer& operator=(PinnedBuffer&& o) noexcept;
+    PinnedBuffer(const PinnedBuffer&) = delete;
+    void* data() const { return p_; }
+    size_t size() const { return bytes_; }
+
+   private:
+    void* p_ = nullptr;
+    size_t bytes_ = 0;
+};
+
+// A dynamic model's frame loop with host data (vertex update + Render +
+// read-back of the results, RayTracerCS.cpp:241-311) pipelined over
+// rt_pipe_*: two frames in flight, uploads and read-backs on copy streams,
+// the frames' rebuild + trace in order on the context stream.  Submit
+// returns the frame's ticket; after Wait(ticket) its host results are
+// complete and its host soup may be rewritten.  Host buffers must be
+// page-locked (PinnedBuffer).  Any output may be null when the pipeline was
+// created without it.
+class FramePipeline {
+   public:
+    FramePipeline(Context& ctx, unsigned int numPrimitives, const rt_camera& camera, const float light[3],
+                  unsigned int lbvhDepth = 20, bool visibility = true, bool mirror = true);
+    ~FramePipeline();
+    FramePipeline(const FramePipeline&) = delete;
+    FramePipeline& operator=(const FramePipeline&) = delete;
+    uint64_t Submit(const float* h_soup, rt_hit* h_primary, uint8_t* h_vis = nullptr, rt_hit* h_mirror = nullptr);
+    void Wait(uint64_t ticket);
+
+   private:
+    Context& m_ctx;
+    rt_lbvh* m_lbvh = nullptr;
+    rt_pipe* m_pipe = nullptr;
+};
+
 }  // namespace rtgb

@@ -1,6 +1,6 @@
 """The C++ drop-in stage classes (host/rt_stages.h: LBVHGpu, StructureConstruction,
-RayTracerCS) driven by host/rt_frame_demo, against the Python binding of the
-same C ABI and the oracle."""
+RayTracerCS, FramePipeline) driven by host/rt_frame_demo, against the Python
+binding of the same C ABI and the oracle."""
 import json
 import subprocess
 
@@ -35,6 +35,10 @@ def test_cpp_stage_classes(gpu_ctx, oracle_mod, tmp_path):
     prim = np.fromfile(str(out) + ".primary", HIT_DTYPE)
     vis = np.fromfile(str(out) + ".vis", np.uint8)
     mir = np.fromfile(str(out) + ".mirror", HIT_DTYPE)
+    # the same frames streamed from pinned host memory through FramePipeline (rt_pipe_*)
+    assert same_bits(np.fromfile(str(out) + ".pipe.primary", HIT_DTYPE), prim)
+    assert np.array_equal(np.fromfile(str(out) + ".pipe.vis", np.uint8), vis)
+    assert same_bits(np.fromfile(str(out) + ".pipe.mirror", HIT_DTYPE), mir)
     # same frame through the Python binding
     lb = LBVH(gpu_ctx, len(tris), depth).Build(torch.from_numpy(tris).cuda())
     rt = RayTracer(gpu_ctx)
