@@ -12,8 +12,11 @@
 // camera.f32: eye, right, up, fwd (3 floats each), tan(fovy/2).  Writes
 // <out_prefix>.primary / .vis / .mirror (raw rt_hit / uint8 arrays of the
 // last frame), the same frames streamed from pinned host memory through
-// FramePipeline to <out_prefix>.pipe.primary / .pipe.vis / .pipe.mirror, and
-// prints one JSON summary line.
+// FramePipeline to <out_prefix>.pipe.primary / .pipe.vis / .pipe.mirror, the
+// colour stage's accumulation image to <out_prefix>.color and a progressive
+// GI image (4 samples in two calls) to <out_prefix>.gi, and prints one JSON
+// summary line.
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -140,6 +143,23 @@ int main(int argc, char** argv) {
             write_raw(out + ".pipe.primary", std::vector<rt_hit>(pp, pp + px));
             write_raw(out + ".pipe.vis", std::vector<uint8_t>(pv, pv + px));
             write_raw(out + ".pipe.mirror", std::vector<rt_hit>(pm, pm + px));
+        }
+        // the colour stage (one material, one bounce, shadows on) and four
+        // progressive GI samples in two calls of two, through RayTracerCS;
+        // written to <out_prefix>.color (accumulation) and <out_prefix>.gi
+        {
+            rt_material mat = {{1.5f, 0.f, 0.f, 0.f}, {0.7f, 0.4f, 0.2f, 1.f}, {0.5f, 0.5f, 0.5f, 1.f}, 0.049f, 0.6f};
+            rt_shade_params sp = {1u, 1, 0, 0, -1, {0.2f, 0.3f, 0.4f}, 7u};
+            rt.RenderColor(sp, &mat, 1);
+            write_raw(out + ".color", rt.DownloadAccumulation());
+            std::vector<float> albedo(3 * (size_t)n, 0.6f), emission(3 * (size_t)n, 0.f);
+            for (size_t k = 0; k < std::min<size_t>(n, 64) * 3; ++k) emission[k] = 2.f;
+            rt.SetGIMaterials(albedo.data(), emission.data());
+            const float sky[3] = {1.f, 1.f, 1.f};
+            rt.RenderGI(2, 2, 11, sky);
+            rt.RenderGI(2, 2, 11, sky);
+            ctx.Check();
+            write_raw(out + ".gi", rt.DownloadGI());
         }
         size_t hits = 0, lit = 0;
         for (auto& h : prim) hits += h.id >= 0;

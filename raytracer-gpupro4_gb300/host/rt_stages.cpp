@@ -227,10 +227,7 @@ void RayTracerCS::Render() {
     // rays and the colour stage's shadow + mirror rays, which start their
     // walks at the primary hit's leaf (the iRoot the reference keeps in
     // g_uIntersections, CSComputeColorRT.hlsl:160)
-    if (m_dynamic || !m_built) {
-        m_construction.GPUBuildStructure(m_depth, static_cast<const float*>(m_soup.data()), m_scene.numPrimitives);
-        m_built = true;
-    }
+    Rebuild();
     rt_lbvh* l = m_construction.lbvh();
     uint32_t* roots = static_cast<uint32_t*>(m_roots.data());
     check(rt_trace_primary_leaves(m_ctx.get(), l, &m_camera, static_cast<rt_hit*>(m_primary.data()), roots, nullptr),
@@ -240,6 +237,75 @@ void RayTracerCS::Render() {
                                       nullptr, nullptr, nullptr),
           m_ctx.get(), "rt_trace_shadow_mirror_from");
     ++m_NumMuestras;
+}
+
+void RayTracerCS::Rebuild() {
+    if (m_dynamic || !m_built) {
+        m_construction.GPUBuildStructure(m_depth, static_cast<const float*>(m_soup.data()), m_scene.numPrimitives);
+        m_built = true;
+    }
+}
+
+void RayTracerCS::RenderColor(const rt_shade_params& params, const rt_material* materials, unsigned int numMaterials,
+                              const int32_t* materialIds) {
+    if (!materials || numMaterials == 0) throw Error(RT_ERR_INVALID, "RayTracerCS::RenderColor: no materials");
+    Rebuild();
+    const size_t px = (size_t)m_camera.width * m_camera.height;
+    m_materials.upload(materials, sizeof(rt_material) * numMaterials, nullptr);
+    if (materialIds) m_materialIds.upload(materialIds, sizeof(int32_t) * m_scene.numPrimitives, nullptr);
+    m_accum.resize(sizeof(float) * 4 * px);
+    m_result.resize(sizeof(float) * 4 * px);
+    cuda_check(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    check(rt_render_whitted(m_ctx.get(), m_construction.lbvh(), &m_camera, m_light, &params,
+                            materialIds ? static_cast<const int32_t*>(m_materialIds.data()) : nullptr,
+                            static_cast<const rt_material*>(m_materials.data()), numMaterials, nullptr,
+                            static_cast<float*>(m_accum.data()), static_cast<float*>(m_result.data())),
+          m_ctx.get(), "rt_render_whitted");
+}
+
+std::vector<float> RayTracerCS::DownloadAccumulation() const {
+    m_ctx.Sync();
+    std::vector<float> v((size_t)m_camera.width * m_camera.height * 4);
+    m_accum.download(v.data(), sizeof(float) * v.size(), nullptr);
+    return v;
+}
+
+std::vector<float> RayTracerCS::DownloadResult() const {
+    m_ctx.Sync();
+    std::vector<float> v((size_t)m_camera.width * m_camera.height * 4);
+    m_result.download(v.data(), sizeof(float) * v.size(), nullptr);
+    return v;
+}
+
+void RayTracerCS::SetGIMaterials(const float* albedo, const float* emission) {
+    if (!albedo || !emission) throw Error(RT_ERR_INVALID, "RayTracerCS::SetGIMaterials: null array");
+    m_albedo.upload(albedo, sizeof(float) * 3 * m_scene.numPrimitives, nullptr);
+    m_emission.upload(emission, sizeof(float) * 3 * m_scene.numPrimitives, nullptr);
+    cuda_check(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+}
+
+void RayTracerCS::RenderGI(unsigned int spp, unsigned int bounces, uint64_t seed, const float sky[3]) {
+    if (!m_albedo.data() || !m_emission.data())
+        throw Error(RT_ERR_INVALID, "RayTracerCS::RenderGI: SetGIMaterials first");
+    Rebuild();
+    m_gi.resize(sizeof(float) * 4 * (size_t)m_camera.width * m_camera.height);
+    rt_pt_params p;
+    p.spp = spp;
+    p.bounces = bounces;
+    p.seed = seed;
+    for (int c = 0; c < 3; ++c) p.sky[c] = sky[c];
+    p.first_sample = m_giSamples;
+    check(rt_pathtrace(m_ctx.get(), m_construction.lbvh(), static_cast<const float*>(m_albedo.data()),
+                       static_cast<const float*>(m_emission.data()), &m_camera, &p, static_cast<float*>(m_gi.data())),
+          m_ctx.get(), "rt_pathtrace");
+    m_giSamples += spp;
+}
+
+std::vector<float> RayTracerCS::DownloadGI() const {
+    m_ctx.Sync();
+    std::vector<float> v((size_t)m_camera.width * m_camera.height * 4);
+    m_gi.download(v.data(), sizeof(float) * v.size(), nullptr);
+    return v;
 }
 
 std::vector<rt_hit> RayTracerCS::DownloadPrimary() const {

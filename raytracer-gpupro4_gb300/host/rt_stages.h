@@ -217,6 +217,28 @@ class RayTracerCS {
     unsigned int GetNumSamples() const { return m_NumMuestras; }
     StructureConstruction& construction() { return m_construction; }
 
+    // The colour stage of Render without global illumination
+    // (RayTracerCS.cpp:284-295, CSComputeColorRT.hlsl): primary rays, then
+    // params.bounces + 1 intersection + colour stages into the accumulation
+    // and result images (g_uAccumulation / g_uResultTexture, w*h float4).
+    // materials: numMaterials host rows; materialIds: host, one per
+    // triangle, or null (all 0).  Rebuilds first when dynamic.
+    void RenderColor(const rt_shade_params& params, const rt_material* materials, unsigned int numMaterials,
+                     const int32_t* materialIds = nullptr);
+    std::vector<float> DownloadAccumulation() const;
+    std::vector<float> DownloadResult() const;
+
+    // Progressive global illumination (CSComputeColorGI.hlsl with the frame
+    // counter of RayTracerCS.cpp:306): each call traces spp more samples per
+    // pixel and blends them into the GI image; ResetGI() restarts it (the
+    // reset on camera motion, RayTracerCS.cpp:246-250).  albedo / emission:
+    // host, n x 3 floats indexed by triangle id.  Rebuilds first when dynamic.
+    void SetGIMaterials(const float* albedo, const float* emission);
+    void RenderGI(unsigned int spp, unsigned int bounces, uint64_t seed, const float sky[3]);
+    void ResetGI() { m_giSamples = 0; }
+    unsigned int GetGISamples() const { return m_giSamples; }
+    std::vector<float> DownloadGI() const;
+
    private:
     Context& m_ctx;
     Scene m_scene;
@@ -227,7 +249,11 @@ class RayTracerCS {
     bool m_built = false;
     StructureConstruction m_construction;
     DeviceBuffer m_soup, m_primary, m_roots, m_vis, m_mirror;
+    DeviceBuffer m_materials, m_materialIds, m_accum, m_result;
+    DeviceBuffer m_albedo, m_emission, m_gi;
     unsigned int m_NumMuestras = 0;
+    unsigned int m_giSamples = 0;
+    void Rebuild();
 };
 
 // Page-locked host buffer (cudaHostAlloc): what rt_pipe_submit copies from

@@ -35,6 +35,18 @@ def test_cpp_stage_classes(gpu_ctx, oracle_mod, tmp_path):
     prim = np.fromfile(str(out) + ".primary", HIT_DTYPE)
     vis = np.fromfile(str(out) + ".vis", np.uint8)
     mir = np.fromfile(str(out) + ".mirror", HIT_DTYPE)
+    # the colour stage and progressive GI through RayTracerCS (RenderColor, RenderGI x 2)
+    lbc = LBVH(gpu_ctx, len(tris), depth).Build(torch.from_numpy(tris).cuda())
+    rtc = RayTracer(gpu_ctx)
+    mats = np.array([[1.5, 0, 0, 0, 0.7, 0.4, 0.2, 1, 0.5, 0.5, 0.5, 1, 0.049, 0.6]], np.float32)
+    acc, _ = rtc.whitted(lbc, cam, light, mats, bounces=1, shadows=True, env_mapping=-1, env_color=(0.2, 0.3, 0.4),
+                         seed=7)
+    assert same_bits(np.fromfile(str(out) + ".color", np.float32), acc.cpu().numpy().reshape(-1))
+    albedo = torch.full((len(tris), 3), 0.6, dtype=torch.float32, device="cuda")
+    emission = torch.zeros((len(tris), 3), dtype=torch.float32, device="cuda")
+    emission[:64] = 2.0
+    gi = rtc.pathtrace(lbc, albedo, emission, cam, 4, 2, 11)  # one call of 4 samples
+    assert same_bits(np.fromfile(str(out) + ".gi", np.float32), gi.cpu().numpy().reshape(-1))
     # the same frames streamed from pinned host memory through FramePipeline (rt_pipe_*)
     assert same_bits(np.fromfile(str(out) + ".pipe.primary", HIT_DTYPE), prim)
     assert np.array_equal(np.fromfile(str(out) + ".pipe.vis", np.uint8), vis)
