@@ -38,3 +38,24 @@ def test_layouts():
     assert _lib.NODE_DTYPE.itemsize == 32  # LBVHNode, LBVH.h:25-28
     assert _lib.HIT_DTYPE.itemsize == 16
     assert _lib.RAY_DTYPE.itemsize == 32
+
+
+def test_null_handles_are_refused_without_touching_the_device(rt_lib):
+    """Entry points given a null context or object return before any CUDA
+    call: RT_ERR_INVALID, or RT_OK for the destroy calls (this runs without a
+    GPU)."""
+    import ctypes as C
+    from rtgpu import _lib as L
+    lib = L.lib()
+    t = C.c_uint64()
+    assert lib.rt_pipe_submit(None, None, None, None, None, C.byref(t)) == L.RT_ERR_INVALID
+    assert lib.rt_pipe_wait(None, 0) == L.RT_ERR_INVALID
+    assert lib.rt_pipe_create(None, None, 1, 0, None, None, 1, 1, None) == L.RT_ERR_INVALID
+    assert lib.rt_frame_launch(None, None) == L.RT_ERR_INVALID
+    assert lib.rt_lbvh_build(None, None, None, 1, 0) == L.RT_ERR_INVALID
+    assert lib.rt_batch_build(None, None, None, 0) == L.RT_ERR_INVALID
+    assert lib.rt_radix_sort(None, None, None, 1, None, 0) == L.RT_ERR_INVALID
+    assert lib.rt_trace_primary(None, None, None, None, None) == L.RT_ERR_INVALID
+    assert lib.rt_pathtrace(None, None, None, None, None, None, None) == L.RT_ERR_INVALID
+    for destroy in ("rt_pipe_destroy", "rt_frame_destroy", "rt_lbvh_destroy", "rt_batch_destroy", "rt_ctx_destroy"):
+        assert getattr(lib, destroy)(None) == L.RT_OK, destroy
